@@ -1,0 +1,123 @@
+"""ctypes binding of the C ABI declared in include/difftactile_gb300.h.
+
+The CUDA library is the only compute path: importing this module without the built library
+raises, and there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+
+class DtEnv(C.Structure):
+    _fields_ = [
+        ("p_begin", C.c_int), ("p_end", C.c_int), ("node_off", C.c_int), ("blk_off", C.c_int),
+        ("nb", C.c_int * 3), ("n", C.c_int * 3), ("bound", C.c_int), ("bc", C.c_int),
+        ("s_begin", C.c_int), ("s_end", C.c_int),
+        ("dx", C.c_float), ("inv_dx", C.c_float), ("p_mass", C.c_float), ("stress_k", C.c_float),
+        ("eps", C.c_float), ("g2p_k", C.c_float), ("dt_g", C.c_float * 3),
+        ("kn", C.c_float), ("kd", C.c_float), ("kt", C.c_float), ("mu_t", C.c_float), ("pad_", C.c_float),
+    ]
+
+
+class DtSensor(C.Structure):
+    _fields_ = [
+        ("v_off", C.c_int), ("nv", C.c_int), ("t_off", C.c_int), ("nt", C.c_int),
+        ("f_off", C.c_int), ("nf", C.c_int), ("env", C.c_int), ("carry", C.c_int),
+        ("dt_over_m", C.c_float), ("mu", C.c_float), ("lam", C.c_float), ("alpha", C.c_float),
+        ("out_dir", C.c_float * 3), ("pad_", C.c_float),
+    ]
+
+
+class DtMaterial(C.Structure):
+    _fields_ = [("mu", C.c_float), ("lam", C.c_float), ("yield_stress", C.c_float), ("model", C.c_int)]
+
+
+_P = C.c_void_p
+WORLD_PTR_FIELDS = [
+    "envs", "sensors", "materials", "p_env", "p_mat", "blk_env", "tets", "tet_B", "tet_sensor", "tris",
+    "v_layer", "v_sensor",
+    "p_state", "p_adj",
+    "g_acc", "g_vout", "g_adj_vout", "g_adj_acc", "blk_flag",
+    "tape_blist", "tape_bcount", "tape_acc", "tape_vout", "tape_cidx",
+    "v_pos", "v_vel", "v_velmid", "v_ext", "v_vpos", "v_cv", "tri_cent",
+    "v_adj_pos", "v_adj_vel", "v_adj_vpos", "v_adj_velmid", "v_adj_ext", "v_adj_cv", "mat_adj",
+    "err",
+]
+WORLD_INT_FIELDS = [
+    "n_envs", "n_particles", "n_sensors", "n_materials", "n_verts", "n_tets", "n_tris",
+    "n_nodes", "n_blocks", "n_frames", "tape_blocks",
+]
+
+
+class DtWorld(C.Structure):
+    _fields_ = ([(n, _P) for n in WORLD_PTR_FIELDS] + [(n, C.c_int) for n in WORLD_INT_FIELDS]
+                + [("dt", C.c_float), ("grad_clip", C.c_float), ("svd_sweeps", C.c_int), ("pad_", C.c_int)])
+
+
+# entry points: name -> (restype, argtypes)
+_W = C.POINTER(DtWorld)
+SIGNATURES = {
+    "dt_abi_version": (C.c_int, []),
+    "dt_sizeof_world": (C.c_size_t, []),
+    "dt_sizeof_env": (C.c_size_t, []),
+    "dt_sizeof_sensor": (C.c_size_t, []),
+    "dt_sizeof_material": (C.c_size_t, []),
+    "dt_step_begin": (C.c_int, [_W, _P]),
+    "dt_substep_fwd": (C.c_int, [_W, C.c_int, _P]),
+    "dt_p2g": (C.c_int, [_W, C.c_int, _P]),
+    "dt_fem_update": (C.c_int, [_W, C.c_int, _P]),
+    "dt_grid_op": (C.c_int, [_W, C.c_int, _P]),
+    "dt_g2p": (C.c_int, [_W, C.c_int, _P]),
+    "dt_fem_update2": (C.c_int, [_W, C.c_int, _P]),
+    "dt_copy_frame": (C.c_int, [_W, C.c_int, C.c_int, _P]),
+    "dt_substep_bwd": (C.c_int, [_W, C.c_int, _P]),
+    "dt_adj_clear": (C.c_int, [_W, _P]),
+    "dt_com": (C.c_int, [_W, C.c_int, _P, _P]),
+    "dt_com_bwd": (C.c_int, [_W, C.c_int, _P, _P]),
+}
+
+ERRORS = {0: "DT_OK", -1: "DT_ERR_ARG", -2: "DT_ERR_LAUNCH", -3: "DT_ERR_CAPACITY"}
+DEVERR = {1: "particle left the grid's safe band", 2: "grid tape capacity exceeded", 4: "non-finite value"}
+
+
+class DtError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (built by ``difftactile_gb300.build.build()``); raise if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError(
+            f"difftactile_gb300 CUDA library not found at {path}; run "
+            "`python -c 'import __graft_entry__ as g; g.build()'` (there is no CPU fallback)")
+    import torch  # noqa: F401  (loads the CUDA runtime the library links against)
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    for name, cls in (("world", DtWorld), ("env", DtEnv), ("sensor", DtSensor), ("material", DtMaterial)):
+        n = getattr(lib, f"dt_sizeof_{name}")()
+        if n != C.sizeof(cls):
+            raise ImportError(f"ABI mismatch: sizeof(dt_{name}) = {n} in the library, {C.sizeof(cls)} in ctypes")
+    if lib.dt_abi_version() != 1:
+        raise ImportError("ABI version mismatch")
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str):
+    if rc != 0:
+        raise DtError(f"{what} failed: {ERRORS.get(rc, rc)}")

@@ -1,0 +1,467 @@
+// Device helpers shared by the forward and adjoint substep kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/difftactile_gb300.h"
+
+#define DT_DEV __device__ __forceinline__
+
+// ------------------------------------------------------------------------------------------
+// small fixed-size linear algebra, row-major, fully unrolled into registers
+// ------------------------------------------------------------------------------------------
+struct m3 {
+  float a[3][3];
+};
+struct v3 {
+  float x, y, z;
+};
+
+DT_DEV v3 mk3(float x, float y, float z) { return v3{x, y, z}; }
+DT_DEV v3 operator+(v3 a, v3 b) { return v3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+DT_DEV v3 operator-(v3 a, v3 b) { return v3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+DT_DEV v3 operator-(v3 a) { return v3{-a.x, -a.y, -a.z}; }
+DT_DEV v3 operator*(float s, v3 a) { return v3{s * a.x, s * a.y, s * a.z}; }
+DT_DEV float dot(v3 a, v3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+DT_DEV v3 cross(v3 a, v3 b) { return v3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+DT_DEV v3 f4to3(float4 a) { return v3{a.x, a.y, a.z}; }
+DT_DEV float4 v3to4(v3 a, float w = 0.f) { return make_float4(a.x, a.y, a.z, w); }
+DT_DEV float get(v3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+
+DT_DEV m3 meye() {
+  m3 r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r.a[i][j] = (i == j) ? 1.f : 0.f;
+  return r;
+}
+DT_DEV m3 mzero() {
+  m3 r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r.a[i][j] = 0.f;
+  return r;
+}
+DT_DEV m3 mmul(const m3& x, const m3& y) {
+  m3 r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r.a[i][j] = x.a[i][0] * y.a[0][j] + x.a[i][1] * y.a[1][j] + x.a[i][2] * y.a[2][j];
+  return r;
+}
+// x * y^T
+DT_DEV m3 mmulT(const m3& x, const m3& y) {
+  m3 r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r.a[i][j] = x.a[i][0] * y.a[j][0] + x.a[i][1] * y.a[j][1] + x.a[i][2] * y.a[j][2];
+  return r;
+}
+// x^T * y
+DT_DEV m3 mTmul(const m3& x, const m3& y) {
+  m3 r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r.a[i][j] = x.a[0][i] * y.a[0][j] + x.a[1][i] * y.a[1][j] + x.a[2][i] * y.a[2][j];
+  return r;
+}
+DT_DEV m3 mT(const m3& x) {
+  m3 r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r.a[i][j] = x.a[j][i];
+  return r;
+}
+DT_DEV m3 madd(const m3& x, const m3& y) {
+  m3 r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r.a[i][j] = x.a[i][j] + y.a[i][j];
+  return r;
+}
+DT_DEV m3 msub(const m3& x, const m3& y) {
+  m3 r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r.a[i][j] = x.a[i][j] - y.a[i][j];
+  return r;
+}
+DT_DEV m3 mscale(float s, const m3& x) {
+  m3 r;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) r.a[i][j] = s * x.a[i][j];
+  return r;
+}
+DT_DEV float mdot(const m3& x, const m3& y) {
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) s += x.a[i][j] * y.a[i][j];
+  return s;
+}
+DT_DEV float mtrace(const m3& x) { return x.a[0][0] + x.a[1][1] + x.a[2][2]; }
+DT_DEV float mdet(const m3& m) {
+  const float(*a)[3] = m.a;
+  return a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+         a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+}
+// cofactor matrix: d det(m) / d m
+DT_DEV m3 mcof(const m3& m) {
+  const float(*a)[3] = m.a;
+  m3 c;
+  c.a[0][0] = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+  c.a[0][1] = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+  c.a[0][2] = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+  c.a[1][0] = a[0][2] * a[2][1] - a[0][1] * a[2][2];
+  c.a[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
+  c.a[1][2] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
+  c.a[2][0] = a[0][1] * a[1][2] - a[0][2] * a[1][1];
+  c.a[2][1] = a[0][2] * a[1][0] - a[0][0] * a[1][2];
+  c.a[2][2] = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+  return c;
+}
+DT_DEV v3 mcol(const m3& m, int j) { return v3{m.a[0][j], m.a[1][j], m.a[2][j]}; }
+DT_DEV v3 mvec(const m3& m, v3 v) {
+  return v3{m.a[0][0] * v.x + m.a[0][1] * v.y + m.a[0][2] * v.z, m.a[1][0] * v.x + m.a[1][1] * v.y + m.a[1][2] * v.z,
+            m.a[2][0] * v.x + m.a[2][1] * v.y + m.a[2][2] * v.z};
+}
+DT_DEV v3 mTvec(const m3& m, v3 v) {
+  return v3{m.a[0][0] * v.x + m.a[1][0] * v.y + m.a[2][0] * v.z, m.a[0][1] * v.x + m.a[1][1] * v.y + m.a[2][1] * v.z,
+            m.a[0][2] * v.x + m.a[1][2] * v.y + m.a[2][2] * v.z};
+}
+
+// ------------------------------------------------------------------------------------------
+// 3x3 SVD, convention of ti.svd: A = U diag(s) V^T with det U = det V = +1, |s0| >= |s1| >= |s2|,
+// s0, s1 >= 0, s2 signed.  Published method: cyclic Jacobi on A^T A with the classical rotation
+// (Golub & Van Loan, Matrix Computations, Alg. 8.4.1), columns of A V sorted by norm with a
+// sign flip per swap, then Givens QR — the outline of McAdams et al. 2011 ("Computing the SVD
+// of 3x3 matrices with minimal branching and elementary floating point operations") with exact
+// rotation angles.
+// ------------------------------------------------------------------------------------------
+DT_DEV void jacobi_rot(float S[3][3], float V[3][3], int p, int q) {
+  float apq = S[p][q];
+  if (apq == 0.f) return;
+  float tau = (S[q][q] - S[p][p]) / (2.f * apq);
+  float t = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
+  float c = 1.f / sqrtf(1.f + t * t);
+  float s = t * c;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float sp = S[k][p], sq = S[k][q];
+    S[k][p] = c * sp - s * sq;
+    S[k][q] = s * sp + c * sq;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float sp = S[p][k], sq = S[q][k];
+    S[p][k] = c * sp - s * sq;
+    S[q][k] = s * sp + c * sq;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float vp = V[k][p], vq = V[k][q];
+    V[k][p] = c * vp - s * vq;
+    V[k][q] = s * vp + c * vq;
+  }
+}
+
+DT_DEV void swap_cols_neg(float B[3][3], float V[3][3], int i, int j) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float b = B[k][i];
+    B[k][i] = B[k][j];
+    B[k][j] = -b;
+    float v = V[k][i];
+    V[k][i] = V[k][j];
+    V[k][j] = -v;
+  }
+}
+
+DT_DEV void qr_givens(float B[3][3], float U[3][3], int i, int j, int col) {
+  float a = B[i][col], b = B[j][col];
+  float r = sqrtf(a * a + b * b);
+  float c = 1.f, s = 0.f;
+  if (r > 1e-30f) {
+    c = a / r;
+    s = b / r;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float bi = B[i][k], bj = B[j][k];
+    B[i][k] = c * bi + s * bj;
+    B[j][k] = -s * bi + c * bj;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float ui = U[k][i], uj = U[k][j];
+    U[k][i] = c * ui + s * uj;
+    U[k][j] = -s * ui + c * uj;
+  }
+}
+
+DT_DEV void svd3(const m3& A, m3& U, v3& sv, m3& V, int sweeps) {
+  float S[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) S[i][j] = A.a[0][i] * A.a[0][j] + A.a[1][i] * A.a[1][j] + A.a[2][i] * A.a[2][j];
+  float Vm[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
+  for (int it = 0; it < sweeps; ++it) {
+    jacobi_rot(S, Vm, 0, 1);
+    jacobi_rot(S, Vm, 0, 2);
+    jacobi_rot(S, Vm, 1, 2);
+  }
+  float B[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) B[i][j] = A.a[i][0] * Vm[0][j] + A.a[i][1] * Vm[1][j] + A.a[i][2] * Vm[2][j];
+#define DT_CN(j) (B[0][j] * B[0][j] + B[1][j] * B[1][j] + B[2][j] * B[2][j])
+  if (DT_CN(0) < DT_CN(1)) swap_cols_neg(B, Vm, 0, 1);
+  if (DT_CN(0) < DT_CN(2)) swap_cols_neg(B, Vm, 0, 2);
+  if (DT_CN(1) < DT_CN(2)) swap_cols_neg(B, Vm, 1, 2);
+#undef DT_CN
+  float Um[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
+  qr_givens(B, Um, 0, 1, 0);
+  qr_givens(B, Um, 0, 2, 0);
+  qr_givens(B, Um, 1, 2, 1);
+  sv = v3{B[0][0], B[1][1], B[2][2]};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      U.a[i][j] = Um[i][j];
+      V.a[i][j] = Vm[i][j];
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// quadratic B-spline (mpm_elastic.py:178-181); weight index i in {0,1,2} selected without
+// dynamic register indexing
+// ------------------------------------------------------------------------------------------
+DT_DEV float bsw(int i, float fx) {
+  float a = 1.5f - fx, b = fx - 1.f, c = fx - 0.5f;
+  return i == 0 ? 0.5f * (a * a) : (i == 1 ? 0.75f - b * b : 0.5f * (c * c));
+}
+DT_DEV float bsdw(int i, float fx) { return i == 0 ? fx - 1.5f : (i == 1 ? -2.f * (fx - 1.f) : fx - 0.5f); }
+
+// ------------------------------------------------------------------------------------------
+// grid addressing: 4x4x4-node blocks, env-major
+// ------------------------------------------------------------------------------------------
+DT_DEV int node_index(const dt_env& E, int i, int j, int k) {
+  int b = ((i >> 2) * E.nb[1] + (j >> 2)) * E.nb[2] + (k >> 2);
+  return E.node_off + (b << 6) + ((i & 3) << 4) + ((j & 3) << 2) + (k & 3);
+}
+DT_DEV int block_index(const dt_env& E, int bi, int bj, int bk) {
+  return E.blk_off + (bi * E.nb[1] + bj) * E.nb[2] + bk;
+}
+
+// ------------------------------------------------------------------------------------------
+// memory helpers
+// ------------------------------------------------------------------------------------------
+DT_DEV void red_add_v4(float4* addr, float4 v) {
+  asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z),
+               "f"(v.w)
+               : "memory");
+}
+DT_DEV float4 ldg4(const float4* p) { return __ldg(p); }
+DT_DEV void set_err(const dt_world& w, int bits) { atomicOr(w.err, bits); }
+
+// particle record access: plane k of frame f
+DT_DEV float4* pplane(const dt_world& w, int f, int k) {
+  return reinterpret_cast<float4*>(w.p_state) + ((size_t)f * 6 + k) * (size_t)w.n_particles;
+}
+DT_DEV float4* padj(const dt_world& w, int buf, int k) {
+  return reinterpret_cast<float4*>(w.p_adj) + ((size_t)buf * 6 + k) * (size_t)w.n_particles;
+}
+DT_DEV float4* vframe(float* base, const dt_world& w, int f) {
+  return reinterpret_cast<float4*>(base) + (size_t)f * (size_t)w.n_verts;
+}
+
+struct PRec {
+  v3 x, v;
+  m3 C, F;
+};
+
+DT_DEV void unpack_rec(const float4 q[6], PRec& r) {
+  r.x = v3{q[0].x, q[0].y, q[0].z};
+  r.v = v3{q[0].w, q[1].x, q[1].y};
+  r.C.a[0][0] = q[1].z;
+  r.C.a[0][1] = q[1].w;
+  r.C.a[0][2] = q[2].x;
+  r.C.a[1][0] = q[2].y;
+  r.C.a[1][1] = q[2].z;
+  r.C.a[1][2] = q[2].w;
+  r.C.a[2][0] = q[3].x;
+  r.C.a[2][1] = q[3].y;
+  r.C.a[2][2] = q[3].z;
+  r.F.a[0][0] = q[3].w;
+  r.F.a[0][1] = q[4].x;
+  r.F.a[0][2] = q[4].y;
+  r.F.a[1][0] = q[4].z;
+  r.F.a[1][1] = q[4].w;
+  r.F.a[1][2] = q[5].x;
+  r.F.a[2][0] = q[5].y;
+  r.F.a[2][1] = q[5].z;
+  r.F.a[2][2] = q[5].w;
+}
+DT_DEV void pack_rec(const PRec& r, float4 q[6]) {
+  q[0] = make_float4(r.x.x, r.x.y, r.x.z, r.v.x);
+  q[1] = make_float4(r.v.y, r.v.z, r.C.a[0][0], r.C.a[0][1]);
+  q[2] = make_float4(r.C.a[0][2], r.C.a[1][0], r.C.a[1][1], r.C.a[1][2]);
+  q[3] = make_float4(r.C.a[2][0], r.C.a[2][1], r.C.a[2][2], r.F.a[0][0]);
+  q[4] = make_float4(r.F.a[0][1], r.F.a[0][2], r.F.a[1][0], r.F.a[1][1]);
+  q[5] = make_float4(r.F.a[1][2], r.F.a[2][0], r.F.a[2][1], r.F.a[2][2]);
+}
+
+DT_DEV bool finite3(v3 a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z); }
+
+// B-spline base cell: truncation toward zero like Taichi's cast(int) (mpm_elastic.py:178)
+DT_DEV bool particle_base(const dt_env& E, v3 x, int base[3], float fx[3]) {
+  float g0 = x.x * E.inv_dx - 0.5f, g1 = x.y * E.inv_dx - 0.5f, g2 = x.z * E.inv_dx - 0.5f;
+  bool ok = (g0 == g0) && (g1 == g1) && (g2 == g2) && fabsf(g0) < 1e6f && fabsf(g1) < 1e6f && fabsf(g2) < 1e6f;
+  base[0] = ok ? (int)g0 : 0;
+  base[1] = ok ? (int)g1 : 0;
+  base[2] = ok ? (int)g2 : 0;
+  fx[0] = x.x * E.inv_dx - (float)base[0];
+  fx[1] = x.y * E.inv_dx - (float)base[1];
+  fx[2] = x.z * E.inv_dx - (float)base[2];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) ok = ok && base[d] >= 0 && base[d] + 2 < E.n[d];
+  return ok;
+}
+
+// ------------------------------------------------------------------------------------------
+// constitutive model of one particle (shared by P2G and its adjoint)
+// ------------------------------------------------------------------------------------------
+struct Stress {
+  m3 Fn, U, V, Fp, R, cauchy;
+  v3 sig;
+  float J;
+  bool yield;
+};
+
+// von Mises return mapping (mpm_plastic.py:151-166); F unchanged unless yielding
+DT_DEV void von_mises(Stress& s, float mu, float ys) {
+  float e0 = logf(fmaxf(s.sig.x, 0.05f)), e1 = logf(fmaxf(s.sig.y, 0.05f)), e2 = logf(fmaxf(s.sig.z, 0.05f));
+  float mean = ((e0 + e1) + e2) / 3.f;
+  float h0 = e0 - mean, h1 = e1 - mean, h2 = e2 - mean;
+  float nrm = sqrtf(((h0 * h0 + h1 * h1) + h2 * h2) + 1e-8f);
+  float dg = nrm - ys / (2.f * mu);
+  s.yield = dg > 0.f;
+  if (s.yield) {
+    float r = dg / nrm;
+    float x0 = expf(e0 - r * h0), x1 = expf(e1 - r * h1), x2 = expf(e2 - r * h2);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        s.Fp.a[i][j] = s.U.a[i][0] * x0 * s.V.a[j][0] + s.U.a[i][1] * x1 * s.V.a[j][1] + s.U.a[i][2] * x2 * s.V.a[j][2];
+  } else {
+    s.Fp = s.Fn;
+  }
+}
+
+DT_DEV void constitutive(const m3& C, const m3& F, float dt, const dt_material& M, int sweeps, Stress& s) {
+  m3 A = meye();
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) A.a[i][j] += dt * C.a[i][j];
+  s.Fn = mmul(A, F);  // compute_new_F, mpm_elastic.py:137
+  svd3(s.Fn, s.U, s.sig, s.V, sweeps);
+  s.R = mmulT(s.U, s.V);
+  s.yield = false;
+  if (M.model == DT_MODEL_VON_MISES) {
+    von_mises(s, M.mu, M.yield_stress);
+    s.J = mdet(s.Fp);
+  } else if (M.model == DT_MODEL_NEOHOOKEAN) {
+    s.Fp = s.Fn;
+    s.J = mdet(s.Fp);
+  } else {
+    s.Fp = s.Fn;
+    s.J = s.sig.x * (s.sig.y * s.sig.z);
+  }
+  if (M.model == DT_MODEL_NEOHOOKEAN) {
+    m3 FFt = mmulT(s.Fp, s.Fp);
+    float lj = M.lam * logf(s.J);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) s.cauchy.a[i][j] = M.mu * (FFt.a[i][j] - (i == j ? 1.f : 0.f)) + (i == j ? lj : 0.f);
+  } else {
+    m3 DFt = mmulT(msub(s.Fp, s.R), s.Fp);
+    float lj = M.lam * s.J * (s.J - 1.f);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) s.cauchy.a[i][j] = 2.f * M.mu * DFt.a[i][j] + (i == j ? lj : 0.f);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// contact geometry (find_sdf, fem_sensor.py:362-394) and force (grasp_plastic.py:205-216)
+// ------------------------------------------------------------------------------------------
+struct SdfRes {
+  float sdf;
+  v3 n;    // plane normal oriented by out_dir (= -norm_v)
+  v3 r;    // triangle mean velocity - node velocity (= -relative_v)
+  bool flag;
+};
+
+DT_DEV SdfRes find_sdf(v3 p1, v3 p2, v3 p3, v3 va, v3 vb, v3 vc, v3 od, v3 p, v3 gv) {
+  v3 e1 = p2 - p1, e2 = p3 - p1;
+  v3 n = cross(e1, e2);
+  float len = sqrtf(dot(n, n));
+  n = (1.f / (len + 1e-10f)) * n;
+  float sg = dot(n, od) < 0.f ? -1.f : 1.f;
+  n = sg * n;
+  float sdf = dot(p - p1, n);
+  v3 proj = p - sdf * n;
+  v3 v0 = p3 - p1, v1 = p2 - p1, v2 = proj - p1;
+  float d00 = dot(v0, v0), d01 = dot(v0, v1), d02 = dot(v0, v2), d11 = dot(v1, v1), d12 = dot(v1, v2);
+  float invd = 1.f / (d00 * d11 - d01 * d01);
+  float u = (d11 * d02 - d01 * d12) * invd;
+  float v = (d00 * d12 - d01 * d02) * invd;
+  const float third = 1.f / 3.f;
+  v3 tv = third * ((va + vb) + vc);
+  SdfRes o;
+  o.sdf = sdf;
+  o.n = n;
+  o.r = tv - gv;
+  o.flag = sdf < 0.f && u >= 0.f && v >= 0.f && (u + v <= 1.f);
+  return o;
+}
+
+DT_DEV v3 contact_force(const dt_env& E, float sdf, v3 n, v3 r) {
+  float nr = dot(n, r);
+  float vn = fmaxf(nr, 0.f);
+  float kk = E.kn + E.kd * vn;
+  v3 fn = (-kk * sdf) * n;
+  v3 vt = r - nr * n;
+  float vtn = sqrtf(dot(vt, vt) + 1e-11f);
+  v3 ft = v3{0.f, 0.f, 0.f};
+  if (vtn > 1e-4f) {
+    float g = fminf(E.kt * vtn, E.mu_t * sqrtf(dot(fn, fn)));
+    ft = v3{(vt.x / vtn) * g, (vt.y / vtn) * g, (vt.z / vtn) * g};
+  }
+  return fn + ft;
+}
+
+// bit-reproducible centroid distance (find_closest, fem_sensor.py:352-353): every operation
+// separately rounded so that the argmin matches the CPU restatement exactly
+DT_DEV float cent_dist(float4 c, float px, float py, float pz) {
+  float dx = __fsub_rn(c.x, px), dy = __fsub_rn(c.y, py), dz = __fsub_rn(c.z, pz);
+  float s = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  return __fsqrt_rn(__fadd_rn(s, 1e-10f));
+}

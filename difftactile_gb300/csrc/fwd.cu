@@ -1,0 +1,489 @@
+// Forward substep kernels (sm_103a).
+//
+// One substep f -> f+1 of the coupled MPM object + FEM sensors, in three launches:
+//   L1 k_fwd_p2g_fem : particles  — compute_new_F, 3x3 SVD, return map, stress, P2G scatter
+//                      (mpm_elastic.py:135-208, mpm_plastic.py:151-256, multi_obj.py:228-252);
+//                      tets       — FEM elastic forces into vel (fem_sensor.py:409-440);
+//                      triangles  — surface-triangle centroids for the contact argmin.
+//   L2 k_fwd_grid    : active grid blocks — occupancy, argmin triangle, SDF, penalty/friction
+//                      contact, grid velocity update with walls (mpm_elastic.py:211-240,
+//                      grasp_plastic.py:205-216,270-299, fem_sensor.py:344-406); writes the
+//                      per-frame grid tape and clears the P2G accumulator.
+//   L3 k_fwd_g2p_fem : particles  — G2P gather, APIC C, advection (mpm_elastic.py:244-260);
+//                      vertices   — FEM integration with the driven base layer
+//                      (fem_sensor.py:444-457, gripper_fem.py:404-418).
+//
+// P2G privatisation: a CTA takes 128 consecutive particles (kept spatially sorted by the host),
+// reduces their base cells to a bounding box and, if the box fits, accumulates the 27-node
+// stencils of all its particles in a shared-memory tile (stencil order rotated by lane to spread
+// same-address shared atomics), then flushes each touched node with one 16-byte vector RED to
+// global memory.  Otherwise each particle issues its 27 vector REDs directly.
+#include "common.cuh"
+#include <climits>
+
+namespace {
+
+constexpr int NT = 128;           // threads per CTA for particle / tet / vertex roles
+constexpr int TILE_MAX = 1728;    // shared P2G tile capacity in nodes (12^3), 27 KB of float4
+constexpr int GRID_NT = 64;       // one 4x4x4 node block per CTA in the grid kernel
+
+__device__ void mark_block(const dt_world& w, int f, int b) {
+  volatile int* fl = w.blk_flag + b;
+  if (*fl == 0 && atomicExch(w.blk_flag + b, 1) == 0) {
+    int s = atomicAdd(w.tape_bcount + f, 1);
+    if (s < w.n_blocks) w.tape_blist[(size_t)f * w.n_blocks + s] = b;
+  }
+}
+
+__device__ __forceinline__ float4 p2g_contrib(const Stress& s, const PRec& r, float p_mass, float stress_k,
+                                              float dx, const float fx[3], int oi, int oj, int ok, float W) {
+  // affine = stress + p_mass C ; contribution = W (p_mass v + affine dpos), dpos = (o - fx) dx
+  float d0 = ((float)oi - fx[0]) * dx, d1 = ((float)oj - fx[1]) * dx, d2 = ((float)ok - fx[2]) * dx;
+  float a[3];
+#pragma unroll
+  for (int r_ = 0; r_ < 3; ++r_) {
+    float A0 = stress_k * s.cauchy.a[r_][0] + p_mass * r.C.a[r_][0];
+    float A1 = stress_k * s.cauchy.a[r_][1] + p_mass * r.C.a[r_][1];
+    float A2 = stress_k * s.cauchy.a[r_][2] + p_mass * r.C.a[r_][2];
+    a[r_] = A0 * d0 + A1 * d1 + A2 * d2;
+  }
+  return make_float4(W * (p_mass * r.v.x + a[0]), W * (p_mass * r.v.y + a[1]), W * (p_mass * r.v.z + a[2]),
+                     W * p_mass);
+}
+
+__device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int* sh) {
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int p = chunk * NT + tid;
+  const bool valid = p < w.n_particles;
+  if (tid == 0) {
+    sh[0] = sh[1] = sh[2] = INT_MAX;
+    sh[3] = sh[4] = sh[5] = INT_MIN;
+    int p0 = chunk * NT, p1 = min(p0 + NT, w.n_particles) - 1;
+    sh[6] = (w.p_env[p0] == w.p_env[p1]) ? 1 : 0;
+  }
+  PRec r;
+  Stress s;
+  int base[3] = {0, 0, 0};
+  float fx[3] = {0.f, 0.f, 0.f};
+  bool ok = false;
+  int env = 0;
+  if (valid) {
+    float4 q[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) q[k] = ldg4(pplane(w, f, k) + p);
+    unpack_rec(q, r);
+    env = __ldg(w.p_env + p);
+    const dt_env& E = w.envs[env];
+    ok = particle_base(E, r.x, base, fx);
+    if (!ok) set_err(w, DT_DEVERR_PARTICLE_OOB);
+    if (ok) {
+      const dt_material M = w.materials[__ldg(w.p_mat + p)];
+      constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s);
+    } else {
+      s.Fp = r.F;
+    }
+    // F[f+1] (mpm_elastic.py:208); plane 3 is shared with C, which G2P writes
+    reinterpret_cast<float*>(pplane(w, f + 1, 3) + p)[3] = s.Fp.a[0][0];
+    pplane(w, f + 1, 4)[p] = make_float4(s.Fp.a[0][1], s.Fp.a[0][2], s.Fp.a[1][0], s.Fp.a[1][1]);
+    pplane(w, f + 1, 5)[p] = make_float4(s.Fp.a[1][2], s.Fp.a[2][0], s.Fp.a[2][1], s.Fp.a[2][2]);
+  }
+  // ---- bounding box of the chunk's base cells ----
+  int lo0 = ok ? base[0] : INT_MAX, lo1 = ok ? base[1] : INT_MAX, lo2 = ok ? base[2] : INT_MAX;
+  int hi0 = ok ? base[0] : INT_MIN, hi1 = ok ? base[1] : INT_MIN, hi2 = ok ? base[2] : INT_MIN;
+  lo0 = __reduce_min_sync(0xffffffffu, lo0);
+  lo1 = __reduce_min_sync(0xffffffffu, lo1);
+  lo2 = __reduce_min_sync(0xffffffffu, lo2);
+  hi0 = __reduce_max_sync(0xffffffffu, hi0);
+  hi1 = __reduce_max_sync(0xffffffffu, hi1);
+  hi2 = __reduce_max_sync(0xffffffffu, hi2);
+  __syncthreads();  // sh[] initialised
+  if (lane == 0 && hi0 != INT_MIN) {
+    atomicMin(sh + 0, lo0);
+    atomicMin(sh + 1, lo1);
+    atomicMin(sh + 2, lo2);
+    atomicMax(sh + 3, hi0);
+    atomicMax(sh + 4, hi1);
+    atomicMax(sh + 5, hi2);
+  }
+  __syncthreads();
+  const int L0 = sh[0], L1 = sh[1], L2 = sh[2];
+  const bool any = sh[3] != INT_MIN;
+  const int ex = any ? sh[3] - L0 + 3 : 0, ey = any ? sh[4] - L1 + 3 : 0, ez = any ? sh[5] - L2 + 3 : 0;
+  const int tile_n = ex * ey * ez;
+  const bool use_tile = any && sh[6] && tile_n <= TILE_MAX;
+  const int env0 = w.p_env[min(chunk * NT, w.n_particles - 1)];
+
+  if (use_tile) {
+    for (int i = tid; i < tile_n; i += NT) tile[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    if (ok) {
+      const dt_env& E = w.envs[env];
+      const float p_mass = E.p_mass, stress_k = E.stress_k, dx = E.dx;
+      for (int t = 0; t < 27; ++t) {
+        int o = t + lane;
+        o = o >= 27 ? o - 27 : o;
+        o = o >= 27 ? o - 27 : o;
+        const int oi = o / 9, oj = (o / 3) % 3, ok_ = o % 3;
+        const float W = (bsw(oi, fx[0]) * bsw(oj, fx[1])) * bsw(ok_, fx[2]);
+        float4 c = p2g_contrib(s, r, p_mass, stress_k, dx, fx, oi, oj, ok_, W);
+        int ti = ((base[0] + oi - L0) * ey + (base[1] + oj - L1)) * ez + (base[2] + ok_ - L2);
+        float* tp = reinterpret_cast<float*>(tile + ti);
+        atomicAdd(tp + 0, c.x);
+        atomicAdd(tp + 1, c.y);
+        atomicAdd(tp + 2, c.z);
+        atomicAdd(tp + 3, c.w);
+      }
+    }
+    __syncthreads();
+    const dt_env& E0 = w.envs[env0];
+    for (int i = tid; i < tile_n; i += NT) {
+      float4 a = tile[i];
+      if (a.w != 0.f || a.x != 0.f || a.y != 0.f || a.z != 0.f) {
+        int c = i % ez, b_ = (i / ez) % ey, a_ = i / (ey * ez);
+        red_add_v4(reinterpret_cast<float4*>(w.g_acc) + node_index(E0, L0 + a_, L1 + b_, L2 + c), a);
+      }
+    }
+    // mark the blocks covering the box
+    const int b0l = L0 >> 2, b1l = L1 >> 2, b2l = L2 >> 2;
+    const int nb0 = ((L0 + ex - 1) >> 2) - b0l + 1, nb1 = ((L1 + ey - 1) >> 2) - b1l + 1,
+              nb2 = ((L2 + ez - 1) >> 2) - b2l + 1;
+    for (int i = tid; i < nb0 * nb1 * nb2; i += NT) {
+      int c = i % nb2, b_ = (i / nb2) % nb1, a_ = i / (nb1 * nb2);
+      mark_block(w, f, block_index(E0, b0l + a_, b1l + b_, b2l + c));
+    }
+  } else if (ok) {
+    const dt_env& E = w.envs[env];
+    const float p_mass = E.p_mass, stress_k = E.stress_k, dx = E.dx;
+    for (int t = 0; t < 27; ++t) {
+      const int oi = t / 9, oj = (t / 3) % 3, ok_ = t % 3;
+      const float W = (bsw(oi, fx[0]) * bsw(oj, fx[1])) * bsw(ok_, fx[2]);
+      float4 c = p2g_contrib(s, r, p_mass, stress_k, dx, fx, oi, oj, ok_, W);
+      red_add_v4(reinterpret_cast<float4*>(w.g_acc) + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok_), c);
+    }
+    for (int t = 0; t < 8; ++t) {
+      int bi = (base[0] + 2 * (t >> 2)) >> 2, bj = (base[1] + 2 * ((t >> 1) & 1)) >> 2, bk = (base[2] + 2 * (t & 1)) >> 2;
+      mark_block(w, f, block_index(E, bi, bj, bk));
+    }
+  }
+}
+
+// FEM elastic forces of one tet (fem_sensor.py:409-440): stable-Neo-Hookean-like P with current
+// volume weighting; velocity increments accumulated into velmid[f] with vector REDs
+__device__ void fem_tet(const dt_world& w, int f, int t) {
+  const int4 tv = __ldg(reinterpret_cast<const int4*>(w.tets) + t);
+  const dt_sensor& S = w.sensors[__ldg(w.tet_sensor + t)];
+  const float4* Bp = reinterpret_cast<const float4*>(w.tet_B) + 3 * (size_t)t;
+  m3 B;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    float4 row = __ldg(Bp + r);
+    B.a[r][0] = row.x;
+    B.a[r][1] = row.y;
+    B.a[r][2] = row.z;
+  }
+  const float4* P = vframe(w.v_pos, w, f);
+  v3 a = f4to3(P[tv.x]), b = f4to3(P[tv.y]), c = f4to3(P[tv.z]), d = f4to3(P[tv.w]);
+  m3 D;
+  v3 cols[3] = {a - d, b - d, c - d};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    D.a[0][k] = cols[k].x;
+    D.a[1][k] = cols[k].y;
+    D.a[2][k] = cols[k].z;
+  }
+  const float Vi = fabsf(mdet(D)) / 6.f;
+  const m3 Fe = mmul(D, B);
+  const float J = mdet(Fe);
+  const float IC = mdot(Fe, Fe);
+  const m3 cof = mcof(Fe);
+  const float k1 = S.mu * (1.f - 1.f / (IC + 1.f));
+  const float k2 = S.lam * (J - S.alpha);
+  m3 Pk;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Pk.a[i][j] = k1 * Fe.a[i][j] + k2 * cof.a[i][j];
+  const m3 H = mmulT(Pk, B);  // P B^T
+  const float s = -Vi * S.dt_over_m;
+  float4* VM = vframe(w.v_velmid, w, f);
+  v3 h0 = s * mcol(H, 0), h1 = s * mcol(H, 1), h2 = s * mcol(H, 2);
+  red_add_v4(VM + tv.x, v3to4(h0));
+  red_add_v4(VM + tv.y, v3to4(h1));
+  red_add_v4(VM + tv.z, v3to4(h2));
+  red_add_v4(VM + tv.w, v3to4(-((h0 + h1) + h2)));
+}
+
+__device__ void tri_centroid(const dt_world& w, int f, int t) {
+  const int4 tr = __ldg(reinterpret_cast<const int4*>(w.tris) + t);
+  const float4* P = vframe(w.v_pos, w, f);
+  float4 a = P[tr.x], b = P[tr.y], c = P[tr.z];
+  const float third = 1.f / 3.f;
+  float4 o;
+  o.x = __fmul_rn(third, __fadd_rn(__fadd_rn(a.x, b.x), c.x));
+  o.y = __fmul_rn(third, __fadd_rn(__fadd_rn(a.y, b.y), c.y));
+  o.z = __fmul_rn(third, __fadd_rn(__fadd_rn(a.z, b.z), c.z));
+  o.w = 0.f;
+  reinterpret_cast<float4*>(w.tri_cent)[t] = o;
+}
+
+__global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
+  __shared__ float4 tile[TILE_MAX];
+  __shared__ int sh[8];
+  int b = blockIdx.x;
+  if (b < nb_p) {
+    p2g_chunk(w, f, b, tile, sh);
+    return;
+  }
+  b -= nb_p;
+  if (b < nb_t) {
+    int t = b * NT + threadIdx.x;
+    if (t < w.n_tets) fem_tet(w, f, t);
+    return;
+  }
+  b -= nb_t;
+  if (b < nb_f) {
+    int t = b * NT + threadIdx.x;
+    if (t < w.n_tris) tri_centroid(w, f, t);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// L2: grid update + contact over the frame's active blocks
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f) {
+  const int cnt = *((volatile int*)(w.tape_bcount + f));
+  const int l = threadIdx.x;
+  const float third = 1.f / 3.f;
+  float4* acc = reinterpret_cast<float4*>(w.g_acc);
+  float4* vout = reinterpret_cast<float4*>(w.g_vout);
+  const float4* P = vframe(w.v_pos, w, f);
+  const float4* VM = vframe(w.v_velmid, w, f);
+  float4* EXT = vframe(w.v_ext, w, f);
+  const float4* cent = reinterpret_cast<const float4*>(w.tri_cent);
+  const int4* tris = reinterpret_cast<const int4*>(w.tris);
+  for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
+    const int b = w.tape_blist[(size_t)f * w.n_blocks + e];
+    const dt_env& E = w.envs[__ldg(w.blk_env + b)];
+    const int lb = b - E.blk_off;
+    const int bk = lb % E.nb[2], bj = (lb / E.nb[2]) % E.nb[1], bi = lb / (E.nb[1] * E.nb[2]);
+    const int i = 4 * bi + (l >> 4), j = 4 * bj + ((l >> 2) & 3), k = 4 * bk + (l & 3);
+    const int g = E.node_off + (lb << 6) + l;
+    const float4 a = acc[g];
+    const float m = a.w;
+    float4 vo = make_float4(0.f, 0.f, 0.f, 0.f);
+    int cid[DT_MAX_SENSORS_PER_ENV] = {-1, -1, -1, -1};
+    if (m > E.eps) {  // check_grid_occupy, mpm_elastic.py:213
+      const v3 mv = f4to3(a);
+      const float inv_m = 1.f / (m + E.eps);
+      const v3 cur_v = v3{mv.x / (m + E.eps), mv.y / (m + E.eps), mv.z / (m + E.eps)};
+      const float px = __fmul_rn(__fadd_rn((float)i, 0.5f), E.dx), py = __fmul_rn(__fadd_rn((float)j, 0.5f), E.dx),
+                  pz = __fmul_rn(__fadd_rn((float)k, 0.5f), E.dx);
+      v3 gf = v3{0.f, 0.f, 0.f};
+#pragma unroll
+      for (int q = 0; q < DT_MAX_SENSORS_PER_ENV; ++q) {
+        const int si = E.s_begin + q;
+        if (si >= E.s_end) break;
+        const dt_sensor& S = w.sensors[si];
+        float best = 100.f;
+        int kk = -1;
+        for (int t = 0; t < S.nf; ++t) {
+          float dd = cent_dist(__ldg(cent + S.f_off + t), px, py, pz);
+          if (dd < best) {
+            best = dd;
+            kk = t;
+          }
+        }
+        cid[q] = kk;
+        if (kk < 0) continue;
+        const int4 tr = __ldg(tris + S.f_off + kk);
+        SdfRes sr = find_sdf(f4to3(P[tr.x]), f4to3(P[tr.y]), f4to3(P[tr.z]), f4to3(VM[tr.x]), f4to3(VM[tr.y]),
+                             f4to3(VM[tr.z]), v3{S.out_dir[0], S.out_dir[1], S.out_dir[2]}, v3{px, py, pz}, cur_v);
+        if (!sr.flag) continue;
+        const v3 ext = contact_force(E, sr.sdf, sr.n, sr.r);
+        gf = gf + w.dt * ext;
+        const float4 fe = v3to4(third * (-ext));
+        red_add_v4(EXT + tr.x, fe);
+        red_add_v4(EXT + tr.y, fe);
+        red_add_v4(EXT + tr.z, fe);
+      }
+      // grid_op, mpm_elastic.py:220-238
+      v3 u = (inv_m * mv + inv_m * gf) + v3{E.dt_g[0], E.dt_g[1], E.dt_g[2]};
+      const int b_ = E.bound;
+      if (i < b_ && u.x < 0.f) u.x = 0.f;
+      if (i > E.n[0] - b_ && u.x > 0.f) u.x = 0.f;
+      if (j < b_ && u.y < 0.f) u.y = 0.f;
+      if (j > E.n[1] - b_ && u.y > 0.f) u.y = 0.f;
+      if (k < b_ && u.z < 0.f) u.z = 0.f;
+      if (k > E.n[2] - b_ && u.z > 0.f) u.z = 0.f;
+      if (E.bc == DT_BC_STICKY_FLOOR && j < b_) u = v3{0.f, 0.f, 0.f};
+      if (!finite3(u)) set_err(w, DT_DEVERR_NONFINITE);
+      vo = v3to4(u);
+    }
+    vout[g] = vo;
+    if (e < w.tape_blocks) {
+      const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + l;
+      reinterpret_cast<float4*>(w.tape_acc)[ti] = a;
+      reinterpret_cast<float4*>(w.tape_vout)[ti] = vo;
+      reinterpret_cast<int4*>(w.tape_cidx)[ti] = make_int4(cid[0], cid[1], cid[2], cid[3]);
+    } else if (l == 0) {
+      set_err(w, DT_DEVERR_TAPE_FULL);
+    }
+    acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (l == 0) w.blk_flag[b] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// L3: G2P + FEM integration
+// ---------------------------------------------------------------------------------------------
+__device__ void g2p_particle(const dt_world& w, int f, int p) {
+  const float4 q0 = ldg4(pplane(w, f, 0) + p);
+  const v3 x = f4to3(q0);
+  const dt_env& E = w.envs[__ldg(w.p_env + p)];
+  int base[3];
+  float fx[3];
+  float* q3n = reinterpret_cast<float*>(pplane(w, f + 1, 3) + p);
+  if (!particle_base(E, x, base, fx)) {
+    // carry the particle unchanged (its scatter was skipped and the error flag is set)
+    pplane(w, f + 1, 0)[p] = q0;
+    pplane(w, f + 1, 1)[p] = ldg4(pplane(w, f, 1) + p);
+    pplane(w, f + 1, 2)[p] = ldg4(pplane(w, f, 2) + p);
+    float4 q3 = ldg4(pplane(w, f, 3) + p);
+    *reinterpret_cast<float2*>(q3n) = make_float2(q3.x, q3.y);
+    q3n[2] = q3.z;
+    return;
+  }
+  const float4* vout = reinterpret_cast<const float4*>(w.g_vout);
+  v3 nv = v3{0.f, 0.f, 0.f};
+  m3 nC = mzero();
+  float wts[3][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) wts[i][d] = bsw(i, fx[d]);
+#pragma unroll
+  for (int oi = 0; oi < 3; ++oi)
+#pragma unroll
+    for (int oj = 0; oj < 3; ++oj)
+#pragma unroll
+      for (int ok = 0; ok < 3; ++ok) {
+        const v3 gv = f4to3(__ldg(vout + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok)));
+        const float W = (wts[oi][0] * wts[oj][1]) * wts[ok][2];
+        const float kw = E.g2p_k * W;
+        const float d[3] = {(float)oi - fx[0], (float)oj - fx[1], (float)ok - fx[2]};
+        nv = nv + W * gv;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          nC.a[0][c] += kw * (gv.x * d[c]);
+          nC.a[1][c] += kw * (gv.y * d[c]);
+          nC.a[2][c] += kw * (gv.z * d[c]);
+        }
+      }
+  const v3 nx = x + w.dt * nv;
+  if (!finite3(nx)) set_err(w, DT_DEVERR_NONFINITE);
+  pplane(w, f + 1, 0)[p] = make_float4(nx.x, nx.y, nx.z, nv.x);
+  pplane(w, f + 1, 1)[p] = make_float4(nv.y, nv.z, nC.a[0][0], nC.a[0][1]);
+  pplane(w, f + 1, 2)[p] = make_float4(nC.a[0][2], nC.a[1][0], nC.a[1][1], nC.a[1][2]);
+  *reinterpret_cast<float2*>(q3n) = make_float2(nC.a[2][0], nC.a[2][1]);
+  q3n[2] = nC.a[2][2];
+}
+
+__device__ void fem_integrate(const dt_world& w, int f, int i) {
+  const dt_sensor& S = w.sensors[__ldg(w.v_sensor + i)];
+  const v3 vm = f4to3(vframe(w.v_velmid, w, f)[i]);
+  const v3 ex = f4to3(vframe(w.v_ext, w, f)[i]);
+  const v3 cvf = f4to3(vframe(w.v_cv, w, f)[i]);
+  const v3 cvn = f4to3(vframe(w.v_cv, w, f + 1)[i]);
+  v3 vo = vm + S.dt_over_m * ex;
+  if (__ldg(w.v_layer + i) == 0) vo = cvf;  // kinematic base layer
+  const v3 vel1 = S.carry ? vo + (cvn - cvf) : vo;
+  const v3 pos1 = f4to3(vframe(w.v_pos, w, f)[i]) + w.dt * vo;
+  const v3 vp1 = f4to3(vframe(w.v_vpos, w, f)[i]) + w.dt * cvf;
+  vframe(w.v_vel, w, f + 1)[i] = v3to4(vel1);
+  vframe(w.v_pos, w, f + 1)[i] = v3to4(pos1);
+  vframe(w.v_vpos, w, f + 1)[i] = v3to4(vp1);
+  // prepare frame f+1's accumulators
+  vframe(w.v_velmid, w, f + 1)[i] = v3to4(vel1);
+  vframe(w.v_ext, w, f + 1)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void __launch_bounds__(NT) k_fwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
+  int b = blockIdx.x;
+  if (b < nb_p) {
+    int p = b * NT + threadIdx.x;
+    if (p < w.n_particles) g2p_particle(w, f, p);
+    return;
+  }
+  b -= nb_p;
+  if (b < nb_v) {
+    int i = b * NT + threadIdx.x;
+    if (i < w.n_verts) fem_integrate(w, f, i);
+  }
+}
+
+inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+inline int check(const dt_world* w, int f) {
+  if (!w || f < 0 || f + 1 >= w->n_frames) return DT_ERR_ARG;
+  return DT_OK;
+}
+inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
+
+int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
+  int nb_p = parts ? cdiv(w->n_particles, NT) : 0;
+  int nb_t = fem ? cdiv(w->n_tets, NT) : 0;
+  int nb_f = fem ? cdiv(w->n_tris, NT) : 0;
+  int tot = nb_p + nb_t + nb_f;
+  if (tot == 0) return DT_OK;
+  k_fwd_p2g_fem<<<tot, NT, 0, st>>>(*w, f, nb_p, nb_t, nb_f);
+  return launched();
+}
+int launch_l2(const dt_world* w, int f, cudaStream_t st) {
+  int nb = w->n_blocks < 152 * 16 ? w->n_blocks : 152 * 16;
+  if (nb <= 0) return DT_OK;
+  k_fwd_grid<<<nb, GRID_NT, 0, st>>>(*w, f);
+  return launched();
+}
+int launch_l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
+  int nb_p = parts ? cdiv(w->n_particles, NT) : 0;
+  int nb_v = fem ? cdiv(w->n_verts, NT) : 0;
+  if (nb_p + nb_v == 0) return DT_OK;
+  k_fwd_g2p_fem<<<nb_p + nb_v, NT, 0, st>>>(*w, f, nb_p, nb_v);
+  return launched();
+}
+
+}  // namespace
+
+extern "C" {
+
+int dt_substep_fwd(const dt_world* w, int f, cudaStream_t stream) {
+  int rc = check(w, f);
+  if (rc) return rc;
+  if ((rc = launch_l1(w, f, true, true, stream))) return rc;
+  if ((rc = launch_l2(w, f, stream))) return rc;
+  return launch_l3(w, f, true, true, stream);
+}
+
+int dt_p2g(const dt_world* w, int f, cudaStream_t stream) {
+  int rc = check(w, f);
+  return rc ? rc : launch_l1(w, f, true, false, stream);
+}
+int dt_fem_update(const dt_world* w, int f, cudaStream_t stream) {
+  int rc = check(w, f);
+  return rc ? rc : launch_l1(w, f, false, true, stream);
+}
+int dt_grid_op(const dt_world* w, int f, cudaStream_t stream) {
+  int rc = check(w, f);
+  return rc ? rc : launch_l2(w, f, stream);
+}
+int dt_g2p(const dt_world* w, int f, cudaStream_t stream) {
+  int rc = check(w, f);
+  return rc ? rc : launch_l3(w, f, true, false, stream);
+}
+int dt_fem_update2(const dt_world* w, int f, cudaStream_t stream) {
+  int rc = check(w, f);
+  return rc ? rc : launch_l3(w, f, false, true, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,334 @@
+"""Device-resident world: flat, offset-indexed layout of many environments + the C-ABI calls.
+
+All buffers are torch tensors on one CUDA device (torch is used for allocation and streams only);
+every compute step is a call into libdifftactile_gb300.so through ctypes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .scene import EnvSpec, SensorSpec
+
+F32 = torch.float32
+I32 = torch.int32
+
+
+def _morton_key(cell: np.ndarray) -> np.ndarray:
+    """Block-major key of a cell: 4x4x4 block id (Morton-interleaved) then the cell in the block."""
+    c = cell.astype(np.int64)
+    b = c >> 2
+    key = np.zeros(len(c), np.int64)
+    for bit in range(10):
+        for d in range(3):
+            key |= ((b[:, d] >> bit) & 1) << (3 * bit + (2 - d) + 6)
+    key |= ((c[:, 0] & 3) << 4) | ((c[:, 1] & 3) << 2) | (c[:, 2] & 3)
+    return key
+
+
+class World:
+    """Flat device layout of ``envs`` (list of EnvSpec) with ``n_frames`` frames per step."""
+
+    def __init__(self, envs: list[EnvSpec], n_frames: int, dt: float, device="cuda", tape_blocks: int | None = None,
+                 grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True):
+        self.lib = N.load()
+        self.device = torch.device(device)
+        self.specs = envs
+        self.n_frames = int(n_frames)
+        self.dt = float(dt)
+        dev = self.device
+
+        # ---------------- particles ----------------
+        perm, p_env, p_mat, env_rows, mats, mat_off = [], [], [], [], [], 0
+        node_off = blk_off = p_off = 0
+        sensors: list[tuple[int, SensorSpec]] = []
+        blk_env = []
+        for e, s in enumerate(envs):
+            n = s.n_particles
+            nb = [(g + 3) // 4 for g in s.n_grid]
+            if sort_particles and n:
+                cell = np.floor(s.x.astype(np.float64) / s.dx - 0.5).clip(0, max(s.n_grid) - 1).astype(np.int64)
+                order = np.argsort(_morton_key(cell), kind="stable")
+            else:
+                order = np.arange(n)
+            perm.append(order + p_off)
+            p_env.append(np.full(n, e, np.int32))
+            mid = np.zeros(n, np.int32) if s.mat is None else np.asarray(s.mat, np.int32)
+            p_mat.append(mid[order] + mat_off)
+            mats.extend(s.materials)
+            row = N.DtEnv()
+            row.p_begin, row.p_end = p_off, p_off + n
+            row.node_off, row.blk_off = node_off, blk_off
+            row.nb[:] = nb
+            row.n[:] = list(s.n_grid)
+            row.bound, row.bc = s.bound, s.bc
+            row.s_begin = len(sensors)
+            for sp in s.sensors:
+                sensors.append((e, sp))
+            row.s_end = len(sensors)
+            if row.s_end - row.s_begin > 4:
+                raise ValueError("at most 4 sensors per environment")
+            dx = float(s.dx)
+            inv_dx = 1.0 / dx
+            row.dx, row.inv_dx = dx, inv_dx
+            row.p_mass = s.p_mass
+            row.stress_k = -self.dt * s.volume * 4 * inv_dx * inv_dx
+            row.eps = s.eps
+            row.g2p_k = 4 * inv_dx
+            row.dt_g[:] = [self.dt * g for g in s.gravity]
+            row.kn, row.kd, row.kt, row.mu_t = s.kn, s.kd, s.kt, s.mu_t
+            env_rows.append(row)
+            nblk = nb[0] * nb[1] * nb[2]
+            blk_env.append(np.full(nblk, e, np.int32))
+            node_off += 64 * nblk
+            blk_off += nblk
+            p_off += n
+            mat_off += len(s.materials)
+        self.n_envs = len(envs)
+        self.n_particles = p_off
+        self.n_nodes, self.n_blocks = node_off, blk_off
+        self.perm = np.concatenate(perm) if perm else np.zeros(0, np.int64)  # sorted slot -> user index
+        self.inv_perm = np.empty_like(self.perm)
+        self.inv_perm[self.perm] = np.arange(len(self.perm))
+        self._perm_t = torch.as_tensor(self.perm, device=dev)
+        self._inv_perm_t = torch.as_tensor(self.inv_perm, device=dev)
+        self.env_rows = env_rows
+
+        # ---------------- sensors ----------------
+        v_off = t_off = f_off = 0
+        verts, tets, tris, layer, v_sensor, t_sensor, Bs, srows = [], [], [], [], [], [], [], []
+        for si, (e, sp) in enumerate(sensors):
+            nv, nt, nf = len(sp.verts), len(sp.tets), len(sp.tris)
+            verts.append(sp.verts.astype(np.float32))
+            tets.append(sp.tets.astype(np.int32) + v_off)
+            tris.append(np.concatenate([sp.tris.astype(np.int32) + v_off, np.full((nf, 1), si, np.int32)], 1))
+            layer.append(sp.layer.astype(np.int32))
+            v_sensor.append(np.full(nv, si, np.int32))
+            t_sensor.append(np.full(nt, si, np.int32))
+            B = sp.rest_inverse()
+            Bp = np.zeros((nt, 3, 4), np.float32)
+            Bp[:, :, :3] = B
+            Bs.append(Bp.reshape(nt, 12))
+            r = N.DtSensor()
+            r.v_off, r.nv, r.t_off, r.nt, r.f_off, r.nf = v_off, nv, t_off, nt, f_off, nf
+            r.env, r.carry = e, sp.carry
+            mu, lam = sp.lame()
+            r.dt_over_m = self.dt / sp.mass
+            r.mu, r.lam = mu, lam
+            r.alpha = float(np.float32(1) + np.float32(0.75) * np.float32(mu) / np.float32(lam))
+            r.out_dir[:] = [float(c) for c in sp.out_dir]
+            srows.append(r)
+            v_off, t_off, f_off = v_off + nv, t_off + nt, f_off + nf
+        self.sensor_specs = [sp for _, sp in sensors]
+        self.sensor_env = [e for e, _ in sensors]
+        self.sensor_rows = srows
+        self.n_sensors = len(sensors)
+        self.n_verts, self.n_tets, self.n_tris = v_off, t_off, f_off
+
+        cat = lambda xs, shape, dt_: (np.concatenate(xs, 0) if xs else np.zeros(shape, dt_))  # noqa: E731
+        self.rest_verts = cat(verts, (0, 3), np.float32)
+        self.t = {}
+        t = self.t
+
+        def dtensor(a, dtype):
+            return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype, device=dev)
+
+        def zeros(shape, dtype=F32):
+            return torch.zeros(shape, dtype=dtype, device=dev)
+
+        def struct_tensor(rows, cls):
+            buf = bytearray(C.sizeof(cls) * max(len(rows), 1))
+            for i, r_ in enumerate(rows):
+                C.memmove(C.addressof(C.c_char.from_buffer(buf, i * C.sizeof(cls))), C.addressof(r_), C.sizeof(cls))
+            return torch.frombuffer(buf, dtype=torch.uint8).to(dev)
+
+        mat_rows = []
+        for m in mats:
+            r = N.DtMaterial()
+            mu, lam = m.mu_lam
+            r.mu, r.lam, r.yield_stress, r.model = mu, lam, m.yield_stress, m.model
+            mat_rows.append(r)
+        self.materials = mats
+        self.n_materials = len(mats)
+        t["envs"] = struct_tensor(env_rows, N.DtEnv)
+        t["sensors"] = struct_tensor(srows, N.DtSensor)
+        t["materials"] = struct_tensor(mat_rows, N.DtMaterial)
+        t["p_env"] = dtensor(cat(p_env, (0,), np.int32), I32)
+        t["p_mat"] = dtensor(cat(p_mat, (0,), np.int32), I32)
+        t["blk_env"] = dtensor(cat(blk_env, (0,), np.int32), I32)
+        t["tets"] = dtensor(cat(tets, (0, 4), np.int32), I32)
+        t["tet_B"] = dtensor(cat(Bs, (0, 12), np.float32), F32)
+        t["tet_sensor"] = dtensor(cat(t_sensor, (0,), np.int32), I32)
+        t["tris"] = dtensor(cat(tris, (0, 4), np.int32), I32)
+        t["v_layer"] = dtensor(cat(layer, (0,), np.int32), I32)
+        t["v_sensor"] = dtensor(cat(v_sensor, (0,), np.int32), I32)
+
+        Fn, Np, V, NN, NB = self.n_frames, self.n_particles, self.n_verts, self.n_nodes, self.n_blocks
+        self.tape_blocks = int(tape_blocks if tape_blocks is not None else NB)
+        TB = self.tape_blocks
+        t["p_state"] = zeros((Fn, 6, Np, 4))
+        t["p_adj"] = zeros((2, 6, Np, 4))
+        t["g_acc"] = zeros((NN, 4))
+        t["g_vout"] = zeros((NN, 4))
+        t["g_adj_vout"] = zeros((NN, 4))
+        t["g_adj_acc"] = zeros((NN, 4))
+        t["blk_flag"] = zeros((NB,), I32)
+        t["tape_blist"] = zeros((Fn, NB), I32)
+        t["tape_bcount"] = zeros((Fn,), I32)
+        t["tape_acc"] = zeros((Fn, TB * 64, 4))
+        t["tape_vout"] = zeros((Fn, TB * 64, 4))
+        t["tape_cidx"] = zeros((Fn, TB * 64, 4), I32)
+        for k in ("v_pos", "v_vel", "v_velmid", "v_ext", "v_vpos", "v_cv"):
+            t[k] = zeros((Fn, V, 4))
+        t["tri_cent"] = zeros((self.n_tris, 4))
+        for k in ("v_adj_pos", "v_adj_vel", "v_adj_vpos"):
+            t[k] = zeros((2, V, 4))
+        t["v_adj_velmid"] = zeros((V, 4))
+        t["v_adj_ext"] = zeros((V, 4))
+        t["v_adj_cv"] = zeros((Fn, V, 4))
+        t["mat_adj"] = zeros((max(self.n_materials, 1), 4))
+        t["err"] = zeros((4,), I32)
+
+        w = N.DtWorld()
+        for name in N.WORLD_PTR_FIELDS:
+            setattr(w, name, t[name].data_ptr() if t[name].numel() else None)
+        w.n_envs, w.n_particles, w.n_sensors, w.n_materials = self.n_envs, Np, self.n_sensors, self.n_materials
+        w.n_verts, w.n_tets, w.n_tris = V, self.n_tets, self.n_tris
+        w.n_nodes, w.n_blocks, w.n_frames, w.tape_blocks = NN, NB, Fn, TB
+        w.dt, w.grad_clip, w.svd_sweeps = self.dt, float(grad_clip), int(svd_sweeps)
+        self.w = w
+        self.wp = C.pointer(w)
+
+        # FEM rest state in frame 0
+        if V:
+            vp = torch.zeros((V, 4), dtype=F32, device=dev)
+            vp[:, :3] = torch.as_tensor(self.rest_verts, device=dev)
+            t["v_pos"][0] = vp
+            t["v_vpos"][0] = vp
+        # initial particle state (user order), F = I
+        xs = np.concatenate([s.x for s in envs], 0) if envs else np.zeros((0, 3), np.float32)
+        vs = np.concatenate([(np.zeros_like(s.x) if s.v is None else np.broadcast_to(s.v, s.x.shape)) for s in envs], 0) \
+            if envs else np.zeros((0, 3), np.float32)
+        self.set_particles(0, x=xs, v=vs, C=np.zeros((Np, 3, 3), np.float32),
+                           F=np.broadcast_to(np.eye(3, dtype=np.float32), (Np, 3, 3)))
+
+    # ------------------------------------------------------------------------------------------
+    @property
+    def stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def call(self, name, *args):
+        N.check(getattr(self.lib, name)(self.wp, *args, self.stream), name)
+
+    # ---- particle state in user order ----
+    def set_particles(self, frame, x=None, v=None, C=None, F=None):
+        rec = self.t["p_state"][frame].permute(1, 0, 2).reshape(self.n_particles, 24)  # view? no: permute copy
+        rec = rec.clone()
+        put = lambda a: torch.as_tensor(np.asarray(a, np.float32) if not torch.is_tensor(a) else a,  # noqa: E731
+                                        dtype=F32, device=self.device)
+        if x is not None:
+            rec[:, 0:3] = put(x).reshape(-1, 3)[self._perm_t]
+        if v is not None:
+            rec[:, 3:6] = put(v).reshape(-1, 3)[self._perm_t]
+        if C is not None:
+            rec[:, 6:15] = put(C).reshape(-1, 9)[self._perm_t]
+        if F is not None:
+            rec[:, 15:24] = put(F).reshape(-1, 9)[self._perm_t]
+        self.t["p_state"][frame].copy_(rec.reshape(self.n_particles, 6, 4).permute(1, 0, 2))
+
+    def particles(self, frame):
+        """dict of torch tensors x [N,3], v [N,3], C [N,3,3], F [N,3,3] of ``frame`` in user order."""
+        rec = self.t["p_state"][frame].permute(1, 0, 2).reshape(self.n_particles, 24)[self._inv_perm_t]
+        return {"x": rec[:, 0:3], "v": rec[:, 3:6], "C": rec[:, 6:15].reshape(-1, 3, 3),
+                "F": rec[:, 15:24].reshape(-1, 3, 3)}
+
+    def particle_adjoint(self, frame):
+        rec = self.t["p_adj"][frame & 1].permute(1, 0, 2).reshape(self.n_particles, 24)[self._inv_perm_t]
+        return {"x": rec[:, 0:3], "v": rec[:, 3:6], "C": rec[:, 6:15].reshape(-1, 3, 3),
+                "F": rec[:, 15:24].reshape(-1, 3, 3)}
+
+    def set_particle_adjoint(self, frame, x=None, v=None, C=None, F=None):
+        rec = torch.zeros((self.n_particles, 24), dtype=F32, device=self.device)
+        for a, sl in ((x, slice(0, 3)), (v, slice(3, 6)), (C, slice(6, 15)), (F, slice(15, 24))):
+            if a is not None:
+                rec[:, sl] = torch.as_tensor(a, dtype=F32, device=self.device).reshape(self.n_particles, -1)[self._perm_t]
+        self.t["p_adj"][frame & 1].copy_(rec.reshape(self.n_particles, 6, 4).permute(1, 0, 2))
+
+    # ---- sensor state ----
+    def vslice(self, s):
+        r = self.sensor_rows[s]
+        return slice(r.v_off, r.v_off + r.nv)
+
+    def sensor_frame(self, name, frame, s):
+        return self.t[name][frame, self.vslice(s), :3]
+
+    def set_control_velocity(self, s, cv, frames=None):
+        """cv: [V,3] (all frames) or [n_frames, V, 3]."""
+        cv = torch.as_tensor(cv, dtype=F32, device=self.device)
+        sl = self.vslice(s)
+        if cv.dim() == 2:
+            self.t["v_cv"][:, sl, :3] = cv
+        else:
+            self.t["v_cv"][:, sl, :3] = cv
+
+    # ---- grid tape readback (tests, debugging): dense (i,j,k) arrays of frame f for env e ----
+    def dense_grid(self, f, e=0):
+        row = self.env_rows[e]
+        n0, n1, n2 = row.n
+        nb = list(row.nb)
+        cnt = int(self.t["tape_bcount"][f].item())
+        cnt = min(cnt, self.tape_blocks)
+        bl = self.t["tape_blist"][f, :cnt].long()
+        acc = self.t["tape_acc"][f].view(-1, 64, 4)[:cnt]
+        vo = self.t["tape_vout"][f].view(-1, 64, 4)[:cnt]
+        ci = self.t["tape_cidx"][f].view(-1, 64, 4)[:cnt]
+        sel = (bl >= row.blk_off) & (bl < row.blk_off + nb[0] * nb[1] * nb[2])
+        bl, acc, vo, ci = bl[sel] - row.blk_off, acc[sel], vo[sel], ci[sel]
+        bk = bl % nb[2]
+        bj = (bl // nb[2]) % nb[1]
+        bi = bl // (nb[1] * nb[2])
+        l = torch.arange(64, device=self.device)
+        I = (4 * bi[:, None] + (l >> 4)[None]).reshape(-1)
+        J = (4 * bj[:, None] + ((l >> 2) & 3)[None]).reshape(-1)
+        K = (4 * bk[:, None] + (l & 3)[None]).reshape(-1)
+        shape = (4 * nb[0], 4 * nb[1], 4 * nb[2])
+        m = torch.zeros(shape, device=self.device)
+        mv = torch.zeros(shape + (3,), device=self.device)
+        v = torch.zeros(shape + (3,), device=self.device)
+        cidx = torch.full(shape + (4,), -1, dtype=I32, device=self.device)
+        m[I, J, K] = acc[..., 3].reshape(-1)
+        mv[I, J, K] = acc[..., :3].reshape(-1, 3)
+        v[I, J, K] = vo[..., :3].reshape(-1, 3)
+        cidx[I, J, K] = ci.reshape(-1, 4)
+        return {"m": m[:n0, :n1, :n2], "mv": mv[:n0, :n1, :n2], "v_out": v[:n0, :n1, :n2],
+                "cidx": cidx[:n0, :n1, :n2]}
+
+    def error_word(self) -> int:
+        return int(self.t["err"][0].item())
+
+    def clear_error(self):
+        self.t["err"].zero_()
+
+    # ---- C-ABI wrappers ----
+    def step_begin(self):
+        self.call("dt_step_begin")
+
+    def substep(self, f):
+        self.call("dt_substep_fwd", int(f))
+
+    def substep_bwd(self, f):
+        self.call("dt_substep_bwd", int(f))
+
+    def copy_frame(self, src, dst):
+        self.call("dt_copy_frame", int(src), int(dst))
+
+    def adj_clear(self):
+        self.call("dt_adj_clear")
+
+    def com(self, f):
+        out = torch.empty((self.n_envs, 4), dtype=F32, device=self.device)
+        N.check(self.lib.dt_com(self.wp, int(f), out.data_ptr(), self.stream), "dt_com")
+        return out[:, :3]

@@ -1,0 +1,219 @@
+/*
+ * difftactile_gb300 — C ABI of the GB300-native DiffTactile simulation substep.
+ *
+ * One substep couples an MLS-MPM object (quadratic B-spline P2G -> grid update with walls and
+ * penalty contact -> G2P, deformation-gradient update with optional von-Mises return mapping)
+ * with FEM tetrahedral elastomer sensors (tet elastic forces, explicit integration with a
+ * kinematically driven base layer) through a grid-node <-> surface-triangle penalty/friction
+ * contact.  Every forward kernel has a hand-written adjoint.
+ *
+ * Ownership: the library allocates nothing (except where an entry point says otherwise).  The
+ * caller allocates every device buffer named in dt_world, fills the static tables, and passes
+ * a host pointer to the dt_world descriptor to each call.  All calls are asynchronous on the
+ * given stream and return DT_OK or a negative DT_ERR_* code for argument errors detected on the
+ * host.  Errors found on the device (a particle that left the grid's safe band, a non-finite
+ * value) are OR-ed into err[0] as DT_DEVERR_* bits; read err[0] after the stream completes.
+ *
+ * Reference interfaces replaced (paths inside the DiffTactile project):
+ *   MPMObj.compute_new_F/svd/p2g         difftactile/object_model/mpm_elastic.py:135-208,
+ *                                        difftactile/object_model/mpm_plastic.py:181-256,
+ *                                        difftactile/object_model/multi_obj.py:228-252
+ *   MPMObj.check_grid_occupy/grid_op     difftactile/object_model/mpm_elastic.py:211-240
+ *   MPMObj.g2p                           difftactile/object_model/mpm_elastic.py:244-260
+ *   FEMDomeSensor.update/update2         difftactile/sensor_model/fem_sensor.py:409-457,
+ *                                        difftactile/sensor_model/gripper_fem.py:375-418
+ *   Contact.check_collision/collision    difftactile/tasks/grasp_plastic.py:270-299 with
+ *                                        find_closest/find_sdf fem_sensor.py:344-394 and
+ *                                        calculate_contact_force grasp_plastic.py:205-216
+ *   Contact.update / update_grad         difftactile/tasks/grasp_plastic.py:151-178
+ *   MPMObj.svd_grad                      difftactile/object_model/mpm_elastic.py:145-173
+ *   Contact.clamp_grid                   difftactile/tasks/grasp_plastic.py:192-202
+ *
+ * Layouts (all float buffers are IEEE fp32, all index buffers int32):
+ *   particle state tape  p_state[n_frames][6][n_particles][4]: plane k of frame f holds floats
+ *                        4k..4k+3 of the 24-float record
+ *                        [x0 x1 x2 v0 | v1 v2 C00 C01 | C02 C10 C11 C12 | C20 C21 C22 F00 |
+ *                         F01 F02 F10 F11 | F12 F20 F21 F22]   (C, F row-major)
+ *   particle adjoint     p_adj[2][6][n_particles][4], same record layout, double-buffered.
+ *   grid                 flat over all envs in 4x4x4-node blocks: node (i,j,k) of env e lives at
+ *                        e.node_off + 64*((bi*nb1 + bj)*nb2 + bk) + 16*(i&3) + 4*(j&3) + (k&3),
+ *                        bi = i>>2 ...; g_acc = (momentum.xyz, mass), g_vout = (v.xyz, 0).
+ *   FEM vertex frames    v_pos/v_vel/v_velmid/v_ext/v_vpos/v_cv [n_frames][n_verts][4] (xyz, 0).
+ */
+#ifndef DIFFTACTILE_GB300_H
+#define DIFFTACTILE_GB300_H
+
+#include <stddef.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DT_ABI_VERSION 1
+
+#define DT_OK 0
+#define DT_ERR_ARG (-1)        /* null pointer, bad size or frame index */
+#define DT_ERR_LAUNCH (-2)     /* a kernel launch failed (cudaGetLastError) */
+#define DT_ERR_CAPACITY (-3)   /* a size exceeds a compiled or documented maximum */
+
+/* device error bits, OR-ed into err[0] */
+#define DT_DEVERR_PARTICLE_OOB 1   /* a particle's B-spline stencil left the grid: it was skipped */
+#define DT_DEVERR_TAPE_FULL    2   /* more active grid blocks than tape_blocks in one frame */
+#define DT_DEVERR_NONFINITE    4   /* NaN/Inf met in a grid node or a particle */
+
+#define DT_MAX_SENSORS_PER_ENV 4
+#define DT_BLOCK_NODES 64
+
+/* material model ids */
+#define DT_MODEL_COROTATED 0   /* fixed-corotated, J = det(Sigma)         mpm_elastic.py:183-187 */
+#define DT_MODEL_VON_MISES 1   /* fixed-corotated + von-Mises return map  mpm_plastic.py:151-166,228-235 */
+#define DT_MODEL_NEOHOOKEAN 2  /* Kirchhoff stress mu(FF^T - I) + lam log(J) I                 */
+
+/* grid boundary conditions */
+#define DT_BC_SLIP_WALLS 0     /* reference: zero the inward normal velocity within `bound` nodes */
+#define DT_BC_STICKY_FLOOR 1   /* slip walls, but all velocity zeroed on the floor band (j < bound) */
+
+typedef struct dt_env {
+  int p_begin, p_end;   /* particle range of this environment's object */
+  int node_off;         /* first node of this env's grid in the flat grid arrays (multiple of 64) */
+  int blk_off;          /* first block of this env */
+  int nb[3];            /* blocks per axis */
+  int n[3];             /* grid nodes per axis (n_grid in the reference); n[d] <= 4*nb[d] */
+  int bound;            /* wall band in nodes (reference: 3) */
+  int bc;               /* DT_BC_* */
+  int s_begin, s_end;   /* sensors in contact with this env's object */
+  float dx, inv_dx;     /* grid spacing and its inverse (each rounded from double) */
+  float p_mass;         /* particle mass */
+  float stress_k;       /* -dt * p_vol * 4 * inv_dx^2 (rounded from double) */
+  float eps;            /* grid mass epsilon (1e-5) */
+  float g2p_k;          /* 4 * inv_dx */
+  float dt_g[3];        /* dt * gravity */
+  float kn, kd, kt, mu_t;  /* contact: normal stiffness, normal damping, tangential stiffness, friction */
+  float pad_;
+} dt_env;
+
+typedef struct dt_sensor {
+  int v_off, nv;        /* vertex range in the flat FEM vertex arrays */
+  int t_off, nt;        /* tet range */
+  int f_off, nf;        /* surface triangle range */
+  int env;              /* environment whose object this sensor touches */
+  int carry;            /* 1: vel[f+1] += cv[f+1]-cv[f] (gripper_fem.py:415), 0: fem_sensor.py:454 */
+  float dt_over_m;      /* dt / node mass */
+  float mu, lam, alpha; /* elastomer Lame parameters, alpha = 1 + 0.75 mu/lam */
+  float out_dir[3];     /* rot_h @ (0,1,0): orients surface normals (fem_sensor.py:340,370) */
+  float pad_;
+} dt_sensor;
+
+typedef struct dt_material {
+  float mu, lam, yield_stress;
+  int model;            /* DT_MODEL_* */
+} dt_material;
+
+/* World descriptor: host struct holding device pointers and sizes. */
+typedef struct dt_world {
+  /* ---- static tables (device) ---- */
+  const dt_env* envs;            /* [n_envs] */
+  const dt_sensor* sensors;      /* [n_sensors] */
+  const dt_material* materials;  /* [n_materials] */
+  const int* p_env;              /* [n_particles] env of each particle, non-decreasing */
+  const int* p_mat;              /* [n_particles] material index of each particle */
+  const int* blk_env;            /* [n_blocks] env of each block */
+  const int* tets;               /* [n_tets][4] global vertex ids */
+  const float* tet_B;            /* [n_tets][12] rest-shape inverse, 3 rows padded to 4 */
+  const int* tet_sensor;         /* [n_tets] */
+  const int* tris;               /* [n_tris][4] (a, b, c, sensor) global vertex ids */
+  const int* v_layer;            /* [n_verts] layer id; layer 0 is kinematically driven */
+  const int* v_sensor;           /* [n_verts] */
+  /* ---- particle state ---- */
+  float* p_state;                /* [n_frames][6][n_particles][4] */
+  float* p_adj;                  /* [2][6][n_particles][4] */
+  /* ---- grid working arrays (zero-invariant where noted) ---- */
+  float* g_acc;                  /* [n_nodes][4] P2G accumulator, zero between substeps */
+  float* g_vout;                 /* [n_nodes][4] */
+  float* g_adj_vout;             /* [n_nodes][4] G2P adjoint accumulator, zero between substeps */
+  float* g_adj_acc;              /* [n_nodes][4] */
+  int* blk_flag;                 /* [n_blocks] zero between substeps */
+  /* ---- per-frame grid tape ---- */
+  int* tape_blist;               /* [n_frames][n_blocks] active block ids */
+  int* tape_bcount;              /* [n_frames] */
+  float* tape_acc;               /* [n_frames][tape_blocks*64][4] */
+  float* tape_vout;              /* [n_frames][tape_blocks*64][4] */
+  int* tape_cidx;                /* [n_frames][tape_blocks*64][4] argmin triangle per env sensor */
+  /* ---- FEM frames ---- */
+  float* v_pos;                  /* [n_frames][n_verts][4] */
+  float* v_vel;                  /* [n_frames][n_verts][4] */
+  float* v_velmid;               /* [n_frames][n_verts][4] vel after elastic forces */
+  float* v_ext;                  /* [n_frames][n_verts][4] contact force accumulator */
+  float* v_vpos;                 /* [n_frames][n_verts][4] virtual (kinematic) position */
+  float* v_cv;                   /* [n_frames][n_verts][4] control velocity per frame */
+  float* tri_cent;               /* [n_tris][4] working: centroids of the current frame */
+  /* ---- FEM adjoints ---- */
+  float* v_adj_pos;              /* [2][n_verts][4] */
+  float* v_adj_vel;              /* [2][n_verts][4] */
+  float* v_adj_vpos;             /* [2][n_verts][4] */
+  float* v_adj_velmid;           /* [n_verts][4] */
+  float* v_adj_ext;              /* [n_verts][4] */
+  float* v_adj_cv;               /* [n_frames][n_verts][4] */
+  float* mat_adj;                /* [n_materials][4] (d/dmu, d/dlam, 0, 0) accumulated */
+  int* err;                      /* [4] device error word */
+  /* ---- sizes ---- */
+  int n_envs, n_particles, n_sensors, n_materials;
+  int n_verts, n_tets, n_tris;
+  int n_nodes, n_blocks, n_frames, tape_blocks;
+  float dt;
+  float grad_clip;               /* backward clamp of grid-mass and sensor grads; 0 disables */
+  int svd_sweeps;                /* cyclic Jacobi sweeps of the 3x3 SVD (4 is enough for fp32) */
+  int pad_;
+} dt_world;
+
+/* ---- introspection ---- */
+int dt_abi_version(void);
+size_t dt_sizeof_world(void);
+size_t dt_sizeof_env(void);
+size_t dt_sizeof_sensor(void);
+size_t dt_sizeof_material(void);
+
+/* ---- step set-up ----
+ * Clears the grid tape counters of every frame and prepares FEM frame 0 (velmid = vel, ext = 0).
+ * Call once before the substeps of a control step (the reference calls Contact.reset(),
+ * grasp_plastic.py:386). */
+int dt_step_begin(const dt_world* w, cudaStream_t stream);
+
+/* ---- forward substep f -> f+1 (replaces Contact.update(f), grasp_plastic.py:151-164) ----
+ * Three launches: P2G + FEM tet forces + triangle centroids; grid update + contact; G2P + FEM
+ * integration.  Requires 0 <= f < n_frames-1. */
+int dt_substep_fwd(const dt_world* w, int f, cudaStream_t stream);
+
+/* The same substep split into the reference's per-object calls, for drop-in use of the
+ * reference method sequence.  dt_substep_fwd(f) == p2g(f); fem_update(f); grid_op(f) (which
+ * includes check_grid_occupy, check_collision and collision); g2p(f); fem_update2(f). */
+int dt_p2g(const dt_world* w, int f, cudaStream_t stream);         /* mpm_elastic.py:135-208 */
+int dt_fem_update(const dt_world* w, int f, cudaStream_t stream);  /* fem_sensor.py:409-440 */
+int dt_grid_op(const dt_world* w, int f, cudaStream_t stream);     /* mpm_elastic.py:211-240 + grasp_plastic.py:270-299 */
+int dt_g2p(const dt_world* w, int f, cudaStream_t stream);         /* mpm_elastic.py:244-260 */
+int dt_fem_update2(const dt_world* w, int f, cudaStream_t stream); /* fem_sensor.py:444-457 */
+
+/* Copy frame `src` of the particle and FEM state to frame `dst` (mpm_elastic.py:263-268,
+ * fem_sensor.py:461-465). */
+int dt_copy_frame(const dt_world* w, int src, int dst, cudaStream_t stream);
+
+/* ---- backward substep (replaces Contact.update_grad(f), grasp_plastic.py:167-178) ----
+ * Consumes the adjoint of frame f+1 held in p_adj[(f+1)&1], v_adj_*[(f+1)&1] and produces the
+ * adjoint of frame f in p_adj[f&1], v_adj_*[f&1]; accumulates v_adj_cv[f], v_adj_cv[f+1] and
+ * mat_adj.  The forward tape of frame f (p_state[f], grid tape f, FEM frame f) must be intact. */
+int dt_substep_bwd(const dt_world* w, int f, cudaStream_t stream);
+
+/* Zero the adjoint buffers (p_adj, v_adj_*, mat_adj, g_adj_*) before a backward sweep. */
+int dt_adj_clear(const dt_world* w, cudaStream_t stream);
+
+/* ---- readouts ---- */
+/* Per-env centre of mass of frame f: out[n_envs][4] (xyz, 0) (grasp_plastic.py:259-261). */
+int dt_com(const dt_world* w, int f, float* out, cudaStream_t stream);
+/* Adjoint of dt_com: adds adj_com[e]/count to x-adjoint of every particle of env e in p_adj[f&1]. */
+int dt_com_bwd(const dt_world* w, int f, const float* adj_com, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DIFFTACTILE_GB300_H */

@@ -1,0 +1,784 @@
+// ORACLE — test infrastructure only.  CPU restatement of the DiffTactile simulation substep
+// (Taichi kernels of the reference), used as the parity checker of the CUDA path and as the
+// timed CPU baseline.  It is never linked into or called by the product path.
+//
+// Parity status: UNPINNED against the reference's own outputs.  The reference is Taichi 1.6.0
+// code (un-vendored third-party JIT, not importable in this image) and ships no tests, golden
+// vectors or fixtures for this path, so nothing the reference produced can be compared here.
+// The restatement is pinned instead by analytic known-answer tests (rest state, rigid
+// translation, partition of unity, momentum conservation, FEM rest/dilation, contact force,
+// argmin vs brute force) in tests/test_oracle_kat.py, and its adjoint by central finite
+// differences in double precision.
+//
+// Structure follows the reference kernel by kernel, on a dense per-frame grid in (i, j, k)
+// row-major order exactly like the Taichi fields, processing particles/nodes/tets in index
+// order:
+//   compute_new_F   difftactile/object_model/mpm_elastic.py:135-137
+//   svd             difftactile/object_model/mpm_elastic.py:140-142 (ti.svd; restated below as
+//                   cyclic Jacobi on A^T A + column sort + Givens QR, see svd3)
+//   p2g             difftactile/object_model/mpm_elastic.py:176-208,
+//                   difftactile/object_model/mpm_plastic.py:222-256 (von Mises :151-166),
+//                   difftactile/object_model/multi_obj.py:228-252 (per-particle material)
+//   check_grid_occupy  difftactile/object_model/mpm_elastic.py:211-214
+//   check_collision difftactile/tasks/grasp_plastic.py:270-276 + find_closest
+//                   difftactile/sensor_model/fem_sensor.py:344-359
+//   collision       difftactile/tasks/grasp_plastic.py:280-299 + find_sdf fem_sensor.py:362-394
+//                   + calculate_contact_force grasp_plastic.py:205-216
+//                   + update_contact_force mpm_elastic.py:131-132, fem_sensor.py:402-406
+//   grid_op         difftactile/object_model/mpm_elastic.py:217-240
+//   g2p             difftactile/object_model/mpm_elastic.py:244-260
+//   FEM update      difftactile/sensor_model/fem_sensor.py:409-440 (= gripper_fem.py:375-401)
+//   FEM update2     difftactile/sensor_model/fem_sensor.py:444-457, gripper_fem.py:404-418
+//   order           Contact.update, difftactile/tasks/grasp_plastic.py:151-164
+//
+// Build: oracle/build.py (g++ -O2 -ffp-contract=off -fopenmp -shared).  -ffp-contract=off keeps
+// every float operation separately rounded, so the argmin of find_closest is bit-reproducible.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+extern "C" {
+
+typedef struct orc_sensor {
+  int nv, nt, nf;
+  const int* tets;    // [nt][4] local vertex ids
+  const int* tris;    // [nf][3] local vertex ids
+  const int* layer;   // [nv]
+  const double* B;    // [nt][9] rest-shape inverse (row-major)
+  double mass, mu, lam;
+  double out_dir[3];
+  int carry;          // 1: gripper_fem.py:415 velocity carry term
+  int pad_;
+} orc_sensor;
+
+typedef struct orc_scene {
+  int n_particles;
+  int n[3];
+  int bound, bc;
+  double dx, inv_dx, p_vol, p_mass, dt, eps;
+  double grav[3];
+  double kn, kd, kt, mu_t;
+  int n_materials;
+  int n_sensors;
+  const double* mat_mu;
+  const double* mat_lam;
+  const double* mat_yield;
+  const int* mat_model;
+  const int* p_mat;   // [n_particles]
+  const orc_sensor* sensors;
+  int svd_sweeps;
+  int n_threads;      // OpenMP threads for the timed baseline (<=1: sequential)
+  double grad_clip;   // backward clamp (grasp_plastic.py:192-202); 0 disables
+} orc_scene;
+
+}  // extern "C"
+
+namespace {
+
+enum { MODEL_COROTATED = 0, MODEL_VON_MISES = 1, MODEL_NEOHOOKEAN = 2 };
+
+template <typename T>
+struct M3 {
+  T a[3][3];
+};
+
+template <typename T>
+inline M3<T> mzero() {
+  M3<T> m;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) m.a[i][j] = T(0);
+  return m;
+}
+template <typename T>
+inline M3<T> meye() {
+  M3<T> m = mzero<T>();
+  m.a[0][0] = m.a[1][1] = m.a[2][2] = T(1);
+  return m;
+}
+template <typename T>
+inline M3<T> mmul(const M3<T>& x, const M3<T>& y) {
+  M3<T> r;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      T s = x.a[i][0] * y.a[0][j];
+      s = s + x.a[i][1] * y.a[1][j];
+      s = s + x.a[i][2] * y.a[2][j];
+      r.a[i][j] = s;
+    }
+  return r;
+}
+template <typename T>
+inline M3<T> mT(const M3<T>& x) {
+  M3<T> r;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) r.a[i][j] = x.a[j][i];
+  return r;
+}
+template <typename T>
+inline T mdet(const M3<T>& m) {
+  const T(*a)[3] = m.a;
+  return a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) -
+         a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+         a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+}
+// cofactor matrix: cof[i][j] = d det / d a[i][j]
+template <typename T>
+inline M3<T> mcof(const M3<T>& m) {
+  const T(*a)[3] = m.a;
+  M3<T> c;
+  c.a[0][0] = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+  c.a[0][1] = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+  c.a[0][2] = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+  c.a[1][0] = a[0][2] * a[2][1] - a[0][1] * a[2][2];
+  c.a[1][1] = a[0][0] * a[2][2] - a[0][2] * a[2][0];
+  c.a[1][2] = a[0][1] * a[2][0] - a[0][0] * a[2][1];
+  c.a[2][0] = a[0][1] * a[1][2] - a[0][2] * a[1][1];
+  c.a[2][1] = a[0][2] * a[1][0] - a[0][0] * a[1][2];
+  c.a[2][2] = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+  return c;
+}
+
+// ---------------------------------------------------------------------------------------------
+// 3x3 SVD with the convention of ti.svd: A = U diag(s) V^T, det U = det V = +1, |s0|>=|s1|>=|s2|,
+// s0, s1 >= 0 and s2 carrying the sign of det A.
+// Method (published, restated): cyclic Jacobi eigen-decomposition of A^T A with the classical
+// rotation of Golub & Van Loan, "Matrix Computations", Alg. 8.4.1 (sym.schur2); columns of
+// B = A V sorted by norm with a sign flip per swap to keep det V = +1; Givens QR of B for U and
+// the signed singular values — the outline of McAdams et al. 2011, "Computing the SVD of 3x3
+// matrices with minimal branching and elementary floating point operations", with exact rather
+// than approximate rotation angles.
+template <typename T>
+inline void jacobi_rot(T S[3][3], T V[3][3], int p, int q) {
+  T apq = S[p][q];
+  if (apq == T(0)) return;
+  T tau = (S[q][q] - S[p][p]) / (T(2) * apq);
+  T t = (tau >= T(0) ? T(1) : T(-1)) / (std::fabs(tau) + std::sqrt(T(1) + tau * tau));
+  T c = T(1) / std::sqrt(T(1) + t * t);
+  T s = t * c;
+  for (int k = 0; k < 3; ++k) {  // S <- S J
+    T sp = S[k][p], sq = S[k][q];
+    S[k][p] = c * sp - s * sq;
+    S[k][q] = s * sp + c * sq;
+  }
+  for (int k = 0; k < 3; ++k) {  // S <- J^T S
+    T sp = S[p][k], sq = S[q][k];
+    S[p][k] = c * sp - s * sq;
+    S[q][k] = s * sp + c * sq;
+  }
+  for (int k = 0; k < 3; ++k) {  // V <- V J
+    T vp = V[k][p], vq = V[k][q];
+    V[k][p] = c * vp - s * vq;
+    V[k][q] = s * vp + c * vq;
+  }
+}
+
+template <typename T>
+inline void swap_cols_neg(T B[3][3], T V[3][3], int i, int j) {
+  for (int k = 0; k < 3; ++k) {
+    T b = B[k][i];
+    B[k][i] = B[k][j];
+    B[k][j] = -b;
+    T v = V[k][i];
+    V[k][i] = V[k][j];
+    V[k][j] = -v;
+  }
+}
+
+template <typename T>
+inline void qr_givens(T B[3][3], T U[3][3], int i, int j, int col) {
+  // zero B[j][col] by rotating rows i and j
+  T a = B[i][col], b = B[j][col];
+  T r = std::sqrt(a * a + b * b);
+  T c = T(1), s = T(0);
+  if (r > T(1e-30)) {
+    c = a / r;
+    s = b / r;
+  }
+  for (int k = 0; k < 3; ++k) {
+    T bi = B[i][k], bj = B[j][k];
+    B[i][k] = c * bi + s * bj;
+    B[j][k] = -s * bi + c * bj;
+  }
+  for (int k = 0; k < 3; ++k) {  // U <- U G^T
+    T ui = U[k][i], uj = U[k][j];
+    U[k][i] = c * ui + s * uj;
+    U[k][j] = -s * ui + c * uj;
+  }
+}
+
+template <typename T>
+void svd3(const M3<T>& A, M3<T>& U, T s[3], M3<T>& V, int sweeps) {
+  T S[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      T acc = A.a[0][i] * A.a[0][j];
+      acc = acc + A.a[1][i] * A.a[1][j];
+      acc = acc + A.a[2][i] * A.a[2][j];
+      S[i][j] = acc;
+    }
+  T Vm[3][3] = {{T(1), T(0), T(0)}, {T(0), T(1), T(0)}, {T(0), T(0), T(1)}};
+  for (int it = 0; it < sweeps; ++it) {
+    jacobi_rot(S, Vm, 0, 1);
+    jacobi_rot(S, Vm, 0, 2);
+    jacobi_rot(S, Vm, 1, 2);
+  }
+  T B[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      T acc = A.a[i][0] * Vm[0][j];
+      acc = acc + A.a[i][1] * Vm[1][j];
+      acc = acc + A.a[i][2] * Vm[2][j];
+      B[i][j] = acc;
+    }
+  auto cn = [&](int j) {
+    T r = B[0][j] * B[0][j];
+    r = r + B[1][j] * B[1][j];
+    r = r + B[2][j] * B[2][j];
+    return r;
+  };
+  if (cn(0) < cn(1)) swap_cols_neg(B, Vm, 0, 1);
+  if (cn(0) < cn(2)) swap_cols_neg(B, Vm, 0, 2);
+  if (cn(1) < cn(2)) swap_cols_neg(B, Vm, 1, 2);
+  T Um[3][3] = {{T(1), T(0), T(0)}, {T(0), T(1), T(0)}, {T(0), T(0), T(1)}};
+  qr_givens(B, Um, 0, 1, 0);
+  qr_givens(B, Um, 0, 2, 0);
+  qr_givens(B, Um, 1, 2, 1);
+  s[0] = B[0][0];
+  s[1] = B[1][1];
+  s[2] = B[2][2];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      U.a[i][j] = Um[i][j];
+      V.a[i][j] = Vm[i][j];
+    }
+}
+
+// quadratic B-spline weights (mpm_elastic.py:181) and their derivatives
+template <typename T>
+inline void bspline(T fx, T w[3], T dw[3]) {
+  T a = T(1.5) - fx, b = fx - T(1), c = fx - T(0.5);
+  w[0] = T(0.5) * (a * a);
+  w[1] = T(0.75) - b * b;
+  w[2] = T(0.5) * (c * c);
+  dw[0] = fx - T(1.5);
+  dw[1] = T(-2) * b;
+  dw[2] = c;
+}
+
+template <typename T>
+struct Consts {
+  T dx, inv_dx, p_mass, stress_k, eps, g2p_k, dt;
+  T dt_g[3];
+  T kn, kd, kt, mu_t;
+  T third;
+};
+
+template <typename T>
+Consts<T> make_consts(const orc_scene* sc) {
+  Consts<T> k;
+  k.dx = T(sc->dx);
+  k.inv_dx = T(sc->inv_dx);
+  k.p_mass = T(sc->p_mass);
+  k.stress_k = T(-sc->dt * sc->p_vol * 4.0 * sc->inv_dx * sc->inv_dx);
+  k.eps = T(sc->eps);
+  k.g2p_k = T(4.0 * sc->inv_dx);
+  k.dt = T(sc->dt);
+  for (int d = 0; d < 3; ++d) k.dt_g[d] = T(sc->dt * sc->grav[d]);
+  k.kn = T(sc->kn);
+  k.kd = T(sc->kd);
+  k.kt = T(sc->kt);
+  k.mu_t = T(sc->mu_t);
+  k.third = T(1.0 / 3.0);
+  return k;
+}
+
+inline size_t gidx(const int* n, int i, int j, int k) { return (size_t(i) * n[1] + j) * n[2] + k; }
+
+// von Mises return mapping, mpm_plastic.py:151-166.  Returns F unchanged when not yielding.
+template <typename T>
+M3<T> von_mises(const M3<T>& F, const M3<T>& U, const T sig[3], const M3<T>& V, T mu, T yield_stress) {
+  T eps[3];
+  for (int d = 0; d < 3; ++d) eps[d] = std::log(std::max(sig[d], T(0.05)));
+  T mean = ((eps[0] + eps[1]) + eps[2]) / T(3);
+  T eh[3] = {eps[0] - mean, eps[1] - mean, eps[2] - mean};
+  T nrm = std::sqrt(((eh[0] * eh[0] + eh[1] * eh[1]) + eh[2] * eh[2]) + T(1e-8));
+  T dg = nrm - yield_stress / (T(2) * mu);
+  if (dg > T(0)) {
+    T e[3];
+    for (int d = 0; d < 3; ++d) e[d] = std::exp(eps[d] - (dg / nrm) * eh[d]);
+    M3<T> r;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        T acc = U.a[i][0] * e[0] * V.a[j][0];
+        acc = acc + U.a[i][1] * e[1] * V.a[j][1];
+        acc = acc + U.a[i][2] * e[2] * V.a[j][2];
+        r.a[i][j] = acc;
+      }
+    return r;
+  }
+  return F;
+}
+
+template <typename T>
+inline void cross(const T a[3], const T b[3], T r[3]) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+template <typename T>
+inline T dot3(const T a[3], const T b[3]) {
+  return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+}
+
+// find_closest, fem_sensor.py:344-359: argmin of centroid distance, strict '<', start 100.
+template <typename T>
+int find_closest(const orc_sensor& s, const T* pos, const T p[3]) {
+  T best = T(100.0);
+  int bi = -1;
+  const T third = T(1.0 / 3.0);
+  for (int k = 0; k < s.nf; ++k) {
+    const int* t = s.tris + 3 * k;
+    T d[3];
+    for (int c = 0; c < 3; ++c) {
+      T pc = third * ((pos[3 * t[0] + c] + pos[3 * t[1] + c]) + pos[3 * t[2] + c]);
+      d[c] = pc - p[c];
+    }
+    T off = std::sqrt(((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) + T(1e-10));
+    if (off < best) {
+      best = off;
+      bi = k;
+    }
+  }
+  return bi;
+}
+
+template <typename T>
+struct SdfOut {
+  T sdf, nrm[3], rel[3];
+  bool flag;
+};
+
+// find_sdf, fem_sensor.py:362-394.  Returns the normal already flipped (= -norm_v) and the
+// relative velocity already negated (= -relative_v), as passed to calculate_contact_force.
+template <typename T>
+SdfOut<T> find_sdf(const orc_sensor& s, const T* pos, const T* vel, int k, const T p[3], const T gv[3]) {
+  const int* t = s.tris + 3 * k;
+  const T* p1 = pos + 3 * t[0];
+  const T* p2 = pos + 3 * t[1];
+  const T* p3 = pos + 3 * t[2];
+  T e1[3], e2[3], n[3];
+  for (int c = 0; c < 3; ++c) {
+    e1[c] = p2[c] - p1[c];
+    e2[c] = p3[c] - p1[c];
+  }
+  cross(e1, e2, n);
+  T len = std::sqrt(dot3(n, n));
+  T inv = T(1) / (len + T(1e-10));
+  for (int c = 0; c < 3; ++c) n[c] = inv * n[c];
+  T od[3] = {T(s.out_dir[0]), T(s.out_dir[1]), T(s.out_dir[2])};
+  T sg = dot3(n, od) < T(0) ? T(-1) : T(1);
+  for (int c = 0; c < 3; ++c) n[c] = sg * n[c];
+  T ds[3] = {p[0] - p1[0], p[1] - p1[1], p[2] - p1[2]};
+  T sdf = dot3(ds, n);
+  T proj[3];
+  for (int c = 0; c < 3; ++c) proj[c] = p[c] - sdf * n[c];
+  T v0[3], v1[3], v2[3];
+  for (int c = 0; c < 3; ++c) {
+    v0[c] = p3[c] - p1[c];
+    v1[c] = p2[c] - p1[c];
+    v2[c] = proj[c] - p1[c];
+  }
+  T d00 = dot3(v0, v0), d01 = dot3(v0, v1), d02 = dot3(v0, v2), d11 = dot3(v1, v1), d12 = dot3(v1, v2);
+  T invd = T(1) / (d00 * d11 - d01 * d01);
+  T u = (d11 * d02 - d01 * d12) * invd;
+  T v = (d00 * d12 - d01 * d02) * invd;
+  SdfOut<T> o;
+  o.sdf = sdf;
+  const T third = T(1.0 / 3.0);
+  for (int c = 0; c < 3; ++c) {
+    o.nrm[c] = n[c];
+    T tv = third * ((vel[3 * t[0] + c] + vel[3 * t[1] + c]) + vel[3 * t[2] + c]);
+    o.rel[c] = -(gv[c] - tv);
+  }
+  o.flag = sdf < T(0) && u >= T(0) && v >= T(0) && (u + v <= T(1));
+  return o;
+}
+
+// calculate_contact_force, grasp_plastic.py:205-216, called with (sdf, n, r) = (sdf, -norm_v, -rel_v)
+template <typename T>
+void contact_force(const Consts<T>& K, T sdf, const T n[3], const T r[3], T ext[3]) {
+  T nr = dot3(n, r);
+  T vn = std::max(nr, T(0));
+  T fn[3];
+  T kk = K.kn + K.kd * vn;
+  for (int c = 0; c < 3; ++c) fn[c] = -kk * sdf * n[c];
+  T vt[3];
+  for (int c = 0; c < 3; ++c) vt[c] = r[c] - nr * n[c];
+  T vtn = std::sqrt(dot3(vt, vt) + T(1e-11));
+  T ft[3] = {T(0), T(0), T(0)};
+  if (vtn > T(1e-4)) {
+    T fnn = std::sqrt(dot3(fn, fn));
+    T g = std::min(K.kt * vtn, K.mu_t * fnn);
+    for (int c = 0; c < 3; ++c) ft[c] = (vt[c] / vtn) * g;
+  }
+  for (int c = 0; c < 3; ++c) ext[c] = fn[c] + ft[c];
+}
+
+template <typename T>
+struct Particle {
+  M3<T> C, F;
+  T x[3], v[3];
+};
+
+template <typename T>
+inline Particle<T> load_particle(const T* x, const T* v, const T* C, const T* F, int p) {
+  Particle<T> q;
+  for (int d = 0; d < 3; ++d) {
+    q.x[d] = x[3 * p + d];
+    q.v[d] = v[3 * p + d];
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      q.C.a[i][j] = C[9 * p + 3 * i + j];
+      q.F.a[i][j] = F[9 * p + 3 * i + j];
+    }
+  return q;
+}
+
+// Per-particle forward quantities shared by p2g and its adjoint.
+template <typename T>
+struct P2GFwd {
+  int base[3];
+  T fx[3], w[3][3], dw[3][3];
+  M3<T> Fn, U, V, Fp, R, affine, cauchy;
+  T sig[3], J;
+  int model;
+  bool yield;
+  T mu, lam, ys;
+};
+
+template <typename T>
+bool particle_base(const orc_scene* sc, const Consts<T>& K, const T x[3], int base[3], T fx[3]) {
+  bool ok = true;
+  for (int d = 0; d < 3; ++d) {
+    T g = x[d] * K.inv_dx - T(0.5);
+    base[d] = int(g);  // truncation toward zero, like Taichi's cast(int)
+    fx[d] = x[d] * K.inv_dx - T(base[d]);
+    if (!(g == g) || base[d] < 0 || base[d] + 2 >= sc->n[d]) ok = false;
+  }
+  return ok;
+}
+
+template <typename T>
+void p2g_particle(const orc_scene* sc, const Consts<T>& K, const Particle<T>& q, int p, P2GFwd<T>& o) {
+  for (int d = 0; d < 3; ++d) {
+    T wd[3], dwd[3];
+    bspline(o.fx[d], wd, dwd);
+    for (int i = 0; i < 3; ++i) {
+      o.w[i][d] = wd[i];
+      o.dw[i][d] = dwd[i];
+    }
+  }
+  // compute_new_F: (I + dt C) F
+  M3<T> A = meye<T>();
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) A.a[i][j] = A.a[i][j] + K.dt * q.C.a[i][j];
+  o.Fn = mmul(A, q.F);
+  svd3(o.Fn, o.U, o.sig, o.V, sc->svd_sweeps);
+  int m = sc->p_mat ? sc->p_mat[p] : 0;
+  o.mu = T(sc->mat_mu[m]);
+  o.lam = T(sc->mat_lam[m]);
+  o.ys = T(sc->mat_yield[m]);
+  o.model = sc->mat_model[m];
+  o.yield = false;
+  o.R = mmul(o.U, mT(o.V));
+  if (o.model == MODEL_VON_MISES) {
+    o.Fp = von_mises(o.Fn, o.U, o.sig, o.V, o.mu, o.ys);
+    o.yield = std::memcmp(&o.Fp, &o.Fn, sizeof(o.Fp)) != 0;
+    o.J = mdet(o.Fp);
+  } else if (o.model == MODEL_NEOHOOKEAN) {
+    o.Fp = o.Fn;
+    o.J = mdet(o.Fp);
+  } else {
+    o.Fp = o.Fn;
+    o.J = o.sig[0] * (o.sig[1] * o.sig[2]);
+  }
+  M3<T> c;
+  if (o.model == MODEL_NEOHOOKEAN) {
+    M3<T> FFt = mmul(o.Fp, mT(o.Fp));
+    T lj = o.lam * std::log(o.J);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) c.a[i][j] = o.mu * (FFt.a[i][j] - (i == j ? T(1) : T(0))) + (i == j ? lj : T(0));
+  } else {
+    M3<T> D;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) D.a[i][j] = o.Fp.a[i][j] - o.R.a[i][j];
+    M3<T> DFt = mmul(D, mT(o.Fp));
+    T lj = o.lam * o.J * (o.J - T(1));
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) c.a[i][j] = T(2) * o.mu * DFt.a[i][j] + (i == j ? lj : T(0));
+  }
+  o.cauchy = c;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) o.affine.a[i][j] = K.stress_k * c.a[i][j] + K.p_mass * q.C.a[i][j];
+}
+
+}  // namespace
+
+// =============================================================================================
+// Forward substep, reference order of Contact.update (grasp_plastic.py:151-164).
+// Sensor arrays are per sensor, [nv][3]; vel[s] is updated in place by the elastic forces
+// (as the Taichi kernel does) and afterwards holds the post-force velocity used by contact.
+// Dense grid outputs are [n0*n1*n2] (*3 for vectors) and are overwritten.
+// =============================================================================================
+template <typename T>
+static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C, const T* F, T* x1, T* v1,
+                        T* C1, T* F1, T* const* pos, T* const* vel, const T* const* vpos, const T* const* cv,
+                        const T* const* cv1, T* const* pos1, T* const* vel1, T* const* vpos1, T* const* ext,
+                        T* grid_m, T* grid_v_in, T* grid_v_out, T* grid_f, int* cidx) {
+  const Consts<T> K = make_consts<T>(sc);
+  const int* n = sc->n;
+  const size_t nn = size_t(n[0]) * n[1] * n[2];
+  const int NS = sc->n_sensors;
+  int err = 0;
+  std::fill(grid_m, grid_m + nn, T(0));
+  std::fill(grid_v_in, grid_v_in + 3 * nn, T(0));
+  std::fill(grid_v_out, grid_v_out + 3 * nn, T(0));
+  std::fill(grid_f, grid_f + 3 * nn, T(0));
+  for (size_t i = 0; i < nn * size_t(NS > 0 ? NS : 1); ++i) cidx[i] = -1;
+  for (int s = 0; s < NS; ++s) std::fill(ext[s], ext[s] + 3 * sc->sensors[s].nv, T(0));
+
+  // ---- compute_new_F + svd + p2g ----
+  for (int p = 0; p < sc->n_particles; ++p) {
+    Particle<T> q = load_particle(x, v, C, F, p);
+    P2GFwd<T> o;
+    if (!particle_base(sc, K, q.x, o.base, o.fx)) {
+      err |= 1;
+      for (int i = 0; i < 9; ++i) F1[9 * p + i] = F[9 * p + i];
+      continue;
+    }
+    p2g_particle(sc, K, q, p, o);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const int off[3] = {i, j, k};
+          T dpos[3];
+          for (int d = 0; d < 3; ++d) dpos[d] = (T(off[d]) - o.fx[d]) * K.dx;
+          T W = (o.w[i][0] * o.w[j][1]) * o.w[k][2];
+          size_t g = gidx(n, o.base[0] + i, o.base[1] + j, o.base[2] + k);
+          for (int r = 0; r < 3; ++r) {
+            T ad = o.affine.a[r][0] * dpos[0];
+            ad = ad + o.affine.a[r][1] * dpos[1];
+            ad = ad + o.affine.a[r][2] * dpos[2];
+            grid_v_in[3 * g + r] += W * (K.p_mass * q.v[r] + ad);
+          }
+          grid_m[g] += W * K.p_mass;
+        }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) F1[9 * p + 3 * i + j] = o.Fp.a[i][j];
+  }
+
+  // ---- FEM update (fem_sensor.py:409-440) ----
+  for (int s = 0; s < NS; ++s) {
+    const orc_sensor& S = sc->sensors[s];
+    const T dt = T(sc->dt), mass = T(S.mass), mu = T(S.mu), lam = T(S.lam);
+    const T alpha = T(1) + T(0.75) * mu / lam;
+    T* P = pos[s];
+    T* Vl = vel[s];
+    for (int t = 0; t < S.nt; ++t) {
+      const int* tv = S.tets + 4 * t;
+      M3<T> D, B;
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+          D.a[r][c] = P[3 * tv[c] + r] - P[3 * tv[3] + r];
+          B.a[r][c] = T(S.B[9 * t + 3 * r + c]);
+        }
+      T Vi = std::fabs(mdet(D)) / T(6);
+      M3<T> Fe = mmul(D, B);
+      T J = mdet(Fe);
+      T IC = T(0);
+      for (int i = 0; i < 3; ++i) {
+        T cc = Fe.a[0][i] * Fe.a[0][i];
+        cc = cc + Fe.a[1][i] * Fe.a[1][i];
+        cc = cc + Fe.a[2][i] * Fe.a[2][i];
+        IC = IC + cc;
+      }
+      M3<T> cof = mcof(Fe);  // columns: F1xF2, F2xF0, F0xF1
+      M3<T> Pk;
+      T k1 = mu * (T(1) - T(1) / (IC + T(1)));
+      T k2 = lam * (J - alpha);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Pk.a[i][j] = k1 * Fe.a[i][j] + k2 * cof.a[i][j];
+      M3<T> H = mmul(Pk, mT(B));
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) H.a[i][j] = -Vi * H.a[i][j];
+      for (int k = 0; k < 3; ++k)
+        for (int r = 0; r < 3; ++r) {
+          T fo = H.a[r][k];
+          Vl[3 * tv[k] + r] += dt * fo / mass;
+          Vl[3 * tv[3] + r] += T(-1) * dt * fo / mass;
+        }
+    }
+  }
+
+  // ---- check_grid_occupy + check_collision + collision + grid_op ----
+  for (int i = 0; i < n[0]; ++i)
+    for (int j = 0; j < n[1]; ++j)
+      for (int k = 0; k < n[2]; ++k) {
+        size_t g = gidx(n, i, j, k);
+        T m = grid_m[g];
+        if (!(m > K.eps)) continue;
+        T p[3] = {(T(i) + T(0.5)) * K.dx, (T(j) + T(0.5)) * K.dx, (T(k) + T(0.5)) * K.dx};
+        T cur_v[3];
+        for (int c = 0; c < 3; ++c) cur_v[c] = grid_v_in[3 * g + c] / (m + K.eps);
+        for (int s = 0; s < NS; ++s) {
+          const orc_sensor& S = sc->sensors[s];
+          int kk = find_closest(S, pos[s], p);
+          cidx[g * NS + s] = kk;
+          if (kk < 0) continue;
+          SdfOut<T> so = find_sdf(S, pos[s], vel[s], kk, p, cur_v);
+          if (!so.flag) continue;
+          T e[3];
+          contact_force(K, so.sdf, so.nrm, so.rel, e);
+          for (int c = 0; c < 3; ++c) grid_f[3 * g + c] += e[c] * K.dt;
+          const int* t = S.tris + 3 * kk;
+          for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c) ext[s][3 * t[a] + c] += K.third * (T(-1) * e[c]);
+        }
+        T inv_m = T(1) / (m + K.eps);
+        T vo[3];
+        for (int c = 0; c < 3; ++c) {
+          T a = T(0) + inv_m * grid_v_in[3 * g + c];
+          a = a + inv_m * grid_f[3 * g + c];
+          vo[c] = a + K.dt_g[c];
+        }
+        const int idx[3] = {i, j, k};
+        for (int d = 0; d < 3; ++d) {
+          if (idx[d] < sc->bound && vo[d] < T(0)) vo[d] = T(0);
+          if (idx[d] > n[d] - sc->bound && vo[d] > T(0)) vo[d] = T(0);
+        }
+        if (sc->bc == 1 && j < sc->bound) vo[0] = vo[1] = vo[2] = T(0);
+        for (int c = 0; c < 3; ++c) grid_v_out[3 * g + c] = vo[c];
+      }
+
+  // ---- g2p ----
+  for (int p = 0; p < sc->n_particles; ++p) {
+    T xp[3];
+    for (int d = 0; d < 3; ++d) xp[d] = x[3 * p + d];
+    int base[3];
+    T fx[3];
+    if (!particle_base(sc, K, xp, base, fx)) {
+      for (int d = 0; d < 3; ++d) {
+        x1[3 * p + d] = x[3 * p + d];
+        v1[3 * p + d] = v[3 * p + d];
+      }
+      for (int i = 0; i < 9; ++i) C1[9 * p + i] = C[9 * p + i];
+      continue;
+    }
+    T w[3][3], dw[3][3];
+    for (int d = 0; d < 3; ++d) {
+      T wd[3], dwd[3];
+      bspline(fx[d], wd, dwd);
+      for (int i = 0; i < 3; ++i) {
+        w[i][d] = wd[i];
+        dw[i][d] = dwd[i];
+      }
+    }
+    T nv[3] = {T(0), T(0), T(0)};
+    M3<T> nC = mzero<T>();
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const int off[3] = {i, j, k};
+          T dpos[3];
+          for (int d = 0; d < 3; ++d) dpos[d] = T(off[d]) - fx[d];
+          size_t g = gidx(n, base[0] + i, base[1] + j, base[2] + k);
+          const T* gv = grid_v_out + 3 * g;
+          T W = (w[i][0] * w[j][1]) * w[k][2];
+          T kw = K.g2p_k * W;
+          for (int r = 0; r < 3; ++r) {
+            nv[r] += W * gv[r];
+            for (int c = 0; c < 3; ++c) nC.a[r][c] += kw * (gv[r] * dpos[c]);
+          }
+        }
+    for (int d = 0; d < 3; ++d) {
+      v1[3 * p + d] = nv[d];
+      x1[3 * p + d] = xp[d] + K.dt * nv[d];
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) C1[9 * p + 3 * i + j] = nC.a[i][j];
+  }
+
+  // ---- FEM update2 (fem_sensor.py:444-457, gripper_fem.py:404-418) ----
+  for (int s = 0; s < NS; ++s) {
+    const orc_sensor& S = sc->sensors[s];
+    const T dt = T(sc->dt), mass = T(S.mass);
+    for (int i = 0; i < S.nv; ++i) {
+      T vo[3];
+      for (int c = 0; c < 3; ++c) vo[c] = (T(0) + vel[s][3 * i + c]) + dt * ext[s][3 * i + c] / mass;
+      if (S.layer[i] == 0)
+        for (int c = 0; c < 3; ++c) vo[c] = cv[s][3 * i + c];
+      for (int c = 0; c < 3; ++c) {
+        T carry = S.carry ? (cv1[s][3 * i + c] - cv[s][3 * i + c]) : T(0);
+        vel1[s][3 * i + c] = vo[c] + carry;
+        pos1[s][3 * i + c] = pos[s][3 * i + c] + dt * vo[c];
+        vpos1[s][3 * i + c] = vpos[s][3 * i + c] + dt * cv[s][3 * i + c];
+      }
+    }
+  }
+  return err;
+}
+
+extern "C" {
+
+int orc_substep_f32(const orc_scene* sc, const float* x, const float* v, const float* C, const float* F, float* x1,
+                    float* v1, float* C1, float* F1, float* const* pos, float* const* vel, const float* const* vpos,
+                    const float* const* cv, const float* const* cv1, float* const* pos1, float* const* vel1,
+                    float* const* vpos1, float* const* ext, float* grid_m, float* grid_v_in, float* grid_v_out,
+                    float* grid_f, int* cidx) {
+  return substep_impl<float>(sc, x, v, C, F, x1, v1, C1, F1, pos, vel, vpos, cv, cv1, pos1, vel1, vpos1, ext, grid_m,
+                             grid_v_in, grid_v_out, grid_f, cidx);
+}
+
+int orc_substep_f64(const orc_scene* sc, const double* x, const double* v, const double* C, const double* F,
+                    double* x1, double* v1, double* C1, double* F1, double* const* pos, double* const* vel,
+                    const double* const* vpos, const double* const* cv, const double* const* cv1,
+                    double* const* pos1, double* const* vel1, double* const* vpos1, double* const* ext,
+                    double* grid_m, double* grid_v_in, double* grid_v_out, double* grid_f, int* cidx) {
+  return substep_impl<double>(sc, x, v, C, F, x1, v1, C1, F1, pos, vel, vpos, cv, cv1, pos1, vel1, vpos1, ext,
+                              grid_m, grid_v_in, grid_v_out, grid_f, cidx);
+}
+
+// Standalone 3x3 SVD (for SVD-convention and accuracy tests): A, U, V [n][9], s [n][3].
+void orc_svd3_f32(int n, const float* A, float* U, float* s, float* V, int sweeps) {
+  for (int i = 0; i < n; ++i) {
+    M3<float> a, u, v;
+    std::memcpy(a.a, A + 9 * i, sizeof(a.a));
+    svd3(a, u, s + 3 * i, v, sweeps);
+    std::memcpy(U + 9 * i, u.a, sizeof(u.a));
+    std::memcpy(V + 9 * i, v.a, sizeof(v.a));
+  }
+}
+void orc_svd3_f64(int n, const double* A, double* U, double* s, double* V, int sweeps) {
+  for (int i = 0; i < n; ++i) {
+    M3<double> a, u, v;
+    std::memcpy(a.a, A + 9 * i, sizeof(a.a));
+    svd3(a, u, s + 3 * i, v, sweeps);
+    std::memcpy(U + 9 * i, u.a, sizeof(u.a));
+    std::memcpy(V + 9 * i, v.a, sizeof(v.a));
+  }
+}
+
+// Standalone argmin (find_closest) over one sensor for a list of query points [nq][3].
+void orc_find_closest_f32(const orc_sensor* s, const float* pos, int nq, const float* q, int* out) {
+  for (int i = 0; i < nq; ++i) out[i] = find_closest(*s, pos, q + 3 * i);
+}
+
+int orc_abi_version(void) { return 1; }
+
+}  // extern "C"

@@ -1,0 +1,49 @@
+"""Small seeded scenes the oracle finishes in seconds (parity cases)."""
+import numpy as np
+
+from difftactile_gb300 import scene as S
+
+
+def elastic_cube(n=32, side_cells=6, ppc=8, seed=0, v=(0.0, 0.0, 0.0), model=S.MODEL_COROTATED, gravity=(0, -9.8, 0),
+                 rho=1000.0, E=5e3, nu=0.3, bc=S.BC_SLIP_WALLS, center=(0.5, 0.5, 0.5)):
+    dx = 1.0 / n
+    x = S.cube_particles(center, side_cells * dx, dx, ppc, seed)
+    rng = np.random.default_rng(seed + 100)
+    vv = np.asarray(v, np.float32) + 0.05 * rng.standard_normal(x.shape).astype(np.float32)
+    return S.EnvSpec(x=x, v=vv, materials=[S.Material(E, nu, 50.0, model)], n_grid=(n, n, n), dx=dx, rho=rho,
+                     gravity=gravity, bc=bc)
+
+
+def pad_over_box(n=32, box_cells=(6, 4, 6), pad=(6, 6, 2), ppc=8, seed=1, model=S.MODEL_VON_MISES, yield_stress=5.0,
+                 two_pads=False):
+    """An elastoplastic box resting low in the domain with a hex pad whose contact surface is half a
+    cell above the box top, so that grid nodes above the box start inside the pad."""
+    dx = 1.0 / n
+    lo = np.array([n / 2 - box_cells[0] / 2, 4, n / 2 - box_cells[2] / 2]) * dx
+    hi = lo + np.array(box_cells) * dx
+    x = S.box_particles(lo, hi, dx, ppc, seed)
+    rng = np.random.default_rng(seed + 7)
+    v = 0.02 * rng.standard_normal(x.shape).astype(np.float32)
+    sensors = []
+    top = hi[1]
+    sp = S.hex_pad_sensor([0.5 + 0.13 * dx, top + 0.5 * dx, 0.5 - 0.21 * dx], nx=pad[0], nz=pad[1], ny=pad[2], h=dx)
+    sensors.append(sp)
+    if two_pads:
+        sp2 = S.hex_pad_sensor([0.5 - 0.07 * dx, top + 0.9 * dx, 0.5 + 0.11 * dx], nx=pad[0] - 2, nz=pad[1] - 2, ny=pad[2],
+                               h=dx)
+        sensors.append(sp2)
+    return S.EnvSpec(x=x, v=v, materials=[S.Material(5e3, 0.3, yield_stress, model)], n_grid=(n, n, n), dx=dx,
+                     rho=1000.0, sensors=sensors, kn=1e4, kd=100.0, kt=100.0, mu_t=1.0)
+
+
+def control_velocity(sp, seed=3, scale=0.05, down=-0.1):
+    rng = np.random.default_rng(seed)
+    base = np.array([0.0, down, 0.0]) + scale * rng.standard_normal(3)
+    return np.broadcast_to(base, sp.verts.shape).astype(np.float32).copy()
+
+
+def rel_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = max(np.linalg.norm(b), 1e-30)
+    return float(np.linalg.norm(a - b) / den)
