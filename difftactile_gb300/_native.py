@@ -56,7 +56,8 @@ WORLD_INT_FIELDS = [
 
 class DtWorld(C.Structure):
     _fields_ = ([(n, _P) for n in WORLD_PTR_FIELDS] + [(n, C.c_int) for n in WORLD_INT_FIELDS]
-                + [("dt", C.c_float), ("grad_clip", C.c_float), ("svd_sweeps", C.c_int), ("pad_", C.c_int)])
+                + [("dt", C.c_float), ("grad_clip", C.c_float), ("svd_sweeps", C.c_int),
+                   ("svd_grad_mode", C.c_int)])
 
 
 # entry points: name -> (restype, argtypes)
@@ -76,6 +77,7 @@ SIGNATURES = {
     "dt_fem_update2": (C.c_int, [_W, C.c_int, _P]),
     "dt_copy_frame": (C.c_int, [_W, C.c_int, C.c_int, _P]),
     "dt_substep_bwd": (C.c_int, [_W, C.c_int, _P]),
+    "dt_substep_bwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),
     "dt_adj_clear": (C.c_int, [_W, _P]),
     "dt_com": (C.c_int, [_W, C.c_int, _P, _P]),
     "dt_com_bwd": (C.c_int, [_W, C.c_int, _P, _P]),

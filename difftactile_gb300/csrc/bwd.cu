@@ -1,12 +1,699 @@
-// Adjoint substep kernels (sm_103a) — placeholder until the adjoints land.
+// Adjoint substep kernels (sm_103a): the reverse of Contact.update (grasp_plastic.py:151-164)
+// in the order of Contact.update_grad (grasp_plastic.py:167-178):
+//   B0 k_bwd_restore   : grid velocities of frame f back from the tape into the dense grid
+//   B1 k_bwd_g2p_fem   : particles — G2P adjoint (scatter into the grid adjoint, x adjoint);
+//                        vertices  — FEM integration adjoint + clamp_grid on sensor grads
+//   B2 k_bwd_grid      : active blocks of frame f — grid_op adjoint, clamp of the grid-mass grad,
+//                        contact adjoint (argmin held constant, as the reference computes it in a
+//                        non-differentiated kernel) into grid and sensor adjoints
+//   B3 k_bwd_p2g_fem   : particles — P2G adjoint (gather), stress/return-map adjoint, SVD adjoint
+//                        of mpm_elastic.py:145-173 (1/(s_j^2-s_i^2) clamped at +-1e-8),
+//                        F-update adjoint, material (mu, lambda) grads;
+//                        tets      — FEM elastic-force adjoint into position grads;
+//                        vertices  — velocity adjoint of frame f
+// Adjoint of frame f+1 is read from buffer (f+1)&1, adjoint of frame f written to buffer f&1.
 #include "common.cuh"
+
+namespace {
+
+constexpr int NT = 128;
+constexpr int GRID_NT = 64;
+
+DT_DEV float clampg(float a, float c) { return c > 0.f ? fminf(fmaxf(a, -c), c) : a; }
+DT_DEV v3 clampg(v3 a, float c) { return v3{clampg(a.x, c), clampg(a.y, c), clampg(a.z, c)}; }
+DT_DEV float4 ld4(const float4* p) { return *p; }
+
+// the reference's clamp of the singular-value gap (mpm_elastic.py:150-155)
+DT_DEV float gap_clamp(float a) { return a >= 0.f ? fmaxf(a, 1e-8f) : fminf(a, -1e-8f); }
+
+// SVD adjoint, mpm_elastic.py:158-173: F_bar = U [ (ff o (U^T Ub - Ub^T U)) S + diag(sb)
+// + S (ff o (V^T Vb - Vb^T V)) ] V^T with ff_ij = 1/clamp(s_j^2 - s_i^2).  The adjoint Rb of the
+// rotation R = U V^T is passed separately: with M = U^T Rb V it contributes Ub = Rb V, Vb = Rb^T U,
+// i.e. ff_ij (M - M^T)_ij (s_j - s_i), which the stable mode evaluates as (M - M^T)_ij / (s_i + s_j).
+DT_DEV m3 svd_grad(const m3& U, v3 s, const m3& V, const m3& Ub_in, v3 sb, const m3& Vb_in, const m3& Rb, int mode) {
+  const float sv[3] = {s.x, s.y, s.z};
+  m3 Ub = Ub_in, Vb = Vb_in;
+  if (mode == DT_SVDGRAD_REFERENCE) {
+    Ub = madd(Ub, mmul(Rb, V));
+    Vb = madd(Vb, mTmul(Rb, U));
+  }
+  const m3 M = mmul(mTmul(U, Rb), V);
+  const m3 UtUb = mTmul(U, Ub), UbtU = mTmul(Ub, U), VtVb = mTmul(V, Vb), VbtV = mTmul(Vb, V);
+  m3 inner;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float v = 0.f;
+      if (i != j) {
+        const float ff = 1.f / gap_clamp(sv[j] * sv[j] - sv[i] * sv[i]);
+        v = ff * (UtUb.a[i][j] - UbtU.a[i][j]) * sv[j] + sv[i] * ff * (VtVb.a[i][j] - VbtV.a[i][j]);
+        if (mode != DT_SVDGRAD_REFERENCE) v += (M.a[i][j] - M.a[j][i]) / gap_clamp(sv[i] + sv[j]);
+      } else {
+        v = i == 0 ? sb.x : (i == 1 ? sb.y : sb.z);
+      }
+      inner.a[i][j] = v;
+    }
+  return mmulT(mmul(U, inner), V);
+}
+
+// ---------------------------------------------------------------------------------------------
+// B0
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(GRID_NT) k_bwd_restore(dt_world w, int f) {
+  const int cnt = min(w.tape_bcount[f], w.tape_blocks);
+  const int l = threadIdx.x;
+  for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
+    const int b = w.tape_blist[(size_t)f * w.n_blocks + e];
+    const dt_env& E = w.envs[__ldg(w.blk_env + b)];
+    const int g = E.node_off + ((b - E.blk_off) << 6) + l;
+    reinterpret_cast<float4*>(w.g_vout)[g] =
+        reinterpret_cast<const float4*>(w.tape_vout)[((size_t)f * w.tape_blocks + e) * 64 + l];
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// B1
+// ---------------------------------------------------------------------------------------------
+__device__ void g2p_bwd(const dt_world& w, int f, int p) {
+  const int nb = (f + 1) & 1, cb = f & 1;
+  const float4 a0 = ld4(padj(w, nb, 0) + p), a1 = ld4(padj(w, nb, 1) + p), a2 = ld4(padj(w, nb, 2) + p),
+               a3 = ld4(padj(w, nb, 3) + p);
+  const v3 xb1 = v3{a0.x, a0.y, a0.z};
+  const v3 vb1 = v3{a0.w, a1.x, a1.y};
+  m3 Cb;
+  Cb.a[0][0] = a1.z;
+  Cb.a[0][1] = a1.w;
+  Cb.a[0][2] = a2.x;
+  Cb.a[1][0] = a2.y;
+  Cb.a[1][1] = a2.z;
+  Cb.a[1][2] = a2.w;
+  Cb.a[2][0] = a3.x;
+  Cb.a[2][1] = a3.y;
+  Cb.a[2][2] = a3.z;
+  const v3 x = f4to3(ldg4(pplane(w, f, 0) + p));
+  const dt_env& E = w.envs[__ldg(w.p_env + p)];
+  int base[3];
+  float fx[3];
+  float4* out0 = padj(w, cb, 0) + p;
+  if (!particle_base(E, x, base, fx)) {
+    *out0 = make_float4(xb1.x, xb1.y, xb1.z, 0.f);  // carried unchanged in the forward pass
+    return;
+  }
+  // x_new = x + dt v_new
+  const v3 vnb = vb1 + w.dt * xb1;
+  float fxb[3] = {0.f, 0.f, 0.f};
+  const float4* vout = reinterpret_cast<const float4*>(w.g_vout);
+  float4* avout = reinterpret_cast<float4*>(w.g_adj_vout);
+  float wts[3][3], dws[3][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      wts[i][d] = bsw(i, fx[d]);
+      dws[i][d] = bsdw(i, fx[d]);
+    }
+#pragma unroll
+  for (int oi = 0; oi < 3; ++oi)
+#pragma unroll
+    for (int oj = 0; oj < 3; ++oj)
+#pragma unroll
+      for (int ok = 0; ok < 3; ++ok) {
+        const int n = node_index(E, base[0] + oi, base[1] + oj, base[2] + ok);
+        const v3 gv = f4to3(__ldg(vout + n));
+        const float W = (wts[oi][0] * wts[oj][1]) * wts[ok][2];
+        const float kw = E.g2p_k * W;
+        const v3 d = v3{(float)oi - fx[0], (float)oj - fx[1], (float)ok - fx[2]};
+        const v3 Cd = mvec(Cb, d);       // C_bar d
+        const v3 Ctg = mTvec(Cb, gv);    // C_bar^T gv
+        // v_out adjoint
+        const v3 gvb = W * vnb + kw * Cd;
+        red_add_v4(avout + n, v3to4(gvb));
+        // weight adjoint and offset adjoint
+        const float Wb = dot(gv, vnb) + E.g2p_k * dot(gv, Cd);
+        fxb[0] += Wb * (dws[oi][0] * wts[oj][1] * wts[ok][2]) - kw * Ctg.x;
+        fxb[1] += Wb * (wts[oi][0] * dws[oj][1] * wts[ok][2]) - kw * Ctg.y;
+        fxb[2] += Wb * (wts[oi][0] * wts[oj][1] * dws[ok][2]) - kw * Ctg.z;
+      }
+  const v3 xb = xb1 + E.inv_dx * v3{fxb[0], fxb[1], fxb[2]};
+  *out0 = make_float4(xb.x, xb.y, xb.z, 0.f);
+}
+
+__device__ void integrate_bwd(const dt_world& w, int f, int i) {
+  const int nb = (f + 1) & 1, cb = f & 1;
+  const dt_sensor& S = w.sensors[__ldg(w.v_sensor + i)];
+  const size_t V = (size_t)w.n_verts;
+  const v3 posb1 = f4to3(reinterpret_cast<const float4*>(w.v_adj_pos)[nb * V + i]);
+  const v3 velb1 = f4to3(reinterpret_cast<const float4*>(w.v_adj_vel)[nb * V + i]);
+  const v3 vpb1 = f4to3(reinterpret_cast<const float4*>(w.v_adj_vpos)[nb * V + i]);
+  float4* cvb_f = vframe(w.v_adj_cv, w, f) + i;
+  float4* cvb_n = vframe(w.v_adj_cv, w, f + 1) + i;
+  v3 cvb = f4to3(*cvb_f);
+  v3 cvbn = f4to3(*cvb_n);
+  // vpos1 = vpos + dt cv ; pos1 = pos + dt vo ; vel1 = vo + carry (cv1 - cv)
+  cvb = cvb + w.dt * vpb1;
+  v3 vob = velb1 + w.dt * posb1;
+  if (S.carry) {
+    cvbn = cvbn + velb1;
+    cvb = cvb - velb1;
+  }
+  v3 vmb = v3{0.f, 0.f, 0.f}, exb = v3{0.f, 0.f, 0.f};
+  if (__ldg(w.v_layer + i) == 0) {
+    cvb = cvb + vob;
+  } else {
+    vmb = vob;
+    exb = S.dt_over_m * vob;
+  }
+  // clamp_grid on the sensor's pos/vel grads of frame f (grasp_plastic.py:196-202)
+  const v3 posb = clampg(posb1, w.grad_clip);
+  vmb = clampg(vmb, w.grad_clip);
+  reinterpret_cast<float4*>(w.v_adj_pos)[cb * V + i] = v3to4(posb);
+  reinterpret_cast<float4*>(w.v_adj_vpos)[cb * V + i] = v3to4(vpb1);
+  reinterpret_cast<float4*>(w.v_adj_velmid)[i] = v3to4(vmb);
+  reinterpret_cast<float4*>(w.v_adj_ext)[i] = v3to4(exb);
+  *cvb_f = v3to4(cvb);
+  if (S.carry) *cvb_n = v3to4(cvbn);
+}
+
+__global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
+  int b = blockIdx.x;
+  if (b < nb_p) {
+    int p = b * NT + threadIdx.x;
+    if (p < w.n_particles) g2p_bwd(w, f, p);
+    return;
+  }
+  b -= nb_p;
+  if (b < nb_v) {
+    int i = b * NT + threadIdx.x;
+    if (i < w.n_verts) integrate_bwd(w, f, i);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// B2: grid op + contact adjoint
+// ---------------------------------------------------------------------------------------------
+// adjoint of contact_force (grasp_plastic.py:205-216): returns sdf_b, accumulates n_b and r_b
+DT_DEV float contact_force_bwd(const dt_env& E, float sdf, v3 n, v3 r, v3 eb, v3& nb, v3& rb) {
+  const float nr = dot(n, r);
+  const float vn = fmaxf(nr, 0.f);
+  const float kk = E.kn + E.kd * vn;
+  const v3 fn = (-kk * sdf) * n;
+  const v3 vt = r - nr * n;
+  const float vtn = sqrtf(dot(vt, vt) + 1e-11f);
+  v3 fnb = eb;
+  v3 vtb = v3{0.f, 0.f, 0.f};
+  if (vtn > 1e-4f) {
+    const float fnn = sqrtf(dot(fn, fn));
+    const float kv = E.kt * vtn, cap = E.mu_t * fnn;
+    const float g = fminf(kv, cap);
+    const v3 th = (1.f / vtn) * vt;
+    const float gb = dot(th, eb);
+    const v3 thb = g * eb;
+    float vtnb = 0.f;
+    if (kv <= cap) {
+      vtnb += E.kt * gb;
+    } else if (fnn > 0.f) {
+      fnb = fnb + (E.mu_t * gb / fnn) * fn;
+    }
+    vtb = (1.f / vtn) * thb;
+    vtnb += -dot(thb, vt) / (vtn * vtn);
+    vtb = vtb + (vtnb / vtn) * vt;
+  }
+  // vt = r - nr n
+  rb = rb + vtb;
+  float nrb = -dot(n, vtb);
+  nb = nb - nr * vtb;
+  // fn = -kk sdf n
+  const float nfb = dot(n, fnb);
+  const float kkb = -sdf * nfb;
+  const float sdfb = -kk * nfb;
+  nb = nb - (kk * sdf) * fnb;
+  const float vnb = E.kd * kkb;
+  if (nr > 0.f) nrb += vnb;
+  nb = nb + nrb * r;
+  rb = rb + nrb * n;
+  return sdfb;
+}
+
+__global__ void __launch_bounds__(GRID_NT) k_bwd_grid(dt_world w, int f) {
+  const int cnt = min(w.tape_bcount[f], w.tape_blocks);
+  const int l = threadIdx.x;
+  const float third = 1.f / 3.f;
+  const int cb = f & 1;
+  const size_t V = (size_t)w.n_verts;
+  float4* avout = reinterpret_cast<float4*>(w.g_adj_vout);
+  float4* aacc = reinterpret_cast<float4*>(w.g_adj_acc);
+  const float4* P = vframe(w.v_pos, w, f);
+  const float4* VM = vframe(w.v_velmid, w, f);
+  float4* aPos = reinterpret_cast<float4*>(w.v_adj_pos) + cb * V;
+  float4* aVm = reinterpret_cast<float4*>(w.v_adj_velmid);
+  const float4* aExt = reinterpret_cast<const float4*>(w.v_adj_ext);
+  const int4* tris = reinterpret_cast<const int4*>(w.tris);
+  for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
+    const int b = w.tape_blist[(size_t)f * w.n_blocks + e];
+    const dt_env& E = w.envs[__ldg(w.blk_env + b)];
+    const int lb = b - E.blk_off;
+    const int bk = lb % E.nb[2], bj = (lb / E.nb[2]) % E.nb[1], bi = lb / (E.nb[1] * E.nb[2]);
+    const int i = 4 * bi + (l >> 4), j = 4 * bj + ((l >> 2) & 3), k = 4 * bk + (l & 3);
+    const int g = E.node_off + (lb << 6) + l;
+    const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + l;
+    const float4 a = reinterpret_cast<const float4*>(w.tape_acc)[ti];
+    const int4 cid4 = reinterpret_cast<const int4*>(w.tape_cidx)[ti];
+    const v3 vb = f4to3(avout[g]);
+    avout[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float m = a.w;
+    float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (m > E.eps) {
+      const v3 mv = f4to3(a);
+      const float me = m + E.eps;
+      const float inv_m = 1.f / me;
+      const v3 cur_v = v3{mv.x / me, mv.y / me, mv.z / me};
+      const v3 p = v3{__fmul_rn(__fadd_rn((float)i, 0.5f), E.dx), __fmul_rn(__fadd_rn((float)j, 0.5f), E.dx),
+                      __fmul_rn(__fadd_rn((float)k, 0.5f), E.dx)};
+      const int cid[4] = {cid4.x, cid4.y, cid4.z, cid4.w};
+      // forward recompute of the contact force sum
+      v3 gf = v3{0.f, 0.f, 0.f};
+#pragma unroll
+      for (int q = 0; q < DT_MAX_SENSORS_PER_ENV; ++q) {
+        const int si = E.s_begin + q;
+        if (si >= E.s_end) break;
+        if (cid[q] < 0) continue;
+        const dt_sensor& S = w.sensors[si];
+        const int4 tr = __ldg(tris + S.f_off + cid[q]);
+        SdfRes sr = find_sdf(f4to3(P[tr.x]), f4to3(P[tr.y]), f4to3(P[tr.z]), f4to3(VM[tr.x]), f4to3(VM[tr.y]),
+                             f4to3(VM[tr.z]), v3{S.out_dir[0], S.out_dir[1], S.out_dir[2]}, p, cur_v);
+        if (!sr.flag) continue;
+        gf = gf + w.dt * contact_force(E, sr.sdf, sr.n, sr.r);
+      }
+      v3 u = (inv_m * mv + inv_m * gf) + v3{E.dt_g[0], E.dt_g[1], E.dt_g[2]};
+      // boundary-condition masks (mpm_elastic.py:227-238)
+      const int bd = E.bound;
+      bool mx = (i < bd && u.x < 0.f) || (i > E.n[0] - bd && u.x > 0.f);
+      bool my = (j < bd && u.y < 0.f) || (j > E.n[1] - bd && u.y > 0.f);
+      bool mz = (k < bd && u.z < 0.f) || (k > E.n[2] - bd && u.z > 0.f);
+      if (E.bc == DT_BC_STICKY_FLOOR && j < bd) mx = my = mz = true;
+      const v3 ub = v3{mx ? 0.f : vb.x, my ? 0.f : vb.y, mz ? 0.f : vb.z};
+      v3 mvb = inv_m * ub;
+      const v3 gfb = inv_m * ub;
+      const float invb = dot(ub, mv + gf);
+      float mb = clampg(-inv_m * inv_m * invb, w.grad_clip);  // clamp_grid on grid_m.grad
+      // contact adjoint
+      v3 curvb = v3{0.f, 0.f, 0.f};
+#pragma unroll
+      for (int q = 0; q < DT_MAX_SENSORS_PER_ENV; ++q) {
+        const int si = E.s_begin + q;
+        if (si >= E.s_end) break;
+        if (cid[q] < 0) continue;
+        const dt_sensor& S = w.sensors[si];
+        const int4 tr = __ldg(tris + S.f_off + cid[q]);
+        const v3 p1 = f4to3(P[tr.x]), p2 = f4to3(P[tr.y]), p3 = f4to3(P[tr.z]);
+        const v3 od = v3{S.out_dir[0], S.out_dir[1], S.out_dir[2]};
+        SdfRes sr = find_sdf(p1, p2, p3, f4to3(VM[tr.x]), f4to3(VM[tr.y]), f4to3(VM[tr.z]), od, p, cur_v);
+        if (!sr.flag) continue;
+        // ext enters grid_f (x dt) and the three sensor vertices (x -1/3)
+        const v3 exs = (f4to3(aExt[tr.x]) + f4to3(aExt[tr.y])) + f4to3(aExt[tr.z]);
+        const v3 eb = w.dt * gfb - third * exs;
+        v3 nb = v3{0.f, 0.f, 0.f}, rb = v3{0.f, 0.f, 0.f};
+        const float sdfb = contact_force_bwd(E, sr.sdf, sr.n, sr.r, eb, nb, rb);
+        // r = mean tri velocity - cur_v
+        const v3 tvb = third * rb;
+        red_add_v4(aVm + tr.x, v3to4(tvb));
+        red_add_v4(aVm + tr.y, v3to4(tvb));
+        red_add_v4(aVm + tr.z, v3to4(tvb));
+        curvb = curvb - rb;
+        // sdf = (p - p1) . n
+        v3 p1b = -sdfb * sr.n;
+        nb = nb + sdfb * (p - p1);
+        // n = sg * nrm / (|nrm| + 1e-10)
+        const v3 e1 = p2 - p1, e2 = p3 - p1;
+        const v3 nrm = cross(e1, e2);
+        const float L = sqrtf(dot(nrm, nrm));
+        const float sg = dot((1.f / (L + 1e-10f)) * nrm, od) < 0.f ? -1.f : 1.f;
+        v3 nrmb = v3{0.f, 0.f, 0.f};
+        if (L > 0.f) {
+          const float D = L + 1e-10f;
+          nrmb = sg * ((1.f / D) * nb - (dot(nb, nrm) / (D * D * L)) * nrm);
+        }
+        const v3 e1b = cross(e2, nrmb), e2b = cross(nrmb, e1);
+        p1b = p1b - (e1b + e2b);
+        red_add_v4(aPos + tr.x, v3to4(p1b));
+        red_add_v4(aPos + tr.y, v3to4(e1b));
+        red_add_v4(aPos + tr.z, v3to4(e2b));
+      }
+      // cur_v = mv / (m + eps)
+      mvb = mvb + inv_m * curvb;
+      mb += -dot(curvb, mv) * inv_m * inv_m;
+      res = make_float4(mvb.x, mvb.y, mvb.z, mb);
+    }
+    aacc[g] = res;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// B3: P2G + constitutive + SVD adjoint; FEM force adjoint
+// ---------------------------------------------------------------------------------------------
+__device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb, int& mat) {
+  const int nb = (f + 1) & 1, cb = f & 1;
+  float4 q[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) q[k] = ldg4(pplane(w, f, k) + p);
+  PRec r;
+  unpack_rec(q, r);
+  // adjoint of F[f+1]
+  const float4 n3 = ld4(padj(w, nb, 3) + p), n4 = ld4(padj(w, nb, 4) + p), n5 = ld4(padj(w, nb, 5) + p);
+  m3 Fpb;
+  Fpb.a[0][0] = n3.w;
+  Fpb.a[0][1] = n4.x;
+  Fpb.a[0][2] = n4.y;
+  Fpb.a[1][0] = n4.z;
+  Fpb.a[1][1] = n4.w;
+  Fpb.a[1][2] = n5.x;
+  Fpb.a[2][0] = n5.y;
+  Fpb.a[2][1] = n5.z;
+  Fpb.a[2][2] = n5.w;
+  const float4 xpart = ld4(padj(w, cb, 0) + p);  // x adjoint from the G2P adjoint
+  const dt_env& E = w.envs[__ldg(w.p_env + p)];
+  int base[3];
+  float fx[3];
+  PRec out;
+  mat = __ldg(w.p_mat + p);
+  mub = lamb = 0.f;
+  if (!particle_base(E, r.x, base, fx)) {
+    // carried unchanged in the forward pass: adjoint passes straight through
+    const float4 a0 = ld4(padj(w, nb, 0) + p), a1 = ld4(padj(w, nb, 1) + p), a2 = ld4(padj(w, nb, 2) + p),
+                 a3 = ld4(padj(w, nb, 3) + p);
+    float4 o[6] = {make_float4(xpart.x, xpart.y, xpart.z, a0.w), a1, a2, a3, n4, n5};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) padj(w, cb, k)[p] = o[k];
+    return;
+  }
+  const dt_material M = w.materials[mat];
+  Stress s;
+  constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s);
+  const float pm = E.p_mass, dx = E.dx;
+  m3 A;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) A.a[i][j] = E.stress_k * s.cauchy.a[i][j] + pm * r.C.a[i][j];
+  // gather the grid adjoint
+  const float4* aacc = reinterpret_cast<const float4*>(w.g_adj_acc);
+  v3 vb = v3{0.f, 0.f, 0.f};
+  m3 Ab = mzero();
+  float fxb[3] = {0.f, 0.f, 0.f};
+  float wts[3][3], dws[3][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      wts[i][d] = bsw(i, fx[d]);
+      dws[i][d] = bsdw(i, fx[d]);
+    }
+#pragma unroll
+  for (int oi = 0; oi < 3; ++oi)
+#pragma unroll
+    for (int oj = 0; oj < 3; ++oj)
+#pragma unroll
+      for (int ok = 0; ok < 3; ++ok) {
+        const float4 gb = __ldg(aacc + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok));
+        const v3 mvb = f4to3(gb);
+        const float W = (wts[oi][0] * wts[oj][1]) * wts[ok][2];
+        const v3 dp = v3{((float)oi - fx[0]) * dx, ((float)oj - fx[1]) * dx, ((float)ok - fx[2]) * dx};
+        const v3 Adp = mvec(A, dp);
+        vb = vb + (W * pm) * mvb;
+#pragma unroll
+        for (int rr = 0; rr < 3; ++rr) {
+          const float mr = rr == 0 ? mvb.x : (rr == 1 ? mvb.y : mvb.z);
+          Ab.a[rr][0] += W * mr * dp.x;
+          Ab.a[rr][1] += W * mr * dp.y;
+          Ab.a[rr][2] += W * mr * dp.z;
+        }
+        const float Wb = dot(mvb, pm * r.v + Adp) + pm * gb.w;
+        const v3 Atm = mTvec(A, mvb);  // dpos adjoint / W
+        fxb[0] += Wb * (dws[oi][0] * wts[oj][1] * wts[ok][2]) - dx * W * Atm.x;
+        fxb[1] += Wb * (wts[oi][0] * dws[oj][1] * wts[ok][2]) - dx * W * Atm.y;
+        fxb[2] += Wb * (wts[oi][0] * wts[oj][1] * dws[ok][2]) - dx * W * Atm.z;
+      }
+  // affine = stress_k * cauchy + p_mass * C
+  m3 Cb = mscale(pm, Ab);
+  const m3 G = mscale(E.stress_k, Ab);  // cauchy adjoint
+  m3 Ub = mzero(), Vb = mzero(), Rb = mzero();
+  v3 sb = v3{0.f, 0.f, 0.f};
+  float Jb;
+  if (M.model == DT_MODEL_NEOHOOKEAN) {
+    // cauchy = mu (Fp Fp^T - I) + lam log(J) I
+    Fpb = madd(Fpb, mscale(M.mu, mmul(madd(G, mT(G)), s.Fp)));
+    const float trG = mtrace(G);
+    Jb = M.lam * trG / s.J;
+    mub = mdot(G, msub(mmulT(s.Fp, s.Fp), meye()));
+    lamb = logf(s.J) * trG;
+  } else {
+    // cauchy = 2 mu (Fp - R) Fp^T + lam J (J - 1) I
+    const m3 D = msub(s.Fp, s.R);
+    Fpb = madd(Fpb, mscale(2.f * M.mu, madd(mmul(G, s.Fp), mTmul(G, D))));
+    Rb = mscale(-2.f * M.mu, mmul(G, s.Fp));  // R = U V^T, handled inside svd_grad
+    const float trG = mtrace(G);
+    Jb = M.lam * (2.f * s.J - 1.f) * trG;
+    mub = 2.f * mdot(G, mmulT(D, s.Fp));
+    lamb = s.J * (s.J - 1.f) * trG;
+  }
+  m3 Fnb;
+  if (M.model == DT_MODEL_COROTATED) {
+    sb = sb + Jb * v3{s.sig.y * s.sig.z, s.sig.x * s.sig.z, s.sig.x * s.sig.y};
+    Fnb = Fpb;
+  } else {
+    Fpb = madd(Fpb, mscale(Jb, mcof(s.Fp)));  // J = det(Fp)
+    if (M.model == DT_MODEL_VON_MISES && s.yield) {
+      // Fp = U diag(exp(eps')) V^T (mpm_plastic.py:162-165)
+      const float sg[3] = {s.sig.x, s.sig.y, s.sig.z};
+      float ep[3], eh[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) ep[d] = logf(fmaxf(sg[d], 0.05f));
+      const float mean = ((ep[0] + ep[1]) + ep[2]) / 3.f;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) eh[d] = ep[d] - mean;
+      const float nrm = sqrtf(((eh[0] * eh[0] + eh[1] * eh[1]) + eh[2] * eh[2]) + 1e-8f);
+      const float dg = nrm - M.yield_stress / (2.f * M.mu);
+      const float rr = dg / nrm;
+      float ex[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) ex[d] = expf(ep[d] - rr * eh[d]);
+      const m3 UtFV = mmul(mTmul(s.U, Fpb), s.V);
+      m3 Ue = s.U, Ve = s.V;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          Ue.a[i][d] *= ex[d];
+          Ve.a[i][d] *= ex[d];
+        }
+      Ub = madd(Ub, mmul(Fpb, Ve));   // Fpb V diag(e)
+      Vb = madd(Vb, mTmul(Fpb, Ue));  // Fpb^T U diag(e)
+      float epb[3], ehb[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) epb[d] = UtFV.a[d][d] * ex[d];
+      // eps' = eps - rr * eh,  rr = 1 - ys / (2 mu nrm)
+      float rrb = 0.f;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        ehb[d] = -rr * epb[d];
+        rrb -= epb[d] * eh[d];
+      }
+      const float nrmb = rrb * M.yield_stress / (2.f * M.mu * nrm * nrm);
+      mub += rrb * M.yield_stress / (2.f * M.mu * M.mu * nrm);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) ehb[d] += nrmb * eh[d] / nrm;
+      const float mb_ = ((ehb[0] + ehb[1]) + ehb[2]) / 3.f;
+      float sbv[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float eb_ = epb[d] + ehb[d] - mb_;
+        sbv[d] = sg[d] > 0.05f ? eb_ / sg[d] : 0.f;
+      }
+      sb = sb + v3{sbv[0], sbv[1], sbv[2]};
+      Fnb = mzero();
+    } else {
+      Fnb = Fpb;
+    }
+  }
+  if (M.model != DT_MODEL_NEOHOOKEAN) Fnb = madd(Fnb, svd_grad(s.U, s.sig, s.V, Ub, sb, Vb, Rb, w.svd_grad_mode));
+  // F_new = (I + dt C) F
+  m3 Ad = meye();
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Ad.a[i][j] += w.dt * r.C.a[i][j];
+  out.F = mTmul(Ad, Fnb);
+  Cb = madd(Cb, mscale(w.dt, mmulT(Fnb, r.F)));
+  out.C = Cb;
+  out.v = vb;
+  out.x = v3{xpart.x, xpart.y, xpart.z} + E.inv_dx * v3{fxb[0], fxb[1], fxb[2]};
+  float4 o[6];
+  pack_rec(out, o);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) padj(w, cb, k)[p] = o[k];
+}
+
+__device__ void fem_tet_bwd(const dt_world& w, int f, int t) {
+  const int cb = f & 1;
+  const size_t V = (size_t)w.n_verts;
+  const int4 tv = __ldg(reinterpret_cast<const int4*>(w.tets) + t);
+  const dt_sensor& S = w.sensors[__ldg(w.tet_sensor + t)];
+  const float4* Bp = reinterpret_cast<const float4*>(w.tet_B) + 3 * (size_t)t;
+  m3 B;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    float4 row = __ldg(Bp + r);
+    B.a[r][0] = row.x;
+    B.a[r][1] = row.y;
+    B.a[r][2] = row.z;
+  }
+  const float4* P = vframe(w.v_pos, w, f);
+  const v3 a = f4to3(P[tv.x]), b = f4to3(P[tv.y]), c = f4to3(P[tv.z]), d = f4to3(P[tv.w]);
+  m3 D;
+  const v3 cols[3] = {a - d, b - d, c - d};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    D.a[0][k] = cols[k].x;
+    D.a[1][k] = cols[k].y;
+    D.a[2][k] = cols[k].z;
+  }
+  const float detD = mdet(D);
+  const float Vi = fabsf(detD) / 6.f;
+  const m3 Fe = mmul(D, B);
+  const float J = mdet(Fe);
+  const float IC = mdot(Fe, Fe);
+  const m3 cof = mcof(Fe);
+  const float k1 = S.mu * (1.f - 1.f / (IC + 1.f));
+  const float k2 = S.lam * (J - S.alpha);
+  m3 Pk;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Pk.a[i][j] = k1 * Fe.a[i][j] + k2 * cof.a[i][j];
+  const m3 H = mmulT(Pk, B);
+  const float sc = -Vi * S.dt_over_m;
+  // velocity increments h_k = sc H[:,k] to v_k, -sum to v_3
+  const float4* aVm = reinterpret_cast<const float4*>(w.v_adj_velmid);
+  const v3 g3 = f4to3(aVm[tv.w]);
+  const v3 hb[3] = {f4to3(aVm[tv.x]) - g3, f4to3(aVm[tv.y]) - g3, f4to3(aVm[tv.z]) - g3};
+  m3 Hb;
+  float scb = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    Hb.a[0][k] = sc * hb[k].x;
+    Hb.a[1][k] = sc * hb[k].y;
+    Hb.a[2][k] = sc * hb[k].z;
+    scb += dot(hb[k], mcol(H, k));
+  }
+  const float Vib = -S.dt_over_m * scb;
+  const m3 Pb = mmul(Hb, B);  // H = P B^T
+  // P = k1 F + k2 cof(F)
+  m3 Fb = mscale(k1, Pb);
+  const float k1b = mdot(Pb, Fe), k2b = mdot(Pb, cof);
+  {
+    const v3 f0 = mcol(Fe, 0), f1 = mcol(Fe, 1), f2 = mcol(Fe, 2);
+    const v3 p0 = mcol(Pb, 0), p1 = mcol(Pb, 1), p2 = mcol(Pb, 2);
+    const v3 g0 = cross(p1, f2) + cross(f1, p2);
+    const v3 g1 = cross(f2, p0) + cross(p2, f0);
+    const v3 g2 = cross(p0, f1) + cross(f0, p1);
+    const v3 gg[3] = {g0, g1, g2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      Fb.a[0][k] += k2 * gg[k].x;
+      Fb.a[1][k] += k2 * gg[k].y;
+      Fb.a[2][k] += k2 * gg[k].z;
+    }
+  }
+  const float ICb = k1b * S.mu / ((IC + 1.f) * (IC + 1.f));
+  const float Jb = S.lam * k2b;
+  Fb = madd(Fb, madd(mscale(2.f * ICb, Fe), mscale(Jb, cof)));
+  m3 Db = mmulT(Fb, B);  // F = D B
+  const float sgn = detD < 0.f ? -1.f : (detD > 0.f ? 1.f : 0.f);
+  Db = madd(Db, mscale(Vib * sgn / 6.f, mcof(D)));
+  const v3 ab = mcol(Db, 0), bb = mcol(Db, 1), cbv = mcol(Db, 2);
+  float4* aPos = reinterpret_cast<float4*>(w.v_adj_pos) + cb * V;
+  red_add_v4(aPos + tv.x, v3to4(ab));
+  red_add_v4(aPos + tv.y, v3to4(bb));
+  red_add_v4(aPos + tv.z, v3to4(cbv));
+  red_add_v4(aPos + tv.w, v3to4(-((ab + bb) + cbv)));
+}
+
+__global__ void __launch_bounds__(NT) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v) {
+  int b = blockIdx.x;
+  if (b < nb_p) {
+    const int p = b * NT + threadIdx.x;
+    float mub = 0.f, lamb = 0.f;
+    int mat = -1;
+    if (p < w.n_particles) p2g_bwd(w, f, p, mub, lamb, mat);
+    // material grads: warp-aggregate when the warp shares one material
+    const int m0 = __shfl_sync(0xffffffffu, mat, 0);
+    const bool same = __all_sync(0xffffffffu, mat == m0 || mat < 0);
+    if (same) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        mub += __shfl_xor_sync(0xffffffffu, mub, o);
+        lamb += __shfl_xor_sync(0xffffffffu, lamb, o);
+      }
+      if ((threadIdx.x & 31) == 0 && m0 >= 0) {
+        atomicAdd(w.mat_adj + 4 * m0 + 0, mub);
+        atomicAdd(w.mat_adj + 4 * m0 + 1, lamb);
+      }
+    } else if (mat >= 0) {
+      atomicAdd(w.mat_adj + 4 * mat + 0, mub);
+      atomicAdd(w.mat_adj + 4 * mat + 1, lamb);
+    }
+    return;
+  }
+  b -= nb_p;
+  if (b < nb_t) {
+    const int t = b * NT + threadIdx.x;
+    if (t < w.n_tets) fem_tet_bwd(w, f, t);
+    return;
+  }
+  b -= nb_t;
+  if (b < nb_v) {
+    const int i = b * NT + threadIdx.x;
+    if (i < w.n_verts)
+      reinterpret_cast<float4*>(w.v_adj_vel)[(size_t)(f & 1) * w.n_verts + i] =
+          reinterpret_cast<const float4*>(w.v_adj_velmid)[i];
+  }
+}
+
+inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
+
+}  // namespace
 
 extern "C" {
 
+int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t stream) {
+  if (!w || f < 0 || f + 1 >= w->n_frames || stage < 0 || stage > 3) return DT_ERR_ARG;
+  const int ng = w->n_blocks < 152 * 16 ? w->n_blocks : 152 * 16;
+  const int nb_p = cdiv(w->n_particles, NT), nb_v = cdiv(w->n_verts, NT), nb_t = cdiv(w->n_tets, NT);
+  switch (stage) {
+    case 0:
+      if (ng > 0) k_bwd_restore<<<ng, GRID_NT, 0, stream>>>(*w, f);
+      break;
+    case 1:
+      if (nb_p + nb_v) k_bwd_g2p_fem<<<nb_p + nb_v, NT, 0, stream>>>(*w, f, nb_p, nb_v);
+      break;
+    case 2:
+      if (ng > 0) k_bwd_grid<<<ng, GRID_NT, 0, stream>>>(*w, f);
+      break;
+    default:
+      if (nb_p + nb_t + nb_v) k_bwd_p2g_fem<<<nb_p + nb_t + nb_v, NT, 0, stream>>>(*w, f, nb_p, nb_t, nb_v);
+  }
+  return launched();
+}
+
 int dt_substep_bwd(const dt_world* w, int f, cudaStream_t stream) {
-  (void)stream;
   if (!w || f < 0 || f + 1 >= w->n_frames) return DT_ERR_ARG;
-  return DT_ERR_ARG;
+  for (int s = 0; s < 4; ++s) {
+    const int rc = dt_substep_bwd_stage(w, f, s, stream);
+    if (rc) return rc;
+  }
+  return DT_OK;
 }
 
 }  // extern "C"

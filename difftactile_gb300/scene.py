@@ -30,9 +30,13 @@ class Material:
     nu: float
     yield_stress: float = 0.0
     model: int = MODEL_COROTATED
+    mu: float | None = None    # explicit Lame parameters override E, nu (tasks set them directly,
+    lam: float | None = None   # grasp_plastic.py:65-68)
 
     @property
     def mu_lam(self):
+        if self.mu is not None and self.lam is not None:
+            return float(self.mu), float(self.lam)
         return lame(self.E, self.nu)
 
 

@@ -33,7 +33,8 @@ class World:
     """Flat device layout of ``envs`` (list of EnvSpec) with ``n_frames`` frames per step."""
 
     def __init__(self, envs: list[EnvSpec], n_frames: int, dt: float, device="cuda", tape_blocks: int | None = None,
-                 grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True):
+                 grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True,
+                 svd_grad_mode: int = 0):
         self.lib = N.load()
         self.device = torch.device(device)
         self.specs = envs
@@ -199,6 +200,7 @@ class World:
         w.n_verts, w.n_tets, w.n_tris = V, self.n_tets, self.n_tris
         w.n_nodes, w.n_blocks, w.n_frames, w.tape_blocks = NN, NB, Fn, TB
         w.dt, w.grad_clip, w.svd_sweeps = self.dt, float(grad_clip), int(svd_sweeps)
+        w.svd_grad_mode = int(svd_grad_mode)
         self.w = w
         self.wp = C.pointer(w)
 
@@ -227,7 +229,7 @@ class World:
     def set_particles(self, frame, x=None, v=None, C=None, F=None):
         rec = self.t["p_state"][frame].permute(1, 0, 2).reshape(self.n_particles, 24)  # view? no: permute copy
         rec = rec.clone()
-        put = lambda a: torch.as_tensor(np.asarray(a, np.float32) if not torch.is_tensor(a) else a,  # noqa: E731
+        put = lambda a: torch.as_tensor(np.array(a, np.float32) if not torch.is_tensor(a) else a,  # noqa: E731
                                         dtype=F32, device=self.device)
         if x is not None:
             rec[:, 0:3] = put(x).reshape(-1, 3)[self._perm_t]

@@ -164,8 +164,15 @@ typedef struct dt_world {
   float dt;
   float grad_clip;               /* backward clamp of grid-mass and sensor grads; 0 disables */
   int svd_sweeps;                /* cyclic Jacobi sweeps of the 3x3 SVD (4 is enough for fp32) */
-  int pad_;
+  int svd_grad_mode;             /* DT_SVDGRAD_* */
 } dt_world;
+
+/* SVD adjoint of the rotation R = U V^T used by the corotated stress:
+ * STABLE evaluates the reference formula's rotation term in the algebraically equal form
+ * (M - M^T)_ij / (s_i + s_j), M = U^T dR V (exact in floating point near F = I);
+ * REFERENCE evaluates mpm_elastic.py:158-173 literally, ff_ij = 1/clamp(s_j^2 - s_i^2, 1e-8). */
+#define DT_SVDGRAD_STABLE 0
+#define DT_SVDGRAD_REFERENCE 1
 
 /* ---- introspection ---- */
 int dt_abi_version(void);
@@ -203,6 +210,12 @@ int dt_copy_frame(const dt_world* w, int src, int dst, cudaStream_t stream);
  * adjoint of frame f in p_adj[f&1], v_adj_*[f&1]; accumulates v_adj_cv[f], v_adj_cv[f+1] and
  * mat_adj.  The forward tape of frame f (p_state[f], grid tape f, FEM frame f) must be intact. */
 int dt_substep_bwd(const dt_world* w, int f, cudaStream_t stream);
+
+/* dt_substep_bwd split into its four launches, the per-kernel .grad calls of update_grad
+ * (grasp_plastic.py:167-178): stage 0 restores frame f's grid velocities from the tape; stage 1 is
+ * fem.update2.grad + g2p.grad; stage 2 is grid_op.grad + clamp_grid + collision.grad; stage 3 is
+ * fem.update.grad + p2g.grad + svd_grad + compute_new_F.grad.  Run stages 0..3 in order. */
+int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t stream);
 
 /* Zero the adjoint buffers (p_adj, v_adj_*, mat_adj, g_adj_*) before a backward sweep. */
 int dt_adj_clear(const dt_world* w, cudaStream_t stream);

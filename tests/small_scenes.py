@@ -16,8 +16,10 @@ def elastic_cube(n=32, side_cells=6, ppc=8, seed=0, v=(0.0, 0.0, 0.0), model=S.M
 
 def pad_over_box(n=32, box_cells=(6, 4, 6), pad=(6, 6, 2), ppc=8, seed=1, model=S.MODEL_VON_MISES, yield_stress=5.0,
                  two_pads=False):
-    """An elastoplastic box resting low in the domain with a hex pad whose contact surface is half a
-    cell above the box top, so that grid nodes above the box start inside the pad."""
+    """An elastoplastic box resting low in the domain with a hex pad whose contact surface is 0.37
+    cell above the box top, so that grid nodes above the box start inside the pad.  The offset is not
+    a multiple of half a cell: a surface through node centres ((j + 0.5) dx) would put nodes exactly
+    at sdf = 0, where the contact force has a kink and finite differences are meaningless."""
     dx = 1.0 / n
     lo = np.array([n / 2 - box_cells[0] / 2, 4, n / 2 - box_cells[2] / 2]) * dx
     hi = lo + np.array(box_cells) * dx
@@ -26,10 +28,10 @@ def pad_over_box(n=32, box_cells=(6, 4, 6), pad=(6, 6, 2), ppc=8, seed=1, model=
     v = 0.02 * rng.standard_normal(x.shape).astype(np.float32)
     sensors = []
     top = hi[1]
-    sp = S.hex_pad_sensor([0.5 + 0.13 * dx, top + 0.5 * dx, 0.5 - 0.21 * dx], nx=pad[0], nz=pad[1], ny=pad[2], h=dx)
+    sp = S.hex_pad_sensor([0.5 + 0.13 * dx, top + 0.37 * dx, 0.5 - 0.21 * dx], nx=pad[0], nz=pad[1], ny=pad[2], h=dx)
     sensors.append(sp)
     if two_pads:
-        sp2 = S.hex_pad_sensor([0.5 - 0.07 * dx, top + 0.9 * dx, 0.5 + 0.11 * dx], nx=pad[0] - 2, nz=pad[1] - 2, ny=pad[2],
+        sp2 = S.hex_pad_sensor([0.5 - 0.07 * dx, top + 0.83 * dx, 0.5 + 0.11 * dx], nx=pad[0] - 2, nz=pad[1] - 2, ny=pad[2],
                                h=dx)
         sensors.append(sp2)
     return S.EnvSpec(x=x, v=v, materials=[S.Material(5e3, 0.3, yield_stress, model)], n_grid=(n, n, n), dx=dx,
