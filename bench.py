@@ -1,0 +1,327 @@
+"""Benchmark: forward+backward particle-substeps/s of the differentiable DiffTactile substep on one
+GB300 (replicas on N GPUs under torchrun).
+
+One bench step = one training iteration of the sensor-press task: 100 control steps x 20 substeps
+forward (device checkpoint of every step start), then the backward sweep (recompute of each step's
+substep tape + adjoint substeps) down to the action gradients.  The unit counts each particle
+advanced one substep forward and back-propagated once: n_particles x 100 x 20 per bench step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="sensor_press", choices=["sensor_press", "batched_population"])
+    ap.add_argument("--horizon", type=int, default=None, help="control steps (default: the config's)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def make_config(name, horizon):
+    from difftactile_gb300 import configs
+    if name == "sensor_press":
+        return configs.sensor_press(n_steps=horizon or 100)
+    return configs.batched_population(n_steps=horizon or 200)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (clocks, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# algorithmic bytes per unit of each fused launch (documented in the design doc)
+BYTES = {
+    ("fwd", 0): {"particle": 96 + 36, "node": 16, "tet": 148, "tri": 68},
+    ("fwd", 1): {"node": 96},
+    ("fwd", 2): {"particle": 16 + 60, "node": 16, "vert": 176},
+    ("bwd", 0): {"node": 32},
+    ("bwd", 1): {"particle": 16 + 64 + 16, "node": 32, "vert": 128},
+    ("bwd", 2): {"node": 80},
+    ("bwd", 3): {"particle": 96 + 48 + 96, "node": 16, "tet": 196, "vert": 32},
+}
+NAMES = {("fwd", 0): "k_fwd_p2g_fem", ("fwd", 1): "k_fwd_grid", ("fwd", 2): "k_fwd_g2p_fem",
+         ("bwd", 0): "k_bwd_restore", ("bwd", 1): "k_bwd_g2p_fem", ("bwd", 2): "k_bwd_grid",
+         ("bwd", 3): "k_bwd_p2g_fem"}
+
+
+def algo_bytes(key, units):
+    return sum(b * units.get(u, 0) for u, b in BYTES[key].items())
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from difftactile_gb300.trajectory import PoseTrajectory
+    from difftactile_gb300.world import World
+
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world_size > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world_size > 1:
+            dist.barrier()
+
+    cfg = make_config(args.config, args.horizon)
+    w = World(cfg.envs, n_frames=cfg.substeps + 1, dt=cfg.dt, device=dev)
+    traj = PoseTrajectory(w, cfg.n_steps, cfg.ckpt_every, cfg.loss_terms)
+    acts = torch.as_tensor(cfg.actions, dtype=torch.float64, device=dev)
+    t = w.t
+    init = [t["p_state"][0].clone(), t["v_pos"][0].clone(), t["v_vel"][0].clone(), t["v_vpos"][0].clone()]
+
+    def reset():
+        t["p_state"][0].copy_(init[0])
+        t["v_pos"][0].copy_(init[1])
+        t["v_vel"][0].copy_(init[2])
+        t["v_vpos"][0].copy_(init[3])
+
+    def iteration():
+        reset()
+        loss = traj.forward(acts)
+        g = traj.backward()
+        return loss, g
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # ---- per-kernel breakdown (untimed): probe each launch over one full iteration ----
+    iteration()
+    torch.cuda.synchronize()
+    breakdown = {}
+    for key in NAMES:
+        w.set_probe(*key)
+        iteration()
+        ms, n = w.probe_ms()
+        breakdown[key] = (ms, n)
+    w.set_probe(None)
+    tot = sum(ms * n for ms, n in breakdown.values())
+    dom = max(breakdown, key=lambda k: breakdown[k][0] * breakdown[k][1])
+
+    for _ in range(max(args.warmup, 0)):
+        iteration()
+    torch.cuda.synchronize()
+    if w.error_word():
+        raise RuntimeError(f"device error word {w.error_word()} during warm-up")
+
+    # ---- timed region ----
+    clocks = Clocks(local)
+    w.set_probe(*dom)
+    traj.launches = 0
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()  # L2 flush between timed iterations (256 MiB > 129 MB L2)
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        loss, g = iteration()
+        e1.record()
+        torch.cuda.synchronize()
+        barrier()
+        times.append(e0.elapsed_time(e1))
+    dom_ms, dom_n = w.probe_ms()
+    w.set_probe(None)
+    clk = clocks.stop()
+    launches_per_iter = traj.launches // max(args.steps, 1) + 2  # + loss readout/adjoint seeds
+    ms = sum(times) / len(times)
+    if world_size > 1:
+        tm = torch.tensor([ms], device=dev)
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        ms = float(tm.item())
+    units = cfg.n_particles * cfg.n_steps * cfg.substeps
+    value = units * world_size / (ms / 1e3)
+
+    # ---- roofline of the dominant kernel ----
+    cnt = t["tape_bcount"].clamp(max=w.tape_blocks).double().mean().item()
+    unit_counts = {"particle": w.n_particles, "node": 64 * cnt, "tet": w.n_tets, "tri": w.n_tris,
+                   "vert": w.n_verts}
+    peak, peak_kind = peaks()
+    ab = algo_bytes(dom, unit_counts)
+    achieved = ab / (dom_ms / 1e3) / 1e9
+
+    out = {"metric": "fwd+bwd particle-substeps/s", "value": value, "unit": "particle-substeps/s",
+           "n_gpus": world_size, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded scene generators)",
+           "config": {"workload": cfg.name, "particles": cfg.n_particles, "control_steps": cfg.n_steps,
+                      "substeps": cfg.substeps, "grid": list(cfg.envs[0].n_grid), "envs": len(cfg.envs),
+                      "fem_tets": w.n_tets, "fem_nodes": w.n_verts, "surface_tris": w.n_tris,
+                      "checkpoint_every": cfg.ckpt_every, "l2": "flushed between timed iterations (256 MiB write)",
+                      "parallelism": f"replicas x{world_size}"},
+           "gpu_launches": launches_per_iter * args.steps,
+           "roofline": {"kernel": NAMES[dom], "bound": "hbm", "achieved": achieved, "peak": peak,
+                        "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                        "algorithmic_bytes_per_launch": ab, "launch_ms": dom_ms, "launches_timed": dom_n},
+           "kernel_breakdown": {NAMES[k]: {"ms_per_launch": v[0], "launches": v[1],
+                                           "share": v[0] * v[1] / tot} for k, v in breakdown.items()},
+           "loss": float(loss.item()), "grad_norm": float(g.norm().item())}
+    if clk:
+        out["clocks"] = clk
+
+    # ---- end to end through the public API with host buffers ----
+    if not args.no_e2e:
+        h_act = torch.as_tensor(cfg.actions, dtype=torch.float32).pin_memory()
+        xs = np.concatenate([e.x for e in cfg.envs], 0)
+        h_x = torch.as_tensor(xs, dtype=torch.float32).pin_memory()
+        h_v = torch.zeros_like(h_x).pin_memory()
+        e2e = []
+        for i in range(args.steps + 1):
+            flush.zero_()
+            torch.cuda.synchronize()
+            barrier()
+            t0 = time.perf_counter()
+            d_act = h_act.to(dev, non_blocking=True)
+            d_x = h_x.to(dev, non_blocking=True)
+            d_v = h_v.to(dev, non_blocking=True)
+            reset()
+            w.set_particles(0, x=d_x, v=d_v)
+            loss = traj.forward(d_act.double())
+            g = traj.backward()
+            res = torch.cat([loss.double(), g.reshape(-1)]).cpu()
+            t1 = time.perf_counter()
+            if i > 0:
+                e2e.append(t1 - t0)
+        e_ms = 1e3 * sum(e2e) / len(e2e)
+        if world_size > 1:
+            tm = torch.tensor([e_ms], device=dev)
+            dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+            e_ms = float(tm.item())
+        out["e2e"] = {"value": units * world_size / (e_ms / 1e3), "unit": "particle-substeps/s",
+                      "ms_per_step": e_ms,
+                      "h2d_bytes_per_step": int(h_act.numel() * 4 + h_x.numel() * 4 + h_v.numel() * 4),
+                      "d2h_bytes_per_step": int(res.numel() * 8)}
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(cfg, threads=os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(out))
+    if world_size > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(cfg, threads, target_s=15.0):
+    """The oracle (CPU restatement of the reference step) on the host cores: a bounded sample of
+    whole substeps of the same scene, forward + backward."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    env = cfg.envs[0]
+    o = O.Oracle(env, cfg.dt, np.float32, n_threads=threads)
+    st = o.initial_state()
+    sp = env.sensors[0] if env.sensors else None
+    cv = [np.zeros((len(s.verts), 3), np.float32) for s in env.sensors]
+    done, t0 = 0, time.perf_counter()
+    fwd_only = not hasattr(o, "substep_bwd")
+    while time.perf_counter() - t0 < target_s and done < cfg.substeps:
+        st1, _ = o.substep(st, cv=cv, cv1=cv)
+        if not fwd_only:
+            o.substep_bwd(st, st1, cv)
+        st = st1
+        done += 1
+    dt_ = time.perf_counter() - t0
+    del sp
+    return {"value": env.n_particles * done / dt_, "unit": "particle-substeps/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{done} substeps of env 0 of {cfg.name} ({env.n_particles} particles)"
+                      + (" forward only" if fwd_only else " forward+backward")}
+
+
+def run_reference(args):
+    """The reference's CPU path (its Taichi CPU backend is not installable here; the oracle, a C++
+    restatement of the same kernels, runs on all host cores instead)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfg = make_config(args.config, args.horizon)
+    threads = os.cpu_count() or 1
+    for _ in range(max(args.warmup, 0)):
+        cpu_baseline(cfg, threads, target_s=2.0)
+    vals = [cpu_baseline(cfg, threads, target_s=10.0) for _ in range(max(args.steps, 1))]
+    v = sum(x["value"] for x in vals) / len(vals)
+    units = cfg.n_particles * cfg.n_steps * cfg.substeps
+    out = {"impl": "reference", "metric": "fwd+bwd particle-substeps/s", "value": v, "unit": "particle-substeps/s",
+           "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": units / v * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded scene generators)",
+           "config": {"workload": cfg.name, "particles": cfg.n_particles, "control_steps": cfg.n_steps,
+                      "substeps": cfg.substeps},
+           "cpu_baseline": dict(vals[-1], value=v),
+           "e2e": {"value": v, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

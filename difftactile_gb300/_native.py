@@ -70,6 +70,7 @@ SIGNATURES = {
     "dt_sizeof_material": (C.c_size_t, []),
     "dt_step_begin": (C.c_int, [_W, _P]),
     "dt_substep_fwd": (C.c_int, [_W, C.c_int, _P]),
+    "dt_substep_fwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),
     "dt_p2g": (C.c_int, [_W, C.c_int, _P]),
     "dt_fem_update": (C.c_int, [_W, C.c_int, _P]),
     "dt_grid_op": (C.c_int, [_W, C.c_int, _P]),
@@ -81,6 +82,10 @@ SIGNATURES = {
     "dt_adj_clear": (C.c_int, [_W, _P]),
     "dt_com": (C.c_int, [_W, C.c_int, _P, _P]),
     "dt_com_bwd": (C.c_int, [_W, C.c_int, _P, _P]),
+    "dt_pose_control_vel": (C.c_int, [_W, C.c_int, _P, C.c_float, _P]),
+    "dt_pose_control_vel_bwd": (C.c_int, [_W, C.c_int, _P, C.c_float, _P, _P]),
+    "dt_marker_loss": (C.c_int, [_W, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
+    "dt_marker_loss_bwd": (C.c_int, [_W, C.c_int, C.c_int, C.c_int, _P, C.c_float, _P]),
 }
 
 ERRORS = {0: "DT_OK", -1: "DT_ERR_ARG", -2: "DT_ERR_LAUNCH", -3: "DT_ERR_CAPACITY"}

@@ -465,6 +465,21 @@ int dt_substep_fwd(const dt_world* w, int f, cudaStream_t stream) {
   return launch_l3(w, f, true, true, stream);
 }
 
+int dt_substep_fwd_stage(const dt_world* w, int f, int stage, cudaStream_t stream) {
+  int rc = check(w, f);
+  if (rc) return rc;
+  switch (stage) {
+    case 0:
+      return launch_l1(w, f, true, true, stream);
+    case 1:
+      return launch_l2(w, f, stream);
+    case 2:
+      return launch_l3(w, f, true, true, stream);
+    default:
+      return DT_ERR_ARG;
+  }
+}
+
 int dt_p2g(const dt_world* w, int f, cudaStream_t stream) {
   int rc = check(w, f);
   return rc ? rc : launch_l1(w, f, true, false, stream);

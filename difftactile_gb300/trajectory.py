@@ -1,0 +1,168 @@
+"""Differentiable rollouts with device checkpoints: forward keeps the start state of every k-th
+control step; backward recomputes each segment, then each step's substep tape, and runs the
+adjoint substeps in reverse.
+
+The reference keeps the start of every step in host RAM (memory_to_cache / memory_from_cache,
+object_model/mpm_elastic.py:300-320, sensor_model/fem_sensor.py:501-521) and recomputes the
+substeps of one step during the backward sweep (tasks/grasp_plastic.py:594-648); that is k = 1.
+Here the checkpoints stay in HBM and k is a parameter (k = 50 for the long-horizon task).
+
+Actions are per step and per pose-controlled sensor: (d_pos[3], d_ori[3]) as in
+set_pose_control (fem_sensor.py:229-245): rot_v = d_ori dt S, trans_v = d_pos dt S, the step
+transform dtrans_h = T_world eul2mat(rot_v, trans_v) T_world^-1 drives the base layer through the
+control velocity (fem_sensor.py:259-266).  The 4x4 algebra runs in float64 torch on the device;
+the per-vertex control velocities and everything after them are CUDA kernels.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .world import World
+
+
+def eul2mat_zyx(rot_deg: torch.Tensor, trans: torch.Tensor) -> torch.Tensor:
+    """Batched 4x4 transforms with R = Rz Ry Rx (fem_sensor.py:196-210); [..., 3] -> [..., 4, 4]."""
+    r = torch.deg2rad(rot_deg)
+    cx, cy, cz = torch.cos(r[..., 0]), torch.cos(r[..., 1]), torch.cos(r[..., 2])
+    sx, sy, sz = torch.sin(r[..., 0]), torch.sin(r[..., 1]), torch.sin(r[..., 2])
+    o, z = torch.ones_like(cx), torch.zeros_like(cx)
+    Rx = torch.stack([o, z, z, z, cx, -sx, z, sx, cx], -1).reshape(*cx.shape, 3, 3)
+    Ry = torch.stack([cy, z, sy, z, o, z, -sy, z, cy], -1).reshape(*cx.shape, 3, 3)
+    Rz = torch.stack([cz, -sz, z, sz, cz, z, z, z, o], -1).reshape(*cx.shape, 3, 3)
+    R = Rz @ Ry @ Rx
+    top = torch.cat([R, trans[..., :, None]], -1)
+    bottom = torch.zeros(*cx.shape, 1, 4, dtype=R.dtype, device=R.device)
+    bottom[..., 0, 3] = 1
+    return torch.cat([top, bottom], -2)
+
+
+class PoseTrajectory:
+    """T control steps x S substeps of a World whose sensors are pose-controlled.
+
+    ``loss_terms``: list of (sensor, layer, target [nv,3]) marker-displacement terms read at the
+    final frame.
+    """
+
+    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=()):
+        self.w = world
+        self.T = int(n_steps)
+        self.S = world.n_frames - 1
+        self.k = max(1, int(ckpt_every))
+        dev = world.device
+        self.n_ck = (self.T + self.k - 1) // self.k
+        Np, V = world.n_particles, world.n_verts
+        self.ck_p = torch.zeros((self.n_ck, 6, Np, 4), device=dev)
+        self.ck_v = torch.zeros((self.n_ck, 3, V, 4), device=dev)
+        if self.k > 1:
+            self.seg_p = torch.zeros((self.k, 6, Np, 4), device=dev)
+            self.seg_v = torch.zeros((self.k, 3, V, 4), device=dev)
+        self.inv_T = 1.0 / (world.dt * self.S)
+        self.TW = []
+        for sp in world.sensor_specs:
+            M = sp.trans_world if sp.trans_world is not None else np.eye(4)
+            self.TW.append(torch.as_tensor(M, dtype=torch.float64, device=dev))
+        self.loss_terms = []
+        for s, layer, target in loss_terms:
+            tg = torch.zeros((world.sensor_rows[s].nv, 4), device=dev)
+            tg[:, :3] = torch.as_tensor(np.asarray(target), dtype=torch.float32, device=dev)
+            self.loss_terms.append((s, int(layer), tg))
+        self.loss = torch.zeros(1, device=dev)
+        self.Ab = None
+        self.Ab_bar = None
+        self.launches = 0
+
+    # ------------------------------------------------------------------ state save / load
+    def _save(self, P, Vv, i):
+        t = self.w.t
+        P[i].copy_(t["p_state"][0])
+        Vv[i, 0].copy_(t["v_pos"][0])
+        Vv[i, 1].copy_(t["v_vel"][0])
+        Vv[i, 2].copy_(t["v_vpos"][0])
+
+    def _load(self, P, Vv, i):
+        t = self.w.t
+        t["p_state"][0].copy_(P[i])
+        t["v_pos"][0].copy_(Vv[i, 0])
+        t["v_vel"][0].copy_(Vv[i, 1])
+        t["v_vpos"][0].copy_(Vv[i, 2])
+
+    # ------------------------------------------------------------------ actions
+    def step_transforms(self, actions: torch.Tensor) -> torch.Tensor:
+        """actions [T, n_sensors, 6] (float64) -> Ab [T, n_sensors, 12] (float64, differentiable)."""
+        S = self.S
+        out = []
+        for s in range(self.w.n_sensors):
+            a = actions[:, s]
+            M = eul2mat_zyx(a[:, 3:6] * self.w.dt * S, a[:, 0:3] * self.w.dt * S)
+            TW = self.TW[s]
+            D = TW @ M @ torch.linalg.inv(TW)
+            out.append(D[:, :3, :].reshape(-1, 12))
+        return torch.stack(out, 1)
+
+    # ------------------------------------------------------------------ one control step
+    def _step(self, t, copy_end=True):
+        w = self.w
+        st = w.stream
+        for s in range(w.n_sensors):
+            N.check(w.lib.dt_pose_control_vel(w.wp, s, self.Ab32[t, s].data_ptr(), self.inv_T, st), "pose cv")
+        w.step_begin()
+        for f in range(self.S):
+            w.substep(f)
+        self.launches += w.n_sensors + 1 + 3 * self.S
+        if copy_end:
+            w.copy_frame(self.S, 0)
+
+    def forward(self, actions: torch.Tensor) -> torch.Tensor:
+        """Roll out; returns the final-frame loss (device scalar)."""
+        self.actions = actions.detach().double().requires_grad_(True)
+        self.Ab = self.step_transforms(self.actions)
+        self.Ab32 = self.Ab.detach().float().contiguous()
+        for t in range(self.T):
+            if t % self.k == 0:
+                self._save(self.ck_p, self.ck_v, t // self.k)
+            self._step(t)
+        return self.readout()
+
+    def readout(self) -> torch.Tensor:
+        w = self.w
+        self.loss.zero_()
+        for s, layer, tg in self.loss_terms:
+            N.check(w.lib.dt_marker_loss(w.wp, s, 0, layer, tg.data_ptr(), self.loss.data_ptr(), w.stream), "loss")
+            self.launches += 1
+        return self.loss
+
+    def backward(self, loss_bar: float = 1.0) -> torch.Tensor:
+        """Adjoint sweep; returns d loss / d actions [T, n_sensors, 6] (float64).  Initial-state
+        adjoints are left in the world's frame-0 adjoint buffers, material grads in mat_adj."""
+        w = self.w
+        st = w.stream
+        w.adj_clear()
+        for s, layer, tg in self.loss_terms:
+            N.check(w.lib.dt_marker_loss_bwd(w.wp, s, self.S, layer, tg.data_ptr(), float(loss_bar), st), "loss bwd")
+        self.Ab_bar = torch.zeros_like(self.Ab32)
+        for seg in reversed(range(self.n_ck)):
+            t0, t1 = seg * self.k, min((seg + 1) * self.k, self.T)
+            self._load(self.ck_p, self.ck_v, seg)
+            if self.k > 1:
+                for t in range(t0, t1):
+                    self._save(self.seg_p, self.seg_v, t - t0)
+                    if t + 1 < t1:
+                        self._step(t)
+            for t in reversed(range(t0, t1)):
+                if self.k > 1:
+                    self._load(self.seg_p, self.seg_v, t - t0)
+                self._step(t, copy_end=False)
+                w.t["v_adj_cv"].zero_()
+                for f in reversed(range(self.S)):
+                    w.substep_bwd(f)
+                for s in range(w.n_sensors):
+                    N.check(w.lib.dt_pose_control_vel_bwd(w.wp, s, self.Ab32[t, s].data_ptr(), self.inv_T,
+                                                          self.Ab_bar[t, s].data_ptr(), st), "pose cv bwd")
+                self.launches += 4 * self.S + w.n_sensors
+                if self.S & 1:  # frame 0's adjoint (buffer 0) is frame S's of the previous step (buffer 1)
+                    for name in ("p_adj", "v_adj_pos", "v_adj_vel", "v_adj_vpos"):
+                        w.t[name][1].copy_(w.t[name][0])
+        (g,) = torch.autograd.grad(self.Ab, self.actions, self.Ab_bar.double())
+        return g

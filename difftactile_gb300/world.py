@@ -318,11 +318,42 @@ class World:
     def step_begin(self):
         self.call("dt_step_begin")
 
+    # ``probe = ("fwd" | "bwd", stage)`` times that launch of every substep with CUDA events on the
+    # launching stream; the event pairs accumulate in ``probe_events``.
+    probe = None
+
+    def _staged(self, name, f, n_stages, kind):
+        for s in range(n_stages):
+            timed = self.probe[0] == kind and self.probe[1] == s
+            if timed:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+            self.call(name, int(f), s)
+            if timed:
+                e1.record()
+                self.probe_events.append((e0, e1))
+
     def substep(self, f):
-        self.call("dt_substep_fwd", int(f))
+        if self.probe is not None and self.probe[0] == "fwd":
+            self._staged("dt_substep_fwd_stage", f, 3, "fwd")
+        else:
+            self.call("dt_substep_fwd", int(f))
 
     def substep_bwd(self, f):
-        self.call("dt_substep_bwd", int(f))
+        if self.probe is not None and self.probe[0] == "bwd":
+            self._staged("dt_substep_bwd_stage", f, 4, "bwd")
+        else:
+            self.call("dt_substep_bwd", int(f))
+
+    def set_probe(self, kind=None, stage=None):
+        self.probe = None if kind is None else (kind, int(stage))
+        self.probe_events = []
+
+    def probe_ms(self):
+        """Mean duration (ms) of the probed launches recorded so far (synchronises)."""
+        torch.cuda.synchronize()
+        ts = [a.elapsed_time(b) for a, b in self.probe_events]
+        return (sum(ts) / len(ts)) if ts else float("nan"), len(ts)
 
     def copy_frame(self, src, dst):
         self.call("dt_copy_frame", int(src), int(dst))

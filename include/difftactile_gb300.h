@@ -192,6 +192,10 @@ int dt_step_begin(const dt_world* w, cudaStream_t stream);
  * integration.  Requires 0 <= f < n_frames-1. */
 int dt_substep_fwd(const dt_world* w, int f, cudaStream_t stream);
 
+/* dt_substep_fwd split into its three launches (stage 0: P2G + FEM forces + centroids; 1: grid
+ * update + contact; 2: G2P + FEM integration), for timing and for callers that interleave work. */
+int dt_substep_fwd_stage(const dt_world* w, int f, int stage, cudaStream_t stream);
+
 /* The same substep split into the reference's per-object calls, for drop-in use of the
  * reference method sequence.  dt_substep_fwd(f) == p2g(f); fem_update(f); grid_op(f) (which
  * includes check_grid_occupy, check_collision and collision); g2p(f); fem_update2(f). */
@@ -225,6 +229,25 @@ int dt_adj_clear(const dt_world* w, cudaStream_t stream);
 int dt_com(const dt_world* w, int f, float* out, cudaStream_t stream);
 /* Adjoint of dt_com: adds adj_com[e]/count to x-adjoint of every particle of env e in p_adj[f&1]. */
 int dt_com_bwd(const dt_world* w, int f, const float* adj_com, cudaStream_t stream);
+
+/* ---- action input: pose control (fem_sensor.py:229-266, set_pose_control + set_control_vel) ----
+ * cv_i = ((A vp_i + b) - vp_i) * inv_T for every vertex i of sensor s, vp = virtual positions of
+ * frame 0, (A | b) = rows 0..2 of the step transform dtrans_h given as 12 device floats (row-major
+ * 3x4), inv_T = 1 / (dt * substeps); written into every frame of v_cv. */
+int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, cudaStream_t stream);
+/* Adjoint: Ab_bar[12] (device) += sum_i cvb_i [vp_i, 1]^T inv_T and v_adj_vpos[0] += (A - I)^T cvb_i
+ * inv_T, with cvb_i the control-velocity adjoint summed over the frames of v_adj_cv. */
+int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv_T, float* Ab_bar,
+                            cudaStream_t stream);
+
+/* ---- tactile readout: marker-displacement loss (cf. grasp_plastic.py:241-256) ----
+ * loss[0] (device) += sum over vertices i of sensor s with layer id `layer` of
+ * |(pos_i - vpos_i) - target_i|^2 at frame f; target is [nv][4] device floats (xyz, pad). */
+int dt_marker_loss(const dt_world* w, int s, int f, int layer, const float* target, float* loss,
+                   cudaStream_t stream);
+/* Adjoint: adds 2 loss_bar (disp - target) to v_adj_pos[f&1] and its negative to v_adj_vpos[f&1]. */
+int dt_marker_loss_bwd(const dt_world* w, int s, int f, int layer, const float* target, float loss_bar,
+                       cudaStream_t stream);
 
 #ifdef __cplusplus
 }
