@@ -273,22 +273,20 @@ def cpu_baseline(cfg, threads, target_s=15.0):
     env = cfg.envs[0]
     o = O.Oracle(env, cfg.dt, np.float32, n_threads=threads)
     st = o.initial_state()
-    sp = env.sensors[0] if env.sensors else None
     cv = [np.zeros((len(s.verts), 3), np.float32) for s in env.sensors]
+    adj = {k: np.ones_like(st[k]) for k in ("x", "v", "C", "F")}
     done, t0 = 0, time.perf_counter()
-    fwd_only = not hasattr(o, "substep_bwd")
+    # the same work per substep as the GPU's checkpointed sweep: forward, then recompute + adjoint
     while time.perf_counter() - t0 < target_s and done < cfg.substeps:
         st1, _ = o.substep(st, cv=cv, cv1=cv)
-        if not fwd_only:
-            o.substep_bwd(st, st1, cv)
+        o.substep_bwd(st, adj, cv=cv, cv1=cv)
         st = st1
         done += 1
     dt_ = time.perf_counter() - t0
-    del sp
     return {"value": env.n_particles * done / dt_, "unit": "particle-substeps/s", "cores": threads,
             "kind": "port",
-            "sample": f"{done} substeps of env 0 of {cfg.name} ({env.n_particles} particles)"
-                      + (" forward only" if fwd_only else " forward+backward")}
+            "sample": f"{done} substeps of env 0 of {cfg.name} ({env.n_particles} particles), forward + "
+                      f"recompute + adjoint per substep, float32, {threads} OpenMP threads"}
 
 
 def run_reference(args):

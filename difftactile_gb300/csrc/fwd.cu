@@ -25,7 +25,8 @@ namespace {
 
 constexpr int NT = 128;           // threads per CTA for particle / tet / vertex roles
 constexpr int TILE_MAX = 1728;    // shared P2G tile capacity in nodes (12^3), 27 KB of float4
-constexpr int GRID_NT = 64;       // one 4x4x4 node block per CTA in the grid kernel
+constexpr int GRID_NT = 256;      // one 4x4x4 node block (4 lanes per node) per CTA in the grid kernel
+constexpr int SMEM_CENT_MAX = 12288;  // triangle centroids staged in shared memory (192 KB)
 
 __device__ void mark_block(const dt_world& w, int f, int b) {
   volatile int* fl = w.blk_flag + b;
@@ -249,11 +250,23 @@ __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p,
 }
 
 // ---------------------------------------------------------------------------------------------
-// L2: grid update + contact over the frame's active blocks
+// L2: grid update + contact over the frame's active blocks.  256 threads per 4x4x4 block: four
+// lanes per node share the node's argmin over the sensor's triangle centroids (staged in shared
+// memory), each lane scanning every fourth triangle with two independent trackers; the
+// (distance, index) pairs are combined lexicographically, which is exactly the sequential scan's
+// first-minimum-wins result.  Lane 0 of each node then does the contact force and the grid update.
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f) {
+struct Best {
+  float d;
+  int i;
+};
+DT_DEV Best lexmin(Best a, Best b) { return (b.d < a.d || (b.d == a.d && b.i < a.i)) ? b : a; }
+
+__global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f, int smem_cap) {
+  extern __shared__ float4 scent[];
   const int cnt = *((volatile int*)(w.tape_bcount + f));
-  const int l = threadIdx.x;
+  const int tid = threadIdx.x;
+  const int l = tid >> 2, sub = tid & 3;
   const float third = 1.f / 3.f;
   float4* acc = reinterpret_cast<float4*>(w.g_acc);
   float4* vout = reinterpret_cast<float4*>(w.g_vout);
@@ -262,6 +275,7 @@ __global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f) {
   float4* EXT = vframe(w.v_ext, w, f);
   const float4* cent = reinterpret_cast<const float4*>(w.tri_cent);
   const int4* tris = reinterpret_cast<const int4*>(w.tris);
+  int staged = -1;
   for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
     const int b = w.tape_blist[(size_t)f * w.n_blocks + e];
     const dt_env& E = w.envs[__ldg(w.blk_env + b)];
@@ -271,66 +285,96 @@ __global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f) {
     const int g = E.node_off + (lb << 6) + l;
     const float4 a = acc[g];
     const float m = a.w;
-    float4 vo = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool occ = m > E.eps;  // check_grid_occupy, mpm_elastic.py:213
+    const v3 mv = f4to3(a);
+    const float me = m + E.eps;
+    const v3 cur_v = v3{mv.x / me, mv.y / me, mv.z / me};
+    const float px = __fmul_rn(__fadd_rn((float)i, 0.5f), E.dx), py = __fmul_rn(__fadd_rn((float)j, 0.5f), E.dx),
+                pz = __fmul_rn(__fadd_rn((float)k, 0.5f), E.dx);
+    v3 gf = v3{0.f, 0.f, 0.f};
     int cid[DT_MAX_SENSORS_PER_ENV] = {-1, -1, -1, -1};
-    if (m > E.eps) {  // check_grid_occupy, mpm_elastic.py:213
-      const v3 mv = f4to3(a);
-      const float inv_m = 1.f / (m + E.eps);
-      const v3 cur_v = v3{mv.x / (m + E.eps), mv.y / (m + E.eps), mv.z / (m + E.eps)};
-      const float px = __fmul_rn(__fadd_rn((float)i, 0.5f), E.dx), py = __fmul_rn(__fadd_rn((float)j, 0.5f), E.dx),
-                  pz = __fmul_rn(__fadd_rn((float)k, 0.5f), E.dx);
-      v3 gf = v3{0.f, 0.f, 0.f};
 #pragma unroll
-      for (int q = 0; q < DT_MAX_SENSORS_PER_ENV; ++q) {
-        const int si = E.s_begin + q;
-        if (si >= E.s_end) break;
-        const dt_sensor& S = w.sensors[si];
-        float best = 100.f;
-        int kk = -1;
-        for (int t = 0; t < S.nf; ++t) {
-          float dd = cent_dist(__ldg(cent + S.f_off + t), px, py, pz);
-          if (dd < best) {
-            best = dd;
-            kk = t;
+    for (int q = 0; q < DT_MAX_SENSORS_PER_ENV; ++q) {
+      const int si = E.s_begin + q;  // block-uniform
+      if (si >= E.s_end) break;
+      const dt_sensor& S = w.sensors[si];
+      const int nf = S.nf;
+      const bool in_smem = nf <= smem_cap;
+      if (in_smem && staged != si) {
+        __syncthreads();
+        for (int t = tid; t < nf; t += GRID_NT) scent[t] = __ldg(cent + S.f_off + t);
+        __syncthreads();
+        staged = si;
+      }
+      // find_closest (fem_sensor.py:344-359)
+      Best b0{100.f, -1}, b1{100.f, -1};
+      if (occ) {
+        if (in_smem) {
+          for (int t = sub; t < nf; t += 8) {
+            const float d0 = cent_dist(scent[t], px, py, pz);
+            if (d0 < b0.d) b0 = Best{d0, t};
+            const int t1 = t + 4;
+            if (t1 < nf) {
+              const float d1 = cent_dist(scent[t1], px, py, pz);
+              if (d1 < b1.d) b1 = Best{d1, t1};
+            }
+          }
+        } else {
+          for (int t = sub; t < nf; t += 4) {
+            const float d0 = cent_dist(__ldg(cent + S.f_off + t), px, py, pz);
+            if (d0 < b0.d) b0 = Best{d0, t};
           }
         }
-        cid[q] = kk;
-        if (kk < 0) continue;
-        const int4 tr = __ldg(tris + S.f_off + kk);
-        SdfRes sr = find_sdf(f4to3(P[tr.x]), f4to3(P[tr.y]), f4to3(P[tr.z]), f4to3(VM[tr.x]), f4to3(VM[tr.y]),
-                             f4to3(VM[tr.z]), v3{S.out_dir[0], S.out_dir[1], S.out_dir[2]}, v3{px, py, pz}, cur_v);
-        if (!sr.flag) continue;
-        const v3 ext = contact_force(E, sr.sdf, sr.n, sr.r);
-        gf = gf + w.dt * ext;
-        const float4 fe = v3to4(third * (-ext));
-        red_add_v4(EXT + tr.x, fe);
-        red_add_v4(EXT + tr.y, fe);
-        red_add_v4(EXT + tr.z, fe);
       }
-      // grid_op, mpm_elastic.py:220-238
-      v3 u = (inv_m * mv + inv_m * gf) + v3{E.dt_g[0], E.dt_g[1], E.dt_g[2]};
-      const int b_ = E.bound;
-      if (i < b_ && u.x < 0.f) u.x = 0.f;
-      if (i > E.n[0] - b_ && u.x > 0.f) u.x = 0.f;
-      if (j < b_ && u.y < 0.f) u.y = 0.f;
-      if (j > E.n[1] - b_ && u.y > 0.f) u.y = 0.f;
-      if (k < b_ && u.z < 0.f) u.z = 0.f;
-      if (k > E.n[2] - b_ && u.z > 0.f) u.z = 0.f;
-      if (E.bc == DT_BC_STICKY_FLOOR && j < b_) u = v3{0.f, 0.f, 0.f};
-      if (!finite3(u)) set_err(w, DT_DEVERR_NONFINITE);
-      vo = v3to4(u);
+      Best bb = lexmin(b0, b1);
+#pragma unroll
+      for (int o = 1; o <= 2; o <<= 1) {
+        Best other{__shfl_xor_sync(0xffffffffu, bb.d, o), __shfl_xor_sync(0xffffffffu, bb.i, o)};
+        bb = lexmin(bb, other);
+      }
+      const int kk = bb.i;
+      cid[q] = kk;
+      if (sub != 0 || !occ || kk < 0) continue;
+      const int4 tr = __ldg(tris + S.f_off + kk);
+      SdfRes sr = find_sdf(f4to3(P[tr.x]), f4to3(P[tr.y]), f4to3(P[tr.z]), f4to3(VM[tr.x]), f4to3(VM[tr.y]),
+                           f4to3(VM[tr.z]), v3{S.out_dir[0], S.out_dir[1], S.out_dir[2]}, v3{px, py, pz}, cur_v);
+      if (!sr.flag) continue;
+      const v3 ext = contact_force(E, sr.sdf, sr.n, sr.r);
+      gf = gf + w.dt * ext;
+      const float4 fe = v3to4(third * (-ext));
+      red_add_v4(EXT + tr.x, fe);
+      red_add_v4(EXT + tr.y, fe);
+      red_add_v4(EXT + tr.z, fe);
     }
-    vout[g] = vo;
-    if (e < w.tape_blocks) {
-      const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + l;
-      reinterpret_cast<float4*>(w.tape_acc)[ti] = a;
-      reinterpret_cast<float4*>(w.tape_vout)[ti] = vo;
-      reinterpret_cast<int4*>(w.tape_cidx)[ti] = make_int4(cid[0], cid[1], cid[2], cid[3]);
-    } else if (l == 0) {
-      set_err(w, DT_DEVERR_TAPE_FULL);
+    if (sub == 0) {
+      float4 vo = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (occ) {
+        // grid_op, mpm_elastic.py:220-238
+        const float inv_m = 1.f / me;
+        v3 u = (inv_m * mv + inv_m * gf) + v3{E.dt_g[0], E.dt_g[1], E.dt_g[2]};
+        const int b_ = E.bound;
+        if (i < b_ && u.x < 0.f) u.x = 0.f;
+        if (i > E.n[0] - b_ && u.x > 0.f) u.x = 0.f;
+        if (j < b_ && u.y < 0.f) u.y = 0.f;
+        if (j > E.n[1] - b_ && u.y > 0.f) u.y = 0.f;
+        if (k < b_ && u.z < 0.f) u.z = 0.f;
+        if (k > E.n[2] - b_ && u.z > 0.f) u.z = 0.f;
+        if (E.bc == DT_BC_STICKY_FLOOR && j < b_) u = v3{0.f, 0.f, 0.f};
+        if (!finite3(u)) set_err(w, DT_DEVERR_NONFINITE);
+        vo = v3to4(u);
+      }
+      vout[g] = vo;
+      if (e < w.tape_blocks) {
+        const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + l;
+        reinterpret_cast<float4*>(w.tape_acc)[ti] = a;
+        reinterpret_cast<float4*>(w.tape_vout)[ti] = vo;
+        reinterpret_cast<int4*>(w.tape_cidx)[ti] = make_int4(cid[0], cid[1], cid[2], cid[3]);
+      } else if (l == 0) {
+        set_err(w, DT_DEVERR_TAPE_FULL);
+      }
+      acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (l == 0) w.blk_flag[b] = 0;
     }
-    acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (l == 0) w.blk_flag[b] = 0;
   }
 }
 
@@ -440,9 +484,17 @@ int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   return launched();
 }
 int launch_l2(const dt_world* w, int f, cudaStream_t st) {
-  int nb = w->n_blocks < 152 * 16 ? w->n_blocks : 152 * 16;
+  int nb = w->n_blocks < 152 * 8 ? w->n_blocks : 152 * 8;
   if (nb <= 0) return DT_OK;
-  k_fwd_grid<<<nb, GRID_NT, 0, st>>>(*w, f);
+  const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
+  const size_t smem = (size_t)(cap > 0 ? cap : 1) * sizeof(float4);
+  static size_t configured = 0;
+  if (smem > 48 * 1024 && smem > configured) {
+    if (cudaFuncSetAttribute(k_fwd_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return DT_ERR_LAUNCH;
+    configured = smem;
+  }
+  k_fwd_grid<<<nb, GRID_NT, smem, st>>>(*w, f, cap);
   return launched();
 }
 int launch_l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {

@@ -59,10 +59,11 @@ class PoseTrajectory:
             self.seg_p = torch.zeros((self.k, 6, Np, 4), device=dev)
             self.seg_v = torch.zeros((self.k, 3, V, 4), device=dev)
         self.inv_T = 1.0 / (world.dt * self.S)
-        self.TW = []
+        self.TW, self.TW_inv = [], []
         for sp in world.sensor_specs:
             M = sp.trans_world if sp.trans_world is not None else np.eye(4)
             self.TW.append(torch.as_tensor(M, dtype=torch.float64, device=dev))
+            self.TW_inv.append(torch.as_tensor(np.linalg.inv(M), dtype=torch.float64, device=dev))
         self.loss_terms = []
         for s, layer, target in loss_terms:
             tg = torch.zeros((world.sensor_rows[s].nv, 4), device=dev)
@@ -96,8 +97,7 @@ class PoseTrajectory:
         for s in range(self.w.n_sensors):
             a = actions[:, s]
             M = eul2mat_zyx(a[:, 3:6] * self.w.dt * S, a[:, 0:3] * self.w.dt * S)
-            TW = self.TW[s]
-            D = TW @ M @ torch.linalg.inv(TW)
+            D = self.TW[s] @ M @ self.TW_inv[s]
             out.append(D[:, :3, :].reshape(-1, 12))
         return torch.stack(out, 1)
 

@@ -201,6 +201,7 @@ class World:
         w.n_nodes, w.n_blocks, w.n_frames, w.tape_blocks = NN, NB, Fn, TB
         w.dt, w.grad_clip, w.svd_sweeps = self.dt, float(grad_clip), int(svd_sweeps)
         w.svd_grad_mode = int(svd_grad_mode)
+        w.max_sensor_tris = max([r.nf for r in srows], default=0)
         self.w = w
         self.wp = C.pointer(w)
 

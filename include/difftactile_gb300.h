@@ -165,6 +165,8 @@ typedef struct dt_world {
   float grad_clip;               /* backward clamp of grid-mass and sensor grads; 0 disables */
   int svd_sweeps;                /* cyclic Jacobi sweeps of the 3x3 SVD (4 is enough for fp32) */
   int svd_grad_mode;             /* DT_SVDGRAD_* */
+  int max_sensor_tris;           /* largest nf over the sensors (sizes the contact search's staging) */
+  int pad_;
 } dt_world;
 
 /* SVD adjoint of the rotation R = U V^T used by the corotated stress:

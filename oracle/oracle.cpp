@@ -301,13 +301,15 @@ inline size_t gidx(const int* n, int i, int j, int k) { return (size_t(i) * n[1]
 
 // von Mises return mapping, mpm_plastic.py:151-166.  Returns F unchanged when not yielding.
 template <typename T>
-M3<T> von_mises(const M3<T>& F, const M3<T>& U, const T sig[3], const M3<T>& V, T mu, T yield_stress) {
+M3<T> von_mises(const M3<T>& F, const M3<T>& U, const T sig[3], const M3<T>& V, T mu, T yield_stress,
+                bool* yielded = nullptr) {
   T eps[3];
   for (int d = 0; d < 3; ++d) eps[d] = std::log(std::max(sig[d], T(0.05)));
   T mean = ((eps[0] + eps[1]) + eps[2]) / T(3);
   T eh[3] = {eps[0] - mean, eps[1] - mean, eps[2] - mean};
   T nrm = std::sqrt(((eh[0] * eh[0] + eh[1] * eh[1]) + eh[2] * eh[2]) + T(1e-8));
   T dg = nrm - yield_stress / (T(2) * mu);
+  if (yielded) *yielded = dg > T(0);
   if (dg > T(0)) {
     T e[3];
     for (int d = 0; d < 3; ++d) e[d] = std::exp(eps[d] - (dg / nrm) * eh[d]);
@@ -498,8 +500,7 @@ void p2g_particle(const orc_scene* sc, const Consts<T>& K, const Particle<T>& q,
   o.yield = false;
   o.R = mmul(o.U, mT(o.V));
   if (o.model == MODEL_VON_MISES) {
-    o.Fp = von_mises(o.Fn, o.U, o.sig, o.V, o.mu, o.ys);
-    o.yield = std::memcmp(&o.Fp, &o.Fn, sizeof(o.Fp)) != 0;
+    o.Fp = von_mises(o.Fn, o.U, o.sig, o.V, o.mu, o.ys, &o.yield);
     o.J = mdet(o.Fp);
   } else if (o.model == MODEL_NEOHOOKEAN) {
     o.Fp = o.Fn;
@@ -534,8 +535,20 @@ void p2g_particle(const orc_scene* sc, const Consts<T>& K, const Particle<T>& q,
 // Forward substep, reference order of Contact.update (grasp_plastic.py:151-164).
 // Sensor arrays are per sensor, [nv][3]; vel[s] is updated in place by the elastic forces
 // (as the Taichi kernel does) and afterwards holds the post-force velocity used by contact.
-// Dense grid outputs are [n0*n1*n2] (*3 for vectors) and are overwritten.
+// Dense grid outputs are [n0*n1*n2] (*3 for vectors) and are overwritten.  With n_threads > 1 the
+// loops run in parallel with atomic scatters (the Taichi CPU backend's execution model); with one
+// thread the summation order is the sequential index order.
 // =============================================================================================
+template <typename T>
+inline void aadd(T& a, T b, bool atomic) {
+  if (atomic) {
+#pragma omp atomic
+    a += b;
+  } else {
+    a += b;
+  }
+}
+
 template <typename T>
 static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C, const T* F, T* x1, T* v1,
                         T* C1, T* F1, T* const* pos, T* const* vel, const T* const* vpos, const T* const* cv,
@@ -545,6 +558,8 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
   const int* n = sc->n;
   const size_t nn = size_t(n[0]) * n[1] * n[2];
   const int NS = sc->n_sensors;
+  const int nt = sc->n_threads > 1 ? sc->n_threads : 1;
+  const bool at = nt > 1;
   int err = 0;
   std::fill(grid_m, grid_m + nn, T(0));
   std::fill(grid_v_in, grid_v_in + 3 * nn, T(0));
@@ -554,6 +569,7 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
   for (int s = 0; s < NS; ++s) std::fill(ext[s], ext[s] + 3 * sc->sensors[s].nv, T(0));
 
   // ---- compute_new_F + svd + p2g ----
+#pragma omp parallel for num_threads(nt) schedule(static) reduction(| : err) if (at)
   for (int p = 0; p < sc->n_particles; ++p) {
     Particle<T> q = load_particle(x, v, C, F, p);
     P2GFwd<T> o;
@@ -575,9 +591,9 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
             T ad = o.affine.a[r][0] * dpos[0];
             ad = ad + o.affine.a[r][1] * dpos[1];
             ad = ad + o.affine.a[r][2] * dpos[2];
-            grid_v_in[3 * g + r] += W * (K.p_mass * q.v[r] + ad);
+            aadd(grid_v_in[3 * g + r], W * (K.p_mass * q.v[r] + ad), at);
           }
-          grid_m[g] += W * K.p_mass;
+          aadd(grid_m[g], W * K.p_mass, at);
         }
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) F1[9 * p + 3 * i + j] = o.Fp.a[i][j];
@@ -590,6 +606,7 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
     const T alpha = T(1) + T(0.75) * mu / lam;
     T* P = pos[s];
     T* Vl = vel[s];
+#pragma omp parallel for num_threads(nt) schedule(static) if (at)
     for (int t = 0; t < S.nt; ++t) {
       const int* tv = S.tets + 4 * t;
       M3<T> D, B;
@@ -620,13 +637,14 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
       for (int k = 0; k < 3; ++k)
         for (int r = 0; r < 3; ++r) {
           T fo = H.a[r][k];
-          Vl[3 * tv[k] + r] += dt * fo / mass;
-          Vl[3 * tv[3] + r] += T(-1) * dt * fo / mass;
+          aadd(Vl[3 * tv[k] + r], dt * fo / mass, at);
+          aadd(Vl[3 * tv[3] + r], T(-1) * dt * fo / mass, at);
         }
     }
   }
 
   // ---- check_grid_occupy + check_collision + collision + grid_op ----
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 1) if (at)
   for (int i = 0; i < n[0]; ++i)
     for (int j = 0; j < n[1]; ++j)
       for (int k = 0; k < n[2]; ++k) {
@@ -648,7 +666,7 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
           for (int c = 0; c < 3; ++c) grid_f[3 * g + c] += e[c] * K.dt;
           const int* t = S.tris + 3 * kk;
           for (int a = 0; a < 3; ++a)
-            for (int c = 0; c < 3; ++c) ext[s][3 * t[a] + c] += K.third * (T(-1) * e[c]);
+            for (int c = 0; c < 3; ++c) aadd(ext[s][3 * t[a] + c], K.third * (T(-1) * e[c]), at);
         }
         T inv_m = T(1) / (m + K.eps);
         T vo[3];
@@ -667,6 +685,7 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
       }
 
   // ---- g2p ----
+#pragma omp parallel for num_threads(nt) schedule(static) if (at)
   for (int p = 0; p < sc->n_particles; ++p) {
     T xp[3];
     for (int d = 0; d < 3; ++d) xp[d] = x[3 * p + d];
@@ -734,6 +753,536 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
   return err;
 }
 
+// =============================================================================================
+// Adjoint substep, order of Contact.update_grad (grasp_plastic.py:167-178): fem.update2.grad,
+// g2p.grad, grid_op.grad, clamp_grid, collision.grad (argmin held constant), fem.update.grad,
+// p2g.grad, svd_grad (mpm_elastic.py:145-173), compute_new_F.grad.  Recomputes the forward
+// substep internally.  Adjoint inputs are those of frame f+1; outputs those of frame f; cvb, cvb1
+// (control-velocity adjoints of frames f, f+1) and mat_b ([n_materials][2]: d/dmu, d/dlam) are
+// accumulated.
+// =============================================================================================
+template <typename T>
+inline T clampg(T a, T c) {
+  return c > T(0) ? std::min(std::max(a, -c), c) : a;
+}
+template <typename T>
+inline T gap_clamp(T a) {
+  return a >= T(0) ? std::max(a, T(1e-8)) : std::min(a, T(-1e-8));
+}
+
+// adjoint of contact_force: returns sdf_b, accumulates n_b, r_b
+template <typename T>
+T contact_force_bwd(const Consts<T>& K, T sdf, const T n[3], const T r[3], const T eb[3], T nb[3], T rb[3]) {
+  T nr = dot3(n, r);
+  T vn = std::max(nr, T(0));
+  T kk = K.kn + K.kd * vn;
+  T fn[3], vt[3];
+  for (int c = 0; c < 3; ++c) {
+    fn[c] = -kk * sdf * n[c];
+    vt[c] = r[c] - nr * n[c];
+  }
+  T vtn = std::sqrt(dot3(vt, vt) + T(1e-11));
+  T fnb[3] = {eb[0], eb[1], eb[2]};
+  T vtb[3] = {T(0), T(0), T(0)};
+  if (vtn > T(1e-4)) {
+    T fnn = std::sqrt(dot3(fn, fn));
+    T kv = K.kt * vtn, cap = K.mu_t * fnn;
+    T g = std::min(kv, cap);
+    T th[3] = {vt[0] / vtn, vt[1] / vtn, vt[2] / vtn};
+    T gb = dot3(th, eb);
+    T thb[3] = {g * eb[0], g * eb[1], g * eb[2]};
+    T vtnb = T(0);
+    if (kv <= cap)
+      vtnb += K.kt * gb;
+    else if (fnn > T(0))
+      for (int c = 0; c < 3; ++c) fnb[c] += (K.mu_t * gb / fnn) * fn[c];
+    for (int c = 0; c < 3; ++c) vtb[c] = thb[c] / vtn;
+    vtnb += -dot3(thb, vt) / (vtn * vtn);
+    for (int c = 0; c < 3; ++c) vtb[c] += (vtnb / vtn) * vt[c];
+  }
+  T nrb = -dot3(n, vtb);
+  for (int c = 0; c < 3; ++c) {
+    rb[c] += vtb[c];
+    nb[c] -= nr * vtb[c];
+  }
+  T nfb = dot3(n, fnb);
+  T kkb = -sdf * nfb;
+  T sdfb = -kk * nfb;
+  for (int c = 0; c < 3; ++c) nb[c] -= (kk * sdf) * fnb[c];
+  if (nr > T(0)) nrb += K.kd * kkb;
+  for (int c = 0; c < 3; ++c) {
+    nb[c] += nrb * r[c];
+    rb[c] += nrb * n[c];
+  }
+  return sdfb;
+}
+
+template <typename T>
+M3<T> svd_grad(const M3<T>& U, const T s[3], const M3<T>& V, const M3<T>& Ub0, const T sb[3], const M3<T>& Vb0,
+               const M3<T>& Rb, int mode) {
+  M3<T> Ub = Ub0, Vb = Vb0;
+  if (mode == 1) {
+    M3<T> a = mmul(Rb, V), b = mmul(mT(Rb), U);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        Ub.a[i][j] += a.a[i][j];
+        Vb.a[i][j] += b.a[i][j];
+      }
+  }
+  M3<T> M = mmul(mmul(mT(U), Rb), V);
+  M3<T> UtUb = mmul(mT(U), Ub), UbtU = mmul(mT(Ub), U), VtVb = mmul(mT(V), Vb), VbtV = mmul(mT(Vb), V);
+  M3<T> inner;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      T val;
+      if (i != j) {
+        T ff = T(1) / gap_clamp(s[j] * s[j] - s[i] * s[i]);
+        val = ff * (UtUb.a[i][j] - UbtU.a[i][j]) * s[j] + s[i] * ff * (VtVb.a[i][j] - VbtV.a[i][j]);
+        if (mode != 1) val += (M.a[i][j] - M.a[j][i]) / gap_clamp(s[i] + s[j]);
+      } else {
+        val = sb[i];
+      }
+      inner.a[i][j] = val;
+    }
+  return mmul(mmul(U, inner), mT(V));
+}
+
+template <typename T>
+static int substep_bwd_impl(const orc_scene* sc, const T* x, const T* v, const T* C, const T* F,
+                            const T* const* pos, const T* const* vel, const T* const* vpos, const T* const* cv,
+                            const T* const* cv1, const T* xb1, const T* vb1, const T* Cb1, const T* Fb1,
+                            const T* const* posb1, const T* const* velb1, const T* const* vpb1, T* xb, T* vb, T* Cb,
+                            T* Fb, T* const* posb, T* const* velb, T* const* vpb, T* const* cvb, T* const* cvb1,
+                            T* mat_b, int svd_grad_mode) {
+  const Consts<T> K = make_consts<T>(sc);
+  const int* n = sc->n;
+  const size_t nn = size_t(n[0]) * n[1] * n[2];
+  const int NS = sc->n_sensors;
+  const int Np = sc->n_particles;
+  const int nt = sc->n_threads > 1 ? sc->n_threads : 1;
+  const bool at = nt > 1;
+  const T clip = T(sc->grad_clip);
+  // ---- forward recompute ----
+  std::vector<T> x1(3 * Np), v1(3 * Np), C1(9 * Np), F1(9 * Np);
+  std::vector<std::vector<T>> pos_c(NS), vel_c(NS), p1(NS), vl1(NS), vp1(NS), ext(NS);
+  std::vector<T*> pos_p(NS), vel_p(NS), p1_p(NS), vl1_p(NS), vp1_p(NS), ext_p(NS);
+  for (int s = 0; s < NS; ++s) {
+    const int nv = sc->sensors[s].nv;
+    pos_c[s].assign(pos[s], pos[s] + 3 * nv);
+    vel_c[s].assign(vel[s], vel[s] + 3 * nv);
+    p1[s].resize(3 * nv);
+    vl1[s].resize(3 * nv);
+    vp1[s].resize(3 * nv);
+    ext[s].resize(3 * nv);
+    pos_p[s] = pos_c[s].data();
+    vel_p[s] = vel_c[s].data();
+    p1_p[s] = p1[s].data();
+    vl1_p[s] = vl1[s].data();
+    vp1_p[s] = vp1[s].data();
+    ext_p[s] = ext[s].data();
+  }
+  std::vector<T> gm(nn), gvi(3 * nn), gvo(3 * nn), gf(3 * nn);
+  std::vector<int> cid(nn * size_t(NS > 0 ? NS : 1));
+  substep_impl<T>(sc, x, v, C, F, x1.data(), v1.data(), C1.data(), F1.data(), pos_p.data(), vel_p.data(), vpos, cv,
+                  cv1, p1_p.data(), vl1_p.data(), vp1_p.data(), ext_p.data(), gm.data(), gvi.data(), gvo.data(),
+                  gf.data(), cid.data());
+  // vel_c now holds the post-elastic-force velocities (vel_mid)
+
+  // ---- fem.update2.grad + clamp_grid on the sensor grads ----
+  std::vector<std::vector<T>> vmb(NS), exb(NS);
+  for (int s = 0; s < NS; ++s) {
+    const orc_sensor& S = sc->sensors[s];
+    const T dt = T(sc->dt), mass = T(S.mass);
+    vmb[s].assign(3 * S.nv, T(0));
+    exb[s].assign(3 * S.nv, T(0));
+    for (int i = 0; i < S.nv; ++i)
+      for (int c = 0; c < 3; ++c) {
+        const int q = 3 * i + c;
+        vpb[s][q] = vpb1[s][q];
+        cvb[s][q] += dt * vpb1[s][q];
+        T vob = velb1[s][q] + dt * posb1[s][q];
+        if (S.carry) {
+          cvb1[s][q] += velb1[s][q];
+          cvb[s][q] -= velb1[s][q];
+        }
+        if (S.layer[i] == 0) {
+          cvb[s][q] += vob;
+        } else {
+          vmb[s][q] = vob;
+          exb[s][q] = dt * vob / mass;
+        }
+        posb[s][q] = clampg(posb1[s][q], clip);
+        vmb[s][q] = clampg(vmb[s][q], clip);
+      }
+  }
+
+  // ---- g2p.grad ----
+  std::vector<T> gvb(3 * nn, T(0));
+#pragma omp parallel for num_threads(nt) schedule(static) if (at)
+  for (int p = 0; p < Np; ++p) {
+    T xp[3];
+    for (int d = 0; d < 3; ++d) xp[d] = x[3 * p + d];
+    int base[3];
+    T fx[3];
+    if (!particle_base(sc, K, xp, base, fx)) {
+      for (int d = 0; d < 3; ++d) {
+        xb[3 * p + d] = xb1[3 * p + d];
+        vb[3 * p + d] = vb1[3 * p + d];
+      }
+      for (int i = 0; i < 9; ++i) {
+        Cb[9 * p + i] = Cb1[9 * p + i];
+        Fb[9 * p + i] = Fb1[9 * p + i];
+      }
+      continue;
+    }
+    T w[3][3], dw[3][3];
+    for (int d = 0; d < 3; ++d) {
+      T wd[3], dwd[3];
+      bspline(fx[d], wd, dwd);
+      for (int i = 0; i < 3; ++i) {
+        w[i][d] = wd[i];
+        dw[i][d] = dwd[i];
+      }
+    }
+    T vnb[3], fxb[3] = {T(0), T(0), T(0)};
+    for (int d = 0; d < 3; ++d) vnb[d] = vb1[3 * p + d] + K.dt * xb1[3 * p + d];
+    const T* Cbp = Cb1 + 9 * p;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const int off[3] = {i, j, k};
+          T d[3];
+          for (int c = 0; c < 3; ++c) d[c] = T(off[c]) - fx[c];
+          size_t g = gidx(n, base[0] + i, base[1] + j, base[2] + k);
+          const T* gv = gvo.data() + 3 * g;
+          T W = (w[i][0] * w[j][1]) * w[k][2];
+          T kw = K.g2p_k * W;
+          T Cd[3], Ctg[3];
+          for (int r = 0; r < 3; ++r) {
+            Cd[r] = Cbp[3 * r] * d[0] + Cbp[3 * r + 1] * d[1] + Cbp[3 * r + 2] * d[2];
+            Ctg[r] = Cbp[r] * gv[0] + Cbp[3 + r] * gv[1] + Cbp[6 + r] * gv[2];
+          }
+          for (int r = 0; r < 3; ++r) aadd(gvb[3 * g + r], W * vnb[r] + kw * Cd[r], at);
+          T Wb = dot3(gv, vnb) + K.g2p_k * dot3(gv, Cd);
+          fxb[0] += Wb * (dw[i][0] * w[j][1] * w[k][2]) - kw * Ctg[0];
+          fxb[1] += Wb * (w[i][0] * dw[j][1] * w[k][2]) - kw * Ctg[1];
+          fxb[2] += Wb * (w[i][0] * w[j][1] * dw[k][2]) - kw * Ctg[2];
+        }
+    for (int d = 0; d < 3; ++d) xb[3 * p + d] = xb1[3 * p + d] + K.inv_dx * fxb[d];
+  }
+
+  // ---- grid_op.grad + clamp_grid + collision.grad ----
+  std::vector<T> accb(4 * nn, T(0));
+  for (int i = 0; i < n[0]; ++i)
+    for (int j = 0; j < n[1]; ++j)
+      for (int k = 0; k < n[2]; ++k) {
+        size_t g = gidx(n, i, j, k);
+        T m = gm[g];
+        if (!(m > K.eps)) continue;
+        const T me = m + K.eps, inv_m = T(1) / me;
+        const T* mv = gvi.data() + 3 * g;
+        T cur_v[3] = {mv[0] / me, mv[1] / me, mv[2] / me};
+        T u[3];
+        for (int c = 0; c < 3; ++c) u[c] = (T(0) + inv_m * mv[c]) + inv_m * gf[3 * g + c] + K.dt_g[c];
+        const int idx[3] = {i, j, k};
+        bool mask[3];
+        for (int d = 0; d < 3; ++d)
+          mask[d] = (idx[d] < sc->bound && u[d] < T(0)) || (idx[d] > n[d] - sc->bound && u[d] > T(0));
+        if (sc->bc == 1 && j < sc->bound) mask[0] = mask[1] = mask[2] = true;
+        T ub[3], mvb[3], gfb[3];
+        for (int c = 0; c < 3; ++c) {
+          ub[c] = mask[c] ? T(0) : gvb[3 * g + c];
+          mvb[c] = inv_m * ub[c];
+          gfb[c] = inv_m * ub[c];
+        }
+        T invb = ub[0] * (mv[0] + gf[3 * g + 0]) + ub[1] * (mv[1] + gf[3 * g + 1]) + ub[2] * (mv[2] + gf[3 * g + 2]);
+        T mb = clampg(-inv_m * inv_m * invb, clip);
+        T p[3] = {(T(i) + T(0.5)) * K.dx, (T(j) + T(0.5)) * K.dx, (T(k) + T(0.5)) * K.dx};
+        T curvb[3] = {T(0), T(0), T(0)};
+        for (int s = 0; s < NS; ++s) {
+          const orc_sensor& S = sc->sensors[s];
+          const int kk = cid[g * NS + s];
+          if (kk < 0) continue;
+          SdfOut<T> so = find_sdf(S, pos[s], vel_c[s].data(), kk, p, cur_v);
+          if (!so.flag) continue;
+          const int* t = S.tris + 3 * kk;
+          T eb[3];
+          for (int c = 0; c < 3; ++c)
+            eb[c] = K.dt * gfb[c] - K.third * ((exb[s][3 * t[0] + c] + exb[s][3 * t[1] + c]) + exb[s][3 * t[2] + c]);
+          T nb[3] = {T(0), T(0), T(0)}, rb[3] = {T(0), T(0), T(0)};
+          T sdfb = contact_force_bwd(K, so.sdf, so.nrm, so.rel, eb, nb, rb);
+          for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c) vmb[s][3 * t[a] + c] += K.third * rb[c];
+          for (int c = 0; c < 3; ++c) curvb[c] -= rb[c];
+          const T* p1 = pos[s] + 3 * t[0];
+          const T* p2 = pos[s] + 3 * t[1];
+          const T* p3 = pos[s] + 3 * t[2];
+          T p1b[3], e1[3], e2[3], nrm[3];
+          for (int c = 0; c < 3; ++c) {
+            p1b[c] = -sdfb * so.nrm[c];
+            nb[c] += sdfb * (p[c] - p1[c]);
+            e1[c] = p2[c] - p1[c];
+            e2[c] = p3[c] - p1[c];
+          }
+          cross(e1, e2, nrm);
+          T L = std::sqrt(dot3(nrm, nrm));
+          T od[3] = {T(S.out_dir[0]), T(S.out_dir[1]), T(S.out_dir[2])};
+          T inv = T(1) / (L + T(1e-10));
+          T nn_[3] = {inv * nrm[0], inv * nrm[1], inv * nrm[2]};
+          T sg = dot3(nn_, od) < T(0) ? T(-1) : T(1);
+          T nrmb[3] = {T(0), T(0), T(0)};
+          if (L > T(0)) {
+            T D = L + T(1e-10);
+            T q = dot3(nb, nrm) / (D * D * L);
+            for (int c = 0; c < 3; ++c) nrmb[c] = sg * (nb[c] / D - q * nrm[c]);
+          }
+          T e1b[3], e2b[3];
+          cross(e2, nrmb, e1b);
+          cross(nrmb, e1, e2b);
+          for (int c = 0; c < 3; ++c) {
+            posb[s][3 * t[0] + c] += p1b[c] - (e1b[c] + e2b[c]);
+            posb[s][3 * t[1] + c] += e1b[c];
+            posb[s][3 * t[2] + c] += e2b[c];
+          }
+        }
+        for (int c = 0; c < 3; ++c) {
+          accb[4 * g + c] = mvb[c] + inv_m * curvb[c];
+        }
+        accb[4 * g + 3] = mb - dot3(curvb, mv) * inv_m * inv_m;
+      }
+
+  // ---- fem.update.grad ----
+  for (int s = 0; s < NS; ++s) {
+    const orc_sensor& S = sc->sensors[s];
+    const T dt = T(sc->dt), mass = T(S.mass), mu = T(S.mu), lam = T(S.lam);
+    const T alpha = T(1) + T(0.75) * mu / lam;
+    const T* P = pos[s];
+    for (int t = 0; t < S.nt; ++t) {
+      const int* tv = S.tets + 4 * t;
+      M3<T> D, B;
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+          D.a[r][c] = P[3 * tv[c] + r] - P[3 * tv[3] + r];
+          B.a[r][c] = T(S.B[9 * t + 3 * r + c]);
+        }
+      T detD = mdet(D);
+      T Vi = std::fabs(detD) / T(6);
+      M3<T> Fe = mmul(D, B);
+      T J = mdet(Fe);
+      T IC = T(0);
+      for (int i = 0; i < 3; ++i)
+        for (int r = 0; r < 3; ++r) IC += Fe.a[r][i] * Fe.a[r][i];
+      M3<T> cof = mcof(Fe);
+      T k1 = mu * (T(1) - T(1) / (IC + T(1)));
+      T k2 = lam * (J - alpha);
+      M3<T> Pk;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Pk.a[i][j] = k1 * Fe.a[i][j] + k2 * cof.a[i][j];
+      M3<T> H = mmul(Pk, mT(B));
+      const T sc_ = -Vi * dt / mass;
+      M3<T> Hb;
+      T scb = T(0);
+      for (int k = 0; k < 3; ++k)
+        for (int r = 0; r < 3; ++r) {
+          T hb = vmb[s][3 * tv[k] + r] - vmb[s][3 * tv[3] + r];
+          Hb.a[r][k] = sc_ * hb;
+          scb += hb * H.a[r][k];
+        }
+      T Vib = -dt / mass * scb;
+      M3<T> Pb = mmul(Hb, B);
+      M3<T> Fb_;
+      T k1b = T(0), k2b = T(0);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          Fb_.a[i][j] = k1 * Pb.a[i][j];
+          k1b += Pb.a[i][j] * Fe.a[i][j];
+          k2b += Pb.a[i][j] * cof.a[i][j];
+        }
+      T f[3][3], pb[3][3];
+      for (int k = 0; k < 3; ++k)
+        for (int r = 0; r < 3; ++r) {
+          f[k][r] = Fe.a[r][k];
+          pb[k][r] = Pb.a[r][k];
+        }
+      T g0[3], g1[3], g2[3], tmp[3];
+      cross(pb[1], f[2], g0);
+      cross(f[1], pb[2], tmp);
+      for (int c = 0; c < 3; ++c) g0[c] += tmp[c];
+      cross(f[2], pb[0], g1);
+      cross(pb[2], f[0], tmp);
+      for (int c = 0; c < 3; ++c) g1[c] += tmp[c];
+      cross(pb[0], f[1], g2);
+      cross(f[0], pb[1], tmp);
+      for (int c = 0; c < 3; ++c) g2[c] += tmp[c];
+      for (int r = 0; r < 3; ++r) {
+        Fb_.a[r][0] += k2 * g0[r];
+        Fb_.a[r][1] += k2 * g1[r];
+        Fb_.a[r][2] += k2 * g2[r];
+      }
+      T ICb = k1b * mu / ((IC + T(1)) * (IC + T(1)));
+      T Jb = lam * k2b;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Fb_.a[i][j] += T(2) * ICb * Fe.a[i][j] + Jb * cof.a[i][j];
+      M3<T> Db = mmul(Fb_, mT(B));
+      T sgn = detD < T(0) ? T(-1) : (detD > T(0) ? T(1) : T(0));
+      M3<T> cD = mcof(D);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Db.a[i][j] += Vib * sgn / T(6) * cD.a[i][j];
+      for (int k = 0; k < 3; ++k)
+        for (int r = 0; r < 3; ++r) {
+          posb[s][3 * tv[k] + r] += Db.a[r][k];
+          posb[s][3 * tv[3] + r] -= Db.a[r][k];
+        }
+    }
+    for (int q = 0; q < 3 * S.nv; ++q) velb[s][q] = vmb[s][q];
+  }
+
+  // ---- p2g.grad + svd_grad + compute_new_F.grad ----
+#pragma omp parallel for num_threads(nt) schedule(static) if (at)
+  for (int p = 0; p < Np; ++p) {
+    Particle<T> q = load_particle(x, v, C, F, p);
+    P2GFwd<T> o;
+    if (!particle_base(sc, K, q.x, o.base, o.fx)) continue;  // passed through above
+    p2g_particle(sc, K, q, p, o);
+    const T pm = K.p_mass, dx = K.dx;
+    T vbp[3] = {T(0), T(0), T(0)}, fxb[3] = {T(0), T(0), T(0)};
+    M3<T> Ab = mzero<T>();
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const int off[3] = {i, j, k};
+          size_t g = gidx(n, o.base[0] + i, o.base[1] + j, o.base[2] + k);
+          const T* gb = accb.data() + 4 * g;
+          T W = (o.w[i][0] * o.w[j][1]) * o.w[k][2];
+          T dp[3];
+          for (int c = 0; c < 3; ++c) dp[c] = (T(off[c]) - o.fx[c]) * dx;
+          T Adp[3], Atm[3];
+          for (int r = 0; r < 3; ++r) {
+            Adp[r] = o.affine.a[r][0] * dp[0] + o.affine.a[r][1] * dp[1] + o.affine.a[r][2] * dp[2];
+            Atm[r] = o.affine.a[0][r] * gb[0] + o.affine.a[1][r] * gb[1] + o.affine.a[2][r] * gb[2];
+          }
+          T Wb = pm * gb[3];
+          for (int r = 0; r < 3; ++r) {
+            vbp[r] += W * pm * gb[r];
+            for (int c = 0; c < 3; ++c) Ab.a[r][c] += W * gb[r] * dp[c];
+            Wb += gb[r] * (pm * q.v[r] + Adp[r]);
+          }
+          fxb[0] += Wb * (o.dw[i][0] * o.w[j][1] * o.w[k][2]) - dx * W * Atm[0];
+          fxb[1] += Wb * (o.w[i][0] * o.dw[j][1] * o.w[k][2]) - dx * W * Atm[1];
+          fxb[2] += Wb * (o.w[i][0] * o.w[j][1] * o.dw[k][2]) - dx * W * Atm[2];
+        }
+    M3<T> Cbp, G, Fpb, Ub = mzero<T>(), Vb = mzero<T>(), Rb = mzero<T>();
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        Cbp.a[i][j] = pm * Ab.a[i][j];
+        G.a[i][j] = K.stress_k * Ab.a[i][j];
+        Fpb.a[i][j] = Fb1[9 * p + 3 * i + j];
+      }
+    T sb[3] = {T(0), T(0), T(0)};
+    T Jb, mub = T(0), lamb = T(0);
+    T trG = G.a[0][0] + G.a[1][1] + G.a[2][2];
+    if (o.model == MODEL_NEOHOOKEAN) {
+      M3<T> GGt, FFt = mmul(o.Fp, mT(o.Fp));
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) GGt.a[i][j] = G.a[i][j] + G.a[j][i];
+      M3<T> t1 = mmul(GGt, o.Fp);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          Fpb.a[i][j] += o.mu * t1.a[i][j];
+          mub += G.a[i][j] * (FFt.a[i][j] - (i == j ? T(1) : T(0)));
+        }
+      Jb = o.lam * trG / o.J;
+      lamb = std::log(o.J) * trG;
+    } else {
+      M3<T> D;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) D.a[i][j] = o.Fp.a[i][j] - o.R.a[i][j];
+      M3<T> GF = mmul(G, o.Fp), GtD = mmul(mT(G), D), DFt = mmul(D, mT(o.Fp));
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          Fpb.a[i][j] += T(2) * o.mu * (GF.a[i][j] + GtD.a[i][j]);
+          Rb.a[i][j] = T(-2) * o.mu * GF.a[i][j];
+          mub += T(2) * G.a[i][j] * DFt.a[i][j];
+        }
+      Jb = o.lam * (T(2) * o.J - T(1)) * trG;
+      lamb = o.J * (o.J - T(1)) * trG;
+    }
+    M3<T> Fnb;
+    if (o.model == MODEL_COROTATED) {
+      sb[0] += Jb * o.sig[1] * o.sig[2];
+      sb[1] += Jb * o.sig[0] * o.sig[2];
+      sb[2] += Jb * o.sig[0] * o.sig[1];
+      Fnb = Fpb;
+    } else {
+      M3<T> cf = mcof(o.Fp);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Fpb.a[i][j] += Jb * cf.a[i][j];
+      if (o.model == MODEL_VON_MISES && o.yield) {
+        T ep[3], eh[3];
+        for (int d = 0; d < 3; ++d) ep[d] = std::log(std::max(o.sig[d], T(0.05)));
+        T mean = ((ep[0] + ep[1]) + ep[2]) / T(3);
+        for (int d = 0; d < 3; ++d) eh[d] = ep[d] - mean;
+        T nrm = std::sqrt(((eh[0] * eh[0] + eh[1] * eh[1]) + eh[2] * eh[2]) + T(1e-8));
+        T dg = nrm - o.ys / (T(2) * o.mu);
+        T rr = dg / nrm;
+        T ex[3];
+        for (int d = 0; d < 3; ++d) ex[d] = std::exp(ep[d] - rr * eh[d]);
+        M3<T> UtFV = mmul(mmul(mT(o.U), Fpb), o.V), Ue = o.U, Ve = o.V;
+        for (int i = 0; i < 3; ++i)
+          for (int d = 0; d < 3; ++d) {
+            Ue.a[i][d] *= ex[d];
+            Ve.a[i][d] *= ex[d];
+          }
+        M3<T> a1 = mmul(Fpb, Ve), a2 = mmul(mT(Fpb), Ue);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            Ub.a[i][j] += a1.a[i][j];
+            Vb.a[i][j] += a2.a[i][j];
+          }
+        T epb[3], ehb[3], rrb = T(0);
+        for (int d = 0; d < 3; ++d) epb[d] = UtFV.a[d][d] * ex[d];
+        for (int d = 0; d < 3; ++d) {
+          ehb[d] = -rr * epb[d];
+          rrb -= epb[d] * eh[d];
+        }
+        T nrmb = rrb * o.ys / (T(2) * o.mu * nrm * nrm);
+        mub += rrb * o.ys / (T(2) * o.mu * o.mu * nrm);
+        for (int d = 0; d < 3; ++d) ehb[d] += nrmb * eh[d] / nrm;
+        T mb_ = ((ehb[0] + ehb[1]) + ehb[2]) / T(3);
+        for (int d = 0; d < 3; ++d) {
+          T e_ = epb[d] + ehb[d] - mb_;
+          sb[d] += o.sig[d] > T(0.05) ? e_ / o.sig[d] : T(0);
+        }
+        Fnb = mzero<T>();
+      } else {
+        Fnb = Fpb;
+      }
+    }
+    if (o.model != MODEL_NEOHOOKEAN) {
+      M3<T> gsv = svd_grad(o.U, o.sig, o.V, Ub, sb, Vb, Rb, svd_grad_mode);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Fnb.a[i][j] += gsv.a[i][j];
+    }
+    M3<T> Ad = meye<T>();
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Ad.a[i][j] += K.dt * q.C.a[i][j];
+    M3<T> Fbo = mmul(mT(Ad), Fnb), CFt = mmul(Fnb, mT(q.F));
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        Fb[9 * p + 3 * i + j] = Fbo.a[i][j];
+        Cb[9 * p + 3 * i + j] = Cbp.a[i][j] + K.dt * CFt.a[i][j];
+      }
+    for (int d = 0; d < 3; ++d) {
+      vb[3 * p + d] = vbp[d];
+      xb[3 * p + d] += K.inv_dx * fxb[d];
+    }
+    const int m = sc->p_mat ? sc->p_mat[p] : 0;
+    aadd(mat_b[2 * m], mub, at);
+    aadd(mat_b[2 * m + 1], lamb, at);
+  }
+  return 0;
+}
+
 extern "C" {
 
 int orc_substep_f32(const orc_scene* sc, const float* x, const float* v, const float* C, const float* F, float* x1,
@@ -777,6 +1326,27 @@ void orc_svd3_f64(int n, const double* A, double* U, double* s, double* V, int s
 // Standalone argmin (find_closest) over one sensor for a list of query points [nq][3].
 void orc_find_closest_f32(const orc_sensor* s, const float* pos, int nq, const float* q, int* out) {
   for (int i = 0; i < nq; ++i) out[i] = find_closest(*s, pos, q + 3 * i);
+}
+
+int orc_substep_bwd_f32(const orc_scene* sc, const float* x, const float* v, const float* C, const float* F,
+                        const float* const* pos, const float* const* vel, const float* const* vpos,
+                        const float* const* cv, const float* const* cv1, const float* xb1, const float* vb1,
+                        const float* Cb1, const float* Fb1, const float* const* posb1, const float* const* velb1,
+                        const float* const* vpb1, float* xb, float* vb, float* Cb, float* Fb, float* const* posb,
+                        float* const* velb, float* const* vpb, float* const* cvb, float* const* cvb1, float* mat_b,
+                        int svd_grad_mode) {
+  return substep_bwd_impl<float>(sc, x, v, C, F, pos, vel, vpos, cv, cv1, xb1, vb1, Cb1, Fb1, posb1, velb1, vpb1, xb,
+                                 vb, Cb, Fb, posb, velb, vpb, cvb, cvb1, mat_b, svd_grad_mode);
+}
+int orc_substep_bwd_f64(const orc_scene* sc, const double* x, const double* v, const double* C, const double* F,
+                        const double* const* pos, const double* const* vel, const double* const* vpos,
+                        const double* const* cv, const double* const* cv1, const double* xb1, const double* vb1,
+                        const double* Cb1, const double* Fb1, const double* const* posb1,
+                        const double* const* velb1, const double* const* vpb1, double* xb, double* vb, double* Cb,
+                        double* Fb, double* const* posb, double* const* velb, double* const* vpb,
+                        double* const* cvb, double* const* cvb1, double* mat_b, int svd_grad_mode) {
+  return substep_bwd_impl<double>(sc, x, v, C, F, pos, vel, vpos, cv, cv1, xb1, vb1, Cb1, Fb1, posb1, velb1, vpb1,
+                                  xb, vb, Cb, Fb, posb, velb, vpb, cvb, cvb1, mat_b, svd_grad_mode);
 }
 
 int orc_abi_version(void) { return 1; }

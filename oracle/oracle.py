@@ -53,6 +53,10 @@ def lib():
             fn.argtypes = [I, P, P, P, P, I]
         L.orc_find_closest_f32.restype = None
         L.orc_find_closest_f32.argtypes = [P, P, I, P, P]
+        for name in ("orc_substep_bwd_f32", "orc_substep_bwd_f64"):
+            fn = getattr(L, name)
+            fn.restype = I
+            fn.argtypes = [P] * 27 + [I]
         _lib = L
     return _lib
 
@@ -163,6 +167,39 @@ class Oracle:
         dbg = {"grid_m": gm, "grid_v_in": gvi, "grid_v_out": gvo, "grid_f": gf, "cidx": cidx, "vel_mid": vel,
                "ext": ext, "err": err}
         return out, dbg
+
+    def substep_bwd(self, st, adj1, cv=None, cv1=None, svd_grad_mode=0):
+        """Adjoint of one substep (recomputes the forward internally).  ``adj1``: adjoint of frame
+        f+1 with keys x, v, C, F (and per-sensor lists pos, vel, vpos).  Returns the adjoint of frame
+        f (same keys) plus per-sensor control-velocity adjoints cv (frame f), cv1 (frame f+1) and the
+        material adjoint mat [n_materials, 2] (d/dmu, d/dlambda)."""
+        T = self.dtype
+        e = self.env
+        N = e.n_particles
+        NS = len(e.sensors)
+        c = lambda a: np.ascontiguousarray(a, T)  # noqa: E731
+        x, v, Cm, F = c(st["x"]), c(st["v"]), c(st["C"]), c(st["F"])
+        zeros_v = [np.zeros((len(sp.verts), 3), T) for sp in e.sensors]
+        pos = [c(a) for a in st.get("pos", [])]
+        vel = [c(a) for a in st.get("vel", [])]
+        vpos = [c(a) for a in st.get("vpos", [])]
+        cv = [c(a) for a in cv] if cv is not None else zeros_v
+        cv1 = [c(a) for a in cv1] if cv1 is not None else cv
+        a1 = {k: c(adj1[k]) for k in ("x", "v", "C", "F")}
+        for k in ("pos", "vel", "vpos"):
+            a1[k] = [c(a) for a in adj1.get(k, zeros_v)]
+        out = {"x": np.zeros((N, 3), T), "v": np.zeros((N, 3), T), "C": np.zeros((N, 3, 3), T),
+               "F": np.zeros((N, 3, 3), T)}
+        for k in ("pos", "vel", "vpos", "cv", "cv1"):
+            out[k] = [np.zeros_like(z) for z in zeros_v]
+        out["mat"] = np.zeros((len(e.materials), 2), T)
+        fn = lib().orc_substep_bwd_f32 if T == np.float32 else lib().orc_substep_bwd_f64
+        fn(C.byref(self.sc), _ptr(x), _ptr(v), _ptr(Cm), _ptr(F), _ptr_array(pos), _ptr_array(vel), _ptr_array(vpos),
+           _ptr_array(cv), _ptr_array(cv1), _ptr(a1["x"]), _ptr(a1["v"]), _ptr(a1["C"]), _ptr(a1["F"]),
+           _ptr_array(a1["pos"]), _ptr_array(a1["vel"]), _ptr_array(a1["vpos"]), _ptr(out["x"]), _ptr(out["v"]),
+           _ptr(out["C"]), _ptr(out["F"]), _ptr_array(out["pos"]), _ptr_array(out["vel"]), _ptr_array(out["vpos"]),
+           _ptr_array(out["cv"]), _ptr_array(out["cv1"]), _ptr(out["mat"]), svd_grad_mode)
+        return out
 
 
 def svd3(A, dtype=np.float32, sweeps=None):

@@ -136,3 +136,22 @@ def test_adjoint_matches_finite_differences(cuda_lib, model, ys):
         if rel > 1e-3:
             failures.append((groups if len(groups) == 1 else "all", pred, fd, rel))
     assert not failures, failures
+
+
+@pytest.mark.parametrize("model,ys", [(S.MODEL_COROTATED, 50.0), (S.MODEL_VON_MISES, 2.0)])
+def test_adjoint_matches_oracle_adjoint(cuda_lib, model, ys):
+    """Whole adjoint arrays of one substep against the oracle's float64 adjoint (norm-wise 1e-3)."""
+    env = SS.pad_over_box(n=40, box_cells=(10, 6, 10), pad=(10, 10, 3), model=model, yield_stress=ys)
+    st0, cv = base_point(env, 7)
+    W = loss_weights(env, env.n_particles, 8)
+    g = gpu_grads(env, st0, cv, W, 1)
+    o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
+    ref = o.substep_bwd({k: (v if not isinstance(v, list) else [a.copy() for a in v]) for k, v in st0.items()}, W,
+                        cv=cv, cv1=cv)
+    errs = {k: SS.rel_err(g[k], ref[k]) for k in ("x", "v", "C", "F")}
+    for k in ("pos", "vel", "vpos"):
+        errs[k] = SS.rel_err(g[k][0], ref[k][0])
+    errs["cv"] = SS.rel_err(g["cv"][0], ref["cv"][0] + ref["cv1"][0])
+    errs["mu"] = abs(g["mu"] - ref["mat"][0, 0]) / abs(ref["mat"][0, 0])
+    errs["lam"] = abs(g["lam"] - ref["mat"][0, 1]) / abs(ref["mat"][0, 1])
+    assert max(errs.values()) < 1e-3, errs
