@@ -71,6 +71,7 @@ SIGNATURES = {
     "dt_step_begin": (C.c_int, [_W, _P]),
     "dt_substep_fwd": (C.c_int, [_W, C.c_int, _P]),
     "dt_substep_fwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),
+    "dt_substep_fwd_noalloc": (C.c_int, [_W, C.c_int, _P]),
     "dt_p2g": (C.c_int, [_W, C.c_int, _P]),
     "dt_fem_update": (C.c_int, [_W, C.c_int, _P]),
     "dt_grid_op": (C.c_int, [_W, C.c_int, _P]),

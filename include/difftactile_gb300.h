@@ -198,6 +198,20 @@ int dt_substep_fwd(const dt_world* w, int f, cudaStream_t stream);
  * update + contact; 2: G2P + FEM integration), for timing and for callers that interleave work. */
 int dt_substep_fwd_stage(const dt_world* w, int f, int stage, cudaStream_t stream);
 
+/* No counterpart in the reference.  dt_substep_fwd for callers that cannot allocate device memory
+ * (their buffers live in memory another allocator owns, e.g. a framework's caching allocator or an
+ * arena reserved at start-up under a fixed device-memory budget, so they may not call cudaMalloc).
+ * The caller provides inputs and outputs as for dt_substep_fwd; the scratch (grid accumulator and
+ * velocities, active-block flags and list, the frame's grid tape, triangle centroids) lives in one
+ * static device array inside the library (~21 MB, held by every GPU that loads the library until the
+ * process exits); w's scratch pointers are ignored and may be NULL.  Limits: n_nodes <= 64^3,
+ * n_blocks <= 4096, n_tris <= 8192, else DT_ERR_CAPACITY.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams, other threads) race.
+ * The grid tape written here is scratch, so dt_substep_bwd cannot follow this call; it allocates
+ * nothing (no cudaMalloc, cudaFree or allocating library routine). */
+int dt_substep_fwd_noalloc(const dt_world* w, int f, cudaStream_t stream);
+
 /* The same substep split into the reference's per-object calls, for drop-in use of the
  * reference method sequence.  dt_substep_fwd(f) == p2g(f); fem_update(f); grid_op(f) (which
  * includes check_grid_occupy, check_collision and collision); g2p(f); fem_update2(f). */
