@@ -57,7 +57,7 @@ WORLD_INT_FIELDS = [
 class DtWorld(C.Structure):
     _fields_ = ([(n, _P) for n in WORLD_PTR_FIELDS] + [(n, C.c_int) for n in WORLD_INT_FIELDS]
                 + [("dt", C.c_float), ("grad_clip", C.c_float), ("svd_sweeps", C.c_int),
-                   ("svd_grad_mode", C.c_int), ("max_sensor_tris", C.c_int), ("pad_", C.c_int)])
+                   ("svd_grad_mode", C.c_int), ("max_sensor_tris", C.c_int), ("scatter_mode", C.c_int)])
 
 
 # entry points: name -> (restype, argtypes)

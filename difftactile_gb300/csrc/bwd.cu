@@ -18,6 +18,9 @@ namespace {
 
 constexpr int NT = 128;
 constexpr int GRID_NT = 64;
+constexpr int TILE_MAX = 1728;  // shared scatter tile capacity in nodes (12^3)
+
+DT_DEV float sel3(const float a[3], int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); }
 
 DT_DEV float clampg(float a, float c) { return c > 0.f ? fminf(fmaxf(a, -c), c) : a; }
 DT_DEV v3 clampg(v3 a, float c) { return v3{clampg(a.x, c), clampg(a.y, c), clampg(a.z, c)}; }
@@ -75,68 +78,89 @@ __global__ void __launch_bounds__(GRID_NT) k_bwd_restore(dt_world w, int f) {
 // ---------------------------------------------------------------------------------------------
 // B1
 // ---------------------------------------------------------------------------------------------
-__device__ void g2p_bwd(const dt_world& w, int f, int p) {
+// G2P adjoint of one CTA's particles: the position adjoint needs the grid velocities (a gather);
+// the grid-velocity adjoint W (vn_bar + 4 inv_dx C_bar (o - fx)) = W (q + o . c) is a 27-node
+// scatter, privatised through the shared-memory tile.
+__device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile, int* sh) {
+  const int p = chunk * NT + threadIdx.x;
+  const bool valid = p < w.n_particles;
   const int nb = (f + 1) & 1, cb = f & 1;
-  const float4 a0 = ld4(padj(w, nb, 0) + p), a1 = ld4(padj(w, nb, 1) + p), a2 = ld4(padj(w, nb, 2) + p),
-               a3 = ld4(padj(w, nb, 3) + p);
-  const v3 xb1 = v3{a0.x, a0.y, a0.z};
-  const v3 vb1 = v3{a0.w, a1.x, a1.y};
-  m3 Cb;
-  Cb.a[0][0] = a1.z;
-  Cb.a[0][1] = a1.w;
-  Cb.a[0][2] = a2.x;
-  Cb.a[1][0] = a2.y;
-  Cb.a[1][1] = a2.z;
-  Cb.a[1][2] = a2.w;
-  Cb.a[2][0] = a3.x;
-  Cb.a[2][1] = a3.y;
-  Cb.a[2][2] = a3.z;
-  const v3 x = f4to3(ldg4(pplane(w, f, 0) + p));
-  const dt_env& E = w.envs[__ldg(w.p_env + p)];
-  int base[3];
-  float fx[3];
-  float4* out0 = padj(w, cb, 0) + p;
-  if (!particle_base(E, x, base, fx)) {
-    *out0 = make_float4(xb1.x, xb1.y, xb1.z, 0.f);  // carried unchanged in the forward pass
-    return;
-  }
-  // x_new = x + dt v_new
-  const v3 vnb = vb1 + w.dt * xb1;
-  float fxb[3] = {0.f, 0.f, 0.f};
-  const float4* vout = reinterpret_cast<const float4*>(w.g_vout);
-  float4* avout = reinterpret_cast<float4*>(w.g_adj_vout);
-  float wts[3][3], dws[3][3];
+  int base[3] = {0, 0, 0};
+  float fx[3] = {0.f, 0.f, 0.f};
+  bool ok = false;
+  int env = 0;
+  float wx[3] = {0.f, 0.f, 0.f}, wy[3] = {0.f, 0.f, 0.f}, wz[3] = {0.f, 0.f, 0.f};
+  v3 q = v3{0.f, 0.f, 0.f}, c0 = q, c1 = q, c2 = q;
+  if (valid) {
+    const float4 a0 = ld4(padj(w, nb, 0) + p), a1 = ld4(padj(w, nb, 1) + p), a2 = ld4(padj(w, nb, 2) + p),
+                 a3 = ld4(padj(w, nb, 3) + p);
+    const v3 xb1 = v3{a0.x, a0.y, a0.z};
+    const v3 vb1 = v3{a0.w, a1.x, a1.y};
+    m3 Cb;
+    Cb.a[0][0] = a1.z;
+    Cb.a[0][1] = a1.w;
+    Cb.a[0][2] = a2.x;
+    Cb.a[1][0] = a2.y;
+    Cb.a[1][1] = a2.z;
+    Cb.a[1][2] = a2.w;
+    Cb.a[2][0] = a3.x;
+    Cb.a[2][1] = a3.y;
+    Cb.a[2][2] = a3.z;
+    const v3 x = f4to3(ldg4(pplane(w, f, 0) + p));
+    env = __ldg(w.p_env + p);
+    const dt_env& E = w.envs[env];
+    float4* out0 = padj(w, cb, 0) + p;
+    ok = particle_base(E, x, base, fx);
+    if (!ok) {
+      *out0 = make_float4(xb1.x, xb1.y, xb1.z, 0.f);  // carried unchanged in the forward pass
+    } else {
+      const v3 vnb = vb1 + w.dt * xb1;  // x_new = x + dt v_new
+      float fxb[3] = {0.f, 0.f, 0.f};
+      const float4* vout = reinterpret_cast<const float4*>(w.g_vout);
+      float dws[3][3];
 #pragma unroll
-  for (int d = 0; d < 3; ++d)
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      wts[i][d] = bsw(i, fx[d]);
-      dws[i][d] = bsdw(i, fx[d]);
-    }
-#pragma unroll
-  for (int oi = 0; oi < 3; ++oi)
-#pragma unroll
-    for (int oj = 0; oj < 3; ++oj)
-#pragma unroll
-      for (int ok = 0; ok < 3; ++ok) {
-        const int n = node_index(E, base[0] + oi, base[1] + oj, base[2] + ok);
-        const v3 gv = f4to3(__ldg(vout + n));
-        const float W = (wts[oi][0] * wts[oj][1]) * wts[ok][2];
-        const float kw = E.g2p_k * W;
-        const v3 d = v3{(float)oi - fx[0], (float)oj - fx[1], (float)ok - fx[2]};
-        const v3 Cd = mvec(Cb, d);       // C_bar d
-        const v3 Ctg = mTvec(Cb, gv);    // C_bar^T gv
-        // v_out adjoint
-        const v3 gvb = W * vnb + kw * Cd;
-        red_add_v4(avout + n, v3to4(gvb));
-        // weight adjoint and offset adjoint
-        const float Wb = dot(gv, vnb) + E.g2p_k * dot(gv, Cd);
-        fxb[0] += Wb * (dws[oi][0] * wts[oj][1] * wts[ok][2]) - kw * Ctg.x;
-        fxb[1] += Wb * (wts[oi][0] * dws[oj][1] * wts[ok][2]) - kw * Ctg.y;
-        fxb[2] += Wb * (wts[oi][0] * wts[oj][1] * dws[ok][2]) - kw * Ctg.z;
+      for (int i = 0; i < 3; ++i) {
+        wx[i] = bsw(i, fx[0]);
+        wy[i] = bsw(i, fx[1]);
+        wz[i] = bsw(i, fx[2]);
+        dws[i][0] = bsdw(i, fx[0]);
+        dws[i][1] = bsdw(i, fx[1]);
+        dws[i][2] = bsdw(i, fx[2]);
       }
-  const v3 xb = xb1 + E.inv_dx * v3{fxb[0], fxb[1], fxb[2]};
-  *out0 = make_float4(xb.x, xb.y, xb.z, 0.f);
+#pragma unroll
+      for (int oi = 0; oi < 3; ++oi)
+#pragma unroll
+        for (int oj = 0; oj < 3; ++oj)
+#pragma unroll
+          for (int ok_ = 0; ok_ < 3; ++ok_) {
+            const v3 gv = f4to3(__ldg(vout + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok_)));
+            const float W = (wx[oi] * wy[oj]) * wz[ok_];
+            const float kw = E.g2p_k * W;
+            const v3 d = v3{(float)oi - fx[0], (float)oj - fx[1], (float)ok_ - fx[2]};
+            const v3 Ctg = mTvec(Cb, gv);  // C_bar^T gv
+            const float Wb = dot(gv, vnb) + E.g2p_k * dot(Ctg, d);
+            fxb[0] += Wb * (dws[oi][0] * wy[oj] * wz[ok_]) - kw * Ctg.x;
+            fxb[1] += Wb * (wx[oi] * dws[oj][1] * wz[ok_]) - kw * Ctg.y;
+            fxb[2] += Wb * (wx[oi] * wy[oj] * dws[ok_][2]) - kw * Ctg.z;
+          }
+      const v3 xb = xb1 + E.inv_dx * v3{fxb[0], fxb[1], fxb[2]};
+      *out0 = make_float4(xb.x, xb.y, xb.z, 0.f);
+      const float gk = E.g2p_k;
+      c0 = gk * mcol(Cb, 0);
+      c1 = gk * mcol(Cb, 1);
+      c2 = gk * mcol(Cb, 2);
+      q = vnb - ((fx[0] * c0 + fx[1] * c1) + fx[2] * c2);
+    }
+  }
+  auto contrib = [&](int oi, int oj, int ok_) {
+    const float W = (sel3(wx, oi) * wy[oj]) * wz[ok_];
+    const v3 t = ((q + (float)oi * c0) + (float)oj * c1) + (float)ok_ * c2;
+    return make_float4(W * t.x, W * t.y, W * t.z, 0.f);
+  };
+  auto no_box = [](const dt_env&, int, int, int, int, int, int) {};
+  auto no_one = [](const dt_env&) {};
+  tile_scatter<NT, TILE_MAX>(w, chunk, ok, env, base, tile, sh, reinterpret_cast<float4*>(w.g_adj_vout), contrib,
+                             no_box, no_one);
 }
 
 __device__ void integrate_bwd(const dt_world& w, int f, int i) {
@@ -176,10 +200,11 @@ __device__ void integrate_bwd(const dt_world& w, int f, int i) {
 }
 
 __global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
+  extern __shared__ float4 tile[];  // TILE_MAX float4 in tile mode, none otherwise
+  __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
-    int p = b * NT + threadIdx.x;
-    if (p < w.n_particles) g2p_bwd(w, f, p);
+    g2p_bwd_chunk(w, f, b, tile, sh);
     return;
   }
   b -= nb_p;
@@ -676,7 +701,7 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
       if (ng > 0) k_bwd_restore<<<ng, GRID_NT, 0, stream>>>(*w, f);
       break;
     case 1:
-      if (nb_p + nb_v) k_bwd_g2p_fem<<<nb_p + nb_v, NT, 0, stream>>>(*w, f, nb_p, nb_v);
+      if (nb_p + nb_v) k_bwd_g2p_fem<<<nb_p + nb_v, NT, (w->scatter_mode == DT_SCATTER_TILE ? TILE_MAX * sizeof(float4) : 0), stream>>>(*w, f, nb_p, nb_v);
       break;
     case 2:
       if (ng > 0) k_bwd_grid<<<ng, GRID_NT, 0, stream>>>(*w, f);

@@ -151,9 +151,10 @@ DT_DEV v3 mTvec(const m3& m, v3 v) {
 DT_DEV void jacobi_rot(float S[3][3], float V[3][3], int p, int q) {
   float apq = S[p][q];
   if (apq == 0.f) return;
-  float tau = (S[q][q] - S[p][p]) / (2.f * apq);
-  float t = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
-  float c = 1.f / sqrtf(1.f + t * t);
+  // reciprocal-based: the rotation only has to be orthogonal to rounding, not correctly rounded
+  float tau = __fdividef(S[q][q] - S[p][p], 2.f * apq);
+  float t = __fdividef(tau >= 0.f ? 1.f : -1.f, fabsf(tau) + sqrtf(fmaf(tau, tau, 1.f)));
+  float c = rsqrtf(fmaf(t, t, 1.f));
   float s = t * c;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -189,11 +190,12 @@ DT_DEV void swap_cols_neg(float B[3][3], float V[3][3], int i, int j) {
 
 DT_DEV void qr_givens(float B[3][3], float U[3][3], int i, int j, int col) {
   float a = B[i][col], b = B[j][col];
-  float r = sqrtf(a * a + b * b);
+  float r2 = a * a + b * b;
   float c = 1.f, s = 0.f;
-  if (r > 1e-30f) {
-    c = a / r;
-    s = b / r;
+  if (r2 > 1e-30f) {
+    const float ir = rsqrtf(r2);
+    c = a * ir;
+    s = b * ir;
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -217,6 +219,10 @@ DT_DEV void svd3(const m3& A, m3& U, v3& sv, m3& V, int sweeps) {
     for (int j = 0; j < 3; ++j) S[i][j] = A.a[0][i] * A.a[0][j] + A.a[1][i] * A.a[1][j] + A.a[2][i] * A.a[2][j];
   float Vm[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
   for (int it = 0; it < sweeps; ++it) {
+    // converged once the off-diagonal is below fp32 resolution of the diagonal
+    const float off = S[0][1] * S[0][1] + S[0][2] * S[0][2] + S[1][2] * S[1][2];
+    const float dia = S[0][0] * S[0][0] + S[1][1] * S[1][1] + S[2][2] * S[2][2];
+    if (off <= 1e-15f * dia) break;
     jacobi_rot(S, Vm, 0, 1);
     jacobi_rot(S, Vm, 0, 2);
     jacobi_rot(S, Vm, 1, 2);
@@ -456,6 +462,99 @@ DT_DEV v3 contact_force(const dt_env& E, float sdf, v3 n, v3 r) {
     ft = v3{(vt.x / vtn) * g, (vt.y / vtn) * g, (vt.z / vtn) * g};
   }
   return fn + ft;
+}
+
+// ------------------------------------------------------------------------------------------
+// Privatised 27-node scatter of one CTA's particles (P2G and the G2P adjoint).
+// The CTA's consecutive particles (spatially sorted) are reduced to the bounding box of their base
+// cells; if the box fits TILE_MAX nodes and all particles share one environment, every particle
+// adds its 27 contributions into a shared-memory tile (i offset rotated by lane to spread
+// same-address atomics), and each touched node is flushed with one 16-byte vector RED.  Otherwise
+// each particle issues its 27 vector REDs directly.  `contrib(oi, oj, ok)` returns the float4 added
+// at node base + (oi, oj, ok); `mark_blocks(lo, hi)` is called for the tile's node box, and
+// `mark_particle()` per particle on the direct path.
+// ------------------------------------------------------------------------------------------
+template <int NT, int TILE_MAX, typename Contrib, typename MarkBox, typename MarkOne>
+DT_DEV void tile_scatter(const dt_world& w, int chunk, bool ok, int env, const int base[3], float4* tile, int* sh,
+                         float4* dst, const Contrib& contrib, const MarkBox& mark_box, const MarkOne& mark_one) {
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  if (tid == 0) {
+    sh[0] = sh[1] = sh[2] = 0x7fffffff;
+    sh[3] = sh[4] = sh[5] = (int)0x80000000;
+    const int p0 = chunk * NT, p1 = min(p0 + NT, w.n_particles) - 1;
+    sh[6] = (w.p_env[p0] == w.p_env[p1]) ? 1 : 0;
+  }
+  __syncthreads();
+  int lo0 = ok ? base[0] : 0x7fffffff, lo1 = ok ? base[1] : 0x7fffffff, lo2 = ok ? base[2] : 0x7fffffff;
+  int hi0 = ok ? base[0] : (int)0x80000000, hi1 = ok ? base[1] : (int)0x80000000,
+      hi2 = ok ? base[2] : (int)0x80000000;
+  lo0 = __reduce_min_sync(0xffffffffu, lo0);
+  lo1 = __reduce_min_sync(0xffffffffu, lo1);
+  lo2 = __reduce_min_sync(0xffffffffu, lo2);
+  hi0 = __reduce_max_sync(0xffffffffu, hi0);
+  hi1 = __reduce_max_sync(0xffffffffu, hi1);
+  hi2 = __reduce_max_sync(0xffffffffu, hi2);
+  if (lane == 0 && hi0 != (int)0x80000000) {
+    atomicMin(sh + 0, lo0);
+    atomicMin(sh + 1, lo1);
+    atomicMin(sh + 2, lo2);
+    atomicMax(sh + 3, hi0);
+    atomicMax(sh + 4, hi1);
+    atomicMax(sh + 5, hi2);
+  }
+  __syncthreads();
+  const int L0 = sh[0], L1 = sh[1], L2 = sh[2];
+  const bool any = sh[3] != (int)0x80000000;
+  const int ex = any ? sh[3] - L0 + 3 : 0, ey = any ? sh[4] - L1 + 3 : 0, ez = any ? sh[5] - L2 + 3 : 0;
+  const int tile_n = ex * ey * ez;
+  const bool use_tile = w.scatter_mode == DT_SCATTER_TILE && any && sh[6] && tile_n <= TILE_MAX;
+  if (use_tile) {
+    for (int i = tid; i < tile_n; i += NT) tile[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    if (ok) {
+      const int r = lane % 3;
+      const int row0 = (base[1] - L1) * ez + (base[2] - L2);
+#pragma unroll
+      for (int ti = 0; ti < 3; ++ti) {
+        int oi = ti + r;
+        oi = oi >= 3 ? oi - 3 : oi;
+        const int rowi = (base[0] + oi - L0) * ey * ez + row0;
+#pragma unroll
+        for (int oj = 0; oj < 3; ++oj)
+#pragma unroll
+          for (int ok_ = 0; ok_ < 3; ++ok_) {
+            const float4 c = contrib(oi, oj, ok_);
+            float* tp = reinterpret_cast<float*>(tile + rowi + oj * ez + ok_);
+            atomicAdd(tp + 0, c.x);
+            atomicAdd(tp + 1, c.y);
+            atomicAdd(tp + 2, c.z);
+            atomicAdd(tp + 3, c.w);
+          }
+      }
+    }
+    __syncthreads();
+    const int env0 = w.p_env[min(chunk * NT, w.n_particles - 1)];
+    const dt_env& E0 = w.envs[env0];
+    for (int i = tid; i < tile_n; i += NT) {
+      const float4 a = tile[i];
+      if (a.w != 0.f || a.x != 0.f || a.y != 0.f || a.z != 0.f) {
+        const int c = i % ez, b_ = (i / ez) % ey, a_ = i / (ey * ez);
+        red_add_v4(dst + node_index(E0, L0 + a_, L1 + b_, L2 + c), a);
+      }
+    }
+    mark_box(E0, L0, L1, L2, L0 + ex - 1, L1 + ey - 1, L2 + ez - 1);
+  } else if (ok) {
+    const dt_env& E = w.envs[env];
+#pragma unroll
+    for (int oi = 0; oi < 3; ++oi)
+#pragma unroll
+      for (int oj = 0; oj < 3; ++oj)
+#pragma unroll
+        for (int ok_ = 0; ok_ < 3; ++ok_)
+          red_add_v4(dst + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok_), contrib(oi, oj, ok_));
+    mark_one(E);
+  }
 }
 
 // bit-reproducible centroid distance (find_closest, fem_sensor.py:352-353): every operation

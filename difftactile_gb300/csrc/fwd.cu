@@ -36,39 +36,23 @@ __device__ void mark_block(const dt_world& w, int f, int b) {
   }
 }
 
-__device__ __forceinline__ float4 p2g_contrib(const Stress& s, const PRec& r, float p_mass, float stress_k,
-                                              float dx, const float fx[3], int oi, int oj, int ok, float W) {
-  // affine = stress + p_mass C ; contribution = W (p_mass v + affine dpos), dpos = (o - fx) dx
-  float d0 = ((float)oi - fx[0]) * dx, d1 = ((float)oj - fx[1]) * dx, d2 = ((float)ok - fx[2]) * dx;
-  float a[3];
-#pragma unroll
-  for (int r_ = 0; r_ < 3; ++r_) {
-    float A0 = stress_k * s.cauchy.a[r_][0] + p_mass * r.C.a[r_][0];
-    float A1 = stress_k * s.cauchy.a[r_][1] + p_mass * r.C.a[r_][1];
-    float A2 = stress_k * s.cauchy.a[r_][2] + p_mass * r.C.a[r_][2];
-    a[r_] = A0 * d0 + A1 * d1 + A2 * d2;
-  }
-  return make_float4(W * (p_mass * r.v.x + a[0]), W * (p_mass * r.v.y + a[1]), W * (p_mass * r.v.z + a[2]),
-                     W * p_mass);
-}
+DT_DEV float sel3(const float a[3], int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); }
 
+// P2G of one CTA's particles (mpm_elastic.py:176-208 / mpm_plastic.py:222-256 / multi_obj.py:228-252):
+// contribution at node base + o is W_o (p_mass v + A (o - fx) dx) = W_o (b + o . (dx A)), with
+// A = stress + p_mass C and b = p_mass v - dx A fx precomputed once per particle.
 __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int* sh) {
-  const int tid = threadIdx.x;
-  const int lane = tid & 31;
-  const int p = chunk * NT + tid;
+  const int p = chunk * NT + threadIdx.x;
   const bool valid = p < w.n_particles;
-  if (tid == 0) {
-    sh[0] = sh[1] = sh[2] = INT_MAX;
-    sh[3] = sh[4] = sh[5] = INT_MIN;
-    int p0 = chunk * NT, p1 = min(p0 + NT, w.n_particles) - 1;
-    sh[6] = (w.p_env[p0] == w.p_env[p1]) ? 1 : 0;
-  }
   PRec r;
   Stress s;
   int base[3] = {0, 0, 0};
   float fx[3] = {0.f, 0.f, 0.f};
   bool ok = false;
   int env = 0;
+  float wx[3] = {0.f, 0.f, 0.f}, wy[3] = {0.f, 0.f, 0.f}, wz[3] = {0.f, 0.f, 0.f};
+  v3 b = v3{0.f, 0.f, 0.f}, c0 = b, c1 = b, c2 = b;
+  float pm = 0.f;
   if (valid) {
     float4 q[6];
 #pragma unroll
@@ -81,6 +65,23 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
     if (ok) {
       const dt_material M = w.materials[__ldg(w.p_mat + p)];
       constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s);
+      pm = E.p_mass;
+      const float dx = E.dx, sk = E.stress_k;
+      m3 A;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) A.a[i][j] = sk * s.cauchy.a[i][j] + pm * r.C.a[i][j];
+      c0 = dx * mcol(A, 0);
+      c1 = dx * mcol(A, 1);
+      c2 = dx * mcol(A, 2);
+      b = pm * r.v - ((fx[0] * c0 + fx[1] * c1) + fx[2] * c2);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        wx[i] = bsw(i, fx[0]);
+        wy[i] = bsw(i, fx[1]);
+        wz[i] = bsw(i, fx[2]);
+      }
     } else {
       s.Fp = r.F;
     }
@@ -89,84 +90,28 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
     pplane(w, f + 1, 4)[p] = make_float4(s.Fp.a[0][1], s.Fp.a[0][2], s.Fp.a[1][0], s.Fp.a[1][1]);
     pplane(w, f + 1, 5)[p] = make_float4(s.Fp.a[1][2], s.Fp.a[2][0], s.Fp.a[2][1], s.Fp.a[2][2]);
   }
-  // ---- bounding box of the chunk's base cells ----
-  int lo0 = ok ? base[0] : INT_MAX, lo1 = ok ? base[1] : INT_MAX, lo2 = ok ? base[2] : INT_MAX;
-  int hi0 = ok ? base[0] : INT_MIN, hi1 = ok ? base[1] : INT_MIN, hi2 = ok ? base[2] : INT_MIN;
-  lo0 = __reduce_min_sync(0xffffffffu, lo0);
-  lo1 = __reduce_min_sync(0xffffffffu, lo1);
-  lo2 = __reduce_min_sync(0xffffffffu, lo2);
-  hi0 = __reduce_max_sync(0xffffffffu, hi0);
-  hi1 = __reduce_max_sync(0xffffffffu, hi1);
-  hi2 = __reduce_max_sync(0xffffffffu, hi2);
-  __syncthreads();  // sh[] initialised
-  if (lane == 0 && hi0 != INT_MIN) {
-    atomicMin(sh + 0, lo0);
-    atomicMin(sh + 1, lo1);
-    atomicMin(sh + 2, lo2);
-    atomicMax(sh + 3, hi0);
-    atomicMax(sh + 4, hi1);
-    atomicMax(sh + 5, hi2);
-  }
-  __syncthreads();
-  const int L0 = sh[0], L1 = sh[1], L2 = sh[2];
-  const bool any = sh[3] != INT_MIN;
-  const int ex = any ? sh[3] - L0 + 3 : 0, ey = any ? sh[4] - L1 + 3 : 0, ez = any ? sh[5] - L2 + 3 : 0;
-  const int tile_n = ex * ey * ez;
-  const bool use_tile = any && sh[6] && tile_n <= TILE_MAX;
-  const int env0 = w.p_env[min(chunk * NT, w.n_particles - 1)];
-
-  if (use_tile) {
-    for (int i = tid; i < tile_n; i += NT) tile[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncthreads();
-    if (ok) {
-      const dt_env& E = w.envs[env];
-      const float p_mass = E.p_mass, stress_k = E.stress_k, dx = E.dx;
-      for (int t = 0; t < 27; ++t) {
-        int o = t + lane;
-        o = o >= 27 ? o - 27 : o;
-        o = o >= 27 ? o - 27 : o;
-        const int oi = o / 9, oj = (o / 3) % 3, ok_ = o % 3;
-        const float W = (bsw(oi, fx[0]) * bsw(oj, fx[1])) * bsw(ok_, fx[2]);
-        float4 c = p2g_contrib(s, r, p_mass, stress_k, dx, fx, oi, oj, ok_, W);
-        int ti = ((base[0] + oi - L0) * ey + (base[1] + oj - L1)) * ez + (base[2] + ok_ - L2);
-        float* tp = reinterpret_cast<float*>(tile + ti);
-        atomicAdd(tp + 0, c.x);
-        atomicAdd(tp + 1, c.y);
-        atomicAdd(tp + 2, c.z);
-        atomicAdd(tp + 3, c.w);
-      }
+  auto contrib = [&](int oi, int oj, int ok_) {
+    const float W = (sel3(wx, oi) * wy[oj]) * wz[ok_];
+    const v3 t = ((b + (float)oi * c0) + (float)oj * c1) + (float)ok_ * c2;
+    return make_float4(W * t.x, W * t.y, W * t.z, W * pm);
+  };
+  auto mark_box = [&](const dt_env& E0, int l0, int l1, int l2, int h0, int h1, int h2) {
+    const int b0 = l0 >> 2, b1 = l1 >> 2, b2 = l2 >> 2;
+    const int n0 = (h0 >> 2) - b0 + 1, n1 = (h1 >> 2) - b1 + 1, n2 = (h2 >> 2) - b2 + 1;
+    for (int i = threadIdx.x; i < n0 * n1 * n2; i += NT) {
+      const int c = i % n2, bb = (i / n2) % n1, a = i / (n1 * n2);
+      mark_block(w, f, block_index(E0, b0 + a, b1 + bb, b2 + c));
     }
-    __syncthreads();
-    const dt_env& E0 = w.envs[env0];
-    for (int i = tid; i < tile_n; i += NT) {
-      float4 a = tile[i];
-      if (a.w != 0.f || a.x != 0.f || a.y != 0.f || a.z != 0.f) {
-        int c = i % ez, b_ = (i / ez) % ey, a_ = i / (ey * ez);
-        red_add_v4(reinterpret_cast<float4*>(w.g_acc) + node_index(E0, L0 + a_, L1 + b_, L2 + c), a);
-      }
-    }
-    // mark the blocks covering the box
-    const int b0l = L0 >> 2, b1l = L1 >> 2, b2l = L2 >> 2;
-    const int nb0 = ((L0 + ex - 1) >> 2) - b0l + 1, nb1 = ((L1 + ey - 1) >> 2) - b1l + 1,
-              nb2 = ((L2 + ez - 1) >> 2) - b2l + 1;
-    for (int i = tid; i < nb0 * nb1 * nb2; i += NT) {
-      int c = i % nb2, b_ = (i / nb2) % nb1, a_ = i / (nb1 * nb2);
-      mark_block(w, f, block_index(E0, b0l + a_, b1l + b_, b2l + c));
-    }
-  } else if (ok) {
-    const dt_env& E = w.envs[env];
-    const float p_mass = E.p_mass, stress_k = E.stress_k, dx = E.dx;
-    for (int t = 0; t < 27; ++t) {
-      const int oi = t / 9, oj = (t / 3) % 3, ok_ = t % 3;
-      const float W = (bsw(oi, fx[0]) * bsw(oj, fx[1])) * bsw(ok_, fx[2]);
-      float4 c = p2g_contrib(s, r, p_mass, stress_k, dx, fx, oi, oj, ok_, W);
-      red_add_v4(reinterpret_cast<float4*>(w.g_acc) + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok_), c);
-    }
+  };
+  auto mark_one = [&](const dt_env& E) {
     for (int t = 0; t < 8; ++t) {
-      int bi = (base[0] + 2 * (t >> 2)) >> 2, bj = (base[1] + 2 * ((t >> 1) & 1)) >> 2, bk = (base[2] + 2 * (t & 1)) >> 2;
+      const int bi = (base[0] + 2 * (t >> 2)) >> 2, bj = (base[1] + 2 * ((t >> 1) & 1)) >> 2,
+                bk = (base[2] + 2 * (t & 1)) >> 2;
       mark_block(w, f, block_index(E, bi, bj, bk));
     }
-  }
+  };
+  tile_scatter<NT, TILE_MAX>(w, chunk, ok, env, base, tile, sh, reinterpret_cast<float4*>(w.g_acc), contrib,
+                             mark_box, mark_one);
 }
 
 // FEM elastic forces of one tet (fem_sensor.py:409-440): stable-Neo-Hookean-like P with current
@@ -229,7 +174,7 @@ __device__ void tri_centroid(const dt_world& w, int f, int t) {
 }
 
 __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
-  __shared__ float4 tile[TILE_MAX];
+  extern __shared__ float4 tile[];  // TILE_MAX float4 in tile mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
@@ -480,7 +425,7 @@ int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   int nb_f = fem ? cdiv(w->n_tris, NT) : 0;
   int tot = nb_p + nb_t + nb_f;
   if (tot == 0) return DT_OK;
-  k_fwd_p2g_fem<<<tot, NT, 0, st>>>(*w, f, nb_p, nb_t, nb_f);
+  k_fwd_p2g_fem<<<tot, NT, (w->scatter_mode == DT_SCATTER_TILE ? TILE_MAX * sizeof(float4) : 0), st>>>(*w, f, nb_p, nb_t, nb_f);
   return launched();
 }
 int launch_l2(const dt_world* w, int f, cudaStream_t st) {

@@ -34,7 +34,7 @@ class World:
 
     def __init__(self, envs: list[EnvSpec], n_frames: int, dt: float, device="cuda", tape_blocks: int | None = None,
                  grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True,
-                 svd_grad_mode: int = 0):
+                 svd_grad_mode: int = 0, scatter_mode: int = 1):
         self.lib = N.load()
         self.device = torch.device(device)
         self.specs = envs
@@ -202,6 +202,7 @@ class World:
         w.dt, w.grad_clip, w.svd_sweeps = self.dt, float(grad_clip), int(svd_sweeps)
         w.svd_grad_mode = int(svd_grad_mode)
         w.max_sensor_tris = max([r.nf for r in srows], default=0)
+        w.scatter_mode = int(scatter_mode)
         self.w = w
         self.wp = C.pointer(w)
 
@@ -219,9 +220,18 @@ class World:
                            F=np.broadcast_to(np.eye(3, dtype=np.float32), (Np, 3, 3)))
 
     # ------------------------------------------------------------------------------------------
+    # launches go to ``stream_override`` when set (e.g. a capture stream), else torch's current stream
+    stream_override = None
+
     @property
     def stream(self):
+        if self.stream_override is not None:
+            return self.stream_override
         return torch.cuda.current_stream(self.device).cuda_stream
+
+    def pin_stream(self, handle=None):
+        """Fix the stream handle used by every launch (None: follow torch's current stream)."""
+        self.stream_override = handle
 
     def call(self, name, *args):
         N.check(getattr(self.lib, name)(self.wp, *args, self.stream), name)

@@ -166,8 +166,13 @@ typedef struct dt_world {
   int svd_sweeps;                /* cyclic Jacobi sweeps of the 3x3 SVD (4 is enough for fp32) */
   int svd_grad_mode;             /* DT_SVDGRAD_* */
   int max_sensor_tris;           /* largest nf over the sensors (sizes the contact search's staging) */
-  int pad_;
+  int scatter_mode;              /* DT_SCATTER_*: how P2G and the G2P adjoint accumulate into the grid */
 } dt_world;
+
+/* 27-node particle scatters: privatised in a shared-memory tile per CTA, or vector REDs straight
+ * to global memory (L2 atomics).  Which is faster depends on particle density; bench/autotune picks. */
+#define DT_SCATTER_TILE 0
+#define DT_SCATTER_GLOBAL 1
 
 /* SVD adjoint of the rotation R = U V^T used by the corotated stress:
  * STABLE evaluates the reference formula's rotation term in the algebraically equal form
