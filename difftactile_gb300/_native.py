@@ -40,7 +40,7 @@ class DtMaterial(C.Structure):
 _P = C.c_void_p
 WORLD_PTR_FIELDS = [
     "envs", "sensors", "materials", "p_env", "p_mat", "blk_env", "tets", "tet_B", "tet_sensor", "tris",
-    "v_layer", "v_sensor",
+    "tri_perm", "v_layer", "v_sensor",
     "p_state", "p_adj",
     "g_acc", "g_vout", "g_adj_vout", "g_adj_acc", "blk_flag",
     "tape_blist", "tape_bcount", "tape_acc", "tape_vout", "tape_cidx",

@@ -37,7 +37,11 @@ def _press_env(n_grid=96, box_cells=20, pad=(20, 20, 5), pad_h=0.0125, seed=1, y
     lo = np.array([cx * n_grid - box_cells / 2, 4.0, cz * n_grid - box_cells / 2]) * dx
     hi = lo + box_cells * dx
     x = S.box_particles(lo, hi, dx, 8, seed)
-    sp = S.hex_pad_sensor([cx, hi[1] + 0.37 * dx, cz], nx=pad[0], nz=pad[1], ny=pad[2], h=pad_h, E=1.5e5, nu=0.45)
+    # pad density scaled so that node masses stay those of the 0.0125 m pad: the explicit penalty
+    # contact (stiffness 1e4 per node) needs k dt^2 / m well below 1 on the pad's vertices too
+    rho_pad = 1000.0 * (0.0125 / pad_h) ** 3
+    sp = S.hex_pad_sensor([cx, hi[1] + 0.37 * dx, cz], nx=pad[0], nz=pad[1], ny=pad[2], h=pad_h, E=1.5e5, nu=0.45,
+                          rho=rho_pad)
     env = S.EnvSpec(x=x, materials=[S.Material(E, nu, yield_stress, S.MODEL_VON_MISES)],
                     n_grid=(n_grid, n_grid, n_grid), dx=dx, rho=1000.0, sensors=[sp],
                     kn=1e4, kd=100.0, kt=100.0, mu_t=0.5)

@@ -160,8 +160,11 @@ __device__ void fem_tet(const dt_world& w, int f, int t) {
   red_add_v4(VM + tv.w, v3to4(-((h0 + h1) + h2)));
 }
 
+// centroid of the triangle at contact-search position t, tagged with its sensor-local index
 __device__ void tri_centroid(const dt_world& w, int f, int t) {
-  const int4 tr = __ldg(reinterpret_cast<const int4*>(w.tris) + t);
+  const int src = w.tri_perm ? __ldg(w.tri_perm + t) : t;
+  const int4 tr = __ldg(reinterpret_cast<const int4*>(w.tris) + src);
+  const dt_sensor& S = w.sensors[tr.w];
   const float4* P = vframe(w.v_pos, w, f);
   float4 a = P[tr.x], b = P[tr.y], c = P[tr.z];
   const float third = 1.f / 3.f;
@@ -169,7 +172,7 @@ __device__ void tri_centroid(const dt_world& w, int f, int t) {
   o.x = __fmul_rn(third, __fadd_rn(__fadd_rn(a.x, b.x), c.x));
   o.y = __fmul_rn(third, __fadd_rn(__fadd_rn(a.y, b.y), c.y));
   o.z = __fmul_rn(third, __fadd_rn(__fadd_rn(a.z, b.z), c.z));
-  o.w = 0.f;
+  o.w = __int_as_float(src - S.f_off);
   reinterpret_cast<float4*>(w.tri_cent)[t] = o;
 }
 
@@ -206,9 +209,17 @@ struct Best {
   int i;
 };
 DT_DEV Best lexmin(Best a, Best b) { return (b.d < a.d || (b.d == a.d && b.i < a.i)) ? b : a; }
+// Euclidean distance from p to an axis-aligned box (0 inside)
+DT_DEV float box_dist(float4 lo, float4 hi, float px, float py, float pz) {
+  const float dx = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.f);
+  const float dy = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.f);
+  const float dz = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.f);
+  return sqrtf(dx * dx + dy * dy + dz * dz);
+}
 
 __global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f, int smem_cap) {
   extern __shared__ float4 scent[];
+  float4* gbox = scent + smem_cap;  // 2 float4 per group of 32 centroids
   const int cnt = *((volatile int*)(w.tape_bcount + f));
   const int tid = threadIdx.x;
   const int l = tid >> 2, sub = tid & 3;
@@ -249,29 +260,75 @@ __global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f, int sme
         __syncthreads();
         for (int t = tid; t < nf; t += GRID_NT) scent[t] = __ldg(cent + S.f_off + t);
         __syncthreads();
+        // bounding boxes of groups of 32 consecutive centroids (lower bounds for the search)
+        const int G = (nf + 31) >> 5;
+        for (int gg = tid; gg < G; gg += GRID_NT) {
+          float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.f);
+          for (int t = 32 * gg; t < min(32 * gg + 32, nf); ++t) {
+            const float4 c = scent[t];
+            lo.x = fminf(lo.x, c.x);
+            lo.y = fminf(lo.y, c.y);
+            lo.z = fminf(lo.z, c.z);
+            hi.x = fmaxf(hi.x, c.x);
+            hi.y = fmaxf(hi.y, c.y);
+            hi.z = fmaxf(hi.z, c.z);
+          }
+          gbox[2 * gg] = lo;
+          gbox[2 * gg + 1] = hi;
+        }
+        __syncthreads();
         staged = si;
       }
-      // find_closest (fem_sensor.py:344-359)
-      Best b0{100.f, -1}, b1{100.f, -1};
-      if (occ) {
-        if (in_smem) {
-          for (int t = sub; t < nf; t += 8) {
-            const float d0 = cent_dist(scent[t], px, py, pz);
-            if (d0 < b0.d) b0 = Best{d0, t};
-            const int t1 = t + 4;
-            if (t1 < nf) {
-              const float d1 = cent_dist(scent[t1], px, py, pz);
-              if (d1 < b1.d) b1 = Best{d1, t1};
+      // find_closest (fem_sensor.py:344-359): exact first-minimum argmin with group pruning.  A group
+      // is skipped only when its box distance exceeds the best distance found by more than 1e-5
+      // relative, far above the few-ulp rounding of either distance, so no member could win or tie.
+      Best bb{100.f, -1};
+      if (in_smem) {
+        const int G = occ ? (nf + 31) >> 5 : 0;
+        Best gbest{3.4e38f, 0x7fffffff};
+        for (int gg = sub; gg < G; gg += 4) {
+          const float lb = box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz);
+          if (lb < gbest.d) gbest = Best{lb, gg};
+        }
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+          Best other{__shfl_xor_sync(0xffffffffu, gbest.d, o), __shfl_xor_sync(0xffffffffu, gbest.i, o)};
+          gbest = lexmin(gbest, other);
+        }
+        // no group is selected when every box distance is NaN (non-finite sensor positions): the
+        // sentinel must not be used as an index; the pruned scan below then covers every group
+        const int g0 = gbest.i < G ? gbest.i : -1;
+        if (g0 >= 0) {
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const int t = 32 * g0 + sub + 4 * jj;
+            if (t < nf) {
+              const float4 c = scent[t];
+              bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
             }
           }
-        } else {
-          for (int t = sub; t < nf; t += 4) {
-            const float d0 = cent_dist(__ldg(cent + S.f_off + t), px, py, pz);
-            if (d0 < b0.d) b0 = Best{d0, t};
+        }
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+          Best other{__shfl_xor_sync(0xffffffffu, bb.d, o), __shfl_xor_sync(0xffffffffu, bb.i, o)};
+          bb = lexmin(bb, other);
+        }
+        const float thr = bb.d * (1.f + 1e-5f);
+        for (int gg = sub; gg < G; gg += 4) {
+          if (gg == g0) continue;
+          if (box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr) continue;
+          const int t1 = min(32 * gg + 32, nf);
+          for (int t = 32 * gg; t < t1; ++t) {
+            const float4 c = scent[t];
+            bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
           }
         }
+      } else if (occ) {
+        for (int t = sub; t < nf; t += 4) {
+          const float4 c = __ldg(cent + S.f_off + t);
+          bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
+        }
       }
-      Best bb = lexmin(b0, b1);
 #pragma unroll
       for (int o = 1; o <= 2; o <<= 1) {
         Best other{__shfl_xor_sync(0xffffffffu, bb.d, o), __shfl_xor_sync(0xffffffffu, bb.i, o)};
@@ -432,7 +489,7 @@ int launch_l2(const dt_world* w, int f, cudaStream_t st) {
   int nb = w->n_blocks < 152 * 8 ? w->n_blocks : 152 * 8;
   if (nb <= 0) return DT_OK;
   const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
-  const size_t smem = (size_t)(cap > 0 ? cap : 1) * sizeof(float4);
+  const size_t smem = (size_t)((cap > 0 ? cap : 1) + 2 * ((cap + 31) / 32)) * sizeof(float4);
   static size_t configured = 0;
   if (smem > 48 * 1024 && smem > configured) {
     if (cudaFuncSetAttribute(k_fwd_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

@@ -101,11 +101,25 @@ class World:
         # ---------------- sensors ----------------
         v_off = t_off = f_off = 0
         verts, tets, tris, layer, v_sensor, t_sensor, Bs, srows = [], [], [], [], [], [], [], []
+        tri_perm = []
         for si, (e, sp) in enumerate(sensors):
             nv, nt, nf = len(sp.verts), len(sp.tets), len(sp.tris)
             verts.append(sp.verts.astype(np.float32))
             tets.append(sp.tets.astype(np.int32) + v_off)
             tris.append(np.concatenate([sp.tris.astype(np.int32) + v_off, np.full((nf, 1), si, np.int32)], 1))
+            # contact-search order: rest centroids sorted by a Morton key, so that groups of 32
+            # consecutive positions are compact patches (ties still resolve on the original index)
+            cen = sp.verts[sp.tris].mean(1).astype(np.float64) if nf else np.zeros((0, 3))
+            if nf:
+                lo, hi = cen.min(0), cen.max(0)
+                qv = ((cen - lo) / np.maximum(hi - lo, 1e-12) * 1023).astype(np.int64)
+                key = np.zeros(nf, np.int64)
+                for bit in range(10):
+                    for d in range(3):
+                        key |= ((qv[:, d] >> bit) & 1) << (3 * bit + d)
+                tri_perm.append(np.argsort(key, kind="stable").astype(np.int32) + f_off)
+            else:
+                tri_perm.append(np.zeros(0, np.int32))
             layer.append(sp.layer.astype(np.int32))
             v_sensor.append(np.full(nv, si, np.int32))
             t_sensor.append(np.full(nt, si, np.int32))
@@ -164,6 +178,7 @@ class World:
         t["tet_B"] = dtensor(cat(Bs, (0, 12), np.float32), F32)
         t["tet_sensor"] = dtensor(cat(t_sensor, (0,), np.int32), I32)
         t["tris"] = dtensor(cat(tris, (0, 4), np.int32), I32)
+        t["tri_perm"] = dtensor(cat(tri_perm, (0,), np.int32), I32)
         t["v_layer"] = dtensor(cat(layer, (0,), np.int32), I32)
         t["v_sensor"] = dtensor(cat(v_sensor, (0,), np.int32), I32)
 

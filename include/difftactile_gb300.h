@@ -123,6 +123,8 @@ typedef struct dt_world {
   const float* tet_B;            /* [n_tets][12] rest-shape inverse, 3 rows padded to 4 */
   const int* tet_sensor;         /* [n_tets] */
   const int* tris;               /* [n_tris][4] (a, b, c, sensor) global vertex ids */
+  const int* tri_perm;           /* [n_tris] contact-search order: position -> triangle (global index),
+                                    spatially compact within each sensor; NULL = identity */
   const int* v_layer;            /* [n_verts] layer id; layer 0 is kinematically driven */
   const int* v_sensor;           /* [n_verts] */
   /* ---- particle state ---- */

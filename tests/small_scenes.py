@@ -49,3 +49,33 @@ def rel_err(a, b):
     b = np.asarray(b, np.float64)
     den = max(np.linalg.norm(b), 1e-30)
     return float(np.linalg.norm(a - b) / den)
+
+
+def aligned_pad_over_box(n=32, box_cells=(8, 4, 8), seed=4):
+    """Pad vertices on grid-node planes in x and z: node centres project onto quad diagonals, where the
+    two triangles' centroids are equidistant (exact argmin ties, resolved to the first index)."""
+    dx = 1.0 / n
+    lo = np.array([n / 2 - box_cells[0] / 2, 4, n / 2 - box_cells[2] / 2]) * dx
+    hi = lo + np.array(box_cells) * dx
+    x = S.box_particles(lo, hi, dx, 8, seed)
+    sp = S.hex_pad_sensor([0.5, hi[1] + 0.37 * dx, 0.5], nx=10, nz=10, ny=2, h=dx)
+    return S.EnvSpec(x=x, materials=[S.Material(5e3, 0.3)], n_grid=(n, n, n), dx=dx, rho=1000.0, sensors=[sp],
+                     kn=1e4, kd=100.0, kt=100.0, mu_t=1.0)
+
+
+def dome_over_box(n=40, seed=5):
+    """The reference's dome elastomer (Delaunay mesh, spatially unordered triangles), scaled to
+    radius 0.15 and pressed with its apex into a box."""
+    dx = 1.0 / n
+    lo = np.array([0.5 - 0.12, 4 * dx, 0.5 - 0.12])
+    hi = np.array([0.5 + 0.12, 4 * dx + 0.2, 0.5 + 0.12])
+    x = S.box_particles(lo, hi, dx, 8, seed)
+    nodes, tets, tris, layer = S.dome_mesh()
+    scale = 0.15 / 1.5
+    # dome apex (outer layer, y max) pointing down into the box top
+    M = S.eul2mat_zyx([180.0, 0.0, 0.0], [0.5, hi[1] + 1.5 * scale - 0.3 * dx, 0.5])
+    world = (M[:3, :3] @ (scale * nodes).T).T + M[:3, 3]
+    sp = S.SensorSpec(verts=world.astype(np.float32), tets=tets, tris=tris, layer=layer, mass=1e-3, E=8e3,
+                      nu=0.43, out_dir=tuple(M[:3, :3] @ np.array([0.0, 1.0, 0.0])), trans_world=M)
+    return S.EnvSpec(x=x, materials=[S.Material(5e3, 0.3)], n_grid=(n, n, n), dx=dx, rho=1000.0, sensors=[sp],
+                     kn=1e4, kd=100.0, kt=100.0, mu_t=1.0)

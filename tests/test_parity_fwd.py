@@ -157,3 +157,17 @@ def test_oob_particle_sets_error_and_is_skipped(cuda_lib):
     assert np.array_equal(got[0], x[0])
     w.clear_error()
     assert w.error_word() == 0
+
+
+@pytest.mark.parametrize("maker", [SS.aligned_pad_over_box, SS.dome_over_box])
+def test_contact_argmin_ties_and_unordered_meshes(cuda_lib, maker):
+    """Exact first-minimum argmin on exact ties (grid-aligned pad) and on a spatially unordered
+    triangle list (Delaunay dome), against the oracle's sequential scan."""
+    env = maker()
+    w = run_gpu([env], 1)
+    _, dbg = run_oracle(env, 1)
+    g = w.dense_grid(0)
+    occ = dbg[0]["grid_m"] > env.eps
+    assert occ.sum() > 100
+    ci = g["cidx"].cpu().numpy()[..., 0]
+    assert np.array_equal(ci[occ], dbg[0]["cidx"][..., 0][occ])
