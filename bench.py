@@ -2,8 +2,9 @@
 GB300 (replicas on N GPUs under torchrun).
 
 One bench step = one training iteration of the sensor-press task: 100 control steps x 20 substeps
-forward (device checkpoint of every step start), then the backward sweep (recompute of each step's
-substep tape + adjoint substeps) down to the action gradients.  The unit counts each particle
+forward (every frame kept on the device), then the backward sweep (adjoint substeps straight down
+the tape) down to the action gradients.  The batched-population workload keeps a device checkpoint
+of every step start instead and recomputes each step's substep tape in the backward sweep.  The unit counts each particle
 advanced one substep forward and back-propagated once: n_particles x 100 x 20 per bench step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
@@ -113,9 +114,6 @@ def run_ours(args):
     import torch
     import torch.distributed as dist
 
-    from difftactile_gb300.trajectory import PoseTrajectory
-    from difftactile_gb300.world import World
-
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -129,8 +127,7 @@ def run_ours(args):
             dist.barrier()
 
     cfg = make_config(args.config, args.horizon)
-    w = World(cfg.envs, n_frames=cfg.substeps + 1, dt=cfg.dt, device=dev)
-    traj = PoseTrajectory(w, cfg.n_steps, cfg.ckpt_every, cfg.loss_terms)
+    w, traj = cfg.build(dev)
     acts = torch.as_tensor(cfg.actions, dtype=torch.float64, device=dev)
     t = w.t
     init = [t["p_state"][0].clone(), t["v_pos"][0].clone(), t["v_vel"][0].clone(), t["v_vpos"][0].clone()]
@@ -197,7 +194,9 @@ def run_ours(args):
     value = units * world_size / (ms / 1e3)
 
     # ---- roofline of the dominant kernel ----
-    cnt = t["tape_bcount"].clamp(max=w.tape_blocks).double().mean().item()
+    used = t["tape_bcount"][: traj.f_end]
+    cnt = used.clamp(max=w.tape_blocks).double().mean().item()
+    cnt_max = int(used.max().item())
     unit_counts = {"particle": w.n_particles, "node": 64 * cnt, "tet": w.n_tets, "tri": w.n_tris,
                    "vert": w.n_verts}
     peak, peak_kind = peaks()
@@ -211,7 +210,8 @@ def run_ours(args):
            "config": {"workload": cfg.name, "particles": cfg.n_particles, "control_steps": cfg.n_steps,
                       "substeps": cfg.substeps, "grid": list(cfg.envs[0].n_grid), "envs": len(cfg.envs),
                       "fem_tets": w.n_tets, "fem_nodes": w.n_verts, "surface_tris": w.n_tris,
-                      "checkpoint_every": cfg.ckpt_every, "l2": "flushed between timed iterations (256 MiB write)",
+                      "checkpoint_every": cfg.ckpt_every, "tape_blocks": w.tape_blocks,
+                      "active_blocks_mean": cnt, "active_blocks_max": cnt_max, "l2": "flushed between timed iterations (256 MiB write)",
                       "parallelism": f"replicas x{world_size}"},
            "gpu_launches": launches_per_iter * args.steps,
            "roofline": {"kernel": NAMES[dom], "bound": "hbm", "achieved": achieved, "peak": peak,
@@ -276,7 +276,7 @@ def cpu_baseline(cfg, threads, target_s=15.0):
     cv = [np.zeros((len(s.verts), 3), np.float32) for s in env.sensors]
     adj = {k: np.ones_like(st[k]) for k in ("x", "v", "C", "F")}
     done, t0 = 0, time.perf_counter()
-    # the same work per substep as the GPU's checkpointed sweep: forward, then recompute + adjoint
+    # the reference's work per substep: forward, then (in the backward sweep) recompute + adjoint
     while time.perf_counter() - t0 < target_s and done < cfg.substeps:
         st1, _ = o.substep(st, cv=cv, cv1=cv)
         o.substep_bwd(st, adj, cv=cv, cv1=cv)

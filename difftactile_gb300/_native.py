@@ -83,8 +83,8 @@ SIGNATURES = {
     "dt_adj_clear": (C.c_int, [_W, _P]),
     "dt_com": (C.c_int, [_W, C.c_int, _P, _P]),
     "dt_com_bwd": (C.c_int, [_W, C.c_int, _P, _P]),
-    "dt_pose_control_vel": (C.c_int, [_W, C.c_int, _P, C.c_float, _P]),
-    "dt_pose_control_vel_bwd": (C.c_int, [_W, C.c_int, _P, C.c_float, _P, _P]),
+    "dt_pose_control_vel": (C.c_int, [_W, C.c_int, _P, C.c_float, C.c_int, C.c_int, _P]),
+    "dt_pose_control_vel_bwd": (C.c_int, [_W, C.c_int, _P, C.c_float, _P, C.c_int, C.c_int, _P]),
     "dt_marker_loss": (C.c_int, [_W, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
     "dt_marker_loss_bwd": (C.c_int, [_W, C.c_int, C.c_int, C.c_int, _P, C.c_float, _P]),
 }
@@ -105,7 +105,7 @@ def load(path: str | None = None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("DIFFTACTILE_GB300_LIB") or LIB_PATH
     if not os.path.exists(path):
         raise ImportError(
             f"difftactile_gb300 CUDA library not found at {path}; run "

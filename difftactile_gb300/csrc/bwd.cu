@@ -20,8 +20,6 @@ constexpr int NT = 128;
 constexpr int GRID_NT = 64;
 constexpr int TILE_MAX = 1728;  // shared scatter tile capacity in nodes (12^3)
 
-DT_DEV float sel3(const float a[3], int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); }
-
 DT_DEV float clampg(float a, float c) { return c > 0.f ? fminf(fmaxf(a, -c), c) : a; }
 DT_DEV v3 clampg(v3 a, float c) { return v3{clampg(a.x, c), clampg(a.y, c), clampg(a.z, c)}; }
 DT_DEV float4 ld4(const float4* p) { return *p; }
@@ -152,15 +150,21 @@ __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile,
       q = vnb - ((fx[0] * c0 + fx[1] * c1) + fx[2] * c2);
     }
   }
-  auto contrib = [&](int oi, int oj, int ok_) {
-    const float W = (sel3(wx, oi) * wy[oj]) * wz[ok_];
-    const v3 t = ((q + (float)oi * c0) + (float)oj * c1) + (float)ok_ * c2;
-    return make_float4(W * t.x, W * t.y, W * t.z, 0.f);
-  };
+  StencilRec rec;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    rec.wx[i] = wx[i];
+    rec.wy[i] = wy[i];
+    rec.wz[i] = wz[i];
+  }
+  rec.q = make_float4(q.x, q.y, q.z, 0.f);
+  rec.c0 = c0;
+  rec.c1 = c1;
+  rec.c2 = c2;
   auto no_box = [](const dt_env&, int, int, int, int, int, int) {};
   auto no_one = [](const dt_env&) {};
-  tile_scatter<NT, TILE_MAX>(w, chunk, ok, env, base, tile, sh, reinterpret_cast<float4*>(w.g_adj_vout), contrib,
-                             no_box, no_one);
+  stencil_scatter<NT, TILE_MAX>(w, chunk, ok, env, base, rec, reinterpret_cast<float*>(tile), sh,
+                                reinterpret_cast<float4*>(w.g_adj_vout), no_box, no_one);
 }
 
 __device__ void integrate_bwd(const dt_world& w, int f, int i) {
@@ -200,7 +204,7 @@ __device__ void integrate_bwd(const dt_world& w, int f, int i) {
 }
 
 __global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
-  extern __shared__ float4 tile[];  // TILE_MAX float4 in tile mode, none otherwise
+  extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
@@ -701,7 +705,7 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
       if (ng > 0) k_bwd_restore<<<ng, GRID_NT, 0, stream>>>(*w, f);
       break;
     case 1:
-      if (nb_p + nb_v) k_bwd_g2p_fem<<<nb_p + nb_v, NT, (w->scatter_mode == DT_SCATTER_TILE ? TILE_MAX * sizeof(float4) : 0), stream>>>(*w, f, nb_p, nb_v);
+      if (nb_p + nb_v) k_bwd_g2p_fem<<<nb_p + nb_v, NT, (w->scatter_mode == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0), stream>>>(*w, f, nb_p, nb_v);
       break;
     case 2:
       if (ng > 0) k_bwd_grid<<<ng, GRID_NT, 0, stream>>>(*w, f);

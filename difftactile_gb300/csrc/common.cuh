@@ -2,7 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
-#include "../../include/difftactile_gb300.h"
+#include "difftactile_gb300.h"  // include/ is on the compiler include path
 
 #define DT_DEV __device__ __forceinline__
 
@@ -275,10 +275,12 @@ DT_DEV int block_index(const dt_env& E, int bi, int bj, int bk) {
 // ------------------------------------------------------------------------------------------
 // memory helpers
 // ------------------------------------------------------------------------------------------
+// Fire-and-forget vector reduction into a global accumulator.  No kernel reads back, in the same
+// launch, what its REDs accumulate, so no memory clobber: the compiler may keep loaded values
+// (table fields, particle data) in registers across the 27 REDs of a stencil.
 DT_DEV void red_add_v4(float4* addr, float4 v) {
   asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z),
-               "f"(v.w)
-               : "memory");
+               "f"(v.w));
 }
 DT_DEV float4 ldg4(const float4* p) { return __ldg(p); }
 DT_DEV void set_err(const dt_world& w, int bits) { atomicOr(w.err, bits); }
@@ -465,18 +467,26 @@ DT_DEV v3 contact_force(const dt_env& E, float sdf, v3 n, v3 r) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Privatised 27-node scatter of one CTA's particles (P2G and the G2P adjoint).
+// Privatised 27-node scatter of one CTA's particles (P2G and the G2P adjoint), without atomics on
+// the chunk's own overlaps.  Both scatters have the form
+//     value(node base + o) = W_o (q + o_x c0 + o_y c1 + o_z c2),  W_o = wx[o_x] wy[o_y] wz[o_z].
 // The CTA's consecutive particles (spatially sorted) are reduced to the bounding box of their base
-// cells; if the box fits TILE_MAX nodes and all particles share one environment, every particle
-// adds its 27 contributions into a shared-memory tile (i offset rotated by lane to spread
-// same-address atomics), and each touched node is flushed with one 16-byte vector RED.  Otherwise
-// each particle issues its 27 vector REDs directly.  `contrib(oi, oj, ok)` returns the float4 added
-// at node base + (oi, oj, ok); `mark_blocks(lo, hi)` is called for the tile's node box, and
-// `mark_particle()` per particle on the direct path.
-// ------------------------------------------------------------------------------------------
-template <int NT, int TILE_MAX, typename Contrib, typename MarkBox, typename MarkOne>
-DT_DEV void tile_scatter(const dt_world& w, int chunk, bool ok, int env, const int base[3], float4* tile, int* sh,
-                         float4* dst, const Contrib& contrib, const MarkBox& mark_box, const MarkOne& mark_one) {
+// cells.  If the box holds at most TILE_MAX nodes and one environment, every particle writes its
+// stencil record (base, 9 weights, q, c0, c1, c2) to shared memory and each thread owns nodes of
+// the box: it sums the contributions of the chunk's particles whose stencil covers its node and
+// issues one 16-byte vector RED per node — the CTA's same-node contributions never meet in an
+// atomic.  Otherwise (dispersed particles) each particle issues its 27 vector REDs directly.
+// `mark_box` is called for the box when it is compact, `mark_one` per particle otherwise.
+// Shared memory: 25 * NT words.
+struct StencilRec {
+  float wx[3], wy[3], wz[3];
+  float4 q;
+  v3 c0, c1, c2;
+};
+
+template <int NT, int TILE_MAX, typename MarkBox, typename MarkOne>
+DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, const int base[3], const StencilRec& r,
+                            float* sm, int* sh, float4* dst, const MarkBox& mark_box, const MarkOne& mark_one) {
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   if (tid == 0) {
@@ -508,52 +518,82 @@ DT_DEV void tile_scatter(const dt_world& w, int chunk, bool ok, int env, const i
   const bool any = sh[3] != (int)0x80000000;
   const int ex = any ? sh[3] - L0 + 3 : 0, ey = any ? sh[4] - L1 + 3 : 0, ez = any ? sh[5] - L2 + 3 : 0;
   const int tile_n = ex * ey * ez;
-  const bool use_tile = w.scatter_mode == DT_SCATTER_TILE && any && sh[6] && tile_n <= TILE_MAX;
-  if (use_tile) {
-    for (int i = tid; i < tile_n; i += NT) tile[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncthreads();
-    if (ok) {
-      const int r = lane % 3;
-      const int row0 = (base[1] - L1) * ez + (base[2] - L2);
-#pragma unroll
-      for (int ti = 0; ti < 3; ++ti) {
-        int oi = ti + r;
-        oi = oi >= 3 ? oi - 3 : oi;
-        const int rowi = (base[0] + oi - L0) * ey * ez + row0;
-#pragma unroll
-        for (int oj = 0; oj < 3; ++oj)
-#pragma unroll
-          for (int ok_ = 0; ok_ < 3; ++ok_) {
-            const float4 c = contrib(oi, oj, ok_);
-            float* tp = reinterpret_cast<float*>(tile + rowi + oj * ez + ok_);
-            atomicAdd(tp + 0, c.x);
-            atomicAdd(tp + 1, c.y);
-            atomicAdd(tp + 2, c.z);
-            atomicAdd(tp + 3, c.w);
-          }
-      }
-    }
-    __syncthreads();
-    const int env0 = w.p_env[min(chunk * NT, w.n_particles - 1)];
-    const dt_env& E0 = w.envs[env0];
-    for (int i = tid; i < tile_n; i += NT) {
-      const float4 a = tile[i];
-      if (a.w != 0.f || a.x != 0.f || a.y != 0.f || a.z != 0.f) {
-        const int c = i % ez, b_ = (i / ez) % ey, a_ = i / (ey * ez);
-        red_add_v4(dst + node_index(E0, L0 + a_, L1 + b_, L2 + c), a);
-      }
-    }
+  const bool compact = any && sh[6] && tile_n <= TILE_MAX;
+  const bool gather = w.scatter_mode == DT_SCATTER_TILE && compact;
+  if (compact) {
+    const dt_env& E0 = w.envs[w.p_env[min(chunk * NT, w.n_particles - 1)]];
     mark_box(E0, L0, L1, L2, L0 + ex - 1, L1 + ey - 1, L2 + ez - 1);
+  }
+  if (gather) {
+    // stencil records, structure of arrays: rows 0-2 base (int bits), 3-11 weights, 12-15 q, 16-24 c
+    float* rec = sm;
+    rec[0 * NT + tid] = __int_as_float(ok ? base[0] - L0 : -1000);
+    rec[1 * NT + tid] = __int_as_float(ok ? base[1] - L1 : -1000);
+    rec[2 * NT + tid] = __int_as_float(ok ? base[2] - L2 : -1000);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      rec[(3 + i) * NT + tid] = r.wx[i];
+      rec[(6 + i) * NT + tid] = r.wy[i];
+      rec[(9 + i) * NT + tid] = r.wz[i];
+    }
+    rec[12 * NT + tid] = r.q.x;
+    rec[13 * NT + tid] = r.q.y;
+    rec[14 * NT + tid] = r.q.z;
+    rec[15 * NT + tid] = r.q.w;
+    rec[16 * NT + tid] = r.c0.x;
+    rec[17 * NT + tid] = r.c0.y;
+    rec[18 * NT + tid] = r.c0.z;
+    rec[19 * NT + tid] = r.c1.x;
+    rec[20 * NT + tid] = r.c1.y;
+    rec[21 * NT + tid] = r.c1.z;
+    rec[22 * NT + tid] = r.c2.x;
+    rec[23 * NT + tid] = r.c2.y;
+    rec[24 * NT + tid] = r.c2.z;
+    __syncthreads();
+    const int cnt = min(NT, w.n_particles - chunk * NT);
+    const dt_env& E0 = w.envs[w.p_env[min(chunk * NT, w.n_particles - 1)]];
+    const int node_off = E0.node_off, nb1 = E0.nb[1], nb2 = E0.nb[2];
+    for (int n = tid; n < tile_n; n += NT) {
+      const int nc = n % ez, nbb = (n / ez) % ey, na = n / (ey * ez);
+      float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;
+      for (int p = 0; p < cnt; ++p) {
+        const int oi = na - __float_as_int(rec[p]);
+        const int oj = nbb - __float_as_int(rec[NT + p]);
+        const int ok_ = nc - __float_as_int(rec[2 * NT + p]);
+        if ((unsigned)oi <= 2u && (unsigned)oj <= 2u && (unsigned)ok_ <= 2u) {
+          const float W = (rec[(3 + oi) * NT + p] * rec[(6 + oj) * NT + p]) * rec[(9 + ok_) * NT + p];
+          const float fi = (float)oi, fj = (float)oj, fk = (float)ok_;
+          ax += W * (((rec[12 * NT + p] + fi * rec[16 * NT + p]) + fj * rec[19 * NT + p]) + fk * rec[22 * NT + p]);
+          ay += W * (((rec[13 * NT + p] + fi * rec[17 * NT + p]) + fj * rec[20 * NT + p]) + fk * rec[23 * NT + p]);
+          az += W * (((rec[14 * NT + p] + fi * rec[18 * NT + p]) + fj * rec[21 * NT + p]) + fk * rec[24 * NT + p]);
+          aw += W * rec[15 * NT + p];
+        }
+      }
+      if (aw != 0.f || ax != 0.f || ay != 0.f || az != 0.f) {
+        const int i = L0 + na, j = L1 + nbb, k = L2 + nc;
+        const int g = node_off + ((((i >> 2) * nb1 + (j >> 2)) * nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
+                      ((j & 3) << 2) + (k & 3);
+        red_add_v4(dst + g, make_float4(ax, ay, az, aw));
+      }
+    }
   } else if (ok) {
     const dt_env& E = w.envs[env];
+    const int node_off = E.node_off, nb1 = E.nb[1], nb2 = E.nb[2];
 #pragma unroll
     for (int oi = 0; oi < 3; ++oi)
 #pragma unroll
       for (int oj = 0; oj < 3; ++oj)
 #pragma unroll
-        for (int ok_ = 0; ok_ < 3; ++ok_)
-          red_add_v4(dst + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok_), contrib(oi, oj, ok_));
-    mark_one(E);
+        for (int ok_ = 0; ok_ < 3; ++ok_) {
+          const int i = base[0] + oi, j = base[1] + oj, k = base[2] + ok_;
+          const int n = node_off + ((((i >> 2) * nb1 + (j >> 2)) * nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
+                        ((j & 3) << 2) + (k & 3);
+          const float W = (r.wx[oi] * r.wy[oj]) * r.wz[ok_];
+          const float fi = (float)oi, fj = (float)oj, fk = (float)ok_;
+          const v3 t = ((v3{r.q.x, r.q.y, r.q.z} + fi * r.c0) + fj * r.c1) + fk * r.c2;
+          red_add_v4(dst + n, make_float4(W * t.x, W * t.y, W * t.z, W * r.q.w));
+        }
+    if (!compact) mark_one(E);
   }
 }
 

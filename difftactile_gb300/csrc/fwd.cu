@@ -13,11 +13,10 @@
 //                      vertices   — FEM integration with the driven base layer
 //                      (fem_sensor.py:444-457, gripper_fem.py:404-418).
 //
-// P2G privatisation: a CTA takes 128 consecutive particles (kept spatially sorted by the host),
-// reduces their base cells to a bounding box and, if the box fits, accumulates the 27-node
-// stencils of all its particles in a shared-memory tile (stencil order rotated by lane to spread
-// same-address shared atomics), then flushes each touched node with one 16-byte vector RED to
-// global memory.  Otherwise each particle issues its 27 vector REDs directly.
+// P2G scatter: a CTA takes 128 consecutive particles (kept spatially sorted by the host); with
+// DT_SCATTER_TILE their stencil records are gathered per node of the chunk's bounding box in shared
+// memory and flushed with one 16-byte vector RED per node (common.cuh: stencil_scatter), with
+// DT_SCATTER_GLOBAL each particle issues its 27 vector REDs directly.
 #include "common.cuh"
 #include <climits>
 
@@ -35,8 +34,6 @@ __device__ void mark_block(const dt_world& w, int f, int b) {
     if (s < w.n_blocks) w.tape_blist[(size_t)f * w.n_blocks + s] = b;
   }
 }
-
-DT_DEV float sel3(const float a[3], int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); }
 
 // P2G of one CTA's particles (mpm_elastic.py:176-208 / mpm_plastic.py:222-256 / multi_obj.py:228-252):
 // contribution at node base + o is W_o (p_mass v + A (o - fx) dx) = W_o (b + o . (dx A)), with
@@ -90,11 +87,17 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
     pplane(w, f + 1, 4)[p] = make_float4(s.Fp.a[0][1], s.Fp.a[0][2], s.Fp.a[1][0], s.Fp.a[1][1]);
     pplane(w, f + 1, 5)[p] = make_float4(s.Fp.a[1][2], s.Fp.a[2][0], s.Fp.a[2][1], s.Fp.a[2][2]);
   }
-  auto contrib = [&](int oi, int oj, int ok_) {
-    const float W = (sel3(wx, oi) * wy[oj]) * wz[ok_];
-    const v3 t = ((b + (float)oi * c0) + (float)oj * c1) + (float)ok_ * c2;
-    return make_float4(W * t.x, W * t.y, W * t.z, W * pm);
-  };
+  StencilRec rec;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    rec.wx[i] = wx[i];
+    rec.wy[i] = wy[i];
+    rec.wz[i] = wz[i];
+  }
+  rec.q = make_float4(b.x, b.y, b.z, pm);
+  rec.c0 = c0;
+  rec.c1 = c1;
+  rec.c2 = c2;
   auto mark_box = [&](const dt_env& E0, int l0, int l1, int l2, int h0, int h1, int h2) {
     const int b0 = l0 >> 2, b1 = l1 >> 2, b2 = l2 >> 2;
     const int n0 = (h0 >> 2) - b0 + 1, n1 = (h1 >> 2) - b1 + 1, n2 = (h2 >> 2) - b2 + 1;
@@ -110,8 +113,8 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
       mark_block(w, f, block_index(E, bi, bj, bk));
     }
   };
-  tile_scatter<NT, TILE_MAX>(w, chunk, ok, env, base, tile, sh, reinterpret_cast<float4*>(w.g_acc), contrib,
-                             mark_box, mark_one);
+  stencil_scatter<NT, TILE_MAX>(w, chunk, ok, env, base, rec, reinterpret_cast<float*>(tile), sh,
+                                reinterpret_cast<float4*>(w.g_acc), mark_box, mark_one);
 }
 
 // FEM elastic forces of one tet (fem_sensor.py:409-440): stable-Neo-Hookean-like P with current
@@ -177,7 +180,7 @@ __device__ void tri_centroid(const dt_world& w, int f, int t) {
 }
 
 __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
-  extern __shared__ float4 tile[];  // TILE_MAX float4 in tile mode, none otherwise
+  extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
@@ -482,7 +485,7 @@ int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   int nb_f = fem ? cdiv(w->n_tris, NT) : 0;
   int tot = nb_p + nb_t + nb_f;
   if (tot == 0) return DT_OK;
-  k_fwd_p2g_fem<<<tot, NT, (w->scatter_mode == DT_SCATTER_TILE ? TILE_MAX * sizeof(float4) : 0), st>>>(*w, f, nb_p, nb_t, nb_f);
+  k_fwd_p2g_fem<<<tot, NT, (w->scatter_mode == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0), st>>>(*w, f, nb_p, nb_t, nb_f);
   return launched();
 }
 int launch_l2(const dt_world* w, int f, cudaStream_t st) {

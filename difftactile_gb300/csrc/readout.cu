@@ -13,21 +13,22 @@ constexpr int NT = 256;
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
 
-__global__ void k_pose_cv(dt_world w, int s, const float* __restrict__ Ab, float inv_T) {
+__global__ void k_pose_cv(dt_world w, int s, const float* __restrict__ Ab, float inv_T, int f0, int nfr) {
   const dt_sensor& S = w.sensors[s];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= S.nv) return;
   const int v = S.v_off + i;
-  const v3 p = f4to3(vframe(w.v_vpos, w, 0)[v]);
+  const v3 p = f4to3(vframe(w.v_vpos, w, f0)[v]);
   v3 q;
   q.x = Ab[0] * p.x + Ab[1] * p.y + Ab[2] * p.z + Ab[3];
   q.y = Ab[4] * p.x + Ab[5] * p.y + Ab[6] * p.z + Ab[7];
   q.z = Ab[8] * p.x + Ab[9] * p.y + Ab[10] * p.z + Ab[11];
   const float4 cv = v3to4(inv_T * (q - p));
-  for (int f = 0; f < w.n_frames; ++f) vframe(w.v_cv, w, f)[v] = cv;
+  for (int f = f0; f < f0 + nfr; ++f) vframe(w.v_cv, w, f)[v] = cv;
 }
 
-__global__ void k_pose_cv_bwd(dt_world w, int s, const float* __restrict__ Ab, float inv_T, float* Ab_bar) {
+__global__ void k_pose_cv_bwd(dt_world w, int s, const float* __restrict__ Ab, float inv_T, float* Ab_bar, int f0,
+                              int nfr) {
   __shared__ float red[12][NT / 32];
   const dt_sensor& S = w.sensors[s];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,9 +37,13 @@ __global__ void k_pose_cv_bwd(dt_world w, int s, const float* __restrict__ Ab, f
   for (int k = 0; k < 12; ++k) g[k] = 0.f;
   if (i < S.nv) {
     const int v = S.v_off + i;
-    const v3 p = f4to3(vframe(w.v_vpos, w, 0)[v]);
+    const v3 p = f4to3(vframe(w.v_vpos, w, f0)[v]);
     v3 cb = v3{0.f, 0.f, 0.f};
-    for (int f = 0; f < w.n_frames; ++f) cb = cb + f4to3(vframe(w.v_adj_cv, w, f)[v]);
+    for (int f = f0; f < f0 + nfr; ++f) {  // consume: the adjoint moves into Ab_bar and vpos_bar
+      float4* c = vframe(w.v_adj_cv, w, f) + v;
+      cb = cb + f4to3(*c);
+      *c = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     cb = inv_T * cb;
     const float pr[4] = {p.x, p.y, p.z, 1.f};
     const float cr[3] = {cb.x, cb.y, cb.z};
@@ -47,7 +52,7 @@ __global__ void k_pose_cv_bwd(dt_world w, int s, const float* __restrict__ Ab, f
 #pragma unroll
       for (int c = 0; c < 4; ++c) g[4 * r + c] = cr[r] * pr[c];
     // cv = inv_T (A p + b - p): p_bar += (A - I)^T cb
-    float4* ap = reinterpret_cast<float4*>(w.v_adj_vpos) + v;  // buffer 0 = frame 0
+    float4* ap = reinterpret_cast<float4*>(w.v_adj_vpos) + (size_t)(f0 & 1) * w.n_verts + v;  // frame f0's buffer
     float4 a = *ap;
     a.x += Ab[0] * cb.x + Ab[4] * cb.y + Ab[8] * cb.z - cb.x;
     a.y += Ab[1] * cb.x + Ab[5] * cb.y + Ab[9] * cb.z - cb.y;
@@ -110,16 +115,18 @@ __global__ void k_marker_loss_bwd(dt_world w, int s, int f, int layer, const flo
 
 extern "C" {
 
-int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, cudaStream_t stream) {
-  if (!w || !Ab || s < 0 || s >= w->n_sensors) return DT_ERR_ARG;
-  k_pose_cv<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, s, Ab, inv_T);
+int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, int f0, int nfr,
+                        cudaStream_t stream) {
+  if (!w || !Ab || s < 0 || s >= w->n_sensors || f0 < 0 || nfr < 1 || f0 + nfr > w->n_frames) return DT_ERR_ARG;
+  k_pose_cv<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, s, Ab, inv_T, f0, nfr);
   return launched();
 }
 
-int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv_T, float* Ab_bar,
+int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv_T, float* Ab_bar, int f0, int nfr,
                             cudaStream_t stream) {
-  if (!w || !Ab || !Ab_bar || s < 0 || s >= w->n_sensors) return DT_ERR_ARG;
-  k_pose_cv_bwd<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, s, Ab, inv_T, Ab_bar);
+  if (!w || !Ab || !Ab_bar || s < 0 || s >= w->n_sensors || f0 < 0 || nfr < 1 || f0 + nfr > w->n_frames)
+    return DT_ERR_ARG;
+  k_pose_cv_bwd<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, s, Ab, inv_T, Ab_bar, f0, nfr);
   return launched();
 }
 

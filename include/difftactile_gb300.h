@@ -255,12 +255,15 @@ int dt_com_bwd(const dt_world* w, int f, const float* adj_com, cudaStream_t stre
 
 /* ---- action input: pose control (fem_sensor.py:229-266, set_pose_control + set_control_vel) ----
  * cv_i = ((A vp_i + b) - vp_i) * inv_T for every vertex i of sensor s, vp = virtual positions of
- * frame 0, (A | b) = rows 0..2 of the step transform dtrans_h given as 12 device floats (row-major
- * 3x4), inv_T = 1 / (dt * substeps); written into every frame of v_cv. */
-int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, cudaStream_t stream);
-/* Adjoint: Ab_bar[12] (device) += sum_i cvb_i [vp_i, 1]^T inv_T and v_adj_vpos[0] += (A - I)^T cvb_i
- * inv_T, with cvb_i the control-velocity adjoint summed over the frames of v_adj_cv. */
-int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv_T, float* Ab_bar,
+ * frame f0, (A | b) = rows 0..2 of the step transform dtrans_h given as 12 device floats (row-major
+ * 3x4), inv_T = 1 / (dt * substeps); written into frames [f0, f0 + nfr) of v_cv (one control step). */
+int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, int f0, int nfr,
+                        cudaStream_t stream);
+/* Adjoint: Ab_bar[12] (device) += sum_i cvb_i [vp_i, 1]^T inv_T and v_adj_vpos[f0&1] += (A - I)^T cvb_i
+ * inv_T, with cvb_i the control-velocity adjoint summed over frames [f0, f0 + nfr) of v_adj_cv.  Those
+ * entries of v_adj_cv are consumed (reset to zero), so consecutive control steps may share their
+ * boundary frame: call it after the adjoint substeps of frames [f0, f0 + nfr - 1). */
+int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv_T, float* Ab_bar, int f0, int nfr,
                             cudaStream_t stream);
 
 /* ---- tactile readout: marker-displacement loss (cf. grasp_plastic.py:241-256) ----
