@@ -79,6 +79,7 @@ __global__ void __launch_bounds__(GRID_NT) k_bwd_restore(dt_world w, int f) {
 // G2P adjoint of one CTA's particles: the position adjoint needs the grid velocities (a gather);
 // the grid-velocity adjoint W (vn_bar + 4 inv_dx C_bar (o - fx)) = W (q + o . c) is a 27-node
 // scatter, privatised through the shared-memory tile.
+template <int MODE>
 __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile, int* sh) {
   const int p = chunk * NT + threadIdx.x;
   const bool valid = p < w.n_particles;
@@ -163,7 +164,7 @@ __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile,
   rec.c2 = c2;
   auto no_box = [](const dt_env&, int, int, int, int, int, int) {};
   auto no_one = [](const dt_env&) {};
-  stencil_scatter<NT, TILE_MAX>(w, chunk, ok, env, base, rec, reinterpret_cast<float*>(tile), sh,
+  stencil_scatter<NT, TILE_MAX, MODE>(w, chunk, ok, env, base, rec, reinterpret_cast<float*>(tile), sh,
                                 reinterpret_cast<float4*>(w.g_adj_vout), no_box, no_one);
 }
 
@@ -203,12 +204,13 @@ __device__ void integrate_bwd(const dt_world& w, int f, int i) {
   if (S.carry) *cvb_n = v3to4(cvbn);
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
-    g2p_bwd_chunk(w, f, b, tile, sh);
+    g2p_bwd_chunk<MODE>(w, f, b, tile, sh);
     return;
   }
   b -= nb_p;
@@ -648,7 +650,7 @@ __device__ void fem_tet_bwd(const dt_world& w, int f, int t) {
   red_add_v4(aPos + tv.w, v3to4(-((ab + bb) + cbv)));
 }
 
-__global__ void __launch_bounds__(NT) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v) {
+__global__ void __launch_bounds__(NT, 4) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v) {
   int b = blockIdx.x;
   if (b < nb_p) {
     const int p = b * NT + threadIdx.x;
@@ -705,7 +707,13 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
       if (ng > 0) k_bwd_restore<<<ng, GRID_NT, 0, stream>>>(*w, f);
       break;
     case 1:
-      if (nb_p + nb_v) k_bwd_g2p_fem<<<nb_p + nb_v, NT, (w->scatter_mode == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0), stream>>>(*w, f, nb_p, nb_v);
+      if (nb_p + nb_v == 0) break;
+      if (w->scatter_mode == DT_SCATTER_TILE)
+        k_bwd_g2p_fem<DT_SCATTER_TILE><<<nb_p + nb_v, NT, 25 * NT * sizeof(float), stream>>>(*w, f, nb_p, nb_v);
+      else if (w->scatter_mode == DT_SCATTER_GLOBAL)
+        k_bwd_g2p_fem<DT_SCATTER_GLOBAL><<<nb_p + nb_v, NT, 0, stream>>>(*w, f, nb_p, nb_v);
+      else
+        k_bwd_g2p_fem<DT_SCATTER_WARP><<<nb_p + nb_v, NT, 0, stream>>>(*w, f, nb_p, nb_v);
       break;
     case 2:
       if (ng > 0) k_bwd_grid<<<ng, GRID_NT, 0, stream>>>(*w, f);

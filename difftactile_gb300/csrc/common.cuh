@@ -484,7 +484,7 @@ struct StencilRec {
   v3 c0, c1, c2;
 };
 
-template <int NT, int TILE_MAX, typename MarkBox, typename MarkOne>
+template <int NT, int TILE_MAX, int MODE, typename MarkBox, typename MarkOne>
 DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, const int base[3], const StencilRec& r,
                             float* sm, int* sh, float4* dst, const MarkBox& mark_box, const MarkOne& mark_one) {
   const int tid = threadIdx.x;
@@ -519,7 +519,7 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
   const int ex = any ? sh[3] - L0 + 3 : 0, ey = any ? sh[4] - L1 + 3 : 0, ez = any ? sh[5] - L2 + 3 : 0;
   const int tile_n = ex * ey * ez;
   const bool compact = any && sh[6] && tile_n <= TILE_MAX;
-  const bool gather = w.scatter_mode == DT_SCATTER_TILE && compact;
+  const bool gather = MODE == DT_SCATTER_TILE && compact;
   if (compact) {
     const dt_env& E0 = w.envs[w.p_env[min(chunk * NT, w.n_particles - 1)]];
     mark_box(E0, L0, L1, L2, L0 + ex - 1, L1 + ey - 1, L2 + ez - 1);
@@ -576,6 +576,57 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
         red_add_v4(dst + g, make_float4(ax, ay, az, aw));
       }
     }
+  } else if constexpr (MODE == DT_SCATTER_WARP) {
+    // segmented reduction over runs of lanes with the same base node (same env and cell): every
+    // lane of the warp takes part in the shuffles; lanes without a particle form runs of their own
+    int node_off = 0, nb1 = 1, nb2 = 1;
+    if (ok) {
+      const dt_env& E = w.envs[env];
+      node_off = E.node_off;
+      nb1 = E.nb[1];
+      nb2 = E.nb[2];
+    }
+    const int key = ok ? node_off + ((((base[0] >> 2) * nb1 + (base[1] >> 2)) * nb2 + (base[2] >> 2)) << 6) +
+                             ((base[0] & 3) << 4) + ((base[1] & 3) << 2) + (base[2] & 3)
+                       : -1 - lane;
+    const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const bool head = lane == 0 || prev != key;
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const unsigned after = lane == 31 ? 0u : (heads >> (lane + 1)) << (lane + 1);
+    const int seg_end = after ? __ffs(after) - 1 : 32;
+    const int run = __reduce_max_sync(0xffffffffu, head ? seg_end - lane : 0);
+    const int steps = run > 1 ? 32 - __clz(run - 1) : 0;
+#pragma unroll
+    for (int oi = 0; oi < 3; ++oi)
+#pragma unroll
+      for (int oj = 0; oj < 3; ++oj)
+#pragma unroll
+        for (int ok_ = 0; ok_ < 3; ++ok_) {
+          const float W = ok ? (r.wx[oi] * r.wy[oj]) * r.wz[ok_] : 0.f;
+          const float fi = (float)oi, fj = (float)oj, fk = (float)ok_;
+          const v3 t = ((v3{r.q.x, r.q.y, r.q.z} + fi * r.c0) + fj * r.c1) + fk * r.c2;
+          float4 a = make_float4(W * t.x, W * t.y, W * t.z, W * r.q.w);
+          for (int s = 0; s < steps; ++s) {
+            const int off = 1 << s;
+            const float bx = __shfl_down_sync(0xffffffffu, a.x, off);
+            const float by = __shfl_down_sync(0xffffffffu, a.y, off);
+            const float bz = __shfl_down_sync(0xffffffffu, a.z, off);
+            const float bw = __shfl_down_sync(0xffffffffu, a.w, off);
+            if (lane + off < seg_end) {
+              a.x += bx;
+              a.y += by;
+              a.z += bz;
+              a.w += bw;
+            }
+          }
+          if (head && ok) {
+            const int i = base[0] + oi, j = base[1] + oj, k = base[2] + ok_;
+            const int n = node_off + ((((i >> 2) * nb1 + (j >> 2)) * nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
+                          ((j & 3) << 2) + (k & 3);
+            red_add_v4(dst + n, a);
+          }
+        }
+    if (ok && !compact) mark_one(w.envs[env]);
   } else if (ok) {
     const dt_env& E = w.envs[env];
     const int node_off = E.node_off, nb1 = E.nb[1], nb2 = E.nb[2];

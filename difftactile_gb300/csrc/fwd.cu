@@ -38,6 +38,7 @@ __device__ void mark_block(const dt_world& w, int f, int b) {
 // P2G of one CTA's particles (mpm_elastic.py:176-208 / mpm_plastic.py:222-256 / multi_obj.py:228-252):
 // contribution at node base + o is W_o (p_mass v + A (o - fx) dx) = W_o (b + o . (dx A)), with
 // A = stress + p_mass C and b = p_mass v - dx A fx precomputed once per particle.
+template <int MODE>
 __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int* sh) {
   const int p = chunk * NT + threadIdx.x;
   const bool valid = p < w.n_particles;
@@ -113,8 +114,8 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
       mark_block(w, f, block_index(E, bi, bj, bk));
     }
   };
-  stencil_scatter<NT, TILE_MAX>(w, chunk, ok, env, base, rec, reinterpret_cast<float*>(tile), sh,
-                                reinterpret_cast<float4*>(w.g_acc), mark_box, mark_one);
+  stencil_scatter<NT, TILE_MAX, MODE>(w, chunk, ok, env, base, rec, reinterpret_cast<float*>(tile), sh,
+                                      reinterpret_cast<float4*>(w.g_acc), mark_box, mark_one);
 }
 
 // FEM elastic forces of one tet (fem_sensor.py:409-440): stable-Neo-Hookean-like P with current
@@ -179,12 +180,13 @@ __device__ void tri_centroid(const dt_world& w, int f, int t) {
   reinterpret_cast<float4*>(w.tri_cent)[t] = o;
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
-    p2g_chunk(w, f, b, tile, sh);
+    p2g_chunk<MODE>(w, f, b, tile, sh);
     return;
   }
   b -= nb_p;
@@ -212,6 +214,14 @@ struct Best {
   int i;
 };
 DT_DEV Best lexmin(Best a, Best b) { return (b.d < a.d || (b.d == a.d && b.i < a.i)) ? b : a; }
+// float min / max over the warp through the order-preserving map of IEEE bits to int32
+DT_DEV int f2ord(float x) {
+  const int i = __float_as_int(x);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+DT_DEV float ord2f(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
+DT_DEV float ord_min(float x) { return ord2f(__reduce_min_sync(0xffffffffu, f2ord(x))); }
+DT_DEV float ord_max(float x) { return ord2f(__reduce_max_sync(0xffffffffu, f2ord(x))); }
 // Euclidean distance from p to an axis-aligned box (0 inside)
 DT_DEV float box_dist(float4 lo, float4 hi, float px, float py, float pz) {
   const float dx = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.f);
@@ -220,7 +230,7 @@ DT_DEV float box_dist(float4 lo, float4 hi, float px, float py, float pz) {
   return sqrtf(dx * dx + dy * dy + dz * dz);
 }
 
-__global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f, int smem_cap) {
+__global__ void __launch_bounds__(GRID_NT, 2) k_fwd_grid(dt_world w, int f, int smem_cap) {
   extern __shared__ float4 scent[];
   float4* gbox = scent + smem_cap;  // 2 float4 per group of 32 centroids
   const int cnt = *((volatile int*)(w.tape_bcount + f));
@@ -251,7 +261,7 @@ __global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f, int sme
     const float px = __fmul_rn(__fadd_rn((float)i, 0.5f), E.dx), py = __fmul_rn(__fadd_rn((float)j, 0.5f), E.dx),
                 pz = __fmul_rn(__fadd_rn((float)k, 0.5f), E.dx);
     v3 gf = v3{0.f, 0.f, 0.f};
-    int cid[DT_MAX_SENSORS_PER_ENV] = {-1, -1, -1, -1};
+    int4 cid = make_int4(-1, -1, -1, -1);  // argmin per sensor slot (DT_MAX_SENSORS_PER_ENV = 4)
 #pragma unroll
     for (int q = 0; q < DT_MAX_SENSORS_PER_ENV; ++q) {
       const int si = E.s_begin + q;  // block-uniform
@@ -263,21 +273,18 @@ __global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f, int sme
         __syncthreads();
         for (int t = tid; t < nf; t += GRID_NT) scent[t] = __ldg(cent + S.f_off + t);
         __syncthreads();
-        // bounding boxes of groups of 32 consecutive centroids (lower bounds for the search)
+        // bounding boxes of groups of 32 consecutive centroids (lower bounds for the search): one
+        // warp per group, min/max over the lanes as order-preserving integer reductions
         const int G = (nf + 31) >> 5;
-        for (int gg = tid; gg < G; gg += GRID_NT) {
-          float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.f);
-          for (int t = 32 * gg; t < min(32 * gg + 32, nf); ++t) {
-            const float4 c = scent[t];
-            lo.x = fminf(lo.x, c.x);
-            lo.y = fminf(lo.y, c.y);
-            lo.z = fminf(lo.z, c.z);
-            hi.x = fmaxf(hi.x, c.x);
-            hi.y = fmaxf(hi.y, c.y);
-            hi.z = fmaxf(hi.z, c.z);
+        for (int gg = tid >> 5; gg < G; gg += GRID_NT / 32) {
+          const int t = 32 * gg + (tid & 31);
+          const float4 c = scent[t < nf ? t : 32 * gg];
+          const float4 lo = make_float4(ord_min(c.x), ord_min(c.y), ord_min(c.z), 0.f);
+          const float4 hi = make_float4(ord_max(c.x), ord_max(c.y), ord_max(c.z), 0.f);
+          if ((tid & 31) == 0) {
+            gbox[2 * gg] = lo;
+            gbox[2 * gg + 1] = hi;
           }
-          gbox[2 * gg] = lo;
-          gbox[2 * gg + 1] = hi;
         }
         __syncthreads();
         staged = si;
@@ -316,14 +323,28 @@ __global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f, int sme
           Best other{__shfl_xor_sync(0xffffffffu, bb.d, o), __shfl_xor_sync(0xffffffffu, bb.i, o)};
           bb = lexmin(bb, other);
         }
+        // the groups that survive the bound are scanned by all four lanes of the node together
         const float thr = bb.d * (1.f + 1e-5f);
-        for (int gg = sub; gg < G; gg += 4) {
-          if (gg == g0) continue;
-          if (box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr) continue;
-          const int t1 = min(32 * gg + 32, nf);
-          for (int t = 32 * gg; t < t1; ++t) {
-            const float4 c = scent[t];
-            bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
+        const int Gu = (nf + 31) >> 5;  // block-uniform trip count around the shuffles
+        for (int gc = 0; gc < Gu; gc += 64) {
+          unsigned long long live = 0ull;
+          const int ge = min(gc + 64, G);
+          for (int gg = gc + sub; gg < ge; gg += 4)
+            if (gg != g0 && !(box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr))
+              live |= 1ull << (gg - gc);
+          live |= __shfl_xor_sync(0xffffffffu, live, 1);
+          live |= __shfl_xor_sync(0xffffffffu, live, 2);
+          while (live) {
+            const int gg = gc + __ffsll((long long)live) - 1;
+            live &= live - 1ull;
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+              const int t = 32 * gg + sub + 4 * jj;
+              if (t < nf) {
+                const float4 c = scent[t];
+                bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
+              }
+            }
           }
         }
       } else if (occ) {
@@ -338,7 +359,10 @@ __global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f, int sme
         bb = lexmin(bb, other);
       }
       const int kk = bb.i;
-      cid[q] = kk;
+      if (q == 0) cid.x = kk;
+      else if (q == 1) cid.y = kk;
+      else if (q == 2) cid.z = kk;
+      else cid.w = kk;
       if (sub != 0 || !occ || kk < 0) continue;
       const int4 tr = __ldg(tris + S.f_off + kk);
       SdfRes sr = find_sdf(f4to3(P[tr.x]), f4to3(P[tr.y]), f4to3(P[tr.z]), f4to3(VM[tr.x]), f4to3(VM[tr.y]),
@@ -373,7 +397,7 @@ __global__ void __launch_bounds__(GRID_NT) k_fwd_grid(dt_world w, int f, int sme
         const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + l;
         reinterpret_cast<float4*>(w.tape_acc)[ti] = a;
         reinterpret_cast<float4*>(w.tape_vout)[ti] = vo;
-        reinterpret_cast<int4*>(w.tape_cidx)[ti] = make_int4(cid[0], cid[1], cid[2], cid[3]);
+        reinterpret_cast<int4*>(w.tape_cidx)[ti] = cid;
       } else if (l == 0) {
         set_err(w, DT_DEVERR_TAPE_FULL);
       }
@@ -485,7 +509,16 @@ int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   int nb_f = fem ? cdiv(w->n_tris, NT) : 0;
   int tot = nb_p + nb_t + nb_f;
   if (tot == 0) return DT_OK;
-  k_fwd_p2g_fem<<<tot, NT, (w->scatter_mode == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0), st>>>(*w, f, nb_p, nb_t, nb_f);
+  switch (w->scatter_mode) {
+    case DT_SCATTER_TILE:
+      k_fwd_p2g_fem<DT_SCATTER_TILE><<<tot, NT, 25 * NT * sizeof(float), st>>>(*w, f, nb_p, nb_t, nb_f);
+      break;
+    case DT_SCATTER_GLOBAL:
+      k_fwd_p2g_fem<DT_SCATTER_GLOBAL><<<tot, NT, 0, st>>>(*w, f, nb_p, nb_t, nb_f);
+      break;
+    default:
+      k_fwd_p2g_fem<DT_SCATTER_WARP><<<tot, NT, 0, st>>>(*w, f, nb_p, nb_t, nb_f);
+  }
   return launched();
 }
 int launch_l2(const dt_world* w, int f, cudaStream_t st) {

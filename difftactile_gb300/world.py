@@ -29,12 +29,34 @@ def _morton_key(cell: np.ndarray) -> np.ndarray:
     return key
 
 
+def _kd_groups(pts: np.ndarray, group: int = 32) -> np.ndarray:
+    """Order of ``pts`` in which consecutive runs of ``group`` points are spatially compact:
+    recursive median splits along the widest axis, the left part a multiple of ``group``."""
+    out: list[np.ndarray] = []
+
+    def split(idx):
+        n = len(idx)
+        if n <= group:
+            out.append(idx)
+            return
+        p = pts[idx]
+        ax = int(np.argmax(p.max(0) - p.min(0)))
+        left = group * ((n + 2 * group - 1) // (2 * group))
+        o = np.argsort(p[:, ax], kind="stable")
+        split(idx[o[:left]])
+        split(idx[o[left:]])
+
+    if len(pts):
+        split(np.arange(len(pts)))
+    return np.concatenate(out) if out else np.zeros(0, np.int64)
+
+
 class World:
     """Flat device layout of ``envs`` (list of EnvSpec) with ``n_frames`` frames per step."""
 
     def __init__(self, envs: list[EnvSpec], n_frames: int, dt: float, device="cuda", tape_blocks: int | None = None,
                  grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True,
-                 svd_grad_mode: int = 0, scatter_mode: int = 1):
+                 svd_grad_mode: int = 0, scatter_mode: int = 2):
         self.lib = N.load()
         self.device = torch.device(device)
         self.specs = envs
@@ -107,19 +129,10 @@ class World:
             verts.append(sp.verts.astype(np.float32))
             tets.append(sp.tets.astype(np.int32) + v_off)
             tris.append(np.concatenate([sp.tris.astype(np.int32) + v_off, np.full((nf, 1), si, np.int32)], 1))
-            # contact-search order: rest centroids sorted by a Morton key, so that groups of 32
-            # consecutive positions are compact patches (ties still resolve on the original index)
+            # contact-search order: groups of 32 consecutive positions are compact patches of the
+            # rest surface (ties in the search still resolve on the original index)
             cen = sp.verts[sp.tris].mean(1).astype(np.float64) if nf else np.zeros((0, 3))
-            if nf:
-                lo, hi = cen.min(0), cen.max(0)
-                qv = ((cen - lo) / np.maximum(hi - lo, 1e-12) * 1023).astype(np.int64)
-                key = np.zeros(nf, np.int64)
-                for bit in range(10):
-                    for d in range(3):
-                        key |= ((qv[:, d] >> bit) & 1) << (3 * bit + d)
-                tri_perm.append(np.argsort(key, kind="stable").astype(np.int32) + f_off)
-            else:
-                tri_perm.append(np.zeros(0, np.int32))
+            tri_perm.append(_kd_groups(cen).astype(np.int32) + f_off)
             layer.append(sp.layer.astype(np.int32))
             v_sensor.append(np.full(nv, si, np.int32))
             t_sensor.append(np.full(nt, si, np.int32))

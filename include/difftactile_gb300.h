@@ -171,10 +171,14 @@ typedef struct dt_world {
   int scatter_mode;              /* DT_SCATTER_*: how P2G and the G2P adjoint accumulate into the grid */
 } dt_world;
 
-/* 27-node particle scatters: privatised in a shared-memory tile per CTA, or vector REDs straight
- * to global memory (L2 atomics).  Which is faster depends on particle density; bench/autotune picks. */
+/* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared
+ * memory and issues one vector RED per touched node; GLOBAL issues one 16-byte vector RED per
+ * particle and node (L2 atomics); WARP first sums, over each run of consecutive lanes whose particles
+ * share a base cell (particles are kept in Morton order, so runs are long), with a segmented
+ * shuffle reduction, then issues one RED per run and node. */
 #define DT_SCATTER_TILE 0
 #define DT_SCATTER_GLOBAL 1
+#define DT_SCATTER_WARP 2
 
 /* SVD adjoint of the rotation R = U V^T used by the corotated stress:
  * STABLE evaluates the reference formula's rotation term in the algebraically equal form

@@ -63,8 +63,8 @@ def oracle_loss(env, st0, cv, W, n_sub, mu_lam=None):
     return L
 
 
-def gpu_grads(env, st0, cv, W, n_sub):
-    w = World([env], n_frames=n_sub + 1, dt=DT, grad_clip=0.0)
+def gpu_grads(env, st0, cv, W, n_sub, **world_kw):
+    w = World([env], n_frames=n_sub + 1, dt=DT, grad_clip=0.0, **world_kw)
     w.set_particles(0, x=st0["x"], v=st0["v"], C=st0["C"], F=st0["F"])
     for s in range(len(env.sensors)):
         sl = w.vslice(s)

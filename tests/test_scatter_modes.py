@@ -1,0 +1,65 @@
+"""The three 27-node scatter strategies (shared-memory gather, per-particle global REDs, warp
+segmented reduction over runs of particles sharing a base cell) give the oracle's forward state
+and adjoint, with particles in Morton order (long runs) and in the user's order (runs of one),
+and across environment boundaries inside a warp."""
+import numpy as np
+import pytest
+import torch
+
+from difftactile_gb300.world import World
+from oracle import oracle as O
+from tests import small_scenes as SS
+from tests.test_parity_bwd import base_point, gpu_grads, loss_weights
+from tests.test_parity_fwd import compare, run_oracle
+
+pytestmark = pytest.mark.gpu
+DT = 1e-4
+MODES = {"tile": 0, "global": 1, "warp": 2}
+
+
+@pytest.mark.parametrize("sort", [True, False])
+@pytest.mark.parametrize("mode", list(MODES))
+def test_forward_three_substeps(cuda_lib, mode, sort):
+    env = SS.pad_over_box()
+    cv = [SS.control_velocity(sp) for sp in env.sensors]
+    w = World([env], n_frames=4, dt=DT, scatter_mode=MODES[mode], sort_particles=sort)
+    for s, c in enumerate(cv):
+        w.set_control_velocity(s, c)
+    w.step_begin()
+    for f in range(3):
+        w.substep(f)
+    torch.cuda.synchronize()
+    assert w.error_word() == 0
+    st, _ = run_oracle(env, 3, cv)
+    compare(w, 3, st)
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_adjoint_one_substep(cuda_lib, mode):
+    env = SS.pad_over_box()
+    st0, cv = base_point(env, 7)
+    W = loss_weights(env, env.n_particles, 8)
+    g = gpu_grads(env, st0, cv, W, 1, scatter_mode=MODES[mode])
+    o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
+    ref = o.substep_bwd({k: (v if not isinstance(v, list) else [a.copy() for a in v]) for k, v in st0.items()}, W,
+                        cv=cv, cv1=cv)
+    errs = {k: SS.rel_err(g[k], ref[k]) for k in ("x", "v", "C", "F")}
+    errs["pos"] = SS.rel_err(g["pos"][0], ref["pos"][0])
+    assert max(errs.values()) < 1e-3, errs
+
+
+def test_warp_runs_across_env_boundaries(cuda_lib):
+    """Env sizes that are not multiples of 32 put two environments in one warp; equal cells of
+    different environments must not merge into one run."""
+    e0 = SS.elastic_cube(n=32, side_cells=3, ppc=3, seed=1)
+    e1 = SS.elastic_cube(n=32, side_cells=3, ppc=3, seed=2)
+    assert e0.n_particles % 32 and e0.n_particles == e1.n_particles
+    w = World([e0, e1], n_frames=3, dt=DT, scatter_mode=MODES["warp"])
+    w.step_begin()
+    for f in range(2):
+        w.substep(f)
+    torch.cuda.synchronize()
+    assert w.error_word() == 0
+    for e, env in enumerate((e0, e1)):
+        st, _ = run_oracle(env, 2)
+        compare(w, 2, st, env_idx=e)
