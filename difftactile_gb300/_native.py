@@ -33,6 +33,14 @@ class DtSensor(C.Structure):
     ]
 
 
+class DtRope(C.Structure):
+    _fields_ = [("p_off", C.c_int), ("n", C.c_int), ("env", C.c_int), ("blk_off", C.c_int),
+                ("mass", C.c_float), ("inv_m", C.c_float), ("rad", C.c_float), ("rest", C.c_float),
+                ("bend", C.c_float), ("alpha_s", C.c_float), ("alpha_b", C.c_float), ("relax_s", C.c_float),
+                ("relax_b", C.c_float), ("table_h", C.c_float), ("friction", C.c_float), ("dt_g", C.c_float * 3),
+                ("pin", C.c_float * 3), ("kn", C.c_float), ("kd", C.c_float), ("kt", C.c_float), ("mu_t", C.c_float)]
+
+
 class DtMaterial(C.Structure):
     _fields_ = [("mu", C.c_float), ("lam", C.c_float), ("yield_stress", C.c_float), ("model", C.c_int)]
 
@@ -48,6 +56,8 @@ WORLD_PTR_FIELDS = [
     "v_adj_pos", "v_adj_vel", "v_adj_vpos", "v_adj_velmid", "v_adj_ext", "v_adj_cv", "mat_adj",
     "err",
 ]
+ROPE_PTR_FIELDS = ["ropes", "r_state", "r_ext", "r_cidx", "r_adj", "r_extb"]
+ROPE_INT_FIELDS = ["n_ropes", "n_rope_particles", "rope_blocks", "max_rope_n"]
 WORLD_INT_FIELDS = [
     "n_envs", "n_particles", "n_sensors", "n_materials", "n_verts", "n_tets", "n_tris",
     "n_nodes", "n_blocks", "n_frames", "tape_blocks",
@@ -57,7 +67,8 @@ WORLD_INT_FIELDS = [
 class DtWorld(C.Structure):
     _fields_ = ([(n, _P) for n in WORLD_PTR_FIELDS] + [(n, C.c_int) for n in WORLD_INT_FIELDS]
                 + [("dt", C.c_float), ("grad_clip", C.c_float), ("svd_sweeps", C.c_int),
-                   ("svd_grad_mode", C.c_int), ("max_sensor_tris", C.c_int), ("scatter_mode", C.c_int)])
+                   ("svd_grad_mode", C.c_int), ("max_sensor_tris", C.c_int), ("scatter_mode", C.c_int)]
+                + [(n, _P) for n in ROPE_PTR_FIELDS] + [(n, C.c_int) for n in ROPE_INT_FIELDS])
 
 
 # entry points: name -> (restype, argtypes)
@@ -68,6 +79,7 @@ SIGNATURES = {
     "dt_sizeof_env": (C.c_size_t, []),
     "dt_sizeof_sensor": (C.c_size_t, []),
     "dt_sizeof_material": (C.c_size_t, []),
+    "dt_sizeof_rope": (C.c_size_t, []),
     "dt_step_begin": (C.c_int, [_W, _P]),
     "dt_substep_fwd": (C.c_int, [_W, C.c_int, _P]),
     "dt_substep_fwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),
@@ -77,6 +89,8 @@ SIGNATURES = {
     "dt_grid_op": (C.c_int, [_W, C.c_int, _P]),
     "dt_g2p": (C.c_int, [_W, C.c_int, _P]),
     "dt_fem_update2": (C.c_int, [_W, C.c_int, _P]),
+    "dt_rope_update": (C.c_int, [_W, C.c_int, _P]),
+    "dt_rope_update_bwd": (C.c_int, [_W, C.c_int, _P]),
     "dt_copy_frame": (C.c_int, [_W, C.c_int, C.c_int, _P]),
     "dt_substep_bwd": (C.c_int, [_W, C.c_int, _P]),
     "dt_substep_bwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),
@@ -116,7 +130,8 @@ def load(path: str | None = None):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    for name, cls in (("world", DtWorld), ("env", DtEnv), ("sensor", DtSensor), ("material", DtMaterial)):
+    for name, cls in (("world", DtWorld), ("env", DtEnv), ("sensor", DtSensor), ("material", DtMaterial),
+                      ("rope", DtRope)):
         n = getattr(lib, f"dt_sizeof_{name}")()
         if n != C.sizeof(cls):
             raise ImportError(f"ABI mismatch: sizeof(dt_{name}) = {n} in the library, {C.sizeof(cls)} in ctypes")

@@ -72,6 +72,7 @@ size_t dt_sizeof_world(void) { return sizeof(dt_world); }
 size_t dt_sizeof_env(void) { return sizeof(dt_env); }
 size_t dt_sizeof_sensor(void) { return sizeof(dt_sensor); }
 size_t dt_sizeof_material(void) { return sizeof(dt_material); }
+size_t dt_sizeof_rope(void) { return sizeof(dt_rope); }
 
 int dt_step_begin(const dt_world* w, cudaStream_t stream) {
   if (!w || w->n_frames < 2) return DT_ERR_ARG;
@@ -95,6 +96,12 @@ int dt_copy_frame(const dt_world* w, int src, int dst, cudaStream_t stream) {
                                   cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
       return DT_ERR_LAUNCH;
   }
+  // rope pos, vel, travel_info (PBDRope.copy_frame, PBD_rope.py:182-187)
+  const size_t rbytes = (size_t)2 * w->n_rope_particles * 16;
+  if (rbytes && cudaMemcpyAsync(w->r_state + (size_t)dst * 2 * w->n_rope_particles * 4,
+                                w->r_state + (size_t)src * 2 * w->n_rope_particles * 4, rbytes,
+                                cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+    return DT_ERR_LAUNCH;
   return DT_OK;
 }
 
@@ -114,6 +121,8 @@ int dt_adj_clear(const dt_world* w, cudaStream_t stream) {
       {w->v_adj_ext, (size_t)w->n_verts * 16},
       {w->v_adj_cv, (size_t)w->n_frames * w->n_verts * 16},
       {w->mat_adj, (size_t)w->n_materials * 16},
+      {w->r_adj, (size_t)4 * w->n_rope_particles * 16},
+      {w->r_extb, (size_t)w->n_rope_particles * 16},
   };
   for (auto& e : z)
     if (e.p && e.n && cudaMemsetAsync(e.p, 0, e.n, stream) != cudaSuccess) return DT_ERR_LAUNCH;

@@ -223,49 +223,6 @@ __global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p,
 // ---------------------------------------------------------------------------------------------
 // B2: grid op + contact adjoint
 // ---------------------------------------------------------------------------------------------
-// adjoint of contact_force (grasp_plastic.py:205-216): returns sdf_b, accumulates n_b and r_b
-DT_DEV float contact_force_bwd(const dt_env& E, float sdf, v3 n, v3 r, v3 eb, v3& nb, v3& rb) {
-  const float nr = dot(n, r);
-  const float vn = fmaxf(nr, 0.f);
-  const float kk = E.kn + E.kd * vn;
-  const v3 fn = (-kk * sdf) * n;
-  const v3 vt = r - nr * n;
-  const float vtn = sqrtf(dot(vt, vt) + 1e-11f);
-  v3 fnb = eb;
-  v3 vtb = v3{0.f, 0.f, 0.f};
-  if (vtn > 1e-4f) {
-    const float fnn = sqrtf(dot(fn, fn));
-    const float kv = E.kt * vtn, cap = E.mu_t * fnn;
-    const float g = fminf(kv, cap);
-    const v3 th = (1.f / vtn) * vt;
-    const float gb = dot(th, eb);
-    const v3 thb = g * eb;
-    float vtnb = 0.f;
-    if (kv <= cap) {
-      vtnb += E.kt * gb;
-    } else if (fnn > 0.f) {
-      fnb = fnb + (E.mu_t * gb / fnn) * fn;
-    }
-    vtb = (1.f / vtn) * thb;
-    vtnb += -dot(thb, vt) / (vtn * vtn);
-    vtb = vtb + (vtnb / vtn) * vt;
-  }
-  // vt = r - nr n
-  rb = rb + vtb;
-  float nrb = -dot(n, vtb);
-  nb = nb - nr * vtb;
-  // fn = -kk sdf n
-  const float nfb = dot(n, fnb);
-  const float kkb = -sdf * nfb;
-  const float sdfb = -kk * nfb;
-  nb = nb - (kk * sdf) * fnb;
-  const float vnb = E.kd * kkb;
-  if (nr > 0.f) nrb += vnb;
-  nb = nb + nrb * r;
-  rb = rb + nrb * n;
-  return sdfb;
-}
-
 __global__ void __launch_bounds__(GRID_NT) k_bwd_grid(dt_world w, int f) {
   const int cnt = min(w.tape_bcount[f], w.tape_blocks);
   const int l = threadIdx.x;
@@ -345,31 +302,18 @@ __global__ void __launch_bounds__(GRID_NT) k_bwd_grid(dt_world w, int f) {
         const v3 exs = (f4to3(aExt[tr.x]) + f4to3(aExt[tr.y])) + f4to3(aExt[tr.z]);
         const v3 eb = w.dt * gfb - third * exs;
         v3 nb = v3{0.f, 0.f, 0.f}, rb = v3{0.f, 0.f, 0.f};
-        const float sdfb = contact_force_bwd(E, sr.sdf, sr.n, sr.r, eb, nb, rb);
+        const float sdfb = contact_force_bwd(contact_k(E), sr.sdf, sr.n, sr.r, eb, nb, rb);
         // r = mean tri velocity - cur_v
         const v3 tvb = third * rb;
         red_add_v4(aVm + tr.x, v3to4(tvb));
         red_add_v4(aVm + tr.y, v3to4(tvb));
         red_add_v4(aVm + tr.z, v3to4(tvb));
         curvb = curvb - rb;
-        // sdf = (p - p1) . n
-        v3 p1b = -sdfb * sr.n;
-        nb = nb + sdfb * (p - p1);
-        // n = sg * nrm / (|nrm| + 1e-10)
-        const v3 e1 = p2 - p1, e2 = p3 - p1;
-        const v3 nrm = cross(e1, e2);
-        const float L = sqrtf(dot(nrm, nrm));
-        const float sg = dot((1.f / (L + 1e-10f)) * nrm, od) < 0.f ? -1.f : 1.f;
-        v3 nrmb = v3{0.f, 0.f, 0.f};
-        if (L > 0.f) {
-          const float D = L + 1e-10f;
-          nrmb = sg * ((1.f / D) * nb - (dot(nb, nrm) / (D * D * L)) * nrm);
-        }
-        const v3 e1b = cross(e2, nrmb), e2b = cross(nrmb, e1);
-        p1b = p1b - (e1b + e2b);
-        red_add_v4(aPos + tr.x, v3to4(p1b));
-        red_add_v4(aPos + tr.y, v3to4(e1b));
-        red_add_v4(aPos + tr.z, v3to4(e2b));
+        v3 b1, b2, b3;
+        tri_geom_bwd(p1, p2, p3, od, p, sr.n, sdfb, nb, b1, b2, b3);
+        red_add_v4(aPos + tr.x, v3to4(b1));
+        red_add_v4(aPos + tr.y, v3to4(b2));
+        red_add_v4(aPos + tr.z, v3to4(b3));
       }
       // cur_v = mv / (m + eps)
       mvb = mvb + inv_m * curvb;
@@ -717,7 +661,8 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
       break;
     case 2:
       if (ng > 0) k_bwd_grid<<<ng, GRID_NT, 0, stream>>>(*w, f);
-      break;
+      if (launched() != DT_OK) return DT_ERR_LAUNCH;
+      return dt_rope_update_bwd(w, f, stream);
     default:
       if (nb_p + nb_t + nb_v) k_bwd_p2g_fem<<<nb_p + nb_t + nb_v, NT, 0, stream>>>(*w, f, nb_p, nb_t, nb_v);
   }

@@ -21,6 +21,8 @@ DT_DEV v3 operator+(v3 a, v3 b) { return v3{a.x + b.x, a.y + b.y, a.z + b.z}; }
 DT_DEV v3 operator-(v3 a, v3 b) { return v3{a.x - b.x, a.y - b.y, a.z - b.z}; }
 DT_DEV v3 operator-(v3 a) { return v3{-a.x, -a.y, -a.z}; }
 DT_DEV v3 operator*(float s, v3 a) { return v3{s * a.x, s * a.y, s * a.z}; }
+DT_DEV v3 operator*(v3 a, float s) { return v3{a.x * s, a.y * s, a.z * s}; }
+DT_DEV v3 operator/(v3 a, float s) { return v3{a.x / s, a.y / s, a.z / s}; }
 DT_DEV float dot(v3 a, v3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 DT_DEV v3 cross(v3 a, v3 b) { return v3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
 DT_DEV v3 f4to3(float4 a) { return v3{a.x, a.y, a.z}; }
@@ -427,7 +429,9 @@ struct SdfRes {
   bool flag;
 };
 
-DT_DEV SdfRes find_sdf(v3 p1, v3 p2, v3 p3, v3 va, v3 vb, v3 vc, v3 od, v3 p, v3 gv) {
+// find_sdf, fem_sensor.py:362-394; `offset` is the PBD collision offset (:387-388), subtracted after
+// the projection
+DT_DEV SdfRes find_sdf(v3 p1, v3 p2, v3 p3, v3 va, v3 vb, v3 vc, v3 od, v3 p, v3 gv, float offset = 0.f) {
   v3 e1 = p2 - p1, e2 = p3 - p1;
   v3 n = cross(e1, e2);
   float len = sqrtf(dot(n, n));
@@ -444,6 +448,7 @@ DT_DEV SdfRes find_sdf(v3 p1, v3 p2, v3 p3, v3 va, v3 vb, v3 vc, v3 od, v3 p, v3
   const float third = 1.f / 3.f;
   v3 tv = third * ((va + vb) + vc);
   SdfRes o;
+  sdf -= offset;
   o.sdf = sdf;
   o.n = n;
   o.r = tv - gv;
@@ -451,19 +456,90 @@ DT_DEV SdfRes find_sdf(v3 p1, v3 p2, v3 p3, v3 va, v3 vb, v3 vc, v3 od, v3 p, v3
   return o;
 }
 
-DT_DEV v3 contact_force(const dt_env& E, float sdf, v3 n, v3 r) {
+// penalty + Coulomb-capped friction contact (calculate_contact_force): grasp_plastic.py:205-216
+// clamps the normal approach speed at 0 (clamp_vn), cable_straightening.py:212-224 does not
+struct ContactK {
+  float kn, kd, kt, mu_t;
+  bool clamp_vn;
+};
+DT_DEV ContactK contact_k(const dt_env& E) { return ContactK{E.kn, E.kd, E.kt, E.mu_t, true}; }
+
+DT_DEV v3 contact_force(const ContactK& K, float sdf, v3 n, v3 r) {
   float nr = dot(n, r);
-  float vn = fmaxf(nr, 0.f);
-  float kk = E.kn + E.kd * vn;
+  float vn = K.clamp_vn ? fmaxf(nr, 0.f) : nr;
+  float kk = K.kn + K.kd * vn;
   v3 fn = (-kk * sdf) * n;
   v3 vt = r - nr * n;
   float vtn = sqrtf(dot(vt, vt) + 1e-11f);
   v3 ft = v3{0.f, 0.f, 0.f};
   if (vtn > 1e-4f) {
-    float g = fminf(E.kt * vtn, E.mu_t * sqrtf(dot(fn, fn)));
+    float g = fminf(K.kt * vtn, K.mu_t * sqrtf(dot(fn, fn)));
     ft = v3{(vt.x / vtn) * g, (vt.y / vtn) * g, (vt.z / vtn) * g};
   }
   return fn + ft;
+}
+DT_DEV v3 contact_force(const dt_env& E, float sdf, v3 n, v3 r) { return contact_force(contact_k(E), sdf, n, r); }
+
+// adjoint of contact_force: returns sdf_b, accumulates n_b and r_b
+DT_DEV float contact_force_bwd(const ContactK& K, float sdf, v3 n, v3 r, v3 eb, v3& nb, v3& rb) {
+  const float nr = dot(n, r);
+  const float vn = K.clamp_vn ? fmaxf(nr, 0.f) : nr;
+  const float kk = K.kn + K.kd * vn;
+  const v3 fn = (-kk * sdf) * n;
+  const v3 vt = r - nr * n;
+  const float vtn = sqrtf(dot(vt, vt) + 1e-11f);
+  v3 fnb = eb;
+  v3 vtb = v3{0.f, 0.f, 0.f};
+  if (vtn > 1e-4f) {
+    const float fnn = sqrtf(dot(fn, fn));
+    const float kv = K.kt * vtn, cap = K.mu_t * fnn;
+    const float g = fminf(kv, cap);
+    const v3 th = (1.f / vtn) * vt;
+    const float gb = dot(th, eb);
+    const v3 thb = g * eb;
+    float vtnb = 0.f;
+    if (kv <= cap) {
+      vtnb += K.kt * gb;
+    } else if (fnn > 0.f) {
+      fnb = fnb + (K.mu_t * gb / fnn) * fn;
+    }
+    vtb = (1.f / vtn) * thb;
+    vtnb += -dot(thb, vt) / (vtn * vtn);
+    vtb = vtb + (vtnb / vtn) * vt;
+  }
+  // vt = r - nr n
+  rb = rb + vtb;
+  float nrb = -dot(n, vtb);
+  nb = nb - nr * vtb;
+  // fn = -kk sdf n
+  const float nfb = dot(n, fnb);
+  const float kkb = -sdf * nfb;
+  const float sdfb = -kk * nfb;
+  nb = nb - (kk * sdf) * fnb;
+  const float vnb = K.kd * kkb;
+  if (!K.clamp_vn || nr > 0.f) nrb += vnb;
+  nb = nb + nrb * r;
+  rb = rb + nrb * n;
+  return sdfb;
+}
+
+// adjoint of the triangle geometry in find_sdf for a contact at p (sdf = (p - p1) . n,
+// n = sg cross(p2 - p1, p3 - p1) / (|.| + 1e-10)): vertex position adjoints b1, b2, b3
+DT_DEV void tri_geom_bwd(v3 p1, v3 p2, v3 p3, v3 od, v3 p, v3 n, float sdfb, v3 nb, v3& b1, v3& b2, v3& b3) {
+  v3 p1b = -sdfb * n;
+  nb = nb + sdfb * (p - p1);
+  const v3 e1 = p2 - p1, e2 = p3 - p1;
+  const v3 nrm = cross(e1, e2);
+  const float L = sqrtf(dot(nrm, nrm));
+  const float sg = dot((1.f / (L + 1e-10f)) * nrm, od) < 0.f ? -1.f : 1.f;
+  v3 nrmb = v3{0.f, 0.f, 0.f};
+  if (L > 0.f) {
+    const float D = L + 1e-10f;
+    nrmb = sg * ((1.f / D) * nb - (dot(nb, nrm) / (D * D * L)) * nrm);
+  }
+  b2 = cross(e2, nrmb);
+  b3 = cross(nrmb, e1);
+  b1 = p1b - (b2 + b3);
 }
 
 // ------------------------------------------------------------------------------------------

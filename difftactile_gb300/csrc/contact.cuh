@@ -1,0 +1,131 @@
+// Surface-triangle argmin shared by the grid-node contact (fwd.cu) and the rope contact (rope.cu):
+// find_closest, fem_sensor.py:344-359 — the first triangle whose centroid distance
+// |c - p| (norm with eps 1e-10) is smallest, or -1 when none is below 100.
+//
+// A sensor's centroids are kept in contact-search order (tri_perm: groups of 32 consecutive
+// positions are compact patches of the rest surface), each carrying its original index in .w.  A CTA
+// stages them in shared memory with the bounding box of every group.  Four lanes (a quad) share one
+// query point: (1) the group with the nearest box, (2) its 32 centroids, (3) every other group
+// whose box is not farther than that distance by more than 1e-5 relative — far above the few-ulp
+// rounding of either distance, so no skipped member could win or tie — all four lanes together.
+// (distance, original index) pairs are combined lexicographically, which is the sequential scan's
+// first-minimum-wins result; every distance is evaluated with separately rounded operations, so the
+// argmin is bit-identical to a sequential CPU scan.
+#pragma once
+#include "common.cuh"
+
+struct Best {
+  float d;
+  int i;
+};
+DT_DEV Best lexmin(Best a, Best b) { return (b.d < a.d || (b.d == a.d && b.i < a.i)) ? b : a; }
+DT_DEV Best quad_min(Best b) {
+#pragma unroll
+  for (int o = 1; o <= 2; o <<= 1) {
+    Best other{__shfl_xor_sync(0xffffffffu, b.d, o), __shfl_xor_sync(0xffffffffu, b.i, o)};
+    b = lexmin(b, other);
+  }
+  return b;
+}
+// float min / max over the warp through the order-preserving map of IEEE bits to int32
+DT_DEV int f2ord(float x) {
+  const int i = __float_as_int(x);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+DT_DEV float ord2f(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
+DT_DEV float ord_min(float x) { return ord2f(__reduce_min_sync(0xffffffffu, f2ord(x))); }
+DT_DEV float ord_max(float x) { return ord2f(__reduce_max_sync(0xffffffffu, f2ord(x))); }
+// Euclidean distance from p to an axis-aligned box (0 inside)
+DT_DEV float box_dist(float4 lo, float4 hi, float px, float py, float pz) {
+  const float dx = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.f);
+  const float dy = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.f);
+  const float dz = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.f);
+  return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
+// Shared-memory words of the staging area for up to `cap` centroids (centroids + 2 boxes per group).
+inline size_t stage_bytes(int cap) { return (size_t)((cap > 0 ? cap : 1) + 2 * ((cap + 31) / 32)) * sizeof(float4); }
+
+// Stage sensor S's centroids and group boxes; every thread of the CTA calls it (barriers inside).
+template <int NTH>
+DT_DEV void stage_sensor(const dt_world& w, const dt_sensor& S, float4* scent, float4* gbox) {
+  const int tid = threadIdx.x, nf = S.nf;
+  const float4* cent = reinterpret_cast<const float4*>(w.tri_cent);
+  __syncthreads();
+  for (int t = tid; t < nf; t += NTH) scent[t] = __ldg(cent + S.f_off + t);
+  __syncthreads();
+  // one warp per group, min/max over the lanes as order-preserving integer reductions
+  const int G = (nf + 31) >> 5;
+  for (int gg = tid >> 5; gg < G; gg += NTH / 32) {
+    const int t = 32 * gg + (tid & 31);
+    const float4 c = scent[t < nf ? t : 32 * gg];
+    const float4 lo = make_float4(ord_min(c.x), ord_min(c.y), ord_min(c.z), 0.f);
+    const float4 hi = make_float4(ord_max(c.x), ord_max(c.y), ord_max(c.z), 0.f);
+    if ((tid & 31) == 0) {
+      gbox[2 * gg] = lo;
+      gbox[2 * gg + 1] = hi;
+    }
+  }
+  __syncthreads();
+}
+
+// Argmin for the quad's query point (px, py, pz); all 32 lanes of the warp call it, `active` false
+// for quads without a query.  Returns the local triangle index (original order) or -1, in every lane
+// of the quad.  in_smem: S staged by stage_sensor; otherwise a direct scan of global centroids.
+DT_DEV int closest_tri(const dt_world& w, const dt_sensor& S, const float4* scent, const float4* gbox, bool in_smem,
+                       bool active, float px, float py, float pz, int sub) {
+  const int nf = S.nf;
+  Best bb{100.f, -1};
+  if (in_smem) {
+    const int Gu = (nf + 31) >> 5;  // warp-uniform trip count around the shuffles
+    const int G = active ? Gu : 0;
+    Best gbest{3.4e38f, 0x7fffffff};
+    for (int gg = sub; gg < G; gg += 4) {
+      const float lb = box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz);
+      if (lb < gbest.d) gbest = Best{lb, gg};
+    }
+    gbest = quad_min(gbest);
+    // no group is selected when every box distance is NaN (non-finite sensor positions): the
+    // sentinel must not be used as an index; the pruned scan below then covers every group
+    const int g0 = gbest.i < G ? gbest.i : -1;
+    if (g0 >= 0) {
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) {
+        const int t = 32 * g0 + sub + 4 * jj;
+        if (t < nf) {
+          const float4 c = scent[t];
+          bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
+        }
+      }
+    }
+    bb = quad_min(bb);
+    const float thr = bb.d * (1.f + 1e-5f);
+    for (int gc = 0; gc < Gu; gc += 64) {
+      unsigned long long live = 0ull;
+      const int ge = min(gc + 64, G);
+      for (int gg = gc + sub; gg < ge; gg += 4)
+        if (gg != g0 && !(box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr)) live |= 1ull << (gg - gc);
+      live |= __shfl_xor_sync(0xffffffffu, live, 1);
+      live |= __shfl_xor_sync(0xffffffffu, live, 2);
+      while (live) {
+        const int gg = gc + __ffsll((long long)live) - 1;
+        live &= live - 1ull;
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+          const int t = 32 * gg + sub + 4 * jj;
+          if (t < nf) {
+            const float4 c = scent[t];
+            bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
+          }
+        }
+      }
+    }
+  } else if (active) {
+    const float4* cent = reinterpret_cast<const float4*>(w.tri_cent) + S.f_off;
+    for (int t = sub; t < nf; t += 4) {
+      const float4 c = __ldg(cent + t);
+      bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
+    }
+  }
+  return quad_min(bb).i;
+}

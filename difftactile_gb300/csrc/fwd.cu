@@ -17,7 +17,7 @@
 // DT_SCATTER_TILE their stencil records are gathered per node of the chunk's bounding box in shared
 // memory and flushed with one 16-byte vector RED per node (common.cuh: stencil_scatter), with
 // DT_SCATTER_GLOBAL each particle issues its 27 vector REDs directly.
-#include "common.cuh"
+#include "contact.cuh"
 #include <climits>
 
 namespace {
@@ -209,27 +209,6 @@ __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p,
 // (distance, index) pairs are combined lexicographically, which is exactly the sequential scan's
 // first-minimum-wins result.  Lane 0 of each node then does the contact force and the grid update.
 // ---------------------------------------------------------------------------------------------
-struct Best {
-  float d;
-  int i;
-};
-DT_DEV Best lexmin(Best a, Best b) { return (b.d < a.d || (b.d == a.d && b.i < a.i)) ? b : a; }
-// float min / max over the warp through the order-preserving map of IEEE bits to int32
-DT_DEV int f2ord(float x) {
-  const int i = __float_as_int(x);
-  return i >= 0 ? i : i ^ 0x7fffffff;
-}
-DT_DEV float ord2f(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
-DT_DEV float ord_min(float x) { return ord2f(__reduce_min_sync(0xffffffffu, f2ord(x))); }
-DT_DEV float ord_max(float x) { return ord2f(__reduce_max_sync(0xffffffffu, f2ord(x))); }
-// Euclidean distance from p to an axis-aligned box (0 inside)
-DT_DEV float box_dist(float4 lo, float4 hi, float px, float py, float pz) {
-  const float dx = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.f);
-  const float dy = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.f);
-  const float dz = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.f);
-  return sqrtf(dx * dx + dy * dy + dz * dz);
-}
-
 __global__ void __launch_bounds__(GRID_NT, 2) k_fwd_grid(dt_world w, int f, int smem_cap) {
   extern __shared__ float4 scent[];
   float4* gbox = scent + smem_cap;  // 2 float4 per group of 32 centroids
@@ -242,7 +221,6 @@ __global__ void __launch_bounds__(GRID_NT, 2) k_fwd_grid(dt_world w, int f, int 
   const float4* P = vframe(w.v_pos, w, f);
   const float4* VM = vframe(w.v_velmid, w, f);
   float4* EXT = vframe(w.v_ext, w, f);
-  const float4* cent = reinterpret_cast<const float4*>(w.tri_cent);
   const int4* tris = reinterpret_cast<const int4*>(w.tris);
   int staged = -1;
   for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
@@ -267,98 +245,12 @@ __global__ void __launch_bounds__(GRID_NT, 2) k_fwd_grid(dt_world w, int f, int 
       const int si = E.s_begin + q;  // block-uniform
       if (si >= E.s_end) break;
       const dt_sensor& S = w.sensors[si];
-      const int nf = S.nf;
-      const bool in_smem = nf <= smem_cap;
-      if (in_smem && staged != si) {
-        __syncthreads();
-        for (int t = tid; t < nf; t += GRID_NT) scent[t] = __ldg(cent + S.f_off + t);
-        __syncthreads();
-        // bounding boxes of groups of 32 consecutive centroids (lower bounds for the search): one
-        // warp per group, min/max over the lanes as order-preserving integer reductions
-        const int G = (nf + 31) >> 5;
-        for (int gg = tid >> 5; gg < G; gg += GRID_NT / 32) {
-          const int t = 32 * gg + (tid & 31);
-          const float4 c = scent[t < nf ? t : 32 * gg];
-          const float4 lo = make_float4(ord_min(c.x), ord_min(c.y), ord_min(c.z), 0.f);
-          const float4 hi = make_float4(ord_max(c.x), ord_max(c.y), ord_max(c.z), 0.f);
-          if ((tid & 31) == 0) {
-            gbox[2 * gg] = lo;
-            gbox[2 * gg + 1] = hi;
-          }
-        }
-        __syncthreads();
+      const bool in_smem = S.nf <= smem_cap;
+      if (in_smem && staged != si) {  // block-uniform
+        stage_sensor<GRID_NT>(w, S, scent, gbox);
         staged = si;
       }
-      // find_closest (fem_sensor.py:344-359): exact first-minimum argmin with group pruning.  A group
-      // is skipped only when its box distance exceeds the best distance found by more than 1e-5
-      // relative, far above the few-ulp rounding of either distance, so no member could win or tie.
-      Best bb{100.f, -1};
-      if (in_smem) {
-        const int G = occ ? (nf + 31) >> 5 : 0;
-        Best gbest{3.4e38f, 0x7fffffff};
-        for (int gg = sub; gg < G; gg += 4) {
-          const float lb = box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz);
-          if (lb < gbest.d) gbest = Best{lb, gg};
-        }
-#pragma unroll
-        for (int o = 1; o <= 2; o <<= 1) {
-          Best other{__shfl_xor_sync(0xffffffffu, gbest.d, o), __shfl_xor_sync(0xffffffffu, gbest.i, o)};
-          gbest = lexmin(gbest, other);
-        }
-        // no group is selected when every box distance is NaN (non-finite sensor positions): the
-        // sentinel must not be used as an index; the pruned scan below then covers every group
-        const int g0 = gbest.i < G ? gbest.i : -1;
-        if (g0 >= 0) {
-#pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            const int t = 32 * g0 + sub + 4 * jj;
-            if (t < nf) {
-              const float4 c = scent[t];
-              bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
-            }
-          }
-        }
-#pragma unroll
-        for (int o = 1; o <= 2; o <<= 1) {
-          Best other{__shfl_xor_sync(0xffffffffu, bb.d, o), __shfl_xor_sync(0xffffffffu, bb.i, o)};
-          bb = lexmin(bb, other);
-        }
-        // the groups that survive the bound are scanned by all four lanes of the node together
-        const float thr = bb.d * (1.f + 1e-5f);
-        const int Gu = (nf + 31) >> 5;  // block-uniform trip count around the shuffles
-        for (int gc = 0; gc < Gu; gc += 64) {
-          unsigned long long live = 0ull;
-          const int ge = min(gc + 64, G);
-          for (int gg = gc + sub; gg < ge; gg += 4)
-            if (gg != g0 && !(box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr))
-              live |= 1ull << (gg - gc);
-          live |= __shfl_xor_sync(0xffffffffu, live, 1);
-          live |= __shfl_xor_sync(0xffffffffu, live, 2);
-          while (live) {
-            const int gg = gc + __ffsll((long long)live) - 1;
-            live &= live - 1ull;
-#pragma unroll
-            for (int jj = 0; jj < 8; ++jj) {
-              const int t = 32 * gg + sub + 4 * jj;
-              if (t < nf) {
-                const float4 c = scent[t];
-                bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
-              }
-            }
-          }
-        }
-      } else if (occ) {
-        for (int t = sub; t < nf; t += 4) {
-          const float4 c = __ldg(cent + S.f_off + t);
-          bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
-        }
-      }
-#pragma unroll
-      for (int o = 1; o <= 2; o <<= 1) {
-        Best other{__shfl_xor_sync(0xffffffffu, bb.d, o), __shfl_xor_sync(0xffffffffu, bb.i, o)};
-        bb = lexmin(bb, other);
-      }
-      const int kk = bb.i;
+      const int kk = closest_tri(w, S, scent, gbox, in_smem, occ, px, py, pz, sub);
       if (q == 0) cid.x = kk;
       else if (q == 1) cid.y = kk;
       else if (q == 2) cid.z = kk;
@@ -525,7 +417,7 @@ int launch_l2(const dt_world* w, int f, cudaStream_t st) {
   int nb = w->n_blocks < 152 * 8 ? w->n_blocks : 152 * 8;
   if (nb <= 0) return DT_OK;
   const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
-  const size_t smem = (size_t)((cap > 0 ? cap : 1) + 2 * ((cap + 31) / 32)) * sizeof(float4);
+  const size_t smem = stage_bytes(cap);
   static size_t configured = 0;
   if (smem > 48 * 1024 && smem > configured) {
     if (cudaFuncSetAttribute(k_fwd_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
@@ -552,6 +444,7 @@ int dt_substep_fwd(const dt_world* w, int f, cudaStream_t stream) {
   if (rc) return rc;
   if ((rc = launch_l1(w, f, true, true, stream))) return rc;
   if ((rc = launch_l2(w, f, stream))) return rc;
+  if ((rc = dt_rope_update(w, f, stream))) return rc;
   return launch_l3(w, f, true, true, stream);
 }
 
@@ -562,7 +455,7 @@ int dt_substep_fwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
     case 0:
       return launch_l1(w, f, true, true, stream);
     case 1:
-      return launch_l2(w, f, stream);
+      return (rc = launch_l2(w, f, stream)) ? rc : dt_rope_update(w, f, stream);
     case 2:
       return launch_l3(w, f, true, true, stream);
     default:

@@ -61,6 +61,12 @@ int dt_substep_fwd_noalloc(const dt_world* w, int f, cudaStream_t stream) {
   v.v_ext = w->v_ext + (size_t)f * Vv;
   v.v_vpos = w->v_vpos + (size_t)f * Vv;
   v.v_cv = w->v_cv + (size_t)f * Vv;
+  const size_t R = (size_t)w->n_rope_particles * 4;  // rope frames: state (2 planes), ext, argmin
+  if (w->n_ropes > 0) {
+    v.r_state = w->r_state + (size_t)f * 2 * R;
+    v.r_ext = w->r_ext + (size_t)f * R;
+    v.r_cidx = w->r_cidx + (size_t)f * R;
+  }
   v.n_frames = 2;
   v.tape_blocks = w->n_blocks;
   v.g_acc = reinterpret_cast<float*>(S + NA_OFF_ACC);

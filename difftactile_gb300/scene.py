@@ -71,6 +71,59 @@ class SensorSpec:
 
 
 @dataclass
+class RopeSpec:
+    """PBD rope (PBDRope.__init__ / init, PBD_rope.py:18-99): ``n`` particles of radius ``rad`` laid out
+    from ``pos`` along ``ori`` at the rest length; node 0 stays pinned at ``pos``.  ``kn, kd, kt, mu_t``
+    are the rope-sensor contact parameters (cable_straightening.py:212-224)."""
+    n: int = 50
+    rad: float = 0.25
+    rho: float = 10.0
+    rest_length: float | None = 0.1    # None: 2 rad (bending 4 rad), else bending 2 rest_length
+    pos: tuple = (0.0, 0.0, 0.0)
+    ori: tuple = (0.0, 0.0, 1.0)
+    table_h: float = 0.0
+    stretch_compliance: float | None = None  # default 1e-5 / rho
+    bend_compliance: float | None = None     # default 1e-5 / rho
+    stretch_relax: float = 0.3
+    bend_relax: float = 0.1
+    friction: float = 0.995
+    gravity: tuple = (0.0, -9.8, 0.0)
+    kn: float = 1e4
+    kd: float = 100.0
+    kt: float = 100.0
+    mu_t: float = 1.0
+    x: np.ndarray | None = None        # [n,3] initial positions overriding the straight layout
+    v: np.ndarray | None = None        # [n,3] initial velocities (default 0)
+
+    @property
+    def mass(self):
+        return self.rho * (np.pi * 4.0 / 3.0) * self.rad ** 3
+
+    @property
+    def rest(self):
+        return 2 * self.rad if self.rest_length is None else self.rest_length
+
+    @property
+    def bend(self):
+        return 4 * self.rad if self.rest_length is None else 2 * self.rest_length
+
+    @property
+    def compliance(self):
+        cs = 1e-5 / self.rho if self.stretch_compliance is None else self.stretch_compliance
+        cb = 1e-5 / self.rho if self.bend_compliance is None else self.bend_compliance
+        return cs, cb
+
+    def init_positions(self) -> np.ndarray:
+        if self.x is not None:
+            return np.asarray(self.x, np.float32)
+        i = np.arange(self.n, dtype=np.float64)[:, None]
+        return (np.asarray(self.pos, np.float64) + np.asarray(self.ori, np.float64) * self.rest * i).astype(np.float32)
+
+    def replace(self, **kw):
+        return dataclasses.replace(self, **kw)
+
+
+@dataclass
 class EnvSpec:
     x: np.ndarray                      # [N,3] particle positions
     materials: list                    # list[Material]
@@ -89,6 +142,7 @@ class EnvSpec:
     kd: float = 100.0
     kt: float = 100.0
     mu_t: float = 1.0
+    ropes: list = field(default_factory=list)     # list[RopeSpec]
 
     @property
     def n_particles(self):

@@ -158,6 +158,32 @@ class World:
 
         cat = lambda xs, shape, dt_: (np.concatenate(xs, 0) if xs else np.zeros(shape, dt_))  # noqa: E731
         self.rest_verts = cat(verts, (0, 3), np.float32)
+
+        # ---------------- PBD ropes (flat over all envs, 64 particles per contact CTA) ----------------
+        rope_rows, r_x, r_v, self.rope_specs = [], [], [], []
+        r_off = r_blk = 0
+        for e, s in enumerate(envs):
+            for rp in getattr(s, "ropes", []):
+                row = N.DtRope()
+                row.p_off, row.n, row.env, row.blk_off = r_off, rp.n, e, r_blk
+                row.mass, row.inv_m, row.rad = rp.mass, 1.0 / rp.mass, rp.rad
+                row.rest, row.bend = rp.rest, rp.bend
+                cs, cb = rp.compliance
+                row.alpha_s, row.alpha_b = cs / self.dt ** 2, cb / self.dt ** 2
+                row.relax_s, row.relax_b = rp.stretch_relax, rp.bend_relax
+                row.table_h, row.friction = rp.table_h, rp.friction
+                row.dt_g[:] = [self.dt * g for g in rp.gravity]
+                x0 = rp.init_positions()
+                row.pin[:] = [float(c) for c in x0[0]]
+                row.kn, row.kd, row.kt, row.mu_t = rp.kn, rp.kd, rp.kt, rp.mu_t
+                rope_rows.append(row)
+                r_x.append(x0)
+                r_v.append(np.zeros((rp.n, 3), np.float32) if rp.v is None else np.asarray(rp.v, np.float32))
+                self.rope_specs.append(rp)
+                r_off += rp.n
+                r_blk += (rp.n + 63) // 64
+        self.rope_rows = rope_rows
+        self.n_ropes, self.n_rope_particles = len(rope_rows), r_off
         self.t = {}
         t = self.t
 
@@ -220,6 +246,13 @@ class World:
         t["v_adj_cv"] = zeros((Fn, V, 4))
         t["mat_adj"] = zeros((max(self.n_materials, 1), 4))
         t["err"] = zeros((4,), I32)
+        NR = self.n_rope_particles
+        t["ropes"] = struct_tensor(rope_rows, N.DtRope)
+        t["r_state"] = zeros((Fn, 2, NR, 4))
+        t["r_ext"] = zeros((Fn, NR, 4))
+        t["r_cidx"] = zeros((Fn, NR, 4), I32)
+        t["r_adj"] = zeros((2, 2, NR, 4))
+        t["r_extb"] = zeros((NR, 4))
 
         w = N.DtWorld()
         for name in N.WORLD_PTR_FIELDS:
@@ -231,6 +264,11 @@ class World:
         w.svd_grad_mode = int(svd_grad_mode)
         w.max_sensor_tris = max([r.nf for r in srows], default=0)
         w.scatter_mode = int(scatter_mode)
+        for name in N.ROPE_PTR_FIELDS:
+            setattr(w, name, t[name].data_ptr() if (self.n_ropes and t[name].numel()) else None)
+        w.n_ropes, w.n_rope_particles = self.n_ropes, NR
+        w.rope_blocks = r_blk
+        w.max_rope_n = max([r.n for r in rope_rows], default=0)
         self.w = w
         self.wp = C.pointer(w)
 
@@ -246,6 +284,8 @@ class World:
             if envs else np.zeros((0, 3), np.float32)
         self.set_particles(0, x=xs, v=vs, C=np.zeros((Np, 3, 3), np.float32),
                            F=np.broadcast_to(np.eye(3, dtype=np.float32), (Np, 3, 3)))
+        for r in range(self.n_ropes):
+            self.set_rope_state(0, r, pos=r_x[r], vel=r_v[r], trav=np.zeros(self.rope_rows[r].n, np.float32))
 
     # ------------------------------------------------------------------------------------------
     # launches go to ``stream_override`` when set (e.g. a capture stream), else torch's current stream
@@ -263,6 +303,36 @@ class World:
 
     def call(self, name, *args):
         N.check(getattr(self.lib, name)(self.wp, *args, self.stream), name)
+
+    # ---- rope state: pos [n,3], vel [n,3], travel_info [n] of rope r at frame f ----
+    def rslice(self, r):
+        row = self.rope_rows[r]
+        return slice(row.p_off, row.p_off + row.n)
+
+    def rope_state(self, f, r):
+        sl = self.rslice(r)
+        st = self.t["r_state"][f]
+        return {"pos": st[0, sl, :3], "vel": st[1, sl, :3], "trav": st[0, sl, 3]}
+
+    def set_rope_state(self, f, r, pos=None, vel=None, trav=None):
+        st = self.rope_state(f, r)
+        for k, a in (("pos", pos), ("vel", vel), ("trav", trav)):
+            if a is not None:
+                st[k].copy_(torch.as_tensor(np.asarray(a, np.float32) if not torch.is_tensor(a) else a,
+                                            dtype=F32, device=self.device).reshape(st[k].shape))
+
+    def rope_adjoint(self, f, r):
+        """Adjoint of rope r's frame f, held in buffer f & 1 during a backward sweep."""
+        sl = self.rslice(r)
+        a = self.t["r_adj"][f & 1]
+        return {"pos": a[0, sl, :3], "vel": a[1, sl, :3], "trav": a[0, sl, 3]}
+
+    def set_rope_adjoint(self, f, r, pos=None, vel=None, trav=None):
+        a = self.rope_adjoint(f, r)
+        for k, v in (("pos", pos), ("vel", vel), ("trav", trav)):
+            if v is not None:
+                a[k].copy_(torch.as_tensor(np.asarray(v, np.float32) if not torch.is_tensor(v) else v,
+                                           dtype=F32, device=self.device).reshape(a[k].shape))
 
     # ---- particle state in user order ----
     def set_particles(self, frame, x=None, v=None, C=None, F=None):

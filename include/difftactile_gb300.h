@@ -110,6 +110,23 @@ typedef struct dt_material {
   int model;            /* DT_MODEL_* */
 } dt_material;
 
+/* PBD rope (PBDRope, PBD_rope.py:16-99) and its contact with the sensors of its environment
+ * (cable_straightening.py:212-224, 288-319).  Node 0 is pinned at pin. */
+typedef struct dt_rope {
+  int p_off, n;         /* particle range in the flat rope arrays */
+  int env;              /* environment whose sensors the rope touches (s_begin..s_end) */
+  int blk_off;          /* first CTA of this rope in the rope-contact launches (64 particles per CTA) */
+  float mass, inv_m;    /* p_mass = rho 4/3 pi rad^3 and its inverse */
+  float rad;            /* particle radius = contact offset */
+  float rest, bend;     /* stretch and bending rest lengths */
+  float alpha_s, alpha_b;   /* compliance / dt^2 */
+  float relax_s, relax_b;   /* relaxation factors */
+  float table_h, friction;  /* floor height, tangential velocity factor on the floor */
+  float dt_g[3];        /* dt * gravity */
+  float pin[3];         /* position of node 0 */
+  float kn, kd, kt, mu_t;   /* rope-sensor contact (no clamp of the normal approach speed) */
+} dt_rope;
+
 /* World descriptor: host struct holding device pointers and sizes. */
 typedef struct dt_world {
   /* ---- static tables (device) ---- */
@@ -169,6 +186,16 @@ typedef struct dt_world {
   int svd_grad_mode;             /* DT_SVDGRAD_* */
   int max_sensor_tris;           /* largest nf over the sensors (sizes the contact search's staging) */
   int scatter_mode;              /* DT_SCATTER_*: how P2G and the G2P adjoint accumulate into the grid */
+  /* ---- PBD ropes (may be empty) ---- */
+  const dt_rope* ropes;          /* [n_ropes] */
+  float* r_state;                /* [n_frames][2][n_rope_particles][4]: (pos.xyz, travel), (vel.xyz, 0) */
+  float* r_ext;                  /* [n_frames][n_rope_particles][4]: contact force * dt summed, contact flag */
+  int* r_cidx;                   /* [n_frames][n_rope_particles][4] argmin triangle per env sensor */
+  float* r_adj;                  /* [2][2][n_rope_particles][4] adjoint of r_state, double-buffered */
+  float* r_extb;                 /* [n_rope_particles][4] working: adjoint of r_ext of the current frame */
+  int n_ropes, n_rope_particles;
+  int rope_blocks;               /* CTAs of the rope-contact launches (sum of ceil(n / 64)) */
+  int max_rope_n;                /* largest n over the ropes (sizes the rope solver's shared memory) */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared
@@ -193,6 +220,7 @@ size_t dt_sizeof_world(void);
 size_t dt_sizeof_env(void);
 size_t dt_sizeof_sensor(void);
 size_t dt_sizeof_material(void);
+size_t dt_sizeof_rope(void);
 
 /* ---- step set-up ----
  * Clears the grid tape counters of every frame and prepares FEM frame 0 (velmid = vel, ext = 0).
@@ -225,15 +253,29 @@ int dt_substep_fwd_noalloc(const dt_world* w, int f, cudaStream_t stream);
 
 /* The same substep split into the reference's per-object calls, for drop-in use of the
  * reference method sequence.  dt_substep_fwd(f) == p2g(f); fem_update(f); grid_op(f) (which
- * includes check_grid_occupy, check_collision and collision); g2p(f); fem_update2(f). */
+ * includes check_grid_occupy, check_collision and collision); rope_update(f); g2p(f);
+ * fem_update2(f).  dt_substep_fwd_stage: stage 0 = p2g + fem_update, 1 = grid_op + rope_update,
+ * 2 = g2p + fem_update2. */
 int dt_p2g(const dt_world* w, int f, cudaStream_t stream);         /* mpm_elastic.py:135-208 */
 int dt_fem_update(const dt_world* w, int f, cudaStream_t stream);  /* fem_sensor.py:409-440 */
 int dt_grid_op(const dt_world* w, int f, cudaStream_t stream);     /* mpm_elastic.py:211-240 + grasp_plastic.py:270-299 */
 int dt_g2p(const dt_world* w, int f, cudaStream_t stream);         /* mpm_elastic.py:244-260 */
 int dt_fem_update2(const dt_world* w, int f, cudaStream_t stream); /* fem_sensor.py:444-457 */
 
-/* Copy frame `src` of the particle and FEM state to frame `dst` (mpm_elastic.py:263-268,
- * fem_sensor.py:461-465). */
+/* Rope part of a substep (no-op without ropes): check_collision + collision of the rope particles
+ * against their env's sensors (cable_straightening.py:288-319) and PBDRope.update(f)
+ * (PBD_rope.py:112-180); writes r_state[f+1], r_ext[f], r_cidx[f] and adds the sensors' contact
+ * forces to v_ext[f].  Runs after the sensors' elastic update and before their update2.  Shared
+ * memory: 32 * max_rope_n bytes (DT_ERR_CAPACITY above 227 KB). */
+int dt_rope_update(const dt_world* w, int f, cudaStream_t stream);
+/* Adjoint of dt_rope_update (rope.update.grad, clamp_grid on the rope's grads, collision.grad;
+ * cable_straightening.py:177-186): consumes r_adj[(f+1)&1] and v_adj_ext (after the FEM
+ * update2 adjoint), writes r_adj[f&1], accumulates v_adj_velmid and v_adj_pos[f&1].  Shared memory:
+ * 64 * max_rope_n bytes. */
+int dt_rope_update_bwd(const dt_world* w, int f, cudaStream_t stream);
+
+/* Copy frame `src` of the particle, FEM and rope state to frame `dst` (mpm_elastic.py:263-268,
+ * fem_sensor.py:461-465, PBD_rope.py:182-187). */
 int dt_copy_frame(const dt_world* w, int src, int dst, cudaStream_t stream);
 
 /* ---- backward substep (replaces Contact.update_grad(f), grasp_plastic.py:167-178) ----
@@ -244,11 +286,12 @@ int dt_substep_bwd(const dt_world* w, int f, cudaStream_t stream);
 
 /* dt_substep_bwd split into its four launches, the per-kernel .grad calls of update_grad
  * (grasp_plastic.py:167-178): stage 0 restores frame f's grid velocities from the tape; stage 1 is
- * fem.update2.grad + g2p.grad; stage 2 is grid_op.grad + clamp_grid + collision.grad; stage 3 is
+ * fem.update2.grad + g2p.grad; stage 2 is grid_op.grad + clamp_grid + collision.grad (and
+ * dt_rope_update_bwd); stage 3 is
  * fem.update.grad + p2g.grad + svd_grad + compute_new_F.grad.  Run stages 0..3 in order. */
 int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t stream);
 
-/* Zero the adjoint buffers (p_adj, v_adj_*, mat_adj, g_adj_*) before a backward sweep. */
+/* Zero the adjoint buffers (p_adj, v_adj_*, mat_adj, g_adj_*, r_adj, r_extb) before a backward sweep. */
 int dt_adj_clear(const dt_world* w, cudaStream_t stream);
 
 /* ---- readouts ---- */

@@ -56,6 +56,37 @@ typedef struct orc_sensor {
   int pad_;
 } orc_sensor;
 
+// PBD rope (PBD_rope.py) with its sensor contact parameters (cable_straightening.py:212-224)
+typedef struct orc_rope {
+  int n;              // particles; node 0 is pinned at pin
+  int pad_;
+  double mass, rad;   // p_mass = rho 4/3 pi rad^3, contact offset = rad
+  double rest, bend;  // rest_length, bending_length
+  double alpha_s, alpha_b;    // compliance / dt^2
+  double relax_s, relax_b;    // stretch_relaxation, bending_relaxation
+  double table_h, friction;   // floor height and tangential velocity factor
+  double grav[3], pin[3];
+  double kn, kd, kt, mu_t;
+} orc_rope;
+
+// per-rope arrays of one substep (element type float or double as the entry point)
+typedef struct orc_rope_io {
+  void* pos;          // [n][3] frame f
+  void* vel;          // [n][3]
+  void* trav;         // [n] travel_info
+  void* pos1;         // [n][3] frame f+1 (written)
+  void* vel1;
+  void* trav1;
+  void* ext;          // [n][3] ext_f[f]: sum of contact force * dt (written)
+  int* cidx;          // [n][n_sensors] argmin per sensor (written)
+  const void* posb1;  // adjoints of frame f+1 (backward)
+  const void* velb1;
+  const void* travb1;
+  void* posb;         // adjoints of frame f (written by the backward)
+  void* velb;
+  void* travb;
+} orc_rope_io;
+
 typedef struct orc_scene {
   int n_particles;
   int n[3];
@@ -74,6 +105,10 @@ typedef struct orc_scene {
   int svd_sweeps;
   int n_threads;      // OpenMP threads for the timed baseline (<=1: sequential)
   double grad_clip;   // backward clamp (grasp_plastic.py:192-202); 0 disables
+  int n_ropes;
+  int pad2_;
+  const orc_rope* ropes;
+  orc_rope_io* rope_io;  // [n_ropes]
 } orc_scene;
 
 }  // extern "C"
@@ -276,6 +311,7 @@ struct Consts {
   T dt_g[3];
   T kn, kd, kt, mu_t;
   T third;
+  bool clamp_vn;  // grasp variant max(v_n, 0); the cable variant (cable_straightening.py:212-224) has none
 };
 
 template <typename T>
@@ -294,6 +330,7 @@ Consts<T> make_consts(const orc_scene* sc) {
   k.kt = T(sc->kt);
   k.mu_t = T(sc->mu_t);
   k.third = T(1.0 / 3.0);
+  k.clamp_vn = true;
   return k;
 }
 
@@ -368,7 +405,8 @@ struct SdfOut {
 // find_sdf, fem_sensor.py:362-394.  Returns the normal already flipped (= -norm_v) and the
 // relative velocity already negated (= -relative_v), as passed to calculate_contact_force.
 template <typename T>
-SdfOut<T> find_sdf(const orc_sensor& s, const T* pos, const T* vel, int k, const T p[3], const T gv[3]) {
+SdfOut<T> find_sdf(const orc_sensor& s, const T* pos, const T* vel, int k, const T p[3], const T gv[3],
+                   T offset = T(0)) {
   const int* t = s.tris + 3 * k;
   const T* p1 = pos + 3 * t[0];
   const T* p2 = pos + 3 * t[1];
@@ -400,6 +438,7 @@ SdfOut<T> find_sdf(const orc_sensor& s, const T* pos, const T* vel, int k, const
   T u = (d11 * d02 - d01 * d12) * invd;
   T v = (d00 * d12 - d01 * d02) * invd;
   SdfOut<T> o;
+  sdf -= offset;  // PBD collision offset (fem_sensor.py:388), after the projection
   o.sdf = sdf;
   const T third = T(1.0 / 3.0);
   for (int c = 0; c < 3; ++c) {
@@ -415,7 +454,7 @@ SdfOut<T> find_sdf(const orc_sensor& s, const T* pos, const T* vel, int k, const
 template <typename T>
 void contact_force(const Consts<T>& K, T sdf, const T n[3], const T r[3], T ext[3]) {
   T nr = dot3(n, r);
-  T vn = std::max(nr, T(0));
+  T vn = K.clamp_vn ? std::max(nr, T(0)) : nr;
   T fn[3];
   T kk = K.kn + K.kd * vn;
   for (int c = 0; c < 3; ++c) fn[c] = -kk * sdf * n[c];
@@ -547,6 +586,104 @@ inline void aadd(T& a, T b, bool atomic) {
   } else {
     a += b;
   }
+}
+
+// ---- PBD rope: check_collision + collision (cable_straightening.py:288-319) and PBDRope.update
+// (PBD_rope.py:112-180), after the sensors' elastic update and before their update2 ----
+template <typename T>
+Consts<T> rope_consts(const orc_scene* sc, const orc_rope& R) {
+  Consts<T> K = make_consts<T>(sc);
+  K.kn = T(R.kn);
+  K.kd = T(R.kd);
+  K.kt = T(R.kt);
+  K.mu_t = T(R.mu_t);
+  K.clamp_vn = false;
+  return K;
+}
+
+// stretch (stride 1) or bending (stride 2) pass, Jacobi: corrections from the positions on entry
+template <typename T>
+void rope_pass(std::vector<T>& tp, int n, int stride, T len, T alpha, T relax, T w) {
+  std::vector<T> dp(3 * n, T(0));
+  for (int e = 0; e + stride < n; ++e) {
+    const T* x1 = &tp[3 * e];
+    const T* x2 = &tp[3 * (e + stride)];
+    T d[3] = {x1[0] - x2[0], x1[1] - x2[1], x1[2] - x2[2]};
+    T L = std::sqrt(dot3(d, d) + T(1e-10));
+    T C = L - len;
+    for (int c = 0; c < 3; ++c) {
+      T dpc = -C / (w + w + alpha) * d[c] / L * relax;
+      dp[3 * e + c] += dpc * w;
+      dp[3 * (e + stride) + c] -= dpc * w;
+    }
+  }
+  for (int i = 0; i < 3 * n; ++i) tp[i] += dp[i];
+}
+
+template <typename T>
+void rope_integrate(const orc_rope& R, T dt, const T* rp, const T* rv, const T* re, std::vector<T>& tp,
+                    std::vector<unsigned char>& floor_hit) {
+  const int n = R.n;
+  tp.assign(3 * n, T(0));
+  floor_hit.assign(n, 0);
+  for (int i = 0; i < n; ++i) {
+    T nv[3];
+    for (int c = 0; c < 3; ++c) nv[c] = (rv[3 * i + c] + re[3 * i + c] / T(R.mass)) + T(R.grav[c]) * dt;
+    T npy = rp[3 * i + 1] + nv[1] * dt;
+    if (npy < T(R.table_h) && nv[1] < T(0)) {  // floor: drop the normal part, damp the tangential
+      floor_hit[i] = 1;
+      nv[1] = nv[1] - nv[1];
+      nv[0] = nv[0] * T(R.friction);
+      nv[1] = nv[1] * T(R.friction);
+      nv[2] = nv[2] * T(R.friction);
+    }
+    for (int c = 0; c < 3; ++c) tp[3 * i + c] = rp[3 * i + c] + nv[c] * dt;
+  }
+}
+
+template <typename T>
+void rope_fwd(const orc_scene* sc, const orc_rope& R, orc_rope_io& io, T* const* pos, T* const* vel,
+              T* const* ext) {
+  const int n = R.n, NS = sc->n_sensors;
+  const T dt = T(sc->dt);
+  const Consts<T> K = rope_consts<T>(sc, R);
+  const T* rp = static_cast<const T*>(io.pos);
+  const T* rv = static_cast<const T*>(io.vel);
+  const T* rt = static_cast<const T*>(io.trav);
+  T* re = static_cast<T*>(io.ext);
+  for (int p = 0; p < n; ++p) {
+    bool any = false;
+    for (int c = 0; c < 3; ++c) re[3 * p + c] = T(0);
+    for (int s = 0; s < NS; ++s) {
+      const orc_sensor& S = sc->sensors[s];
+      int kk = find_closest(S, pos[s], rp + 3 * p);
+      io.cidx[p * NS + s] = kk;
+      if (kk < 0) continue;
+      SdfOut<T> so = find_sdf(S, pos[s], vel[s], kk, rp + 3 * p, rv + 3 * p, T(R.rad));
+      if (!so.flag) continue;
+      T e[3];
+      contact_force(K, so.sdf, so.nrm, so.rel, e);
+      for (int c = 0; c < 3; ++c) re[3 * p + c] += e[c] * dt;  // update_contact_force, PBD_rope.py:104-105
+      const int* t = S.tris + 3 * kk;
+      for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) ext[s][3 * t[a] + c] += K.third * (T(-1) * e[c]);
+      any = true;
+    }
+    static_cast<T*>(io.trav1)[p] = any ? T(1) : rt[p];
+  }
+  std::vector<T> tp;
+  std::vector<unsigned char> fl;
+  rope_integrate(R, dt, rp, rv, re, tp, fl);
+  const T w = T(1) / T(R.mass);
+  rope_pass(tp, n, 1, T(R.rest), T(R.alpha_s), T(R.relax_s), w);
+  rope_pass(tp, n, 2, T(R.bend), T(R.alpha_b), T(R.relax_b), w);
+  T* rp1 = static_cast<T*>(io.pos1);
+  T* rv1 = static_cast<T*>(io.vel1);
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) {
+      rp1[3 * i + c] = i == 0 ? T(R.pin[c]) : tp[3 * i + c];
+      rv1[3 * i + c] = (rp1[3 * i + c] - rp[3 * i + c]) / dt;
+    }
 }
 
 template <typename T>
@@ -684,6 +821,9 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
         for (int c = 0; c < 3; ++c) grid_v_out[3 * g + c] = vo[c];
       }
 
+  // ---- PBD ropes ----
+  for (int r = 0; r < sc->n_ropes; ++r) rope_fwd<T>(sc, sc->ropes[r], sc->rope_io[r], pos, vel, ext);
+
   // ---- g2p ----
 #pragma omp parallel for num_threads(nt) schedule(static) if (at)
   for (int p = 0; p < sc->n_particles; ++p) {
@@ -774,7 +914,7 @@ inline T gap_clamp(T a) {
 template <typename T>
 T contact_force_bwd(const Consts<T>& K, T sdf, const T n[3], const T r[3], const T eb[3], T nb[3], T rb[3]) {
   T nr = dot3(n, r);
-  T vn = std::max(nr, T(0));
+  T vn = K.clamp_vn ? std::max(nr, T(0)) : nr;
   T kk = K.kn + K.kd * vn;
   T fn[3], vt[3];
   for (int c = 0; c < 3; ++c) {
@@ -809,7 +949,7 @@ T contact_force_bwd(const Consts<T>& K, T sdf, const T n[3], const T r[3], const
   T kkb = -sdf * nfb;
   T sdfb = -kk * nfb;
   for (int c = 0; c < 3; ++c) nb[c] -= (kk * sdf) * fnb[c];
-  if (nr > T(0)) nrb += K.kd * kkb;
+  if (!K.clamp_vn || nr > T(0)) nrb += K.kd * kkb;
   for (int c = 0; c < 3; ++c) {
     nb[c] += nrb * r[c];
     rb[c] += nrb * n[c];
@@ -845,6 +985,156 @@ M3<T> svd_grad(const M3<T>& U, const T s[3], const M3<T>& V, const M3<T>& Ub0, c
       inner.a[i][j] = val;
     }
   return mmul(mmul(U, inner), mT(V));
+}
+
+// adjoint of the sensor-triangle geometry of find_sdf (normal and sdf) for a contact at point p:
+// accumulates the triangle vertices' position adjoints
+template <typename T>
+void tri_geom_bwd(const orc_sensor& S, const T* pos, int kk, const T p[3], const SdfOut<T>& so, T sdfb, T nb[3],
+                  T* posb) {
+  const int* t = S.tris + 3 * kk;
+  const T* p1 = pos + 3 * t[0];
+  const T* p2 = pos + 3 * t[1];
+  const T* p3 = pos + 3 * t[2];
+  T p1b[3], e1[3], e2[3], nrm[3];
+  for (int c = 0; c < 3; ++c) {
+    p1b[c] = -sdfb * so.nrm[c];
+    nb[c] += sdfb * (p[c] - p1[c]);
+    e1[c] = p2[c] - p1[c];
+    e2[c] = p3[c] - p1[c];
+  }
+  cross(e1, e2, nrm);
+  T L = std::sqrt(dot3(nrm, nrm));
+  T od[3] = {T(S.out_dir[0]), T(S.out_dir[1]), T(S.out_dir[2])};
+  T inv = T(1) / (L + T(1e-10));
+  T nn_[3] = {inv * nrm[0], inv * nrm[1], inv * nrm[2]};
+  T sg = dot3(nn_, od) < T(0) ? T(-1) : T(1);
+  T nrmb[3] = {T(0), T(0), T(0)};
+  if (L > T(0)) {
+    T D = L + T(1e-10);
+    T q = dot3(nb, nrm) / (D * D * L);
+    for (int c = 0; c < 3; ++c) nrmb[c] = sg * (nb[c] / D - q * nrm[c]);
+  }
+  T e1b[3], e2b[3];
+  cross(e2, nrmb, e1b);
+  cross(nrmb, e1, e2b);
+  for (int c = 0; c < 3; ++c) {
+    posb[3 * t[0] + c] += p1b[c] - (e1b[c] + e2b[c]);
+    posb[3 * t[1] + c] += e1b[c];
+    posb[3 * t[2] + c] += e2b[c];
+  }
+}
+
+// adjoint of one Jacobi pass: tp_out = tp_in + dp(tp_in); tpb holds d/d tp_out on entry and
+// d/d tp_in on return
+template <typename T>
+void rope_pass_bwd(const std::vector<T>& tp_in, std::vector<T>& tpb, int n, int stride, T len, T alpha, T relax,
+                   T w) {
+  std::vector<T> add(3 * n, T(0));
+  const T k = -relax / (w + w + alpha);
+  for (int e = 0; e + stride < n; ++e) {
+    const T* x1 = &tp_in[3 * e];
+    const T* x2 = &tp_in[3 * (e + stride)];
+    T d[3] = {x1[0] - x2[0], x1[1] - x2[1], x1[2] - x2[2]};
+    T L = std::sqrt(dot3(d, d) + T(1e-10));
+    // dp = k (L - len) / L d, applied +w at e and -w at e + stride
+    T dpb[3];
+    for (int c = 0; c < 3; ++c) dpb[c] = w * (tpb[3 * e + c] - tpb[3 * (e + stride) + c]);
+    T a = k * (L - len) / L;
+    T dd = dot3(d, dpb);
+    T bcoef = k * len / (L * L * L) * dd;
+    for (int c = 0; c < 3; ++c) {
+      T db = a * dpb[c] + bcoef * d[c];
+      add[3 * e + c] += db;
+      add[3 * (e + stride) + c] -= db;
+    }
+  }
+  for (int i = 0; i < 3 * n; ++i) tpb[i] += add[i];
+}
+
+// adjoint of rope_fwd (order of cable_straightening.py:177-186: rope.update.grad, clamp_grid, then
+// collision.grad).  The forward has been recomputed (io.ext, io.cidx hold its values); exb are the
+// sensors' external-force adjoints; vmb / posb the sensors' velmid / position adjoints (accumulated).
+template <typename T>
+void rope_bwd(const orc_scene* sc, const orc_rope& R, orc_rope_io& io, T* const* pos, T* const* vel_mid,
+              const std::vector<std::vector<T>>& exb, std::vector<std::vector<T>>& vmb, T* const* posb, T clip) {
+  const int n = R.n, NS = sc->n_sensors;
+  const T dt = T(sc->dt);
+  const Consts<T> K = rope_consts<T>(sc, R);
+  const T* rp = static_cast<const T*>(io.pos);
+  const T* rv = static_cast<const T*>(io.vel);
+  const T* re = static_cast<const T*>(io.ext);
+  const T* pb1 = static_cast<const T*>(io.posb1);
+  const T* vb1 = static_cast<const T*>(io.velb1);
+  const T* tb1 = static_cast<const T*>(io.travb1);
+  T* rpb = static_cast<T*>(io.posb);
+  T* rvb = static_cast<T*>(io.velb);
+  T* rtb = static_cast<T*>(io.travb);
+  const T w = T(1) / T(R.mass);
+  std::vector<T> tp0, tp1;
+  std::vector<unsigned char> fl;
+  rope_integrate(R, dt, rp, rv, re, tp0, fl);
+  tp1 = tp0;
+  rope_pass(tp1, n, 1, T(R.rest), T(R.alpha_s), T(R.relax_s), w);
+  // vel1 = (pos1 - pos) / dt; pos1[0] = pin, pos1[i] = tp2[i]
+  std::vector<T> tpb(3 * n, T(0));
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) {
+      const int q = 3 * i + c;
+      T p1b = pb1[q] + vb1[q] / dt;
+      rpb[q] = -vb1[q] / dt;
+      tpb[q] = i == 0 ? T(0) : p1b;
+    }
+  rope_pass_bwd(tp1, tpb, n, 2, T(R.bend), T(R.alpha_b), T(R.relax_b), w);
+  rope_pass_bwd(tp0, tpb, n, 1, T(R.rest), T(R.alpha_s), T(R.relax_s), w);
+  std::vector<T> reb(3 * n);
+  for (int i = 0; i < n; ++i) {
+    T nvb[3];
+    for (int c = 0; c < 3; ++c) {
+      rpb[3 * i + c] += tpb[3 * i + c];
+      nvb[c] = tpb[3 * i + c] * dt;
+    }
+    if (fl[i]) {
+      nvb[0] *= T(R.friction);
+      nvb[1] = T(0);
+      nvb[2] *= T(R.friction);
+    }
+    for (int c = 0; c < 3; ++c) {
+      rvb[3 * i + c] = nvb[c];
+      reb[3 * i + c] = nvb[c] / T(R.mass);
+    }
+  }
+  // clamp_grid on the rope's frame-f grads (cable_straightening.py:196-199)
+  for (int q = 0; q < 3 * n; ++q) {
+    rpb[q] = clampg(rpb[q], clip);
+    rvb[q] = clampg(rvb[q], clip);
+  }
+  // collision.grad (argmin held constant)
+  for (int p = 0; p < n; ++p) {
+    bool any = false;
+    for (int s = 0; s < NS; ++s) {
+      const orc_sensor& S = sc->sensors[s];
+      const int kk = io.cidx[p * NS + s];
+      if (kk < 0) continue;
+      SdfOut<T> so = find_sdf(S, pos[s], vel_mid[s], kk, rp + 3 * p, rv + 3 * p, T(R.rad));
+      if (!so.flag) continue;
+      any = true;
+      const int* t = S.tris + 3 * kk;
+      T eb[3];
+      for (int c = 0; c < 3; ++c)
+        eb[c] = dt * reb[3 * p + c] - K.third * ((exb[s][3 * t[0] + c] + exb[s][3 * t[1] + c]) + exb[s][3 * t[2] + c]);
+      T nb[3] = {T(0), T(0), T(0)}, rb[3] = {T(0), T(0), T(0)};
+      T sdfb = contact_force_bwd(K, so.sdf, so.nrm, so.rel, eb, nb, rb);
+      for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) vmb[s][3 * t[a] + c] += K.third * rb[c];
+      for (int c = 0; c < 3; ++c) {
+        rvb[3 * p + c] -= rb[c];
+        rpb[3 * p + c] += sdfb * so.nrm[c];
+      }
+      tri_geom_bwd(S, pos[s], kk, rp + 3 * p, so, sdfb, nb, posb[s]);
+    }
+    rtb[p] = any ? T(0) : tb1[p];
+  }
 }
 
 template <typename T>
@@ -915,6 +1205,10 @@ static int substep_bwd_impl(const orc_scene* sc, const T* x, const T* v, const T
         vmb[s][q] = clampg(vmb[s][q], clip);
       }
   }
+
+  // ---- PBD ropes: update.grad, clamp_grid, collision.grad ----
+  for (int r = 0; r < sc->n_ropes; ++r)
+    rope_bwd<T>(sc, sc->ropes[r], sc->rope_io[r], pos_p.data(), vel_p.data(), exb, vmb, posb, clip);
 
   // ---- g2p.grad ----
   std::vector<T> gvb(3 * nn, T(0));

@@ -26,6 +26,19 @@ class OrcSensor(C.Structure):
                 ("lam", C.c_double), ("out_dir", C.c_double * 3), ("carry", C.c_int), ("pad_", C.c_int)]
 
 
+class OrcRope(C.Structure):
+    _fields_ = [("n", C.c_int), ("pad_", C.c_int), ("mass", C.c_double), ("rad", C.c_double),
+                ("rest", C.c_double), ("bend", C.c_double), ("alpha_s", C.c_double), ("alpha_b", C.c_double),
+                ("relax_s", C.c_double), ("relax_b", C.c_double), ("table_h", C.c_double), ("friction", C.c_double),
+                ("grav", C.c_double * 3), ("pin", C.c_double * 3),
+                ("kn", C.c_double), ("kd", C.c_double), ("kt", C.c_double), ("mu_t", C.c_double)]
+
+
+class OrcRopeIO(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("pos", "vel", "trav", "pos1", "vel1", "trav1", "ext", "cidx", "posb1",
+                                          "velb1", "travb1", "posb", "velb", "travb")]
+
+
 class OrcScene(C.Structure):
     _fields_ = [("n_particles", C.c_int), ("n", C.c_int * 3), ("bound", C.c_int), ("bc", C.c_int),
                 ("dx", C.c_double), ("inv_dx", C.c_double), ("p_vol", C.c_double), ("p_mass", C.c_double),
@@ -34,7 +47,8 @@ class OrcScene(C.Structure):
                 ("n_materials", C.c_int), ("n_sensors", C.c_int),
                 ("mat_mu", C.c_void_p), ("mat_lam", C.c_void_p), ("mat_yield", C.c_void_p), ("mat_model", C.c_void_p),
                 ("p_mat", C.c_void_p), ("sensors", C.c_void_p), ("svd_sweeps", C.c_int), ("n_threads", C.c_int),
-                ("grad_clip", C.c_double)]
+                ("grad_clip", C.c_double), ("n_ropes", C.c_int), ("pad2_", C.c_int), ("ropes", C.c_void_p),
+                ("rope_io", C.c_void_p)]
 
 
 def lib():
@@ -117,6 +131,25 @@ class Oracle:
         sc.svd_sweeps = svd_sweeps if svd_sweeps is not None else (4 if self.dtype == np.float32 else 12)
         sc.n_threads = n_threads
         sc.grad_clip = grad_clip
+        ropes = list(getattr(env, "ropes", []))
+        rr = (OrcRope * max(len(ropes), 1))()
+        for i, rp in enumerate(ropes):
+            r = rr[i]
+            r.n = rp.n
+            r.mass, r.rad, r.rest, r.bend = rp.mass, rp.rad, rp.rest, rp.bend
+            cs, cb = rp.compliance
+            r.alpha_s, r.alpha_b = cs / self.dt ** 2, cb / self.dt ** 2
+            r.relax_s, r.relax_b = rp.stretch_relax, rp.bend_relax
+            r.table_h, r.friction = rp.table_h, rp.friction
+            r.grav[:] = list(rp.gravity)
+            r.pin[:] = [float(c) for c in rp.init_positions()[0]]
+            r.kn, r.kd, r.kt, r.mu_t = rp.kn, rp.kd, rp.kt, rp.mu_t
+        self.rope_io = (OrcRopeIO * max(len(ropes), 1))()
+        self.keep += [rr, self.rope_io]
+        sc.n_ropes = len(ropes)
+        sc.ropes = C.cast(rr, C.c_void_p)
+        sc.rope_io = C.cast(self.rope_io, C.c_void_p)
+        self.ropes = ropes
         self.sc = sc
         self.fn = lib().orc_substep_f32 if self.dtype == np.float32 else lib().orc_substep_f64
         self.fn.restype = C.c_int
@@ -130,7 +163,30 @@ class Oracle:
         st["pos"] = [np.array(sp.verts, T) for sp in e.sensors]
         st["vel"] = [np.zeros((len(sp.verts), 3), T) for sp in e.sensors]
         st["vpos"] = [np.array(sp.verts, T) for sp in e.sensors]
+        st["rpos"] = [np.array(rp.init_positions(), T) for rp in self.ropes]
+        st["rvel"] = [np.zeros((rp.n, 3), T) if rp.v is None else np.array(rp.v, T) for rp in self.ropes]
+        st["rtrav"] = [np.zeros(rp.n, T) for rp in self.ropes]
         return st
+
+    def _rope_io(self, st, c, adj1=None):
+        """Fill the per-rope io structs; returns the arrays (kept alive by the caller)."""
+        T = self.dtype
+        NS = len(self.env.sensors)
+        arrs = []
+        for i, rp in enumerate(self.ropes):
+            a = {"pos": c(st["rpos"][i]), "vel": c(st["rvel"][i]), "trav": c(st["rtrav"][i]),
+                 "pos1": np.zeros((rp.n, 3), T), "vel1": np.zeros((rp.n, 3), T), "trav1": np.zeros(rp.n, T),
+                 "ext": np.zeros((rp.n, 3), T), "cidx": np.full((rp.n, max(NS, 1)), -1, np.int32)}
+            if adj1 is not None:
+                a["posb1"] = c(adj1.get("rpos", [np.zeros((rp.n, 3))] * len(self.ropes))[i])
+                a["velb1"] = c(adj1.get("rvel", [np.zeros((rp.n, 3))] * len(self.ropes))[i])
+                a["travb1"] = c(adj1.get("rtrav", [np.zeros(rp.n)] * len(self.ropes))[i])
+                a["posb"], a["velb"], a["travb"] = np.zeros((rp.n, 3), T), np.zeros((rp.n, 3), T), np.zeros(rp.n, T)
+            io = self.rope_io[i]
+            for k, v in a.items():
+                setattr(io, k, v.ctypes.data)
+            arrs.append(a)
+        return arrs
 
     def substep(self, st, cv=None, cv1=None):
         """One substep.  ``cv``/``cv1``: per-sensor control velocities of frames f and f+1 (default 0).
@@ -159,13 +215,17 @@ class Oracle:
         gvo = np.zeros((n0, n1, n2, 3), T)
         gf = np.zeros((n0, n1, n2, 3), T)
         cidx = np.full((n0, n1, n2, max(NS, 1)), -1, np.int32)
+        rio = self._rope_io(st, c)
         err = self.fn(C.byref(self.sc), _ptr(x), _ptr(v), _ptr(Cm), _ptr(F), _ptr(out["x"]), _ptr(out["v"]),
                       _ptr(out["C"]), _ptr(out["F"]), _ptr_array(pos), _ptr_array(vel), _ptr_array(vpos),
                       _ptr_array(cv), _ptr_array(cv1), _ptr_array(pos1), _ptr_array(vel1), _ptr_array(vpos1),
                       _ptr_array(ext), _ptr(gm), _ptr(gvi), _ptr(gvo), _ptr(gf), _ptr(cidx))
         out["pos"], out["vel"], out["vpos"] = pos1, vel1, vpos1
+        out["rpos"] = [a["pos1"] for a in rio]
+        out["rvel"] = [a["vel1"] for a in rio]
+        out["rtrav"] = [a["trav1"] for a in rio]
         dbg = {"grid_m": gm, "grid_v_in": gvi, "grid_v_out": gvo, "grid_f": gf, "cidx": cidx, "vel_mid": vel,
-               "ext": ext, "err": err}
+               "ext": ext, "err": err, "rope_ext": [a["ext"] for a in rio], "rope_cidx": [a["cidx"] for a in rio]}
         return out, dbg
 
     def substep_bwd(self, st, adj1, cv=None, cv1=None, svd_grad_mode=0):
@@ -193,12 +253,16 @@ class Oracle:
         for k in ("pos", "vel", "vpos", "cv", "cv1"):
             out[k] = [np.zeros_like(z) for z in zeros_v]
         out["mat"] = np.zeros((len(e.materials), 2), T)
+        rio = self._rope_io(st, c, adj1)
         fn = lib().orc_substep_bwd_f32 if T == np.float32 else lib().orc_substep_bwd_f64
         fn(C.byref(self.sc), _ptr(x), _ptr(v), _ptr(Cm), _ptr(F), _ptr_array(pos), _ptr_array(vel), _ptr_array(vpos),
            _ptr_array(cv), _ptr_array(cv1), _ptr(a1["x"]), _ptr(a1["v"]), _ptr(a1["C"]), _ptr(a1["F"]),
            _ptr_array(a1["pos"]), _ptr_array(a1["vel"]), _ptr_array(a1["vpos"]), _ptr(out["x"]), _ptr(out["v"]),
            _ptr(out["C"]), _ptr(out["F"]), _ptr_array(out["pos"]), _ptr_array(out["vel"]), _ptr_array(out["vpos"]),
            _ptr_array(out["cv"]), _ptr_array(out["cv1"]), _ptr(out["mat"]), svd_grad_mode)
+        out["rpos"] = [a["posb"] for a in rio]
+        out["rvel"] = [a["velb"] for a in rio]
+        out["rtrav"] = [a["travb"] for a in rio]
         return out
 
 

@@ -79,3 +79,21 @@ def dome_over_box(n=40, seed=5):
                       nu=0.43, out_dir=tuple(M[:3, :3] @ np.array([0.0, 1.0, 0.0])), trans_world=M)
     return S.EnvSpec(x=x, materials=[S.Material(5e3, 0.3)], n_grid=(n, n, n), dx=dx, rho=1000.0, sensors=[sp],
                      kn=1e4, kd=100.0, kt=100.0, mu_t=1.0)
+
+
+def rope_under_pad(n_rope=16, rad=0.01, seed=9, pad=(6, 6, 2), press=0.3, table=True):
+    """A PBD rope lying along x on the table (y = 0) with a hex pad above it whose contact surface
+    is ``press`` radii into the rope's contact band (no MPM particles)."""
+    from difftactile_gb300 import scene as S_
+    rng = np.random.default_rng(seed)
+    rest = 1.6 * rad
+    x0 = 0.5 - rest * (n_rope - 1) / 2
+    pts = np.stack([x0 + rest * np.arange(n_rope), np.full(n_rope, rad), np.full(n_rope, 0.5)], 1)
+    pts[1:] += 0.1 * rad * rng.standard_normal((n_rope - 1, 3))
+    rope = S_.RopeSpec(n=n_rope, rad=rad, rho=1000.0, rest_length=rest, pos=tuple(pts[0]), ori=(1.0, 0.0, 0.0),
+                       table_h=0.0 if table else -1.0, x=pts.astype(np.float32), kn=1e4, kd=10.0, kt=10.0, mu_t=0.5)
+    h = 0.012
+    surf_y = 2 * rad - press * rad
+    sp = S_.hex_pad_sensor([0.5 + 0.13 * h, surf_y, 0.5 - 0.21 * h], nx=pad[0], nz=pad[1], ny=pad[2], h=h)
+    return S_.EnvSpec(x=np.zeros((0, 3), np.float32), materials=[S_.Material(5e3, 0.3)], n_grid=(16, 16, 16),
+                      dx=1.0 / 16, rho=1000.0, sensors=[sp], ropes=[rope])
