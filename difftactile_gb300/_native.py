@@ -41,6 +41,10 @@ class DtRope(C.Structure):
                 ("pin", C.c_float * 3), ("kn", C.c_float), ("kd", C.c_float), ("kt", C.c_float), ("mu_t", C.c_float)]
 
 
+class DtFisheye(C.Structure):
+    _fields_ = [("f", C.c_float), ("m", C.c_float), ("cx", C.c_float), ("cy", C.c_float), ("plane", C.c_float)]
+
+
 class DtMaterial(C.Structure):
     _fields_ = [("mu", C.c_float), ("lam", C.c_float), ("yield_stress", C.c_float), ("model", C.c_int)]
 
@@ -99,6 +103,11 @@ SIGNATURES = {
     "dt_com_bwd": (C.c_int, [_W, C.c_int, _P, _P]),
     "dt_pose_control_vel": (C.c_int, [_W, C.c_int, _P, C.c_float, C.c_int, C.c_int, _P]),
     "dt_pose_control_vel_bwd": (C.c_int, [_W, C.c_int, _P, C.c_float, _P, C.c_int, C.c_int, _P]),
+    "dt_contact_force": (C.c_int, [_W, C.c_int, C.c_int, _P, _P]),
+    "dt_contact_force_bwd": (C.c_int, [_W, C.c_int, _P, _P]),
+    "dt_markers": (C.c_int, [_W, C.c_int, C.c_int, _P, _P, _P, C.c_int, C.c_int, _P, DtFisheye, _P, _P, _P]),
+    "dt_markers_bwd": (C.c_int, [_W, C.c_int, C.c_int, _P, _P, _P, C.c_int, C.c_int, _P, DtFisheye, _P, _P, _P,
+                                 _P]),
     "dt_marker_loss": (C.c_int, [_W, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
     "dt_marker_loss_bwd": (C.c_int, [_W, C.c_int, C.c_int, C.c_int, _P, C.c_float, _P]),
 }

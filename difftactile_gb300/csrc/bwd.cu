@@ -199,7 +199,11 @@ __device__ void integrate_bwd(const dt_world& w, int f, int i) {
   reinterpret_cast<float4*>(w.v_adj_pos)[cb * V + i] = v3to4(posb);
   reinterpret_cast<float4*>(w.v_adj_vpos)[cb * V + i] = v3to4(vpb1);
   reinterpret_cast<float4*>(w.v_adj_velmid)[i] = v3to4(vmb);
-  reinterpret_cast<float4*>(w.v_adj_ext)[i] = v3to4(exb);
+  // v_adj_ext accumulates: a readout of frame f's contact forces may have seeded it (it is reset
+  // after its last use in stage 3)
+  float4* ae = reinterpret_cast<float4*>(w.v_adj_ext) + i;
+  const float4 ae0 = *ae;
+  *ae = make_float4(ae0.x + exb.x, ae0.y + exb.y, ae0.z + exb.z, 0.f);
   *cvb_f = v3to4(cvb);
   if (S.carry) *cvb_n = v3to4(cvbn);
 }
@@ -629,9 +633,11 @@ __global__ void __launch_bounds__(NT, 4) k_bwd_p2g_fem(dt_world w, int f, int nb
   b -= nb_t;
   if (b < nb_v) {
     const int i = b * NT + threadIdx.x;
-    if (i < w.n_verts)
+    if (i < w.n_verts) {
       reinterpret_cast<float4*>(w.v_adj_vel)[(size_t)(f & 1) * w.n_verts + i] =
           reinterpret_cast<const float4*>(w.v_adj_velmid)[i];
+      reinterpret_cast<float4*>(w.v_adj_ext)[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // zero between substeps
+    }
   }
 }
 

@@ -5,6 +5,12 @@
 //   marker loss    surface-node displacement field (pos - virtual pos) against a target field,
 //                  the tactile readout of the press task (cf. compute_marker_motion /
 //                  compute_marker_loss, grasp_plastic.py:241-256)
+//   contact force  compute_contact_force, grasp_plastic.py:218-229: sum over the surface triangles of
+//                  1/6 of the contact force on each of its three vertices
+//   markers        extract_markers, fem_sensor.py:161-187: surface nodes (current and virtual) into the
+//                  sensor frame (inv_trans_h), fisheye projection project_3d_2d
+//                  (sensor_model/fisheye_model.py:12-30), k-nearest inverse-distance interpolation to
+//                  the marker set
 #include "common.cuh"
 
 namespace {
@@ -111,9 +117,215 @@ __global__ void k_marker_loss_bwd(dt_world w, int s, int f, int layer, const flo
   *av = c;
 }
 
+// ---------------------------------------------------------------- contact force readout
+__global__ void k_contact_force(dt_world w, int s, int f, float* out) {
+  __shared__ float red[3][NT / 32];
+  const dt_sensor& S = w.sensors[s];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  v3 a = v3{0.f, 0.f, 0.f};
+  if (t < S.nf) {
+    const int4 tr = __ldg(reinterpret_cast<const int4*>(w.tris) + S.f_off + t);
+    const float4* E = vframe(w.v_ext, w, f);
+    const float k = 1.f / 6.f;
+    a = (k * f4to3(E[tr.x]) + k * f4to3(E[tr.y])) + k * f4to3(E[tr.z]);
+  }
+  float c[3] = {a.x, a.y, a.z};
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c[k] += __shfl_xor_sync(0xffffffffu, c[k], o);
+    if (lane == 0) red[k][wid] = c[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    float x = 0.f;
+    for (int k = 0; k < NT / 32; ++k) x += red[threadIdx.x][k];
+    atomicAdd(out + threadIdx.x, x);
+  }
+}
+
+__global__ void k_contact_force_bwd(dt_world w, int s, const float* __restrict__ gb) {
+  const dt_sensor& S = w.sensors[s];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.nf) return;
+  const int4 tr = __ldg(reinterpret_cast<const int4*>(w.tris) + S.f_off + t);
+  const float k = 1.f / 6.f;
+  const float4 g = make_float4(k * gb[0], k * gb[1], k * gb[2], 0.f);
+  float4* ae = reinterpret_cast<float4*>(w.v_adj_ext);
+  red_add_v4(ae + tr.x, g);
+  red_add_v4(ae + tr.y, g);
+  red_add_v4(ae + tr.z, g);
+}
+
+// ---------------------------------------------------------------- markers
+struct Proj {
+  float2 p;
+  // intermediates for the adjoint
+  v3 a;
+  float an, c, craw, om, r;
+};
+
+// project_3d_2d (fisheye_model.py:12-30): equidistant fisheye r = m f theta around the optical axis z
+DT_DEV Proj fisheye(v3 a, const dt_fisheye& cam) {
+  Proj o;
+  a.z += cam.plane;
+  o.a = a;
+  o.an = sqrtf(dot(a, a) + 1e-10f);
+  o.craw = a.z / o.an;
+  o.c = fmaxf(-1.f, fminf(1.f, o.craw));
+  const float th = acosf(o.c);
+  o.om = atan2f(a.y, a.x + 1e-8f) + 3.14159265358979f;
+  o.r = cam.m * cam.f * th;
+  o.p = make_float2(o.r * cosf(o.om) + cam.cx, o.r * sinf(o.om) + cam.cy);
+  return o;
+}
+
+// adjoint of fisheye: d/da (the plane shift has unit derivative)
+DT_DEV v3 fisheye_bwd(const Proj& o, const dt_fisheye& cam, float2 pb) {
+  const float co = cosf(o.om), so = sinf(o.om);
+  const float rb = pb.x * co + pb.y * so;
+  const float omb = -pb.x * o.r * so + pb.y * o.r * co;
+  const float thb = cam.m * cam.f * rb;
+  // acos'(c) = -1 / sqrt(1 - c^2); no derivative where the cosine was clamped
+  const float cb = (o.craw > -1.f && o.craw < 1.f) ? -thb / sqrtf(fmaxf(1.f - o.c * o.c, 1e-30f)) : 0.f;
+  const float X = o.a.x + 1e-8f, Y = o.a.y;
+  const float den = X * X + Y * Y;
+  v3 ab = v3{den > 0.f ? -omb * Y / den : 0.f, den > 0.f ? omb * X / den : 0.f, 0.f};
+  // c = a.z / an, an = sqrt(|a|^2 + 1e-10)
+  ab.z += cb / o.an;
+  const float anb = -cb * o.a.z / (o.an * o.an);
+  ab = ab + (anb / o.an) * o.a;
+  return ab;
+}
+
+// sensor-frame camera coordinates of world point x: inv_trans_h rows 0..2 applied to (x, 1), then
+// (x, z, y) (fem_sensor.py:168-172)
+DT_DEV v3 cam_coords(const float* M, v3 x) {
+  const float ix = M[0] * x.x + M[1] * x.y + M[2] * x.z + M[3];
+  const float iy = M[4] * x.x + M[5] * x.y + M[6] * x.z + M[7];
+  const float iz = M[8] * x.x + M[9] * x.y + M[10] * x.z + M[11];
+  return v3{ix, iz, iy};
+}
+
+__global__ void k_markers(dt_world w, int s, int f, const int* __restrict__ surf, const int* __restrict__ idx,
+                          const float* __restrict__ wts, int K, int M, const float* __restrict__ Mi, dt_fisheye cam,
+                          float2* pred, float2* virt) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  const dt_sensor& S = w.sensors[s];
+  const float4* P = vframe(w.v_pos, w, f);
+  const float4* VP = vframe(w.v_vpos, w, f);
+  float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+  for (int k = 0; k < K; ++k) {
+    const int v = S.v_off + __ldg(surf + __ldg(idx + m * K + k));
+    const float wk = __ldg(wts + m * K + k);
+    const Proj pp = fisheye(cam_coords(Mi, f4to3(P[v])), cam);
+    const Proj pv = fisheye(cam_coords(Mi, f4to3(VP[v])), cam);
+    a.x += wk * pp.p.x;
+    a.y += wk * pp.p.y;
+    b.x += wk * pv.p.x;
+    b.y += wk * pv.p.y;
+  }
+  pred[m] = a;
+  virt[m] = b;
+}
+
+__global__ void k_markers_bwd(dt_world w, int s, int f, const int* __restrict__ surf, const int* __restrict__ idx,
+                              const float* __restrict__ wts, int K, int M, const float* __restrict__ Mi,
+                              dt_fisheye cam, const float2* __restrict__ pred_b, const float2* __restrict__ virt_b,
+                              float* Mi_b) {
+  __shared__ float red[12][NT / 32];
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  float g[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) g[k] = 0.f;
+  if (m < M) {
+    const dt_sensor& S = w.sensors[s];
+    const size_t V = (size_t)w.n_verts, cb = (size_t)(f & 1);
+    const float4* P = vframe(w.v_pos, w, f);
+    const float4* VP = vframe(w.v_vpos, w, f);
+    float4* aP = reinterpret_cast<float4*>(w.v_adj_pos) + cb * V;
+    float4* aVP = reinterpret_cast<float4*>(w.v_adj_vpos) + cb * V;
+    const float2 gp = pred_b ? pred_b[m] : make_float2(0.f, 0.f);
+    const float2 gv = virt_b ? virt_b[m] : make_float2(0.f, 0.f);
+    for (int k = 0; k < K; ++k) {
+      const int v = S.v_off + __ldg(surf + __ldg(idx + m * K + k));
+      const float wk = __ldg(wts + m * K + k);
+      for (int which = 0; which < 2; ++which) {
+        const float2 lb = which == 0 ? gp : gv;
+        if (lb.x == 0.f && lb.y == 0.f) continue;
+        const v3 x = f4to3(which == 0 ? P[v] : VP[v]);
+        const Proj pr = fisheye(cam_coords(Mi, x), cam);
+        const v3 ab = fisheye_bwd(pr, cam, make_float2(wk * lb.x, wk * lb.y));
+        // cam = (ix, iz, iy)
+        const float ib[3] = {ab.x, ab.z, ab.y};
+        const float hx[4] = {x.x, x.y, x.z, 1.f};
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) g[4 * r + c] += ib[r] * hx[c];
+        const v3 xb = v3{Mi[0] * ib[0] + Mi[4] * ib[1] + Mi[8] * ib[2], Mi[1] * ib[0] + Mi[5] * ib[1] + Mi[9] * ib[2],
+                         Mi[2] * ib[0] + Mi[6] * ib[1] + Mi[10] * ib[2]};
+        red_add_v4((which == 0 ? aP : aVP) + v, v3to4(xb));
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    float x = g[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[k][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 12 && Mi_b) {
+    float x = 0.f;
+    for (int k = 0; k < NT / 32; ++k) x += red[threadIdx.x][k];
+    atomicAdd(Mi_b + threadIdx.x, x);
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+int dt_contact_force(const dt_world* w, int s, int f, float* out, cudaStream_t stream) {
+  if (!w || !out || s < 0 || s >= w->n_sensors || f < 0 || f >= w->n_frames) return DT_ERR_ARG;
+  k_contact_force<<<cdiv(w->max_sensor_tris > 0 ? w->max_sensor_tris : 1, NT), NT, 0, stream>>>(*w, s, f, out);
+  return launched();
+}
+
+int dt_contact_force_bwd(const dt_world* w, int s, const float* out_b, cudaStream_t stream) {
+  if (!w || !out_b || s < 0 || s >= w->n_sensors) return DT_ERR_ARG;
+  k_contact_force_bwd<<<cdiv(w->max_sensor_tris > 0 ? w->max_sensor_tris : 1, NT), NT, 0, stream>>>(*w, s, out_b);
+  return launched();
+}
+
+int dt_markers(const dt_world* w, int s, int f, const int* surf, const int* idx, const float* wts, int K, int M,
+               const float* inv_trans, dt_fisheye cam, float* pred, float* virt, cudaStream_t stream) {
+  if (!w || !surf || !idx || !wts || !inv_trans || !pred || !virt || K < 1 || M < 0 || s < 0 ||
+      s >= w->n_sensors || f < 0 || f >= w->n_frames)
+    return DT_ERR_ARG;
+  if (M == 0) return DT_OK;
+  k_markers<<<cdiv(M, NT), NT, 0, stream>>>(*w, s, f, surf, idx, wts, K, M, inv_trans, cam,
+                                            reinterpret_cast<float2*>(pred), reinterpret_cast<float2*>(virt));
+  return launched();
+}
+
+int dt_markers_bwd(const dt_world* w, int s, int f, const int* surf, const int* idx, const float* wts, int K, int M,
+                   const float* inv_trans, dt_fisheye cam, const float* pred_b, const float* virt_b,
+                   float* inv_trans_b, cudaStream_t stream) {
+  if (!w || !surf || !idx || !wts || !inv_trans || K < 1 || M < 0 || s < 0 || s >= w->n_sensors || f < 0 ||
+      f >= w->n_frames)
+    return DT_ERR_ARG;
+  if (M == 0) return DT_OK;
+  k_markers_bwd<<<cdiv(M, NT), NT, 0, stream>>>(*w, s, f, surf, idx, wts, K, M, inv_trans, cam,
+                                                reinterpret_cast<const float2*>(pred_b),
+                                                reinterpret_cast<const float2*>(virt_b), inv_trans_b);
+  return launched();
+}
 
 int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, int f0, int nfr,
                         cudaStream_t stream) {

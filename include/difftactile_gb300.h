@@ -172,7 +172,8 @@ typedef struct dt_world {
   float* v_adj_vel;              /* [2][n_verts][4] */
   float* v_adj_vpos;             /* [2][n_verts][4] */
   float* v_adj_velmid;           /* [n_verts][4] */
-  float* v_adj_ext;              /* [n_verts][4] */
+  float* v_adj_ext;              /* [n_verts][4] contact-force adjoint of the frame in the backward sweep;
+                                    zero between backward substeps (see dt_contact_force_bwd) */
   float* v_adj_cv;               /* [n_frames][n_verts][4] */
   float* mat_adj;                /* [n_materials][4] (d/dmu, d/dlam, 0, 0) accumulated */
   int* err;                      /* [4] device error word */
@@ -312,6 +313,35 @@ int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, 
  * boundary frame: call it after the adjoint substeps of frames [f0, f0 + nfr - 1). */
 int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv_T, float* Ab_bar, int f0, int nfr,
                             cudaStream_t stream);
+
+/* ---- contact-force readout (compute_contact_force, grasp_plastic.py:218-229) ----
+ * out[0..2] (device, accumulated) += sum over sensor s's surface triangles of 1/6 of the contact
+ * force v_ext[f] on each of the triangle's vertices. */
+int dt_contact_force(const dt_world* w, int s, int f, float* out, cudaStream_t stream);
+/* Adjoint: v_adj_ext += out_b[0..2] / 6 on each surface triangle's vertices.  v_adj_ext is the
+ * adjoint of the contact forces of the frame whose backward substep runs next: call it for frame f
+ * after dt_substep_bwd(f + 1) and before dt_substep_bwd(f). */
+int dt_contact_force_bwd(const dt_world* w, int s, const float* out_b, cudaStream_t stream);
+
+/* ---- marker readout (extract_markers, fem_sensor.py:161-187) ----
+ * Fisheye camera of project_3d_2d (sensor_model/fisheye_model.py:12-30): the point is shifted by
+ * `plane` along the optical axis z, theta = acos(z / |a|), omega = atan2(y, x + 1e-8) + pi,
+ * pixel = m f theta (cos omega, sin omega) + (cx, cy).  The reference's defaults are
+ * f = 8.627e-4, m = 173913.04, cx = 332, cy = 240, plane = 0.02. */
+typedef struct dt_fisheye {
+  float f, m, cx, cy, plane;
+} dt_fisheye;
+/* For marker m: pred[m] = sum_k wts[m K + k] proj(node), virt[m] the same of the virtual positions,
+ * node = surf[idx[m K + k]] (local vertex ids of sensor s), proj = fisheye of (x, z, y) of
+ * inv_trans (rows 0..2 of the 4x4 world-to-sensor transform, 12 device floats) applied to (p, 1).
+ * pred, virt: [M][2] device. */
+int dt_markers(const dt_world* w, int s, int f, const int* surf, const int* idx, const float* wts, int K, int M,
+               const float* inv_trans, dt_fisheye cam, float* pred, float* virt, cudaStream_t stream);
+/* Adjoint: v_adj_pos[f&1] and v_adj_vpos[f&1] += the position adjoints of pred_b, virt_b ([M][2]
+ * device, either may be NULL); inv_trans_b[12] (device, may be NULL) += d/d inv_trans. */
+int dt_markers_bwd(const dt_world* w, int s, int f, const int* surf, const int* idx, const float* wts, int K, int M,
+                   const float* inv_trans, dt_fisheye cam, const float* pred_b, const float* virt_b,
+                   float* inv_trans_b, cudaStream_t stream);
 
 /* ---- tactile readout: marker-displacement loss (cf. grasp_plastic.py:241-256) ----
  * loss[0] (device) += sum over vertices i of sensor s with layer id `layer` of
