@@ -117,6 +117,60 @@ __global__ void k_marker_loss_bwd(dt_world w, int s, int f, int layer, const flo
   *av = c;
 }
 
+// ---------------------------------------------------------------- affine control velocity
+// gripper fingers (fem_sensor1/2_set_control_vel, gripper_kinematics.py:196-216): per frame
+// f0 + k, cv = D_k[:, 0:3] src + D_k[:, 3] with D_k = rows 0..2 of (F_{f+1} - F_f) T0^-1 / dt
+__global__ void k_affine_cv(dt_world w, int s, const float* __restrict__ D, const float4* __restrict__ src, int f0,
+                            int nfr) {
+  const dt_sensor& S = w.sensors[s];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= S.nv) return;
+  const int v = S.v_off + i;
+  const v3 p = f4to3(src[v]);
+  for (int k = 0; k < nfr; ++k) {
+    const float* A = D + 12 * k;
+    const v3 c = v3{A[0] * p.x + A[1] * p.y + A[2] * p.z + A[3], A[4] * p.x + A[5] * p.y + A[6] * p.z + A[7],
+                    A[8] * p.x + A[9] * p.y + A[10] * p.z + A[11]};
+    vframe(w.v_cv, w, f0 + k)[v] = v3to4(c);
+  }
+}
+
+// D_b[k] += sum_i cvb_i(f0 + k) [src_i, 1]^T; the control-velocity adjoint is consumed
+__global__ void k_affine_cv_bwd(dt_world w, int s, const float4* __restrict__ src, int f0, int nfr, float* Db) {
+  __shared__ float red[12][NT / 32];
+  const dt_sensor& S = w.sensors[s];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v3 p = v3{0.f, 0.f, 0.f};
+  if (i < S.nv) p = f4to3(src[S.v_off + i]);
+  for (int k = 0; k < nfr; ++k) {
+    v3 cb = v3{0.f, 0.f, 0.f};
+    if (i < S.nv) {
+      float4* c = vframe(w.v_adj_cv, w, f0 + k) + S.v_off + i;
+      cb = f4to3(*c);
+      *c = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const float pr[4] = {p.x, p.y, p.z, 1.f};
+    const float cr[3] = {cb.x, cb.y, cb.z};
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        float x = cr[r] * pr[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[4 * r + c][wid] = x;
+      }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+      float x = 0.f;
+      for (int q = 0; q < NT / 32; ++q) x += red[threadIdx.x][q];
+      atomicAdd(Db + 12 * k + threadIdx.x, x);
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------- contact force readout
 __global__ void k_contact_force(dt_world w, int s, int f, float* out) {
   __shared__ float red[3][NT / 32];
@@ -290,6 +344,22 @@ __global__ void k_markers_bwd(dt_world w, int s, int f, const int* __restrict__ 
 }  // namespace
 
 extern "C" {
+
+int dt_affine_control_vel(const dt_world* w, int s, const float* D, const float* src, int f0, int nfr,
+                          cudaStream_t stream) {
+  if (!w || !D || !src || s < 0 || s >= w->n_sensors || f0 < 0 || nfr < 1 || f0 + nfr > w->n_frames) return DT_ERR_ARG;
+  k_affine_cv<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, s, D, reinterpret_cast<const float4*>(src), f0, nfr);
+  return launched();
+}
+
+int dt_affine_control_vel_bwd(const dt_world* w, int s, const float* src, int f0, int nfr, float* D_b,
+                              cudaStream_t stream) {
+  if (!w || !D_b || !src || s < 0 || s >= w->n_sensors || f0 < 0 || nfr < 1 || f0 + nfr > w->n_frames)
+    return DT_ERR_ARG;
+  k_affine_cv_bwd<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, s, reinterpret_cast<const float4*>(src), f0, nfr,
+                                                           D_b);
+  return launched();
+}
 
 int dt_contact_force(const dt_world* w, int s, int f, float* out, cudaStream_t stream) {
   if (!w || !out || s < 0 || s >= w->n_sensors || f < 0 || f >= w->n_frames) return DT_ERR_ARG;

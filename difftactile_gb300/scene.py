@@ -245,6 +245,21 @@ def hex_pad_sensor(center_bottom, nx=20, nz=20, ny=5, h=0.0125, rho=1000.0, E=1.
                       out_dir=tuple(out_dir), trans_world=M)
 
 
+def finger_pad_sensor(pose, nx=6, nz=6, ny=2, h=1.0 / 32, rho=1000.0, E=1.5e5, nu=0.45, shift=(0.0, 0.0)):
+    """Hex pad on a gripper finger (gripper_fem.py's sensor placed by init(matrix)): in the finger's
+    frame the pad is centred in x and z with its contact surface at y = 0 facing +y (towards the
+    other finger); ``pose`` is the finger's 4x4 pose, ``shift`` moves the pad within its surface
+    (local x, z).  Velocity carry of gripper_fem.py:415."""
+    pose = np.asarray(pose, np.float64)
+    v, tets, tris, layer = hex_pad_local(nx, nz, ny, h)
+    v = v - np.array([nx * h / 2 - shift[0], ny * h, nz * h / 2 - shift[1]])
+    world = (pose[:3, :3] @ v.T).T + pose[:3, 3]
+    out_dir = pose[:3, :3] @ np.array([0.0, 1.0, 0.0])
+    vol = (nx * h) * (nz * h) * (ny * h)
+    return SensorSpec(verts=world.astype(np.float32), tets=tets, tris=tris, layer=layer, mass=rho * vol / len(v), E=E,
+                      nu=nu, out_dir=tuple(out_dir), trans_world=pose, carry=1)
+
+
 def fibonacci_hemisphere(samples, scale=1.0):
     """Points evenly spread on a hemisphere (fem_sensor.py:280-291)."""
     phi = np.pi * (np.sqrt(5.0) - 1.0)

@@ -8,11 +8,17 @@ object_model/mpm_elastic.py:300-320, sensor_model/fem_sensor.py:501-521) and rec
 substeps of one step during the backward sweep (tasks/grasp_plastic.py:594-648); that is k = 1.
 Here the checkpoints stay in HBM and k is a parameter; k = 0 keeps the whole tape.
 
-Actions are per step and per pose-controlled sensor: (d_pos[3], d_ori[3]) as in
-set_pose_control (fem_sensor.py:229-245): rot_v = d_ori dt S, trans_v = d_pos dt S, the step
-transform dtrans_h = T_world eul2mat(rot_v, trans_v) T_world^-1 drives the base layer through the
-control velocity (fem_sensor.py:259-266).  The 4x4 algebra runs in float64 torch on the device;
-the per-vertex control velocities and everything after them are CUDA kernels.
+Two action models drive the sensors' base layers through per-vertex control velocities:
+  PoseTrajectory     per step and pose-controlled sensor (d_pos[3], d_ori[3]) as in set_pose_control
+                     (fem_sensor.py:229-245): rot_v = d_ori dt S, trans_v = d_pos dt S, the step
+                     transform dtrans_h = T_world eul2mat(rot_v, trans_v) T_world^-1 and the control
+                     velocity (fem_sensor.py:259-266);
+  GripperTrajectory  per step (d_pos[3], d_ori[3], d_gripper) of a parallel-jaw gripper whose two
+                     fingers carry sensors (gripper_kinematics.py:120-216): per-substep finger poses
+                     and control velocities, the sensors' velocities reset to them at every step start
+                     (set_sensor_vel).
+The 4x4 algebra runs in float64 torch on the device with autograd; the per-vertex control
+velocities and everything after them are CUDA kernels with hand-written adjoints.
 """
 from __future__ import annotations
 
@@ -39,8 +45,9 @@ def eul2mat_zyx(rot_deg: torch.Tensor, trans: torch.Tensor) -> torch.Tensor:
     return torch.cat([top, bottom], -2)
 
 
-class PoseTrajectory:
-    """T control steps x S substeps of a World whose sensors are pose-controlled.
+class Trajectory:
+    """T control steps x S substeps of a World whose sensors are driven by actions (subclasses
+    define the action model through controls / _apply / _apply_bwd).
 
     ``ckpt_every`` = k >= 1: the world holds one control step (n_frames = S + 1); the forward keeps
     the start state of every k-th step and the backward recomputes.  ``ckpt_every`` = 0 (full tape):
@@ -68,27 +75,23 @@ class PoseTrajectory:
             self.n_ck = (self.T + self.k - 1) // self.k
         self.f_end = self.T * self.S if self.full else self.S  # frame holding the final state
         dev = world.device
-        Np, V = world.n_particles, world.n_verts
+        Np, V, NR = world.n_particles, world.n_verts, world.n_rope_particles
         if not self.full:
             self.ck_p = torch.zeros((self.n_ck, 6, Np, 4), device=dev)
             self.ck_v = torch.zeros((self.n_ck, 3, V, 4), device=dev)
+            self.ck_r = torch.zeros((self.n_ck, 2, NR, 4), device=dev)
         if not self.full and self.k > 1:
             self.seg_p = torch.zeros((self.k, 6, Np, 4), device=dev)
             self.seg_v = torch.zeros((self.k, 3, V, 4), device=dev)
-        self.inv_T = 1.0 / (world.dt * self.S)
-        self.TW, self.TW_inv = [], []
-        for sp in world.sensor_specs:
-            M = sp.trans_world if sp.trans_world is not None else np.eye(4)
-            self.TW.append(torch.as_tensor(M, dtype=torch.float64, device=dev))
-            self.TW_inv.append(torch.as_tensor(np.linalg.inv(M), dtype=torch.float64, device=dev))
+            self.seg_r = torch.zeros((self.k, 2, NR, 4), device=dev)
         self.loss_terms = []
         for s, layer, target in loss_terms:
             tg = torch.zeros((world.sensor_rows[s].nv, 4), device=dev)
             tg[:, :3] = torch.as_tensor(np.asarray(target), dtype=torch.float32, device=dev)
             self.loss_terms.append((s, int(layer), tg))
         self.loss = torch.zeros(1, device=dev)
-        self.Ab = None
-        self.Ab_bar = None
+        self.ctrl = None
+        self.ctrl_bar = None
         self.launches = 0
 
     @staticmethod
@@ -96,32 +99,35 @@ class PoseTrajectory:
         """World n_frames for a trajectory of ``n_steps`` x ``substeps`` with ``ckpt_every``."""
         return n_steps * substeps + 1 if ckpt_every == 0 else substeps + 1
 
+    # ------------------------------------------------------------------ action model (subclasses)
+    def controls(self, actions: torch.Tensor) -> torch.Tensor:
+        """actions (float64, differentiable) -> per-step control tensor [T, ...] (float64)."""
+        raise NotImplementedError
+
+    def _apply(self, t: int, f0: int):
+        """Launch the control velocities of step t, whose first frame is f0."""
+        raise NotImplementedError
+
+    def _apply_bwd(self, t: int, f0: int):
+        """Adjoint of _apply: accumulate into self.ctrl_bar[t] (after the step's adjoint substeps)."""
+        raise NotImplementedError
+
     # ------------------------------------------------------------------ state save / load
-    def _save(self, P, Vv, i):
+    def _save(self, P, Vv, Rr, i):
         t = self.w.t
         P[i].copy_(t["p_state"][0])
         Vv[i, 0].copy_(t["v_pos"][0])
         Vv[i, 1].copy_(t["v_vel"][0])
         Vv[i, 2].copy_(t["v_vpos"][0])
+        Rr[i].copy_(t["r_state"][0])
 
-    def _load(self, P, Vv, i):
+    def _load(self, P, Vv, Rr, i):
         t = self.w.t
         t["p_state"][0].copy_(P[i])
         t["v_pos"][0].copy_(Vv[i, 0])
         t["v_vel"][0].copy_(Vv[i, 1])
         t["v_vpos"][0].copy_(Vv[i, 2])
-
-    # ------------------------------------------------------------------ actions
-    def step_transforms(self, actions: torch.Tensor) -> torch.Tensor:
-        """actions [T, n_sensors, 6] (float64) -> Ab [T, n_sensors, 12] (float64, differentiable)."""
-        S = self.S
-        out = []
-        for s in range(self.w.n_sensors):
-            a = actions[:, s]
-            M = eul2mat_zyx(a[:, 3:6] * self.w.dt * S, a[:, 0:3] * self.w.dt * S)
-            D = self.TW[s] @ M @ self.TW_inv[s]
-            out.append(D[:, :3, :].reshape(-1, 12))
-        return torch.stack(out, 1)
+        t["r_state"][0].copy_(Rr[i])
 
     # ------------------------------------------------------------------ one control step
     def _f0(self, t):
@@ -129,12 +135,8 @@ class PoseTrajectory:
 
     def _step(self, t, copy_end=True):
         w = self.w
-        st = w.stream
         f0 = self._f0(t)
-        for s in range(w.n_sensors):
-            N.check(w.lib.dt_pose_control_vel(w.wp, s, self.Ab32[t, s].data_ptr(), self.inv_T, f0, self.S + 1, st),
-                    "pose cv")
-        self.launches += w.n_sensors
+        self._apply(t, f0)
         if not self.full:
             w.step_begin()
             self.launches += 1
@@ -147,14 +149,14 @@ class PoseTrajectory:
     def forward(self, actions: torch.Tensor) -> torch.Tensor:
         """Roll out; returns the final-frame loss (device scalar)."""
         self.actions = actions.detach().double().requires_grad_(True)
-        self.Ab = self.step_transforms(self.actions)
-        self.Ab32 = self.Ab.detach().float().contiguous()
+        self.ctrl = self.controls(self.actions)
+        self.ctrl32 = self.ctrl.detach().float().contiguous()
         if self.full:
             self.w.step_begin()
             self.launches += 1
         for t in range(self.T):
             if not self.full and t % self.k == 0:
-                self._save(self.ck_p, self.ck_v, t // self.k)
+                self._save(self.ck_p, self.ck_v, self.ck_r, t // self.k)
             self._step(t)
         return self.readout()
 
@@ -172,14 +174,11 @@ class PoseTrajectory:
         f0 = self._f0(t)
         for f in reversed(range(f0, f0 + self.S)):
             w.substep_bwd(f)
-        for s in range(w.n_sensors):
-            N.check(w.lib.dt_pose_control_vel_bwd(w.wp, s, self.Ab32[t, s].data_ptr(), self.inv_T,
-                                                  self.Ab_bar[t, s].data_ptr(), f0, self.S + 1, w.stream),
-                    "pose cv bwd")
-        self.launches += 4 * self.S + w.n_sensors
+        self.launches += 4 * self.S
+        self._apply_bwd(t, f0)
 
     def backward(self, loss_bar: float = 1.0) -> torch.Tensor:
-        """Adjoint sweep; returns d loss / d actions [T, n_sensors, 6] (float64).  Initial-state
+        """Adjoint sweep; returns d loss / d actions (float64, the actions' shape).  Initial-state
         adjoints are left in the world's frame-0 adjoint buffers, material grads in mat_adj."""
         w = self.w
         st = w.stream
@@ -187,25 +186,210 @@ class PoseTrajectory:
         for s, layer, tg in self.loss_terms:
             N.check(w.lib.dt_marker_loss_bwd(w.wp, s, self.f_end, layer, tg.data_ptr(), float(loss_bar), st),
                     "loss bwd")
-        self.Ab_bar = torch.zeros_like(self.Ab32)
+        self.ctrl_bar = torch.zeros_like(self.ctrl32)
         if self.full:
             for t in reversed(range(self.T)):
                 self._step_bwd(t)
         for seg in reversed(range(self.n_ck)):
             t0, t1 = seg * self.k, min((seg + 1) * self.k, self.T)
-            self._load(self.ck_p, self.ck_v, seg)
+            self._load(self.ck_p, self.ck_v, self.ck_r, seg)
             if self.k > 1:
                 for t in range(t0, t1):
-                    self._save(self.seg_p, self.seg_v, t - t0)
+                    self._save(self.seg_p, self.seg_v, self.seg_r, t - t0)
                     if t + 1 < t1:
                         self._step(t)
             for t in reversed(range(t0, t1)):
                 if self.k > 1:
-                    self._load(self.seg_p, self.seg_v, t - t0)
+                    self._load(self.seg_p, self.seg_v, self.seg_r, t - t0)
                 self._step(t, copy_end=False)
                 self._step_bwd(t)
                 if self.S & 1:  # frame 0's adjoint (buffer 0) is frame S's of the previous step (buffer 1)
-                    for name in ("p_adj", "v_adj_pos", "v_adj_vel", "v_adj_vpos"):
+                    for name in ("p_adj", "v_adj_pos", "v_adj_vel", "v_adj_vpos", "r_adj"):
                         w.t[name][1].copy_(w.t[name][0])
-        (g,) = torch.autograd.grad(self.Ab, self.actions, self.Ab_bar.double())
+        (g,) = torch.autograd.grad(self.ctrl, self.actions, self.ctrl_bar.double())
         return g
+
+
+class PoseTrajectory(Trajectory):
+    """Pose-controlled sensors (dome sensor, set_pose_control / set_control_vel): actions
+    [T, n_sensors, 6] = (d_pos[3], d_ori[3] in degrees per unit time)."""
+
+    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=()):
+        super().__init__(world, n_steps, ckpt_every, loss_terms)
+        dev = world.device
+        self.inv_T = 1.0 / (world.dt * self.S)
+        self.TW, self.TW_inv = [], []
+        for sp in world.sensor_specs:
+            M = sp.trans_world if sp.trans_world is not None else np.eye(4)
+            self.TW.append(torch.as_tensor(M, dtype=torch.float64, device=dev))
+            self.TW_inv.append(torch.as_tensor(np.linalg.inv(M), dtype=torch.float64, device=dev))
+
+    def step_transforms(self, actions: torch.Tensor) -> torch.Tensor:
+        """actions [T, n_sensors, 6] (float64) -> Ab [T, n_sensors, 12] (float64, differentiable)."""
+        S = self.S
+        out = []
+        for s in range(self.w.n_sensors):
+            a = actions[:, s]
+            M = eul2mat_zyx(a[:, 3:6] * self.w.dt * S, a[:, 0:3] * self.w.dt * S)
+            D = self.TW[s] @ M @ self.TW_inv[s]
+            out.append(D[:, :3, :].reshape(-1, 12))
+        return torch.stack(out, 1)
+
+    controls = step_transforms
+
+    def _apply(self, t, f0):
+        w = self.w
+        for s in range(w.n_sensors):
+            N.check(w.lib.dt_pose_control_vel(w.wp, s, self.ctrl32[t, s].data_ptr(), self.inv_T, f0, self.S + 1,
+                                              w.stream), "pose cv")
+        self.launches += w.n_sensors
+
+    def _apply_bwd(self, t, f0):
+        w = self.w
+        for s in range(w.n_sensors):
+            N.check(w.lib.dt_pose_control_vel_bwd(w.wp, s, self.ctrl32[t, s].data_ptr(), self.inv_T,
+                                                  self.ctrl_bar[t, s].data_ptr(), f0, self.S + 1, w.stream),
+                    "pose cv bwd")
+        self.launches += w.n_sensors
+
+    # names kept for callers of the earlier interface
+    @property
+    def Ab(self):
+        return self.ctrl
+
+    @property
+    def Ab32(self):
+        return self.ctrl32
+
+    @property
+    def Ab_bar(self):
+        return self.ctrl_bar
+
+
+class GripperTrajectory(Trajectory):
+    """Two finger sensors of a parallel-jaw gripper (Gripper, gripper_kinematics.py:68-296): actions
+    [T, 7] = (d_pos[3], d_ori[3] in degrees per unit time, d_gripper).  ``kin`` is a
+    GripperKinematics; ``fingers`` the two sensors' indices in the world."""
+
+    def __init__(self, world: World, n_steps: int, kin, fingers=(0, 1), ckpt_every: int = 1, loss_terms=()):
+        super().__init__(world, n_steps, ckpt_every, loss_terms)
+        self.kin = kin
+        self.fingers = tuple(fingers)
+        dev = world.device
+        rest = torch.zeros((world.n_verts, 4), dtype=torch.float32, device=dev)
+        rest[:, :3] = torch.as_tensor(world.rest_verts, device=dev)
+        self.rest = rest
+        self.T0_inv = [torch.linalg.inv(F.cpu()).to(dev) for F in kin.finger_poses0()]
+        self.zero_cv = torch.zeros((1, 4), device=dev)
+
+    def controls(self, actions: torch.Tensor) -> torch.Tensor:
+        """actions [T, 7] -> D [T, 2, S, 12]: rows 0..2 of (F_{f+1} - F_f) T0^-1 / dt per finger and
+        substep (fem_sensor1/2_set_control_vel, gripper_kinematics.py:196-216)."""
+        frames = self.kin.rollout(actions, self.S)  # [T, 2, S + 1, 4, 4]
+        dt = self.w.dt
+        out = []
+        for i in range(2):
+            Fi = frames[:, i]
+            D = (Fi[:, 1:] - Fi[:, :-1]) @ self.T0_inv[i].to(Fi.dtype) / dt
+            out.append(D[..., :3, :].reshape(self.T, self.S, 12))
+        return torch.stack(out, 1)
+
+    def _apply(self, t, f0):
+        w = self.w
+        for i, s in enumerate(self.fingers):
+            N.check(w.lib.dt_affine_control_vel(w.wp, s, self.ctrl32[t, i].data_ptr(), self.rest.data_ptr(), f0,
+                                                self.S, w.stream), "affine cv")
+            sl = w.vslice(s)
+            # frame f0 + S: the next step's first control velocity (written by its own _apply); zero
+            # at the end of the rollout, as the reference never sets control_vel[sub_steps - 1]
+            w.t["v_cv"][f0 + self.S, sl] = 0.0
+            # set_sensor_vel(0) (gripper_fem.py:194-196): the sensor starts the step at its control velocity
+            w.t["v_vel"][f0, sl] = w.t["v_cv"][f0, sl]
+            w.t["v_velmid"][f0, sl] = w.t["v_cv"][f0, sl]
+        self.launches += 2
+
+    def _apply_bwd(self, t, f0):
+        w = self.w
+        b = f0 & 1
+        for i, s in enumerate(self.fingers):
+            sl = w.vslice(s)
+            # adjoint of set_sensor_vel: the velocity that was overwritten gets none
+            w.t["v_adj_cv"][f0, sl] += w.t["v_adj_vel"][b, sl]
+            w.t["v_adj_vel"][b, sl] = 0.0
+            w.t["v_adj_cv"][f0 + self.S, sl] = 0.0
+            N.check(w.lib.dt_affine_control_vel_bwd(w.wp, s, self.rest.data_ptr(), f0, self.S,
+                                                    self.ctrl_bar[t, i].data_ptr(), w.stream), "affine cv bwd")
+        self.launches += 2
+
+
+# ---------------------------------------------------------------------------------------------
+# gripper kinematics
+# ---------------------------------------------------------------------------------------------
+def eul2mat_xyz(rot_deg: torch.Tensor, trans: torch.Tensor) -> torch.Tensor:
+    """4x4 transforms with R = Rx Ry Rz (the gripper's eul2mat, gripper_kinematics.py:280-296)."""
+    r = torch.deg2rad(rot_deg)
+    cx, cy, cz = torch.cos(r[..., 0]), torch.cos(r[..., 1]), torch.cos(r[..., 2])
+    sx, sy, sz = torch.sin(r[..., 0]), torch.sin(r[..., 1]), torch.sin(r[..., 2])
+    o, z = torch.ones_like(cx), torch.zeros_like(cx)
+    Rx = torch.stack([o, z, z, z, cx, -sx, z, sx, cx], -1).reshape(*cx.shape, 3, 3)
+    Ry = torch.stack([cy, z, sy, z, o, z, -sy, z, cy], -1).reshape(*cx.shape, 3, 3)
+    Rz = torch.stack([cz, -sz, z, sz, cz, z, z, z, o], -1).reshape(*cx.shape, 3, 3)
+    R = Rx @ Ry @ Rz
+    top = torch.cat([R, trans[..., :, None]], -1)
+    bottom = torch.zeros(*cx.shape, 1, 4, dtype=R.dtype, device=R.device)
+    bottom[..., 0, 3] = 1
+    return torch.cat([top, bottom], -2)
+
+
+class GripperKinematics:
+    """Kinematic chain of the parallel-jaw gripper (Gripper.init_params / pos_transformation /
+    grip_kinematic, gripper_kinematics.py:120-194), in float64 torch with autograd.
+
+    The end effector sits at ee_world = eul2mat(rot, trans); finger i's pose is
+    ee ee_to_finger_i finger_local_i with ee_to_finger_1 = eul2mat((-90, 0, -90),
+    (-base_width/2 + grip_width, -base_height - finger_height, 0)) and ee_to_finger_2 =
+    eul2mat((-90, 0, 90), (base_width/2 - grip_width, ...)).  Per substep the end effector moves by
+    eul2mat(d_ori dt, d_pos dt) in its own frame and each finger by (0, d_gripper dt, 0) in its own."""
+
+    def __init__(self, rot, trans, grip_width, dt, base_height=2.0, base_width=14.0, finger_height=7.5,
+                 device="cpu"):
+        self.dt = float(dt)
+        self.dev = torch.device(device)
+        f64 = dict(dtype=torch.float64, device=self.dev)
+        self.ee_world = eul2mat_xyz(torch.as_tensor(rot, **f64), torch.as_tensor(trans, **f64))
+        bw, bh, fh, gw = base_width, base_height, finger_height, grip_width
+        self.e2f = [eul2mat_xyz(torch.tensor([-90.0, 0.0, -90.0], **f64),
+                                torch.tensor([-bw / 2 + gw, -bh - fh, 0.0], **f64)),
+                    eul2mat_xyz(torch.tensor([-90.0, 0.0, 90.0], **f64),
+                                torch.tensor([bw / 2 - gw, -bh - fh, 0.0], **f64))]
+
+    def finger_poses0(self):
+        """Finger poses at the start (the sensors are placed with them: init_fem_sensor)."""
+        return [self.ee_world @ e for e in self.e2f]
+
+    def rollout(self, actions: torch.Tensor, S: int) -> torch.Tensor:
+        """actions [T, 7] -> finger poses [T, 2, S + 1, 4, 4] of every step's frames 0..S (frame 0 of
+        step t is frame S of step t - 1)."""
+        T = actions.shape[0]
+        dt = self.dt
+        eye = torch.eye(4, dtype=torch.float64, device=actions.device)
+        ee_world = self.ee_world.to(actions.device)
+        e2f = [e.to(actions.device) for e in self.e2f]
+        ee_local, fl = eye, [eye, eye]
+        F = [ee_world @ e2f[0], ee_world @ e2f[1]]
+        out = []
+        for t in range(T):
+            a = actions[t]
+            E = eul2mat_xyz(a[3:6] * dt, a[0:3] * dt)
+            z = torch.zeros_like(a[6])
+            G = eul2mat_xyz(torch.stack([z, z, z]), torch.stack([z, a[6] * dt, z]))
+            frames = [[F[0]], [F[1]]]
+            for _ in range(S):
+                ee_local = E @ ee_local
+                ee = ee_world @ ee_local
+                for i in range(2):
+                    fl[i] = G @ fl[i]
+                    F[i] = ee @ e2f[i] @ fl[i]
+                    frames[i].append(F[i])
+            out.append(torch.stack([torch.stack(frames[0]), torch.stack(frames[1])]))
+        return torch.stack(out)

@@ -314,6 +314,17 @@ int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, 
 int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv_T, float* Ab_bar, int f0, int nfr,
                             cudaStream_t stream);
 
+/* ---- action input: gripper fingers (gripper_kinematics.py:196-216, fem_sensor1/2_set_control_vel) ----
+ * For k < nfr: v_cv[f0 + k][i] = D[k][:, 0:3] src_i + D[k][:, 3] for every vertex i of sensor s, with
+ * D [nfr][12] (device, row-major 3x4 per frame) and src [n_verts][4] (device) the points the
+ * transforms act on (the sensors' rest positions, with T0^-1 folded into D). */
+int dt_affine_control_vel(const dt_world* w, int s, const float* D, const float* src, int f0, int nfr,
+                          cudaStream_t stream);
+/* Adjoint: D_b[k] += sum_i v_adj_cv[f0 + k][i] [src_i, 1]^T (device, accumulated); the consumed
+ * entries of v_adj_cv are reset to zero. */
+int dt_affine_control_vel_bwd(const dt_world* w, int s, const float* src, int f0, int nfr, float* D_b,
+                              cudaStream_t stream);
+
 /* ---- contact-force readout (compute_contact_force, grasp_plastic.py:218-229) ----
  * out[0..2] (device, accumulated) += sum over sensor s's surface triangles of 1/6 of the contact
  * force v_ext[f] on each of the triangle's vertices. */

@@ -97,3 +97,21 @@ def rope_under_pad(n_rope=16, rad=0.01, seed=9, pad=(6, 6, 2), press=0.3, table=
     sp = S_.hex_pad_sensor([0.5 + 0.13 * h, surf_y, 0.5 - 0.21 * h], nx=pad[0], nz=pad[1], ny=pad[2], h=h)
     return S_.EnvSpec(x=np.zeros((0, 3), np.float32), materials=[S_.Material(5e3, 0.3)], n_grid=(16, 16, 16),
                       dx=1.0 / 16, rho=1000.0, sensors=[sp], ropes=[rope])
+
+
+def gripper_box(n=32, seed=11, grip_width=0.075):
+    """A box held between the two finger pads of a parallel-jaw gripper (end effector at
+    (0.5, 0.5, 0.5), fingers 0.3 apart minus twice the grip width); the pads start 0.1 cell inside
+    the box's faces.  Returns (env, kinematics)."""
+    from difftactile_gb300.trajectory import GripperKinematics
+    dx = 1.0 / n
+    kin = GripperKinematics([0.0, 0.0, 0.0], [0.5, 0.5, 0.5], grip_width, 1e-4, base_height=0.02, base_width=0.3,
+                            finger_height=0.1)
+    F = [f.numpy() for f in kin.finger_poses0()]
+    lo = np.array([0.5 - 2.5 * dx, 0.33, 0.5 - 2.5 * dx])
+    x = S.box_particles(lo, lo + np.array([5, 4, 5]) * dx, dx, 8, seed)
+    # pads shifted off the node planes: node centres must not project onto the quads' diagonals
+    pads = [S.finger_pad_sensor(Fi, nx=6, nz=6, ny=2, h=dx, shift=(0.13 * dx, -0.21 * dx)) for Fi in F]
+    env = S.EnvSpec(x=x, materials=[S.Material(5e3, 0.3, 5.0, S.MODEL_VON_MISES)], n_grid=(n, n, n), dx=dx,
+                    rho=1000.0, sensors=pads, kn=1e4, kd=100.0, kt=100.0, mu_t=1.0, gravity=(0.0, 0.0, 0.0))
+    return env, kin
