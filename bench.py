@@ -36,6 +36,8 @@ def parse():
     ap.add_argument("--horizon", type=int, default=None, help="control steps (default: the config's)")
     ap.add_argument("--scatter", default=None, choices=["tile", "global", "warp"],
                     help="27-node scatter strategy (default: the library's)")
+    ap.add_argument("--no-pdl", action="store_true", help="launch the substep kernels without programmatic "
+                    "dependent launch")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -131,6 +133,7 @@ def run_ours(args):
     cfg = make_config(args.config, args.horizon)
     kw = {} if args.scatter is None else {"scatter_mode": {"tile": 0, "global": 1, "warp": 2}[args.scatter]}
     w, traj = cfg.build(dev, **kw)
+    w.lib.dt_set_pdl(0 if args.no_pdl else 1)
     acts = torch.as_tensor(cfg.actions, dtype=torch.float64, device=dev)
     t = w.t
     init = [t["p_state"][0].clone(), t["v_pos"][0].clone(), t["v_vel"][0].clone(), t["v_vpos"][0].clone()]
@@ -215,6 +218,7 @@ def run_ours(args):
                       "fem_tets": w.n_tets, "fem_nodes": w.n_verts, "surface_tris": w.n_tris,
                       "checkpoint_every": cfg.ckpt_every, "tape_blocks": w.tape_blocks,
                       "scatter": ["tile", "global", "warp"][w.w.scatter_mode],
+                      "programmatic_dependent_launch": not args.no_pdl,
                       "active_blocks_mean": cnt, "active_blocks_max": cnt_max, "l2": "flushed between timed iterations (256 MiB write)",
                       "parallelism": f"replicas x{world_size}"},
            "gpu_launches": launches_per_iter * args.steps,

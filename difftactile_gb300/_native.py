@@ -84,6 +84,7 @@ SIGNATURES = {
     "dt_sizeof_sensor": (C.c_size_t, []),
     "dt_sizeof_material": (C.c_size_t, []),
     "dt_sizeof_rope": (C.c_size_t, []),
+    "dt_set_pdl": (C.c_int, [C.c_int]),
     "dt_step_begin": (C.c_int, [_W, _P]),
     "dt_substep_fwd": (C.c_int, [_W, C.c_int, _P]),
     "dt_substep_fwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),

@@ -74,6 +74,12 @@ size_t dt_sizeof_sensor(void) { return sizeof(dt_sensor); }
 size_t dt_sizeof_material(void) { return sizeof(dt_material); }
 size_t dt_sizeof_rope(void) { return sizeof(dt_rope); }
 
+int dt_set_pdl(int on) {
+  const int old = pdl_flag();
+  pdl_flag() = on ? 1 : 0;
+  return old;
+}
+
 int dt_step_begin(const dt_world* w, cudaStream_t stream) {
   if (!w || w->n_frames < 2) return DT_ERR_ARG;
   int n = w->n_frames > w->n_verts ? w->n_frames : w->n_verts;

@@ -62,6 +62,7 @@ DT_DEV m3 svd_grad(const m3& U, v3 s, const m3& V, const m3& Ub_in, v3 sb, const
 // B0
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(GRID_NT) k_bwd_restore(dt_world w, int f) {
+  pdl_entry();
   const int cnt = min(w.tape_bcount[f], w.tape_blocks);
   const int l = threadIdx.x;
   for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
@@ -210,6 +211,7 @@ __device__ void integrate_bwd(const dt_world& w, int f, int i) {
 
 template <int MODE>
 __global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
+  pdl_entry();
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
@@ -228,6 +230,7 @@ __global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p,
 // B2: grid op + contact adjoint
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(GRID_NT) k_bwd_grid(dt_world w, int f) {
+  pdl_entry();
   const int cnt = min(w.tape_bcount[f], w.tape_blocks);
   const int l = threadIdx.x;
   const float third = 1.f / 3.f;
@@ -599,6 +602,7 @@ __device__ void fem_tet_bwd(const dt_world& w, int f, int t) {
 }
 
 __global__ void __launch_bounds__(NT, 4) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v) {
+  pdl_entry();
   int b = blockIdx.x;
   if (b < nb_p) {
     const int p = b * NT + threadIdx.x;
@@ -652,27 +656,29 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
   if (!w || f < 0 || f + 1 >= w->n_frames || stage < 0 || stage > 3) return DT_ERR_ARG;
   const int ng = w->n_blocks < 152 * 16 ? w->n_blocks : 152 * 16;
   const int nb_p = cdiv(w->n_particles, NT), nb_v = cdiv(w->n_verts, NT), nb_t = cdiv(w->n_tets, NT);
+  cudaError_t e = cudaSuccess;
   switch (stage) {
     case 0:
-      if (ng > 0) k_bwd_restore<<<ng, GRID_NT, 0, stream>>>(*w, f);
+      if (ng > 0) e = launch_k(k_bwd_restore, ng, GRID_NT, 0, stream, *w, f);
       break;
     case 1:
       if (nb_p + nb_v == 0) break;
       if (w->scatter_mode == DT_SCATTER_TILE)
-        k_bwd_g2p_fem<DT_SCATTER_TILE><<<nb_p + nb_v, NT, 25 * NT * sizeof(float), stream>>>(*w, f, nb_p, nb_v);
+        e = launch_k(k_bwd_g2p_fem<DT_SCATTER_TILE>, nb_p + nb_v, NT, 25 * NT * sizeof(float), stream, *w, f, nb_p,
+                     nb_v);
       else if (w->scatter_mode == DT_SCATTER_GLOBAL)
-        k_bwd_g2p_fem<DT_SCATTER_GLOBAL><<<nb_p + nb_v, NT, 0, stream>>>(*w, f, nb_p, nb_v);
+        e = launch_k(k_bwd_g2p_fem<DT_SCATTER_GLOBAL>, nb_p + nb_v, NT, 0, stream, *w, f, nb_p, nb_v);
       else
-        k_bwd_g2p_fem<DT_SCATTER_WARP><<<nb_p + nb_v, NT, 0, stream>>>(*w, f, nb_p, nb_v);
+        e = launch_k(k_bwd_g2p_fem<DT_SCATTER_WARP>, nb_p + nb_v, NT, 0, stream, *w, f, nb_p, nb_v);
       break;
     case 2:
-      if (ng > 0) k_bwd_grid<<<ng, GRID_NT, 0, stream>>>(*w, f);
-      if (launched() != DT_OK) return DT_ERR_LAUNCH;
+      if (ng > 0) e = launch_k(k_bwd_grid, ng, GRID_NT, 0, stream, *w, f);
+      if (e != cudaSuccess) return DT_ERR_LAUNCH;
       return dt_rope_update_bwd(w, f, stream);
     default:
-      if (nb_p + nb_t + nb_v) k_bwd_p2g_fem<<<nb_p + nb_t + nb_v, NT, 0, stream>>>(*w, f, nb_p, nb_t, nb_v);
+      if (nb_p + nb_t + nb_v) e = launch_k(k_bwd_p2g_fem, nb_p + nb_t + nb_v, NT, 0, stream, *w, f, nb_p, nb_t, nb_v);
   }
-  return launched();
+  return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
 
 int dt_substep_bwd(const dt_world* w, int f, cudaStream_t stream) {

@@ -287,6 +287,34 @@ DT_DEV void red_add_v4(float4* addr, float4 v) {
 DT_DEV float4 ldg4(const float4* p) { return __ldg(p); }
 DT_DEV void set_err(const dt_world& w, int bits) { atomicOr(w.err, bits); }
 
+// Programmatic dependent launch.  Kernels of the substep pipeline begin with pdl_entry(): wait
+// until the preceding kernel of the stream has completed and its writes are visible, then let the
+// next kernel be launched (its CTAs become resident and wait in their own pdl_entry), which hides
+// the launch latency between the short dependent kernels of a substep.  Launched without the
+// attribute (pdl_flag() == 0) the wait returns at once.
+DT_DEV void pdl_entry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+inline int& pdl_flag() {
+  static int on = 1;
+  return on;
+}
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_flag() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 // particle record access: plane k of frame f
 DT_DEV float4* pplane(const dt_world& w, int f, int k) {
   return reinterpret_cast<float4*>(w.p_state) + ((size_t)f * 6 + k) * (size_t)w.n_particles;

@@ -182,6 +182,7 @@ __device__ void tri_centroid(const dt_world& w, int f, int t) {
 
 template <int MODE>
 __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
+  pdl_entry();
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
@@ -210,6 +211,7 @@ __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p,
 // first-minimum-wins result.  Lane 0 of each node then does the contact force and the grid update.
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(GRID_NT, 2) k_fwd_grid(dt_world w, int f, int smem_cap) {
+  pdl_entry();
   extern __shared__ float4 scent[];
   float4* gbox = scent + smem_cap;  // 2 float4 per group of 32 centroids
   const int cnt = *((volatile int*)(w.tape_bcount + f));
@@ -374,6 +376,7 @@ __device__ void fem_integrate(const dt_world& w, int f, int i) {
 }
 
 __global__ void __launch_bounds__(NT) k_fwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
+  pdl_entry();
   int b = blockIdx.x;
   if (b < nb_p) {
     int p = b * NT + threadIdx.x;
@@ -401,17 +404,18 @@ int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   int nb_f = fem ? cdiv(w->n_tris, NT) : 0;
   int tot = nb_p + nb_t + nb_f;
   if (tot == 0) return DT_OK;
+  cudaError_t e;
   switch (w->scatter_mode) {
     case DT_SCATTER_TILE:
-      k_fwd_p2g_fem<DT_SCATTER_TILE><<<tot, NT, 25 * NT * sizeof(float), st>>>(*w, f, nb_p, nb_t, nb_f);
+      e = launch_k(k_fwd_p2g_fem<DT_SCATTER_TILE>, tot, NT, 25 * NT * sizeof(float), st, *w, f, nb_p, nb_t, nb_f);
       break;
     case DT_SCATTER_GLOBAL:
-      k_fwd_p2g_fem<DT_SCATTER_GLOBAL><<<tot, NT, 0, st>>>(*w, f, nb_p, nb_t, nb_f);
+      e = launch_k(k_fwd_p2g_fem<DT_SCATTER_GLOBAL>, tot, NT, 0, st, *w, f, nb_p, nb_t, nb_f);
       break;
     default:
-      k_fwd_p2g_fem<DT_SCATTER_WARP><<<tot, NT, 0, st>>>(*w, f, nb_p, nb_t, nb_f);
+      e = launch_k(k_fwd_p2g_fem<DT_SCATTER_WARP>, tot, NT, 0, st, *w, f, nb_p, nb_t, nb_f);
   }
-  return launched();
+  return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
 int launch_l2(const dt_world* w, int f, cudaStream_t st) {
   int nb = w->n_blocks < 152 * 8 ? w->n_blocks : 152 * 8;
@@ -424,15 +428,13 @@ int launch_l2(const dt_world* w, int f, cudaStream_t st) {
       return DT_ERR_LAUNCH;
     configured = smem;
   }
-  k_fwd_grid<<<nb, GRID_NT, smem, st>>>(*w, f, cap);
-  return launched();
+  return launch_k(k_fwd_grid, nb, GRID_NT, smem, st, *w, f, cap) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
 int launch_l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   int nb_p = parts ? cdiv(w->n_particles, NT) : 0;
   int nb_v = fem ? cdiv(w->n_verts, NT) : 0;
   if (nb_p + nb_v == 0) return DT_OK;
-  k_fwd_g2p_fem<<<nb_p + nb_v, NT, 0, st>>>(*w, f, nb_p, nb_v);
-  return launched();
+  return launch_k(k_fwd_g2p_fem, nb_p + nb_v, NT, 0, st, *w, f, nb_p, nb_v) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
 
 }  // namespace

@@ -54,6 +54,7 @@ DT_DEV int rope_of_particle(const dt_world& w, int p) {
 
 // ------------------------------------------------------------------------------- forward
 __global__ void __launch_bounds__(RC_NT) k_rope_contact(dt_world w, int f, int smem_cap) {
+  pdl_entry();
   extern __shared__ float4 scent[];
   float4* gbox = scent + smem_cap;
   const int r = rope_of_block(w, blockIdx.x);
@@ -138,6 +139,7 @@ DT_DEV void rope_pass(float4* tp, float4* cd, int n, int stride, float len, floa
 }
 
 __global__ void __launch_bounds__(RS_NT) k_rope_solve(dt_world w, int f) {
+  pdl_entry();
   extern __shared__ float4 sm[];
   const dt_rope& R = w.ropes[blockIdx.x];
   const int n = R.n;
@@ -188,6 +190,7 @@ DT_DEV void rope_pass_bwd(const float4* tp, float4* tpb, float4* cd, int n, int 
 }
 
 __global__ void __launch_bounds__(RS_NT) k_rope_solve_bwd(dt_world w, int f) {
+  pdl_entry();
   extern __shared__ float4 sm[];
   const dt_rope& R = w.ropes[blockIdx.x];
   const int n = R.n, M = w.max_rope_n;
@@ -231,6 +234,7 @@ __global__ void __launch_bounds__(RS_NT) k_rope_solve_bwd(dt_world w, int f) {
 
 // contact adjoint per rope particle (argmin from the tape); one thread per particle
 __global__ void __launch_bounds__(128) k_rope_contact_bwd(dt_world w, int f) {
+  pdl_entry();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= w.n_rope_particles) return;
   const float4 e = rext(w, f)[p];
@@ -311,9 +315,9 @@ int dt_rope_update(const dt_world* w, int f, cudaStream_t stream) {
   static size_t conf_c = 0, conf_s = 0;
   if ((rc = set_smem((const void*)k_rope_contact, smem, &conf_c))) return rc;
   if ((rc = set_smem((const void*)k_rope_solve, solve_smem, &conf_s))) return rc;
-  if (w->rope_blocks > 0) k_rope_contact<<<w->rope_blocks, RC_NT, smem, stream>>>(*w, f, cap);
-  k_rope_solve<<<w->n_ropes, RS_NT, solve_smem, stream>>>(*w, f);
-  return launched();
+  if (w->rope_blocks > 0 && launch_k(k_rope_contact, w->rope_blocks, RC_NT, smem, stream, *w, f, cap) != cudaSuccess)
+    return DT_ERR_LAUNCH;
+  return launch_k(k_rope_solve, w->n_ropes, RS_NT, solve_smem, stream, *w, f) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
 
 int dt_rope_update_bwd(const dt_world* w, int f, cudaStream_t stream) {
@@ -325,9 +329,10 @@ int dt_rope_update_bwd(const dt_world* w, int f, cudaStream_t stream) {
   static size_t conf = 0;
   int rc;
   if ((rc = set_smem((const void*)k_rope_solve_bwd, smem, &conf))) return rc;
-  k_rope_solve_bwd<<<w->n_ropes, RS_NT, smem, stream>>>(*w, f);
-  k_rope_contact_bwd<<<cdiv(w->n_rope_particles, 128), 128, 0, stream>>>(*w, f);
-  return launched();
+  if (launch_k(k_rope_solve_bwd, w->n_ropes, RS_NT, smem, stream, *w, f) != cudaSuccess) return DT_ERR_LAUNCH;
+  return launch_k(k_rope_contact_bwd, cdiv(w->n_rope_particles, 128), 128, 0, stream, *w, f) == cudaSuccess
+             ? DT_OK
+             : DT_ERR_LAUNCH;
 }
 
 }  // extern "C"

@@ -223,6 +223,11 @@ size_t dt_sizeof_sensor(void);
 size_t dt_sizeof_material(void);
 size_t dt_sizeof_rope(void);
 
+/* No counterpart in the reference.  Library-wide switch for programmatic dependent launch of the
+ * substep kernels (default on: each kernel waits for its predecessor's completion in-kernel, so the
+ * next launch overlaps the previous kernel's tail).  Returns the previous setting. */
+int dt_set_pdl(int on);
+
 /* ---- step set-up ----
  * Clears the grid tape counters of every frame and prepares FEM frame 0 (velmid = vel, ext = 0).
  * Call once before the substeps of a control step (the reference calls Contact.reset(),
