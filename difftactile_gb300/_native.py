@@ -99,6 +99,7 @@ SIGNATURES = {
     "dt_copy_frame": (C.c_int, [_W, C.c_int, C.c_int, _P]),
     "dt_substep_bwd": (C.c_int, [_W, C.c_int, _P]),
     "dt_substep_bwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),
+    "dt_substeps_bwd": (C.c_int, [_W, C.c_int, C.c_int, _P]),
     "dt_adj_clear": (C.c_int, [_W, _P]),
     "dt_com": (C.c_int, [_W, C.c_int, _P, _P]),
     "dt_com_bwd": (C.c_int, [_W, C.c_int, _P, _P]),

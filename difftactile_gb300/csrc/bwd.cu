@@ -61,17 +61,22 @@ DT_DEV m3 svd_grad(const m3& U, v3 s, const m3& V, const m3& Ub_in, v3 sb, const
 // ---------------------------------------------------------------------------------------------
 // B0
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(GRID_NT) k_bwd_restore(dt_world w, int f) {
-  pdl_entry();
+// grid velocities of frame f back from the tape: `per` blocks per CTA pass (64 threads each)
+DT_DEV void restore_blocks(const dt_world& w, int f, int cta, int ncta, int per) {
   const int cnt = min(w.tape_bcount[f], w.tape_blocks);
-  const int l = threadIdx.x;
-  for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
+  const int l = threadIdx.x & 63;
+  for (int e = cta * per + (threadIdx.x >> 6); e < cnt; e += ncta * per) {
     const int b = w.tape_blist[(size_t)f * w.n_blocks + e];
     const dt_env& E = w.envs[__ldg(w.blk_env + b)];
     const int g = E.node_off + ((b - E.blk_off) << 6) + l;
     reinterpret_cast<float4*>(w.g_vout)[g] =
         reinterpret_cast<const float4*>(w.tape_vout)[((size_t)f * w.tape_blocks + e) * 64 + l];
   }
+}
+
+__global__ void __launch_bounds__(GRID_NT) k_bwd_restore(dt_world w, int f) {
+  pdl_entry();
+  restore_blocks(w, f, blockIdx.x, gridDim.x, 1);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -601,7 +606,9 @@ __device__ void fem_tet_bwd(const dt_world& w, int f, int t) {
   red_add_v4(aPos + tv.w, v3to4(-((ab + bb) + cbv)));
 }
 
-__global__ void __launch_bounds__(NT, 4) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v) {
+// nb_r > 0: the last nb_r CTAs restore frame f - 1's grid velocities for the next backward substep
+// (only stage 1 reads g_vout, so this overlaps stage 3 of frame f)
+__global__ void __launch_bounds__(NT, 4) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v, int nb_r) {
   pdl_entry();
   int b = blockIdx.x;
   if (b < nb_p) {
@@ -642,7 +649,10 @@ __global__ void __launch_bounds__(NT, 4) k_bwd_p2g_fem(dt_world w, int f, int nb
           reinterpret_cast<const float4*>(w.v_adj_velmid)[i];
       reinterpret_cast<float4*>(w.v_adj_ext)[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // zero between substeps
     }
+    return;
   }
+  b -= nb_v;
+  if (b < nb_r) restore_blocks(w, f - 1, b, nb_r, NT / 64);
 }
 
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
@@ -676,9 +686,25 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
       if (e != cudaSuccess) return DT_ERR_LAUNCH;
       return dt_rope_update_bwd(w, f, stream);
     default:
-      if (nb_p + nb_t + nb_v) e = launch_k(k_bwd_p2g_fem, nb_p + nb_t + nb_v, NT, 0, stream, *w, f, nb_p, nb_t, nb_v);
+      if (nb_p + nb_t + nb_v)
+        e = launch_k(k_bwd_p2g_fem, nb_p + nb_t + nb_v, NT, 0, stream, *w, f, nb_p, nb_t, nb_v, 0);
   }
   return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
+}
+
+int dt_substeps_bwd(const dt_world* w, int f_hi, int f_lo, cudaStream_t stream) {
+  if (!w || f_lo < 0 || f_hi <= f_lo || f_hi >= w->n_frames) return DT_ERR_ARG;
+  const int nb_p = cdiv(w->n_particles, NT), nb_v = cdiv(w->n_verts, NT), nb_t = cdiv(w->n_tets, NT);
+  const int nb_r = w->n_blocks < 152 * 4 ? cdiv(w->n_blocks, NT / 64) : 152 * 4;
+  int rc = dt_substep_bwd_stage(w, f_hi - 1, 0, stream);
+  for (int f = f_hi - 1; f >= f_lo && !rc; --f) {
+    if ((rc = dt_substep_bwd_stage(w, f, 1, stream)) || (rc = dt_substep_bwd_stage(w, f, 2, stream))) break;
+    const int r = f > f_lo ? nb_r : 0;  // the next (lower) frame's restore rides along
+    if (nb_p + nb_t + nb_v + r &&
+        launch_k(k_bwd_p2g_fem, nb_p + nb_t + nb_v + r, NT, 0, stream, *w, f, nb_p, nb_t, nb_v, r) != cudaSuccess)
+      rc = DT_ERR_LAUNCH;
+  }
+  return rc;
 }
 
 int dt_substep_bwd(const dt_world* w, int f, cudaStream_t stream) {

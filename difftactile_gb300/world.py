@@ -454,6 +454,14 @@ class World:
         else:
             self.call("dt_substep_bwd", int(f))
 
+    def substeps_bwd(self, f_hi, f_lo):
+        """Adjoint substeps f_hi - 1 down to f_lo (dt_substeps_bwd: restores fused into stage 3)."""
+        if self.probe is not None and self.probe[0] == "bwd":
+            for f in reversed(range(f_lo, f_hi)):
+                self._staged("dt_substep_bwd_stage", f, 4, "bwd")
+        else:
+            N.check(self.lib.dt_substeps_bwd(self.wp, int(f_hi), int(f_lo), self.stream), "dt_substeps_bwd")
+
     def set_probe(self, kind=None, stage=None):
         self.probe = None if kind is None else (kind, int(stage))
         self.probe_events = []

@@ -297,6 +297,11 @@ int dt_substep_bwd(const dt_world* w, int f, cudaStream_t stream);
  * fem.update.grad + p2g.grad + svd_grad + compute_new_F.grad.  Run stages 0..3 in order. */
 int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t stream);
 
+/* dt_substep_bwd for f = f_hi - 1 down to f_lo in one call: the restore of frame f - 1 (stage 0) runs
+ * inside stage 3 of frame f, one launch fewer per substep.  Same results as the sequence of
+ * dt_substep_bwd calls. */
+int dt_substeps_bwd(const dt_world* w, int f_hi, int f_lo, cudaStream_t stream);
+
 /* Zero the adjoint buffers (p_adj, v_adj_*, mat_adj, g_adj_*, r_adj, r_extb) before a backward sweep. */
 int dt_adj_clear(const dt_world* w, cudaStream_t stream);
 

@@ -155,3 +155,33 @@ def test_adjoint_matches_oracle_adjoint(cuda_lib, model, ys):
     errs["mu"] = abs(g["mu"] - ref["mat"][0, 0]) / abs(ref["mat"][0, 0])
     errs["lam"] = abs(g["lam"] - ref["mat"][0, 1]) / abs(ref["mat"][0, 1])
     assert max(errs.values()) < 1e-3, errs
+
+
+def test_multi_substep_backward_equals_substep_sequence(cuda_lib):
+    """dt_substeps_bwd (restores fused into the previous stage 3) == dt_substep_bwd per substep, on
+    one forward tape; the bound is ten times the run-to-run spread of two unfused sweeps (atomic
+    accumulation order), at least 1e-6."""
+    env = SS.pad_over_box()
+    n_sub = 4
+    st0, cv = base_point(env, 5)
+    W = loss_weights(env, env.n_particles, 6)
+    w = World([env], n_frames=n_sub + 1, dt=DT, grad_clip=0.0)
+    w.set_particles(0, x=st0["x"], v=st0["v"], C=st0["C"], F=st0["F"])
+    w.set_control_velocity(0, cv[0])
+    w.step_begin()
+    for f in range(n_sub):
+        w.substep(f)
+    outs = []
+    for fused in (False, False, True):
+        w.adj_clear()
+        w.set_particle_adjoint(n_sub, x=W["x"], v=W["v"], C=W["C"], F=W["F"])
+        if fused:
+            w.substeps_bwd(n_sub, 0)
+        else:
+            for f in reversed(range(n_sub)):
+                w.substep_bwd(f)
+        torch.cuda.synchronize()
+        outs.append({k: v.double().cpu().numpy() for k, v in w.particle_adjoint(0).items()})
+    for k in ("x", "v", "C", "F"):
+        spread = SS.rel_err(outs[1][k], outs[0][k])
+        assert SS.rel_err(outs[2][k], outs[0][k]) <= max(10 * spread, 1e-6), (k, spread)
