@@ -109,6 +109,12 @@ NAMES = {("fwd", 0): "k_fwd_p2g_fem", ("fwd", 1): "k_fwd_grid", ("fwd", 2): "k_f
          ("bwd", 3): "k_bwd_p2g_fem"}
 
 
+# DRAM bytes (read + write) per launch from one ncu capture of the sensor-press workload
+# (profiles/kernels_sensor_press.md); per-launch sizes equal the full workload's
+NCU_TRAFFIC = {"sensor_press": {"k_fwd_p2g_fem": 7.876e6, "k_fwd_grid": 0.381e6, "k_bwd_p2g_fem": 12.259e6,
+                                "k_bwd_g2p_fem": 6.150e6}}
+
+
 def algo_bytes(key, units):
     return sum(b * units.get(u, 0) for u, b in BYTES[key].items())
 
@@ -223,7 +229,8 @@ def run_ours(args):
                       "parallelism": f"replicas x{world_size}"},
            "gpu_launches": launches_per_iter * args.steps,
            "roofline": {"kernel": NAMES[dom], "bound": "hbm", "achieved": achieved, "peak": peak,
-                        "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                        "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": NCU_TRAFFIC.get(cfg.name, {}).get(NAMES[dom]),
                         "algorithmic_bytes_per_launch": ab, "launch_ms": dom_ms, "launches_timed": dom_n},
            "kernel_breakdown": {NAMES[k]: {"ms_per_launch": v[0], "launches": v[1],
                                            "share": v[0] * v[1] / tot} for k, v in breakdown.items()},
