@@ -107,6 +107,10 @@ SIGNATURES = {
     "dt_pose_control_vel_bwd": (C.c_int, [_W, C.c_int, _P, C.c_float, _P, C.c_int, C.c_int, _P]),
     "dt_affine_control_vel": (C.c_int, [_W, C.c_int, _P, _P, C.c_int, C.c_int, _P]),
     "dt_affine_control_vel_bwd": (C.c_int, [_W, C.c_int, _P, C.c_int, C.c_int, _P, _P]),
+    "dt_grid_mass": (C.c_int, [_W, C.c_int, C.c_int, _P, _P]),
+    "dt_deform_loss": (C.c_int, [_W, C.c_int, _P, _P, _P, C.c_float, C.c_float, _P, _P]),
+    "dt_deform_loss_bwd": (C.c_int, [_W, C.c_int, C.c_int, _P, _P, _P, C.c_float, C.c_float, C.c_float, _P]),
+    "dt_target_sdf": (C.c_int, [_W, C.c_int, _P, _P, _P, C.c_int, _P]),
     "dt_contact_force": (C.c_int, [_W, C.c_int, C.c_int, _P, _P]),
     "dt_contact_force_bwd": (C.c_int, [_W, C.c_int, _P, _P]),
     "dt_markers": (C.c_int, [_W, C.c_int, C.c_int, _P, _P, _P, C.c_int, C.c_int, _P, DtFisheye, _P, _P, _P]),

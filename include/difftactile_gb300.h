@@ -335,6 +335,25 @@ int dt_affine_control_vel(const dt_world* w, int s, const float* D, const float*
 int dt_affine_control_vel_bwd(const dt_world* w, int s, const float* src, int f0, int nfr, float* D_b,
                               cudaStream_t stream);
 
+/* ---- shape-target (deform) loss (tasks/deform_loss.py:8-146) ----
+ * Grids are [n_nodes] floats in the world's block layout (node_index of env e); nodes outside the
+ * env's n^3 are ignored.  dt_grid_mass adds the mass-only P2G of env e's particles at frame f
+ * (compute_grid_m_kernel, mpm_plastic.py:169-178; node i at i dx) into m (zero it first). */
+int dt_grid_mass(const dt_world* w, int e, int f, float* m, cudaStream_t stream);
+/* loss[0] (device, accumulated) += w_density sum |m - target| + w_sdf sum sdf m over env e's nodes
+ * (compute_density_loss_kernel + compute_sdf_loss_kernel + sum_up_loss_kernel). */
+int dt_deform_loss(const dt_world* w, int e, const float* m, const float* target, const float* sdf, float w_density,
+                   float w_sdf, float* loss, cudaStream_t stream);
+/* Adjoint: the x adjoint of frame f (p_adj[f&1], plane 0) += loss_bar d loss / d x through the mass
+ * P2G (d|.|/d. = sign, 0 at 0). */
+int dt_deform_loss_bwd(const dt_world* w, int e, int f, const float* m, const float* target, const float* sdf,
+                       float w_density, float w_sdf, float loss_bar, cudaStream_t stream);
+/* Target distance field (update_target / update_target_sdf): `passes` rounds (reference: 2 n_grid) of
+ * nearest-seed propagation over offsets in [-3, 3)^3, seeds where target > 1e-4, distance
+ * sqrt(|d|^2 + 1e-8), 1000 where unreached.  scratch: [2][n_nodes][4] floats. */
+int dt_target_sdf(const dt_world* w, int e, const float* target, float* sdf, float* scratch, int passes,
+                  cudaStream_t stream);
+
 /* ---- contact-force readout (compute_contact_force, grasp_plastic.py:218-229) ----
  * out[0..2] (device, accumulated) += sum over sensor s's surface triangles of 1/6 of the contact
  * force v_ext[f] on each of the triangle's vertices. */
