@@ -111,6 +111,8 @@ SIGNATURES = {
     "dt_deform_loss": (C.c_int, [_W, C.c_int, _P, _P, _P, C.c_float, C.c_float, _P, _P]),
     "dt_deform_loss_bwd": (C.c_int, [_W, C.c_int, C.c_int, _P, _P, _P, C.c_float, C.c_float, C.c_float, _P]),
     "dt_target_sdf": (C.c_int, [_W, C.c_int, _P, _P, _P, C.c_int, _P]),
+    "dt_rigid_match": (C.c_int, [_W, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "dt_rigid_match_bwd": (C.c_int, [_W, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P]),
     "dt_contact_force": (C.c_int, [_W, C.c_int, C.c_int, _P, _P]),
     "dt_contact_force_bwd": (C.c_int, [_W, C.c_int, _P, _P]),
     "dt_markers": (C.c_int, [_W, C.c_int, C.c_int, _P, _P, _P, C.c_int, C.c_int, _P, DtFisheye, _P, _P, _P]),

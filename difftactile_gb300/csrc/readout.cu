@@ -7,6 +7,9 @@
 //                  compute_marker_loss, grasp_plastic.py:241-256)
 //   contact force  compute_contact_force, grasp_plastic.py:218-229: sum over the surface triangles of
 //                  1/6 of the contact force on each of its three vertices
+//   rigid match    compute_COM + compute_H, multi_obj.py:309-326: centres of the rigid particles at
+//                  frames f and f+1 (sums divided by the env's particle count, as the reference) and
+//                  H = sum (x_f - c0)(x_{f+1} - c1)^T over them; adjoint scattered back to both frames
 //   markers        extract_markers, fem_sensor.py:161-187: surface nodes (current and virtual) into the
 //                  sensor frame (inv_trans_h), fisheye projection project_3d_2d
 //                  (sensor_model/fisheye_model.py:12-30), k-nearest inverse-distance interpolation to
@@ -168,6 +171,125 @@ __global__ void k_affine_cv_bwd(dt_world w, int s, const float4* __restrict__ sr
       atomicAdd(Db + 12 * k + threadIdx.x, x);
     }
     __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- rigid shape matching
+// out[0..2] += sum x_f / N, out[4..6] += sum x_{f+1} / N over env e's particles of material `mat`
+__global__ void k_rigid_com(dt_world w, int e, int mat, int f, float* out) {
+  __shared__ float red[6][NT / 32];
+  const dt_env& E = w.envs[e];
+  const int p = E.p_begin + blockIdx.x * blockDim.x + threadIdx.x;
+  const float invN = 1.f / (float)(E.p_end - E.p_begin);
+  float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (p < E.p_end && __ldg(w.p_mat + p) == mat) {
+    const float4 a = __ldg(pplane(w, f, 0) + p), b = __ldg(pplane(w, f + 1, 0) + p);
+    v[0] = a.x * invN;
+    v[1] = a.y * invN;
+    v[2] = a.z * invN;
+    v[3] = b.x * invN;
+    v[4] = b.y * invN;
+    v[5] = b.z * invN;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    if (lane == 0) red[k][wid] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    float x = 0.f;
+    for (int q = 0; q < NT / 32; ++q) x += red[threadIdx.x][q];
+    atomicAdd(out + (threadIdx.x < 3 ? threadIdx.x : threadIdx.x + 1), x);
+  }
+}
+
+// out[8..16] += sum (x_f - c0)(x_{f+1} - c1)^T (row-major), c0 = com[0..2], c1 = com[4..6]
+__global__ void k_rigid_H(dt_world w, int e, int mat, int f, const float* __restrict__ com, float* out) {
+  __shared__ float red[9][NT / 32];
+  const dt_env& E = w.envs[e];
+  const int p = E.p_begin + blockIdx.x * blockDim.x + threadIdx.x;
+  float h[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) h[k] = 0.f;
+  if (p < E.p_end && __ldg(w.p_mat + p) == mat) {
+    const float4 a4 = __ldg(pplane(w, f, 0) + p), b4 = __ldg(pplane(w, f + 1, 0) + p);
+    const float a[3] = {a4.x - com[0], a4.y - com[1], a4.z - com[2]};
+    const float b[3] = {b4.x - com[4], b4.y - com[5], b4.z - com[6]};
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) h[3 * r + c] = a[r] * b[c];
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h[k] += __shfl_xor_sync(0xffffffffu, h[k], o);
+    if (lane == 0) red[k][wid] = h[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 9) {
+    float x = 0.f;
+    for (int q = 0; q < NT / 32; ++q) x += red[threadIdx.x][q];
+    atomicAdd(out + 8 + threadIdx.x, x);
+  }
+}
+
+// adjoint of H for the rigid particles: frame f (part 0): x_bar += Hb (b - bbar); frame f+1
+// (part 1): x_bar += Hb^T (a - abar); abar / bbar = sums of a / b divided by N (aux[0..2] / [4..6])
+__global__ void k_rigid_H_bwd(dt_world w, int e, int mat, int f, int part, const float* __restrict__ com,
+                              const float* __restrict__ aux, const float* __restrict__ Hb) {
+  const dt_env& E = w.envs[e];
+  const int p = E.p_begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= E.p_end || __ldg(w.p_mat + p) != mat) return;
+  const int g = part == 0 ? f : f + 1;
+  const float4 a4 = __ldg(pplane(w, f, 0) + p), b4 = __ldg(pplane(w, f + 1, 0) + p);
+  v3 d;
+  if (part == 0) {
+    const float b[3] = {b4.x - com[4] - aux[4], b4.y - com[5] - aux[5], b4.z - com[6] - aux[6]};
+    d = v3{Hb[0] * b[0] + Hb[1] * b[1] + Hb[2] * b[2], Hb[3] * b[0] + Hb[4] * b[1] + Hb[5] * b[2],
+           Hb[6] * b[0] + Hb[7] * b[1] + Hb[8] * b[2]};
+  } else {
+    const float a[3] = {a4.x - com[0] - aux[0], a4.y - com[1] - aux[1], a4.z - com[2] - aux[2]};
+    d = v3{Hb[0] * a[0] + Hb[3] * a[1] + Hb[6] * a[2], Hb[1] * a[0] + Hb[4] * a[1] + Hb[7] * a[2],
+           Hb[2] * a[0] + Hb[5] * a[1] + Hb[8] * a[2]};
+  }
+  float4* ax = reinterpret_cast<float4*>(w.p_adj) + (size_t)(g & 1) * 6 * w.n_particles + p;
+  const float4 x = *ax;
+  *ax = make_float4(x.x + d.x, x.y + d.y, x.z + d.z, x.w);
+}
+
+// aux[0..2] = sum (x_f - c0) / N, aux[4..6] = sum (x_{f+1} - c1) / N over the rigid particles
+__global__ void k_rigid_centred_means(dt_world w, int e, int mat, int f, const float* __restrict__ com, float* aux) {
+  __shared__ float red[6][NT / 32];
+  const dt_env& E = w.envs[e];
+  const int p = E.p_begin + blockIdx.x * blockDim.x + threadIdx.x;
+  const float invN = 1.f / (float)(E.p_end - E.p_begin);
+  float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (p < E.p_end && __ldg(w.p_mat + p) == mat) {
+    const float4 a = __ldg(pplane(w, f, 0) + p), b = __ldg(pplane(w, f + 1, 0) + p);
+    v[0] = (a.x - com[0]) * invN;
+    v[1] = (a.y - com[1]) * invN;
+    v[2] = (a.z - com[2]) * invN;
+    v[3] = (b.x - com[4]) * invN;
+    v[4] = (b.y - com[5]) * invN;
+    v[5] = (b.z - com[6]) * invN;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    if (lane == 0) red[k][wid] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    float x = 0.f;
+    for (int q = 0; q < NT / 32; ++q) x += red[threadIdx.x][q];
+    atomicAdd(aux + (threadIdx.x < 3 ? threadIdx.x : threadIdx.x + 1), x);
   }
 }
 
@@ -358,6 +480,27 @@ int dt_affine_control_vel_bwd(const dt_world* w, int s, const float* src, int f0
     return DT_ERR_ARG;
   k_affine_cv_bwd<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, s, reinterpret_cast<const float4*>(src), f0, nfr,
                                                            D_b);
+  return launched();
+}
+
+int dt_rigid_match(const dt_world* w, int e, int mat, int f, float* out, cudaStream_t stream) {
+  if (!w || !out || e < 0 || e >= w->n_envs || f < 0 || f + 1 >= w->n_frames) return DT_ERR_ARG;
+  if (cudaMemsetAsync(out, 0, 20 * sizeof(float), stream) != cudaSuccess) return DT_ERR_LAUNCH;
+  const int nb = cdiv(w->n_particles > 0 ? w->n_particles : 1, NT);
+  k_rigid_com<<<nb, NT, 0, stream>>>(*w, e, mat, f, out);
+  k_rigid_H<<<nb, NT, 0, stream>>>(*w, e, mat, f, out, out);
+  return launched();
+}
+
+int dt_rigid_match_bwd(const dt_world* w, int e, int mat, int f, int part, const float* out, const float* H_b,
+                       float* scratch, cudaStream_t stream) {
+  if (!w || !out || !H_b || !scratch || e < 0 || e >= w->n_envs || f < 0 || f + 1 >= w->n_frames || part < 0 ||
+      part > 1)
+    return DT_ERR_ARG;
+  if (cudaMemsetAsync(scratch, 0, 8 * sizeof(float), stream) != cudaSuccess) return DT_ERR_LAUNCH;
+  const int nb = cdiv(w->n_particles > 0 ? w->n_particles : 1, NT);
+  k_rigid_centred_means<<<nb, NT, 0, stream>>>(*w, e, mat, f, out, scratch);
+  k_rigid_H_bwd<<<nb, NT, 0, stream>>>(*w, e, mat, f, part, out, scratch, H_b);
   return launched();
 }
 

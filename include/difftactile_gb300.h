@@ -354,6 +354,18 @@ int dt_deform_loss_bwd(const dt_world* w, int e, int f, const float* m, const fl
 int dt_target_sdf(const dt_world* w, int e, const float* target, float* sdf, float* scratch, int passes,
                   cudaStream_t stream);
 
+/* ---- rigid shape matching (multi_obj.py:309-340: compute_COM, compute_H) ----
+ * Over env e's particles of material `mat` (the rigid part), between frames f and f+1:
+ * out[0..2] = c0 = sum x_f / N, out[4..6] = c1 = sum x_{f+1} / N (N: all particles of the env, as the
+ * reference), out[8..16] = H = sum (x_f - c0)(x_{f+1} - c1)^T row-major.  out: 20 device floats,
+ * overwritten.  The 3x3 SVD of H, R = V U^T and the angle readout are left to the caller. */
+int dt_rigid_match(const dt_world* w, int e, int mat, int f, float* out, cudaStream_t stream);
+/* Adjoint for H_b (9 device floats, d loss / d H): part 0 adds d/dx_f to p_adj[f&1], part 1 adds
+ * d/dx_{f+1} to p_adj[(f+1)&1] (call each while that frame's adjoint buffer is current).  out: the
+ * forward's output; scratch: 8 device floats. */
+int dt_rigid_match_bwd(const dt_world* w, int e, int mat, int f, int part, const float* out, const float* H_b,
+                       float* scratch, cudaStream_t stream);
+
 /* ---- contact-force readout (compute_contact_force, grasp_plastic.py:218-229) ----
  * out[0..2] (device, accumulated) += sum over sensor s's surface triangles of 1/6 of the contact
  * force v_ext[f] on each of the triangle's vertices. */
