@@ -38,6 +38,9 @@ def parse():
                     help="27-node scatter strategy (default: the library's)")
     ap.add_argument("--no-pdl", action="store_true", help="launch the substep kernels without programmatic "
                     "dependent launch")
+    ap.add_argument("--plain", type=int, default=0,
+                    help="also time the first K environments one World each (one scene per launch "
+                    "sequence) and report the batched / plain ratio")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -270,12 +273,47 @@ def run_ours(args):
                       "ms_per_step": e_ms,
                       "h2d_bytes_per_step": int(h_act.numel() * 4 + h_x.numel() * 4 + h_v.numel() * 4),
                       "d2h_bytes_per_step": int(res.numel() * 8)}
+    if args.plain > 0:
+        out["plain"] = time_plain(cfg, args, dev, flush)
+        out["batched_over_plain"] = value / out["plain"]["value"]
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(cfg, threads=os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(out))
     if world_size > 1:
         dist.destroy_process_group()
+
+
+def time_plain(cfg, args, dev, flush):
+    """Each of the first K environments in a World of its own, stepped one after the other with the
+    same actions (the one-scene-per-launch path); aggregate particle-substeps/s of the sample."""
+    import torch
+
+    from difftactile_gb300.configs import Config
+
+    k = min(args.plain, len(cfg.envs))
+    total_ms, units = 0.0, 0
+    for e in range(k):
+        sub = Config(cfg.name, [cfg.envs[e]], cfg.dt, cfg.substeps, cfg.n_steps, cfg.actions[:, e:e + 1],
+                     tuple((0, lay, tg) for s, lay, tg in cfg.loss_terms if s == e), cfg.ckpt_every, cfg.tape_blocks)
+        w, traj = sub.build(dev)
+        acts = torch.as_tensor(sub.actions, dtype=torch.float64, device=dev)
+        for _ in range(max(args.warmup, 1)):
+            traj.forward(acts)
+            traj.backward()
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        traj.forward(acts)
+        traj.backward()
+        e1.record()
+        torch.cuda.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        units += cfg.envs[e].n_particles * cfg.n_steps * cfg.substeps
+        del w, traj
+    return {"value": units / (total_ms / 1e3), "unit": "particle-substeps/s", "envs": k, "ms": total_ms,
+            "path": "one World per environment, launched one after the other"}
 
 
 def cpu_baseline(cfg, threads, target_s=15.0):

@@ -117,4 +117,5 @@ def batched_population(n_envs=64, substeps=20, n_steps=200, seed=6, lo=8_000, hi
         sp = env.sensors[0]
         tg = 1e-3 * np.random.default_rng(100 + e).standard_normal(sp.verts.shape)
         terms.append((e, int(sp.layer.max()), tg))
-    return Config("batched_population", envs, 1e-4, substeps, n_steps, acts, tuple(terms))
+    # grid tape: ~14,500 of the 843,000 blocks are active per frame; 32,768 reserved
+    return Config("batched_population", envs, 1e-4, substeps, n_steps, acts, tuple(terms), tape_blocks=32768)

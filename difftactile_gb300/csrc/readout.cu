@@ -36,6 +36,20 @@ __global__ void k_pose_cv(dt_world w, int s, const float* __restrict__ Ab, float
   for (int f = f0; f < f0 + nfr; ++f) vframe(w.v_cv, w, f)[v] = cv;
 }
 
+// every sensor at once: Ab [n_sensors][12], one row per sensor
+__global__ void k_pose_cv_all(dt_world w, const float* __restrict__ Ab, float inv_T, int f0, int nfr) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= w.n_verts) return;
+  const float* A = Ab + 12 * __ldg(w.v_sensor + v);
+  const v3 p = f4to3(vframe(w.v_vpos, w, f0)[v]);
+  v3 q;
+  q.x = A[0] * p.x + A[1] * p.y + A[2] * p.z + A[3];
+  q.y = A[4] * p.x + A[5] * p.y + A[6] * p.z + A[7];
+  q.z = A[8] * p.x + A[9] * p.y + A[10] * p.z + A[11];
+  const float4 cv = v3to4(inv_T * (q - p));
+  for (int f = f0; f < f0 + nfr; ++f) vframe(w.v_cv, w, f)[v] = cv;
+}
+
 __global__ void k_pose_cv_bwd(dt_world w, int s, const float* __restrict__ Ab, float inv_T, float* Ab_bar, int f0,
                               int nfr) {
   __shared__ float red[12][NT / 32];
@@ -544,6 +558,13 @@ int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, 
                         cudaStream_t stream) {
   if (!w || !Ab || s < 0 || s >= w->n_sensors || f0 < 0 || nfr < 1 || f0 + nfr > w->n_frames) return DT_ERR_ARG;
   k_pose_cv<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, s, Ab, inv_T, f0, nfr);
+  return launched();
+}
+
+int dt_pose_control_vel_all(const dt_world* w, const float* Ab, float inv_T, int f0, int nfr, cudaStream_t stream) {
+  if (!w || !Ab || f0 < 0 || nfr < 1 || f0 + nfr > w->n_frames) return DT_ERR_ARG;
+  if (w->n_verts == 0) return DT_OK;
+  k_pose_cv_all<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, Ab, inv_T, f0, nfr);
   return launched();
 }
 

@@ -317,6 +317,9 @@ int dt_com_bwd(const dt_world* w, int f, const float* adj_com, cudaStream_t stre
  * 3x4), inv_T = 1 / (dt * substeps); written into frames [f0, f0 + nfr) of v_cv (one control step). */
 int dt_pose_control_vel(const dt_world* w, int s, const float* Ab, float inv_T, int f0, int nfr,
                         cudaStream_t stream);
+/* dt_pose_control_vel for every sensor in one launch: Ab [n_sensors][12] (device), sensor s's
+ * transform in row s. */
+int dt_pose_control_vel_all(const dt_world* w, const float* Ab, float inv_T, int f0, int nfr, cudaStream_t stream);
 /* Adjoint: Ab_bar[12] (device) += sum_i cvb_i [vp_i, 1]^T inv_T and v_adj_vpos[f0&1] += (A - I)^T cvb_i
  * inv_T, with cvb_i the control-velocity adjoint summed over frames [f0, f0 + nfr) of v_adj_cv.  Those
  * entries of v_adj_cv are consumed (reset to zero), so consecutive control steps may share their
