@@ -119,3 +119,71 @@ def batched_population(n_envs=64, substeps=20, n_steps=200, seed=6, lo=8_000, hi
         terms.append((e, int(sp.layer.max()), tg))
     # grid tape: ~14,500 of the 843,000 blocks are active per frame; 32,768 reserved
     return Config("batched_population", envs, 1e-4, substeps, n_steps, acts, tuple(terms), tape_blocks=32768)
+
+
+def grasp_sphere(n_steps=1000, substeps=25, seed=4, n_grid=128, n_core=20_000, n_shell=180_000, pad=(20, 20, 5),
+                 ckpt_every=50) -> "tuple[Config, object]":
+    """Config 3: a parallel-jaw gripper whose two finger pads (configuration 2's 20x20x5 hex pad each)
+    squeeze a sphere of a stiff core (``n_core`` particles) and a soft shell (``n_shell``, E log-uniform
+    in [1e3, 1e5], seed 4) on an ``n_grid``^3 grid; ``n_steps`` x ``substeps`` with a checkpoint every
+    ``ckpt_every`` steps.  Returns (config, gripper kinematics); the actions are [n_steps, 7] (d_pos,
+    d_ori, d_gripper): close for the first half, then lift."""
+    from .trajectory import GripperKinematics
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / n_grid
+    # sphere radius from the particle count (8 per cell): volume = (n_core + n_shell) / 8 cells
+    vol = (n_core + n_shell) / 8 * dx ** 3
+    R = (3 * vol / (4 * np.pi)) ** (1 / 3)
+    r_core = R * (n_core / (n_core + n_shell)) ** (1 / 3)
+    c = np.array([0.5, 0.08 + R + 4 * dx, 0.5])
+    x = S.sphere_particles(c, R, dx, 8, seed)
+    core = np.linalg.norm(x - c, axis=1) < r_core
+    E_shell = float(np.exp(rng.uniform(np.log(1e3), np.log(1e5))))
+    mats = [S.Material(E_shell, 0.3, 0.0, S.MODEL_COROTATED), S.Material(1e6, 0.3, 0.0, S.MODEL_COROTATED)]
+    h = 2 * R / pad[0]
+    grip = 0.5 * (0.3 - 2 * R) + 0.1 * h  # pads start just inside the sphere's silhouette
+    kin = GripperKinematics([0.0, 0.0, 0.0], [0.5, c[1] + 0.12, 0.5], grip, 1e-4, base_height=0.02, base_width=0.3,
+                            finger_height=0.1)
+    pads = [S.finger_pad_sensor(f.numpy(), nx=pad[0], nz=pad[1], ny=pad[2], h=h, rho=1000.0 * (0.0125 / h) ** 3,
+                                shift=(0.13 * dx, -0.21 * dx))
+            for f in kin.finger_poses0()]
+    env = S.EnvSpec(x=x, materials=mats, mat=core.astype(np.int32), n_grid=(n_grid,) * 3, dx=dx, rho=1000.0,
+                    sensors=pads, kn=1e4, kd=100.0, kt=100.0, mu_t=0.5, bc=S.BC_STICKY_FLOOR)
+    acts = np.zeros((n_steps, 7))
+    acts[: n_steps // 2, 6] = 0.05
+    acts[n_steps // 2:, 1] = 0.05
+    acts += 0.01 * rng.standard_normal(acts.shape)
+    return Config("grasp_sphere", [env], 1e-4, substeps, n_steps, acts, (), ckpt_every), kin
+
+
+def rope_pads(n_envs=16, n_steps=500, substeps=20, seed=5, n_rope=2000, pad=(40, 40, 5), n_particles=32_000,
+              n_grid=160, rope_len=0.6) -> Config:
+    """Config 5: ``n_envs`` environments, each a 40x40x5 hex pad (10,086 nodes, 48,000 tets) pressing a
+    PBD rope of ``n_rope`` particles (``rope_len`` long, compliance 1e-6) lying on an elastic slab of
+    ``n_particles`` MPM particles (4 cells thick) on an ``n_grid``^3 grid; ``n_steps`` x ``substeps``.
+    The rope-pad contact stiffness is scaled to the rope particles' mass (k dt^2 / m = 0.2) so that the
+    explicit penalty contact stays stable for thin ropes."""
+    rng = np.random.default_rng(seed)
+    envs = []
+    dx = 1.0 / n_grid
+    dt = 1e-4
+    for e in range(n_envs):
+        side = max(2, int(round(np.sqrt(n_particles / 8 / 4))))
+        lo = np.array([0.5 - side * dx / 2, 4 * dx, 0.5 - side * dx / 2])
+        x = S.box_particles(lo, lo + np.array([side, 4, side]) * dx, dx, 8, seed * 100 + e)
+        top = float(x[:, 1].max())
+        rest = rope_len / max(n_rope - 1, 1)
+        rad = rest / 1.6
+        xs = np.stack([0.5 - rope_len / 2 + rest * np.arange(n_rope), np.full(n_rope, top + rad),
+                       np.full(n_rope, 0.5 + 0.01 * rng.standard_normal())], 1)
+        mass = 1000.0 * (np.pi * 4.0 / 3.0) * rad ** 3
+        kn = 0.2 * mass / dt ** 2
+        rope = S.RopeSpec(n=n_rope, rad=rad, rho=1000.0, rest_length=rest, pos=tuple(xs[0]), ori=(1.0, 0.0, 0.0),
+                          table_h=top, x=xs.astype(np.float32), stretch_compliance=1e-6, bend_compliance=1e-6,
+                          kn=kn, kd=0.01 * kn * dt, kt=0.01 * kn, mu_t=0.5)
+        h = min(1.2 * rope_len, 0.9) / pad[0]
+        sp = S.hex_pad_sensor([0.5 + 0.13 * dx, top + 1.7 * rad, 0.5 - 0.21 * dx], nx=pad[0], nz=pad[1], ny=pad[2],
+                              h=h, rho=1000.0 * (0.0125 / h) ** 3)
+        envs.append(S.EnvSpec(x=x, materials=[S.Material(5e3, 0.3)], n_grid=(n_grid,) * 3, dx=dx, rho=1000.0,
+                              sensors=[sp], ropes=[rope], kn=1e4, kd=100.0, kt=100.0, mu_t=0.5))
+    return Config("rope_pads", envs, dt, substeps, n_steps, press_actions(n_steps, n_envs), ())
