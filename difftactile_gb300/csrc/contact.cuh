@@ -19,9 +19,11 @@ struct Best {
   int i;
 };
 DT_DEV Best lexmin(Best a, Best b) { return (b.d < a.d || (b.d == a.d && b.i < a.i)) ? b : a; }
-DT_DEV Best quad_min(Best b) {
+// lexicographic minimum over the LPN lanes (a power of two) that share one query
+template <int LPN>
+DT_DEV Best group_min(Best b) {
 #pragma unroll
-  for (int o = 1; o <= 2; o <<= 1) {
+  for (int o = 1; o < LPN; o <<= 1) {
     Best other{__shfl_xor_sync(0xffffffffu, b.d, o), __shfl_xor_sync(0xffffffffu, b.i, o)};
     b = lexmin(b, other);
   }
@@ -69,9 +71,11 @@ DT_DEV void stage_sensor(const dt_world& w, const dt_sensor& S, float4* scent, f
   __syncthreads();
 }
 
-// Argmin for the quad's query point (px, py, pz); all 32 lanes of the warp call it, `active` false
-// for quads without a query.  Returns the local triangle index (original order) or -1, in every lane
-// of the quad.  in_smem: S staged by stage_sensor; otherwise a direct scan of global centroids.
+// Argmin for the query point (px, py, pz) shared by LPN consecutive lanes (`sub` = lane index within
+// them, LPN in {4, 8}); all 32 lanes of the warp call it, `active` false for lane groups without a
+// query.  Returns the local triangle index (original order) or -1, in every lane of the group.
+// in_smem: S staged by stage_sensor; otherwise a direct scan of global centroids.
+template <int LPN>
 DT_DEV int closest_tri(const dt_world& w, const dt_sensor& S, const float4* scent, const float4* gbox, bool in_smem,
                        bool active, float px, float py, float pz, int sub) {
   const int nf = S.nf;
@@ -80,39 +84,39 @@ DT_DEV int closest_tri(const dt_world& w, const dt_sensor& S, const float4* scen
     const int Gu = (nf + 31) >> 5;  // warp-uniform trip count around the shuffles
     const int G = active ? Gu : 0;
     Best gbest{3.4e38f, 0x7fffffff};
-    for (int gg = sub; gg < G; gg += 4) {
+    for (int gg = sub; gg < G; gg += LPN) {
       const float lb = box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz);
       if (lb < gbest.d) gbest = Best{lb, gg};
     }
-    gbest = quad_min(gbest);
+    gbest = group_min<LPN>(gbest);
     // no group is selected when every box distance is NaN (non-finite sensor positions): the
     // sentinel must not be used as an index; the pruned scan below then covers every group
     const int g0 = gbest.i < G ? gbest.i : -1;
     if (g0 >= 0) {
 #pragma unroll
-      for (int jj = 0; jj < 8; ++jj) {
-        const int t = 32 * g0 + sub + 4 * jj;
+      for (int jj = 0; jj < 32 / LPN; ++jj) {
+        const int t = 32 * g0 + sub + LPN * jj;
         if (t < nf) {
           const float4 c = scent[t];
           bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
         }
       }
     }
-    bb = quad_min(bb);
+    bb = group_min<LPN>(bb);
     const float thr = bb.d * (1.f + 1e-5f);
     for (int gc = 0; gc < Gu; gc += 64) {
       unsigned long long live = 0ull;
       const int ge = min(gc + 64, G);
-      for (int gg = gc + sub; gg < ge; gg += 4)
+      for (int gg = gc + sub; gg < ge; gg += LPN)
         if (gg != g0 && !(box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr)) live |= 1ull << (gg - gc);
-      live |= __shfl_xor_sync(0xffffffffu, live, 1);
-      live |= __shfl_xor_sync(0xffffffffu, live, 2);
+#pragma unroll
+      for (int o = 1; o < LPN; o <<= 1) live |= __shfl_xor_sync(0xffffffffu, live, o);
       while (live) {
         const int gg = gc + __ffsll((long long)live) - 1;
         live &= live - 1ull;
 #pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          const int t = 32 * gg + sub + 4 * jj;
+        for (int jj = 0; jj < 32 / LPN; ++jj) {
+          const int t = 32 * gg + sub + LPN * jj;
           if (t < nf) {
             const float4 c = scent[t];
             bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
@@ -122,10 +126,10 @@ DT_DEV int closest_tri(const dt_world& w, const dt_sensor& S, const float4* scen
     }
   } else if (active) {
     const float4* cent = reinterpret_cast<const float4*>(w.tri_cent) + S.f_off;
-    for (int t = sub; t < nf; t += 4) {
+    for (int t = sub; t < nf; t += LPN) {
       const float4 c = __ldg(cent + t);
       bb = lexmin(bb, Best{cent_dist(c, px, py, pz), __float_as_int(c.w)});
     }
   }
-  return quad_min(bb).i;
+  return group_min<LPN>(bb).i;
 }

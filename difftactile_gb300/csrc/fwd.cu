@@ -24,7 +24,8 @@ namespace {
 
 constexpr int NT = 128;           // threads per CTA for particle / tet / vertex roles
 constexpr int TILE_MAX = 1728;    // shared P2G tile capacity in nodes (12^3), 27 KB of float4
-constexpr int GRID_NT = 256;      // one 4x4x4 node block (4 lanes per node) per CTA in the grid kernel
+constexpr int GRID_LPN = 8;                 // lanes per node in the grid kernel's contact search
+constexpr int GRID_NT = 64 * GRID_LPN;     // one 4x4x4 node block per CTA
 constexpr int SMEM_CENT_MAX = 12288;  // triangle centroids staged in shared memory (192 KB)
 
 __device__ void mark_block(const dt_world& w, int f, int b) {
@@ -210,13 +211,13 @@ __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p,
 // (distance, index) pairs are combined lexicographically, which is exactly the sequential scan's
 // first-minimum-wins result.  Lane 0 of each node then does the contact force and the grid update.
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(GRID_NT, 2) k_fwd_grid(dt_world w, int f, int smem_cap) {
+__global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w, int f, int smem_cap) {
   pdl_entry();
   extern __shared__ float4 scent[];
   float4* gbox = scent + smem_cap;  // 2 float4 per group of 32 centroids
   const int cnt = *((volatile int*)(w.tape_bcount + f));
   const int tid = threadIdx.x;
-  const int l = tid >> 2, sub = tid & 3;
+  const int l = tid / GRID_LPN, sub = tid % GRID_LPN;
   const float third = 1.f / 3.f;
   float4* acc = reinterpret_cast<float4*>(w.g_acc);
   float4* vout = reinterpret_cast<float4*>(w.g_vout);
@@ -252,7 +253,7 @@ __global__ void __launch_bounds__(GRID_NT, 2) k_fwd_grid(dt_world w, int f, int 
         stage_sensor<GRID_NT>(w, S, scent, gbox);
         staged = si;
       }
-      const int kk = closest_tri(w, S, scent, gbox, in_smem, occ, px, py, pz, sub);
+      const int kk = closest_tri<GRID_LPN>(w, S, scent, gbox, in_smem, occ, px, py, pz, sub);
       if (q == 0) cid.x = kk;
       else if (q == 1) cid.y = kk;
       else if (q == 2) cid.z = kk;

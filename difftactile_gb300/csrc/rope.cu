@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(RC_NT) k_rope_contact(dt_world w, int f, int s
     const dt_sensor& S = w.sensors[si];
     const bool in_smem = S.nf <= smem_cap;
     if (in_smem) stage_sensor<RC_NT>(w, S, scent, gbox);
-    const int kk = closest_tri(w, S, scent, gbox, in_smem, active, x.x, x.y, x.z, sub);
+    const int kk = closest_tri<4>(w, S, scent, gbox, in_smem, active, x.x, x.y, x.z, sub);
     if (q == 0) cid.x = kk;
     else if (q == 1) cid.y = kk;
     else if (q == 2) cid.z = kk;
