@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--plain", type=int, default=0,
                     help="also time the first K environments one World each (one scene per launch "
                     "sequence) and report the batched / plain ratio")
+    ap.add_argument("--no-svd-tape", action="store_true", help="the adjoint recomputes the SVD instead of "
+                    "reading the forward's from the tape")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -141,6 +143,8 @@ def run_ours(args):
 
     cfg = make_config(args.config, args.horizon)
     kw = {} if args.scatter is None else {"scatter_mode": {"tile": 0, "global": 1, "warp": 2}[args.scatter]}
+    if args.no_svd_tape:
+        kw["svd_tape"] = False
     w, traj = cfg.build(dev, **kw)
     w.lib.dt_set_pdl(0 if args.no_pdl else 1)
     acts = torch.as_tensor(cfg.actions, dtype=torch.float64, device=dev)
@@ -228,6 +232,7 @@ def run_ours(args):
                       "checkpoint_every": cfg.ckpt_every, "tape_blocks": w.tape_blocks,
                       "scatter": ["tile", "global", "warp"][w.w.scatter_mode],
                       "programmatic_dependent_launch": not args.no_pdl,
+                      "svd_tape": w.w.p_svd is not None,
                       "active_blocks_mean": cnt, "active_blocks_max": cnt_max, "l2": "flushed between timed iterations (256 MiB write)",
                       "parallelism": f"replicas x{world_size}"},
            "gpu_launches": launches_per_iter * args.steps,

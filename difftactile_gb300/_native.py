@@ -72,7 +72,8 @@ class DtWorld(C.Structure):
     _fields_ = ([(n, _P) for n in WORLD_PTR_FIELDS] + [(n, C.c_int) for n in WORLD_INT_FIELDS]
                 + [("dt", C.c_float), ("grad_clip", C.c_float), ("svd_sweeps", C.c_int),
                    ("svd_grad_mode", C.c_int), ("max_sensor_tris", C.c_int), ("scatter_mode", C.c_int)]
-                + [(n, _P) for n in ROPE_PTR_FIELDS] + [(n, C.c_int) for n in ROPE_INT_FIELDS])
+                + [(n, _P) for n in ROPE_PTR_FIELDS] + [(n, C.c_int) for n in ROPE_INT_FIELDS]
+                + [("p_svd", _P)])
 
 
 # entry points: name -> (restype, argtypes)

@@ -376,7 +376,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   }
   const dt_material M = w.materials[mat];
   Stress s;
-  constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s);
+  constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s, &w, w.p_svd ? f : -1, p);  // the forward's SVD if taped
   const float pm = E.p_mass, dx = E.dx;
   m3 A;
 #pragma unroll

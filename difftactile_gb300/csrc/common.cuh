@@ -410,14 +410,49 @@ DT_DEV void von_mises(Stress& s, float mu, float ys) {
   }
 }
 
-DT_DEV void constitutive(const m3& C, const m3& F, float dt, const dt_material& M, int sweeps, Stress& s) {
+// the SVD of F_new as stored on the tape: 6 float4 planes per particle and frame,
+// (U00 U01 U02 U10) (U11 U12 U20 U21) (U22 V00 V01 V02) (V10 V11 V12 V20) (V21 V22 s0 s1) (s2 0 0 0)
+DT_DEV float4* svd_plane(const dt_world& w, int f, int k) {
+  return reinterpret_cast<float4*>(w.p_svd) + ((size_t)f * 6 + k) * w.n_particles;
+}
+DT_DEV void store_svd(const dt_world& w, int f, int p, const m3& U, v3 sg, const m3& V) {
+  svd_plane(w, f, 0)[p] = make_float4(U.a[0][0], U.a[0][1], U.a[0][2], U.a[1][0]);
+  svd_plane(w, f, 1)[p] = make_float4(U.a[1][1], U.a[1][2], U.a[2][0], U.a[2][1]);
+  svd_plane(w, f, 2)[p] = make_float4(U.a[2][2], V.a[0][0], V.a[0][1], V.a[0][2]);
+  svd_plane(w, f, 3)[p] = make_float4(V.a[1][0], V.a[1][1], V.a[1][2], V.a[2][0]);
+  svd_plane(w, f, 4)[p] = make_float4(V.a[2][1], V.a[2][2], sg.x, sg.y);
+  svd_plane(w, f, 5)[p] = make_float4(sg.z, 0.f, 0.f, 0.f);
+}
+DT_DEV void load_svd(const dt_world& w, int f, int p, m3& U, v3& sg, m3& V) {
+  const float4 a = svd_plane(w, f, 0)[p], b = svd_plane(w, f, 1)[p], c = svd_plane(w, f, 2)[p],
+               d = svd_plane(w, f, 3)[p], e = svd_plane(w, f, 4)[p], g = svd_plane(w, f, 5)[p];
+  U.a[0][0] = a.x; U.a[0][1] = a.y; U.a[0][2] = a.z; U.a[1][0] = a.w;
+  U.a[1][1] = b.x; U.a[1][2] = b.y; U.a[2][0] = b.z; U.a[2][1] = b.w;
+  U.a[2][2] = c.x; V.a[0][0] = c.y; V.a[0][1] = c.z; V.a[0][2] = c.w;
+  V.a[1][0] = d.x; V.a[1][1] = d.y; V.a[1][2] = d.z; V.a[2][0] = d.w;
+  V.a[2][1] = e.x; V.a[2][2] = e.y; sg = v3{e.z, e.w, g.x};
+}
+
+// constitutive update of one particle (compute_new_F + svd + stress, mpm_elastic.py:135-187,
+// mpm_plastic.py:151-166,228-235).  svd_src: frame whose tape holds the SVD of this F_new (the
+// backward re-reading the forward's), or -1 to compute it.  Neo-Hookean stress needs no SVD.
+DT_DEV void constitutive(const m3& C, const m3& F, float dt, const dt_material& M, int sweeps, Stress& s,
+                         const dt_world* w = nullptr, int svd_src = -1, int p = 0) {
   m3 A = meye();
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) A.a[i][j] += dt * C.a[i][j];
   s.Fn = mmul(A, F);  // compute_new_F, mpm_elastic.py:137
-  svd3(s.Fn, s.U, s.sig, s.V, sweeps);
+  if (M.model == DT_MODEL_NEOHOOKEAN) {
+    s.U = meye();
+    s.V = meye();
+    s.sig = v3{1.f, 1.f, 1.f};
+  } else if (w != nullptr && svd_src >= 0) {
+    load_svd(*w, svd_src, p, s.U, s.sig, s.V);
+  } else {
+    svd3(s.Fn, s.U, s.sig, s.V, sweeps);
+  }
   s.R = mmulT(s.U, s.V);
   s.yield = false;
   if (M.model == DT_MODEL_VON_MISES) {

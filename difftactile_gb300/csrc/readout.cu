@@ -50,37 +50,36 @@ __global__ void k_pose_cv_all(dt_world w, const float* __restrict__ Ab, float in
   for (int f = f0; f < f0 + nfr; ++f) vframe(w.v_cv, w, f)[v] = cv;
 }
 
+// one thread per (frame, vertex): everything below is linear in the per-frame adjoint cvb_f, so the
+// frames are summed by the reductions (Ab_bar) and atomics (v_adj_vpos) instead of a loop per vertex
 __global__ void k_pose_cv_bwd(dt_world w, int s, const float* __restrict__ Ab, float inv_T, float* Ab_bar, int f0,
                               int nfr) {
   __shared__ float red[12][NT / 32];
   const dt_sensor& S = w.sensors[s];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = f0 + blockIdx.y;
   float g[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) g[k] = 0.f;
   if (i < S.nv) {
     const int v = S.v_off + i;
     const v3 p = f4to3(vframe(w.v_vpos, w, f0)[v]);
-    v3 cb = v3{0.f, 0.f, 0.f};
-    for (int f = f0; f < f0 + nfr; ++f) {  // consume: the adjoint moves into Ab_bar and vpos_bar
-      float4* c = vframe(w.v_adj_cv, w, f) + v;
-      cb = cb + f4to3(*c);
-      *c = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4* c = vframe(w.v_adj_cv, w, f) + v;  // consumed: the adjoint moves into Ab_bar and vpos_bar
+    const v3 cb = inv_T * f4to3(*c);
+    *c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (cb.x != 0.f || cb.y != 0.f || cb.z != 0.f) {
+      const float pr[4] = {p.x, p.y, p.z, 1.f};
+      const float cr[3] = {cb.x, cb.y, cb.z};
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) g[4 * r + cc] = cr[r] * pr[cc];
+      // cv = inv_T (A p + b - p): p_bar += (A - I)^T cb, into frame f0's buffer
+      float4* ap = reinterpret_cast<float4*>(w.v_adj_vpos) + (size_t)(f0 & 1) * w.n_verts + v;
+      red_add_v4(ap, make_float4(Ab[0] * cb.x + Ab[4] * cb.y + Ab[8] * cb.z - cb.x,
+                                 Ab[1] * cb.x + Ab[5] * cb.y + Ab[9] * cb.z - cb.y,
+                                 Ab[2] * cb.x + Ab[6] * cb.y + Ab[10] * cb.z - cb.z, 0.f));
     }
-    cb = inv_T * cb;
-    const float pr[4] = {p.x, p.y, p.z, 1.f};
-    const float cr[3] = {cb.x, cb.y, cb.z};
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) g[4 * r + c] = cr[r] * pr[c];
-    // cv = inv_T (A p + b - p): p_bar += (A - I)^T cb
-    float4* ap = reinterpret_cast<float4*>(w.v_adj_vpos) + (size_t)(f0 & 1) * w.n_verts + v;  // frame f0's buffer
-    float4 a = *ap;
-    a.x += Ab[0] * cb.x + Ab[4] * cb.y + Ab[8] * cb.z - cb.x;
-    a.y += Ab[1] * cb.x + Ab[5] * cb.y + Ab[9] * cb.z - cb.y;
-    a.z += Ab[2] * cb.x + Ab[6] * cb.y + Ab[10] * cb.z - cb.z;
-    *ap = a;
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -94,7 +93,7 @@ __global__ void k_pose_cv_bwd(dt_world w, int s, const float* __restrict__ Ab, f
   if (threadIdx.x < 12) {
     float x = 0.f;
     for (int k = 0; k < NT / 32; ++k) x += red[threadIdx.x][k];
-    atomicAdd(Ab_bar + threadIdx.x, x);
+    if (x != 0.f) atomicAdd(Ab_bar + threadIdx.x, x);
   }
 }
 
@@ -572,7 +571,7 @@ int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv
                             cudaStream_t stream) {
   if (!w || !Ab || !Ab_bar || s < 0 || s >= w->n_sensors || f0 < 0 || nfr < 1 || f0 + nfr > w->n_frames)
     return DT_ERR_ARG;
-  k_pose_cv_bwd<<<cdiv(w->n_verts, NT), NT, 0, stream>>>(*w, s, Ab, inv_T, Ab_bar, f0, nfr);
+  k_pose_cv_bwd<<<dim3(cdiv(w->n_verts, NT), nfr), NT, 0, stream>>>(*w, s, Ab, inv_T, Ab_bar, f0, nfr);
   return launched();
 }
 

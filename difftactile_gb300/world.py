@@ -56,7 +56,7 @@ class World:
 
     def __init__(self, envs: list[EnvSpec], n_frames: int, dt: float, device="cuda", tape_blocks: int | None = None,
                  grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True,
-                 svd_grad_mode: int = 0, scatter_mode: int = 2):
+                 svd_grad_mode: int = 0, scatter_mode: int = 2, svd_tape: bool = True):
         self.lib = N.load()
         self.device = torch.device(device)
         self.specs = envs
@@ -253,6 +253,8 @@ class World:
         t["r_cidx"] = zeros((Fn, NR, 4), I32)
         t["r_adj"] = zeros((2, 2, NR, 4))
         t["r_extb"] = zeros((NR, 4))
+        # the forward's SVD per frame, so that the adjoint need not recompute it (96 B per particle-frame)
+        t["p_svd"] = zeros((Fn, 6, Np, 4)) if (svd_tape and Np) else None
 
         w = N.DtWorld()
         for name in N.WORLD_PTR_FIELDS:
@@ -269,6 +271,7 @@ class World:
         w.n_ropes, w.n_rope_particles = self.n_ropes, NR
         w.rope_blocks = r_blk
         w.max_rope_n = max([r.n for r in rope_rows], default=0)
+        w.p_svd = t["p_svd"].data_ptr() if t["p_svd"] is not None else None
         self.w = w
         self.wp = C.pointer(w)
 

@@ -197,6 +197,10 @@ typedef struct dt_world {
   int n_ropes, n_rope_particles;
   int rope_blocks;               /* CTAs of the rope-contact launches (sum of ceil(n / 64)) */
   int max_rope_n;                /* largest n over the ropes (sizes the rope solver's shared memory) */
+  /* ---- optional SVD tape ---- */
+  float* p_svd;                  /* [n_frames][6][n_particles][4]: U, V, sigma of F_new per frame, written
+                                    by the forward, read by the adjoint instead of recomputing; NULL:
+                                    the adjoint recomputes the SVD */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared
