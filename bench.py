@@ -99,7 +99,7 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-# algorithmic bytes per unit of each fused launch (documented in the design doc)
+# algorithmic bytes per unit of each fused launch
 BYTES = {
     ("fwd", 0): {"particle": 96 + 36, "node": 16, "tet": 148, "tri": 68},
     ("fwd", 1): {"node": 96},
