@@ -63,3 +63,26 @@ def test_noalloc_rejects_grids_beyond_its_capacity(cuda_lib):
     assert rc == -3  # DT_ERR_CAPACITY
     torch.cuda.synchronize()
     assert np.allclose(w.particles(1)["x"].cpu().numpy(), 0.0)  # nothing ran
+
+
+def test_noalloc_substep_with_a_rope(cuda_lib):
+    """The rope's frames are shifted with the particle and FEM frames."""
+    env = SS.rope_under_pad()
+    cv = SS.control_velocity(env.sensors[0], scale=0.02, down=-0.05)
+    ref = _world(env, cv)
+    ref.substep(0)
+    ref.substep(1)
+    w = _world(env, cv)
+    bare = N.DtWorld.from_buffer_copy(w.w)
+    for name in SCRATCH:
+        setattr(bare, name, None)
+    stream = torch.cuda.current_stream().cuda_stream
+    for f in (0, 1):
+        rc = w.lib.dt_substep_fwd_noalloc(ctypes.byref(bare), f, stream)
+        assert rc == 0, N.ERRORS.get(rc, rc)
+    torch.cuda.synchronize()
+    assert w.error_word() == 0
+    for f in (1, 2):
+        a, b = ref.rope_state(f, 0), w.rope_state(f, 0)
+        assert SS.rel_err(b["pos"].cpu().numpy(), a["pos"].cpu().numpy()) < 1e-6, f
+        assert SS.rel_err(b["vel"].cpu().numpy(), a["vel"].cpu().numpy()) < 1e-4, f
