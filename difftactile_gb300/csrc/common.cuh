@@ -296,6 +296,17 @@ DT_DEV void pdl_entry() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
+// Opt a kernel into more than 48 KB of dynamic shared memory on the current device (the attribute
+// is per device; `cache` remembers the largest size already set on each of up to 64 devices).
+inline cudaError_t ensure_smem(const void* fn, size_t bytes, size_t (&cache)[64]) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (bytes <= cache[dev]) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cache[dev] = bytes;
+  return e;
+}
 inline int& pdl_flag() {
   static int on = 1;
   return on;

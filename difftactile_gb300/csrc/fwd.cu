@@ -424,12 +424,8 @@ int launch_l2(const dt_world* w, int f, cudaStream_t st) {
   if (nb <= 0) return DT_OK;
   const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
   const size_t smem = stage_bytes(cap);
-  static size_t configured = 0;
-  if (smem > 48 * 1024 && smem > configured) {
-    if (cudaFuncSetAttribute(k_fwd_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return DT_ERR_LAUNCH;
-    configured = smem;
-  }
+  static size_t configured[64] = {};
+  if (ensure_smem((const void*)k_fwd_grid, smem, configured) != cudaSuccess) return DT_ERR_LAUNCH;
   return launch_k(k_fwd_grid, nb, GRID_NT, smem, st, *w, f, cap) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
 int launch_l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {

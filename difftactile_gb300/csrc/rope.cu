@@ -288,13 +288,8 @@ __global__ void __launch_bounds__(128) k_rope_contact_bwd(dt_world w, int f) {
   *av = make_float4(b.x + vb.x, b.y + vb.y, b.z + vb.z, b.w);
 }
 
-int set_smem(const void* fn, size_t bytes, size_t* configured) {
-  if (bytes > 48 * 1024 && bytes > *configured) {
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
-      return DT_ERR_CAPACITY;
-    *configured = bytes;
-  }
-  return DT_OK;
+int set_smem(const void* fn, size_t bytes, size_t (&configured)[64]) {
+  return ensure_smem(fn, bytes, configured) == cudaSuccess ? DT_OK : DT_ERR_CAPACITY;
 }
 
 constexpr int SMEM_CENT_MAX = 12288;
@@ -312,9 +307,9 @@ int dt_rope_update(const dt_world* w, int f, cudaStream_t stream) {
   int rc;
   const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
   const size_t smem = stage_bytes(cap);
-  static size_t conf_c = 0, conf_s = 0;
-  if ((rc = set_smem((const void*)k_rope_contact, smem, &conf_c))) return rc;
-  if ((rc = set_smem((const void*)k_rope_solve, solve_smem, &conf_s))) return rc;
+  static size_t conf_c[64] = {}, conf_s[64] = {};
+  if ((rc = set_smem((const void*)k_rope_contact, smem, conf_c))) return rc;
+  if ((rc = set_smem((const void*)k_rope_solve, solve_smem, conf_s))) return rc;
   if (w->rope_blocks > 0 && launch_k(k_rope_contact, w->rope_blocks, RC_NT, smem, stream, *w, f, cap) != cudaSuccess)
     return DT_ERR_LAUNCH;
   return launch_k(k_rope_solve, w->n_ropes, RS_NT, solve_smem, stream, *w, f) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
@@ -326,9 +321,9 @@ int dt_rope_update_bwd(const dt_world* w, int f, cudaStream_t stream) {
   if (!w->ropes || !w->r_adj || !w->r_extb || w->max_rope_n <= 0) return DT_ERR_ARG;
   const size_t smem = (size_t)4 * w->max_rope_n * sizeof(float4);
   if (smem > 227 * 1024) return DT_ERR_CAPACITY;
-  static size_t conf = 0;
+  static size_t conf[64] = {};
   int rc;
-  if ((rc = set_smem((const void*)k_rope_solve_bwd, smem, &conf))) return rc;
+  if ((rc = set_smem((const void*)k_rope_solve_bwd, smem, conf))) return rc;
   if (launch_k(k_rope_solve_bwd, w->n_ropes, RS_NT, smem, stream, *w, f) != cudaSuccess) return DT_ERR_LAUNCH;
   return launch_k(k_rope_contact_bwd, cdiv(w->n_rope_particles, 128), 128, 0, stream, *w, f) == cudaSuccess
              ? DT_OK
