@@ -24,6 +24,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FALLBACK_HBM_GBS = 6800.0
+PROBE_EVERY = 10  # substeps between the timed region's event-timed launches of the dominant kernel
 
 
 def parse():
@@ -38,11 +39,17 @@ def parse():
                     help="27-node scatter strategy (default: the library's)")
     ap.add_argument("--no-pdl", action="store_true", help="launch the substep kernels without programmatic "
                     "dependent launch")
+    ap.add_argument("--p-block", type=int, default=None, choices=[64, 128, 256],
+                    help="threads per CTA of the particle launches")
+    ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shape instead of "
+                    "the autotuner's choice (also implied by --scatter, --no-pdl or --p-block)")
     ap.add_argument("--plain", type=int, default=0,
                     help="also time the first K environments one World each (one scene per launch "
                     "sequence) and report the batched / plain ratio")
     ap.add_argument("--no-svd-tape", action="store_true", help="the adjoint recomputes the SVD instead of "
                     "reading the forward's from the tape")
+    ap.add_argument("--no-graph", action="store_true", help="launch every substep from the host instead of "
+                    "replaying the rollout's recorded CUDA graphs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -145,8 +152,11 @@ def run_ours(args):
     kw = {} if args.scatter is None else {"scatter_mode": {"tile": 0, "global": 1, "warp": 2}[args.scatter]}
     if args.no_svd_tape:
         kw["svd_tape"] = False
+    if args.p_block is not None:
+        kw["p_block"] = args.p_block
     w, traj = cfg.build(dev, **kw)
     w.lib.dt_set_pdl(0 if args.no_pdl else 1)
+    tune_launch = not (args.no_tune or args.scatter or args.no_pdl or args.p_block)
     acts = torch.as_tensor(cfg.actions, dtype=torch.float64, device=dev)
     t = w.t
     init = [t["p_state"][0].clone(), t["v_pos"][0].clone(), t["v_vel"][0].clone(), t["v_vpos"][0].clone()]
@@ -165,9 +175,19 @@ def run_ours(args):
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    # ---- per-kernel breakdown (untimed): probe each launch over one full iteration ----
+    # ---- launch shape (untimed): the autotuner times every candidate on one mid-rollout substep ----
     iteration()
     torch.cuda.synchronize()
+    tuned = None
+    if tune_launch:
+        from difftactile_gb300 import autotune
+        f_mid = traj.f_end // 2 if traj.full else traj.S // 2
+        tuned = autotune.tune_substep(w, frame=f_mid)
+        tuned["frame"] = f_mid
+        iteration()
+        torch.cuda.synchronize()
+
+    # ---- per-kernel breakdown (untimed, launched from the host): probe each launch over one iteration ----
     breakdown = {}
     for key in NAMES:
         w.set_probe(*key)
@@ -178,6 +198,12 @@ def run_ours(args):
     tot = sum(ms * n for ms, n in breakdown.values())
     dom = max(breakdown, key=lambda k: breakdown[k][0] * breakdown[k][1])
 
+    # the timed iterations carry CUDA-event pairs around every PROBE_EVERY-th launch of the dominant
+    # kernel; with graphs the first warm-up iteration records the rollout (events included) and the
+    # rest replay it
+    w.set_probe(*dom, every=PROBE_EVERY)
+    traj.graph = not args.no_graph
+    traj.reset_graphs()
     for _ in range(max(args.warmup, 0)):
         iteration()
     torch.cuda.synchronize()
@@ -186,9 +212,9 @@ def run_ours(args):
 
     # ---- timed region ----
     clocks = Clocks(local)
-    w.set_probe(*dom)
     traj.launches = 0
-    times = []
+    times, dom_acc = [], []
+    w.probe_events.clear()  # host-recorded pairs of the warm-up; graph-recorded pairs are re-recorded
     for _ in range(args.steps):
         flush.zero_()  # L2 flush between timed iterations (256 MiB > 129 MB L2)
         torch.cuda.synchronize()
@@ -200,9 +226,14 @@ def run_ours(args):
         torch.cuda.synchronize()
         barrier()
         times.append(e0.elapsed_time(e1))
-    dom_ms, dom_n = w.probe_ms()
-    w.set_probe(None)
+        dom_acc.append(w.probe_ms())  # this iteration's launches of the dominant kernel
+        if not traj.graph:
+            w.probe_events.clear()
+    dom_n = sum(n for _, n in dom_acc)
+    dom_ms = sum(m * n for m, n in dom_acc) / max(dom_n, 1)
     clk = clocks.stop()
+    w.set_probe(None)
+    traj.reset_graphs()  # the end-to-end iterations record their own graphs, without the event pairs
     launches_per_iter = traj.launches // max(args.steps, 1) + 2  # + loss readout/adjoint seeds
     ms = sum(times) / len(times)
     if world_size > 1:
@@ -231,7 +262,10 @@ def run_ours(args):
                       "fem_tets": w.n_tets, "fem_nodes": w.n_verts, "surface_tris": w.n_tris,
                       "checkpoint_every": cfg.ckpt_every, "tape_blocks": w.tape_blocks,
                       "scatter": ["tile", "global", "warp"][w.w.scatter_mode],
-                      "programmatic_dependent_launch": not args.no_pdl,
+                      "p_block": int(w.w.p_block),
+                      "programmatic_dependent_launch": bool(w.lib.dt_get_pdl()),
+                      "launch_shape": "autotuned" if tuned else "fixed",
+                      "cuda_graph": traj.graph,
                       "svd_tape": w.w.p_svd is not None,
                       "active_blocks_mean": cnt, "active_blocks_max": cnt_max, "l2": "flushed between timed iterations (256 MiB write)",
                       "parallelism": f"replicas x{world_size}"},
@@ -239,12 +273,16 @@ def run_ours(args):
            "roofline": {"kernel": NAMES[dom], "bound": "hbm", "achieved": achieved, "peak": peak,
                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": NCU_TRAFFIC.get(cfg.name, {}).get(NAMES[dom]),
-                        "algorithmic_bytes_per_launch": ab, "launch_ms": dom_ms, "launches_timed": dom_n},
+                        "algorithmic_bytes_per_launch": ab, "launch_ms": dom_ms, "launches_timed": dom_n,
+                        "timed_every_nth_launch": PROBE_EVERY},
            "kernel_breakdown": {NAMES[k]: {"ms_per_launch": v[0], "launches": v[1],
                                            "share": v[0] * v[1] / tot} for k, v in breakdown.items()},
            "loss": float(loss.item()), "grad_norm": float(g.norm().item())}
     if clk:
         out["clocks"] = clk
+    if tuned:
+        out["autotune"] = {"frame": tuned["frame"], "best": tuned["best"],
+                           "substep_ms": {k: round(v, 4) for k, v in tuned["ms"].items()}}
 
     # ---- end to end through the public API with host buffers ----
     if not args.no_e2e:
@@ -279,7 +317,7 @@ def run_ours(args):
                       "h2d_bytes_per_step": int(h_act.numel() * 4 + h_x.numel() * 4 + h_v.numel() * 4),
                       "d2h_bytes_per_step": int(res.numel() * 8)}
     if args.plain > 0:
-        out["plain"] = time_plain(cfg, args, dev, flush)
+        out["plain"] = time_plain(cfg, args, dev, flush, tune_launch)
         out["batched_over_plain"] = value / out["plain"]["value"]
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(cfg, threads=os.cpu_count() or 1)
@@ -289,7 +327,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def time_plain(cfg, args, dev, flush):
+def time_plain(cfg, args, dev, flush, tune_launch):
     """Each of the first K environments in a World of its own, stepped one after the other with the
     same actions (the one-scene-per-launch path); aggregate particle-substeps/s of the sample."""
     import torch
@@ -303,6 +341,12 @@ def time_plain(cfg, args, dev, flush):
                      tuple((0, lay, tg) for s, lay, tg in cfg.loss_terms if s == e), cfg.ckpt_every, cfg.tape_blocks)
         w, traj = sub.build(dev)
         acts = torch.as_tensor(sub.actions, dtype=torch.float64, device=dev)
+        traj.forward(acts)
+        traj.backward()
+        if tune_launch:  # each single-environment World gets its own launch shape
+            from difftactile_gb300 import autotune
+            autotune.tune_substep(w, frame=traj.f_end // 2 if traj.full else traj.S // 2)
+        traj.graph = not args.no_graph
         for _ in range(max(args.warmup, 1)):
             traj.forward(acts)
             traj.backward()

@@ -73,7 +73,7 @@ class DtWorld(C.Structure):
                 + [("dt", C.c_float), ("grad_clip", C.c_float), ("svd_sweeps", C.c_int),
                    ("svd_grad_mode", C.c_int), ("max_sensor_tris", C.c_int), ("scatter_mode", C.c_int)]
                 + [(n, _P) for n in ROPE_PTR_FIELDS] + [(n, C.c_int) for n in ROPE_INT_FIELDS]
-                + [("p_svd", _P)])
+                + [("p_svd", _P), ("p_block", C.c_int)])
 
 
 # entry points: name -> (restype, argtypes)
@@ -86,6 +86,7 @@ SIGNATURES = {
     "dt_sizeof_material": (C.c_size_t, []),
     "dt_sizeof_rope": (C.c_size_t, []),
     "dt_set_pdl": (C.c_int, [C.c_int]),
+    "dt_get_pdl": (C.c_int, []),
     "dt_step_begin": (C.c_int, [_W, _P]),
     "dt_substep_fwd": (C.c_int, [_W, C.c_int, _P]),
     "dt_substep_fwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),
@@ -156,7 +157,7 @@ def load(path: str | None = None):
         n = getattr(lib, f"dt_sizeof_{name}")()
         if n != C.sizeof(cls):
             raise ImportError(f"ABI mismatch: sizeof(dt_{name}) = {n} in the library, {C.sizeof(cls)} in ctypes")
-    if lib.dt_abi_version() != 1:
+    if lib.dt_abi_version() != 2:
         raise ImportError("ABI version mismatch")
     _lib = lib
     return lib

@@ -1,0 +1,143 @@
+"""Launch-shape autotuner for a World.
+
+The substep's particle-role launches can be shaped three ways, and which is fastest depends on the
+scene (particle count and density, how many environments share the launch):
+  scatter   how P2G and the G2P adjoint accumulate into the grid (dt_world.scatter_mode): a warp
+            segmented reduction before one RED per run and node ("warp"), one RED per particle and
+            node ("global"), or a shared-memory gather tile per CTA ("tile", 128 threads only);
+  p_block   threads per CTA of the particle / tet / vertex launches (dt_world.p_block): 64, 128, 256;
+  pdl       programmatic dependent launch of the substep kernels (dt_set_pdl, library-wide).
+
+``tune_substep`` times every candidate on one forward + backward substep of the world at a chosen
+frame (CUDA events on the launching stream, median of ``reps`` after ``warmup``) and applies the
+fastest; ``tune`` does the same for any callable (e.g. a whole rollout).  Results are kept per
+device and world shape, in memory and optionally in a JSON file, so a second world of the same
+shape skips the measurement.  Recorded CUDA graphs hold the launch shape they were recorded with:
+re-record them (Trajectory.reset_graphs) after tuning.
+"""
+from __future__ import annotations
+
+import json
+import os
+import statistics
+
+import torch
+
+SCATTERS = {"tile": 0, "global": 1, "warp": 2}
+DEFAULT = {"scatter": "warp", "p_block": 128, "pdl": 1}
+
+_cache: dict[str, dict] = {}
+
+
+def candidates(scatters=("warp", "global", "tile"), p_blocks=(64, 128, 256), pdl=(1, 0)):
+    out = []
+    for s in scatters:
+        for b in (p_blocks if s != "tile" else (128,)):
+            for p in pdl:
+                out.append({"scatter": s, "p_block": int(b), "pdl": int(p)})
+    return out
+
+
+def apply(world, cfg: dict):
+    """Set ``cfg`` (scatter, p_block, pdl) on ``world`` (and the library's PDL switch)."""
+    world.w.scatter_mode = SCATTERS[cfg["scatter"]]
+    world.w.p_block = int(cfg["p_block"])
+    world.lib.dt_set_pdl(int(cfg["pdl"]))  # returns the previous setting
+
+
+def current(world) -> dict:
+    inv = {v: k for k, v in SCATTERS.items()}
+    return {"scatter": inv.get(int(world.w.scatter_mode), "warp"), "p_block": int(world.w.p_block) or 128,
+            "pdl": int(world.lib.dt_get_pdl())}
+
+
+def signature(world, tag: str = "") -> str:
+    name = torch.cuda.get_device_name(world.device)
+    return "|".join(str(x) for x in (name, tag, world.n_envs, world.n_particles, world.n_verts, world.n_tets,
+                                     world.n_tris, world.n_blocks, world.n_rope_particles))
+
+
+def _load(path):
+    if path and os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh)
+    return {}
+
+
+def _store(path, key, entry):
+    if not path:
+        return
+    data = _load(path)
+    data[key] = entry
+    tmp = path + ".tmp"
+    with open(tmp, "w") as fh:
+        json.dump(data, fh, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def _time(run, reps, warmup):
+    for _ in range(warmup):
+        run()
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run()
+        e1.record()
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def tune(world, run, cands=None, reps: int = 5, warmup: int = 1, tag: str = "", cache_path: str | None = None,
+         use_cache: bool = True, prepare=None) -> dict:
+    """Time ``run()`` under every candidate launch shape (``prepare()``, untimed, before each
+    candidate's runs), apply the fastest and return {"best": cfg, "ms": {label: median ms}, "cached": bool}."""
+    key = signature(world, tag)
+    if use_cache:
+        hit = _cache.get(key) or _load(cache_path).get(key)
+        if hit is not None:
+            apply(world, hit["best"])
+            _cache[key] = hit
+            return dict(hit, cached=True)
+    cands = cands or candidates()
+    times = {}
+    best, best_ms = None, float("inf")
+    for c in cands:
+        apply(world, c)
+        if prepare is not None:
+            prepare()
+        ms = _time(run, reps, warmup)
+        if world.error_word():
+            raise RuntimeError(f"device error word {world.error_word()} while tuning {c}")
+        times[label(c)] = ms
+        if ms < best_ms:
+            best, best_ms = c, ms
+    apply(world, best)
+    entry = {"best": best, "ms": times}
+    _cache[key] = entry
+    _store(cache_path, key, entry)
+    return dict(entry, cached=False)
+
+
+def tune_substep(world, frame: int = 0, **kw) -> dict:
+    """Tune on one forward substep ``frame`` -> ``frame`` + 1 and its adjoint.  The frame's state
+    must be valid (e.g. after a rollout); frame + 1, the grid tape of ``frame``, the tape counters
+    of every frame and the adjoint buffers are overwritten."""
+    if not 0 <= frame < world.n_frames - 1:
+        raise ValueError(f"frame {frame} outside [0, {world.n_frames - 1})")
+
+    def run():  # the adjoint buffers are cleared once per candidate; repeated sweeps only accumulate
+        world.step_begin()
+        world.substep(frame)
+        world.substeps_bwd(frame + 1, frame)
+
+    kw.setdefault("prepare", world.adj_clear)
+    kw.setdefault("tag", "substep")
+    kw.setdefault("reps", 15)
+    kw.setdefault("warmup", 2)
+    return tune(world, run, **kw)
+
+
+def label(c: dict) -> str:
+    return f"{c['scatter']}/{c['p_block']}/{'pdl' if c['pdl'] else 'nopdl'}"

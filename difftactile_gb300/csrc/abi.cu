@@ -80,6 +80,8 @@ int dt_set_pdl(int on) {
   return old;
 }
 
+int dt_get_pdl(void) { return pdl_flag(); }
+
 int dt_step_begin(const dt_world* w, cudaStream_t stream) {
   if (!w || w->n_frames < 2) return DT_ERR_ARG;
   int n = w->n_frames > w->n_verts ? w->n_frames : w->n_verts;

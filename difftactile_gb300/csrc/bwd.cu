@@ -16,7 +16,7 @@
 
 namespace {
 
-constexpr int NT = 128;
+constexpr int NT_TILE = 128;  // threads per CTA of the G2P adjoint with the TILE scatter
 constexpr int GRID_NT = 64;
 constexpr int TILE_MAX = 1728;  // shared scatter tile capacity in nodes (12^3)
 
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(GRID_NT) k_bwd_restore(dt_world w, int f) {
 // G2P adjoint of one CTA's particles: the position adjoint needs the grid velocities (a gather);
 // the grid-velocity adjoint W (vn_bar + 4 inv_dx C_bar (o - fx)) = W (q + o . c) is a 27-node
 // scatter, privatised through the shared-memory tile.
-template <int MODE>
+template <int MODE, int NT>
 __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile, int* sh) {
   const int p = chunk * NT + threadIdx.x;
   const bool valid = p < w.n_particles;
@@ -214,14 +214,14 @@ __device__ void integrate_bwd(const dt_world& w, int f, int i) {
   if (S.carry) *cvb_n = v3to4(cvbn);
 }
 
-template <int MODE>
+template <int MODE, int NT>
 __global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
   pdl_entry();
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
-    g2p_bwd_chunk<MODE>(w, f, b, tile, sh);
+    g2p_bwd_chunk<MODE, NT>(w, f, b, tile, sh);
     return;
   }
   b -= nb_p;
@@ -608,7 +608,9 @@ __device__ void fem_tet_bwd(const dt_world& w, int f, int t) {
 
 // nb_r > 0: the last nb_r CTAs restore frame f - 1's grid velocities for the next backward substep
 // (only stage 1 reads g_vout, so this overlaps stage 3 of frame f)
-__global__ void __launch_bounds__(NT, 4) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v, int nb_r) {
+template <int NT>  // 512 / NT CTAs per SM: 128 registers per thread
+__global__ void __launch_bounds__(NT, 512 / NT) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v,
+                                                             int nb_r) {
   pdl_entry();
   int b = blockIdx.x;
   if (b < nb_p) {
@@ -658,51 +660,79 @@ __global__ void __launch_bounds__(NT, 4) k_bwd_p2g_fem(dt_world w, int f, int nb
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
 
+// stage 1: G2P adjoint (particles) + integration adjoint (vertices)
+template <int MODE, int NT>
+cudaError_t b1(const dt_world* w, int f, cudaStream_t stream) {
+  const int nb_p = cdiv(w->n_particles, NT), nb_v = cdiv(w->n_verts, NT);
+  if (nb_p + nb_v == 0) return cudaSuccess;
+  const size_t smem = MODE == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0;
+  return launch_k(k_bwd_g2p_fem<MODE, NT>, nb_p + nb_v, NT, smem, stream, *w, f, nb_p, nb_v);
+}
+
+// stage 3: P2G / F adjoint (particles), tet adjoint, vertex hand-over; with `restore`, the last
+// CTAs also restore frame f - 1's grid velocities
+template <int NT>
+cudaError_t b3_nt(const dt_world* w, int f, bool restore, cudaStream_t stream) {
+  const int nb_p = cdiv(w->n_particles, NT), nb_v = cdiv(w->n_verts, NT), nb_t = cdiv(w->n_tets, NT);
+  const int per = NT / 64;  // 64-node blocks a restoring CTA copies per pass
+  const int nb_r = !restore ? 0 : (w->n_blocks < 152 * 4 * per ? cdiv(w->n_blocks, per) : 152 * 4);
+  if (nb_p + nb_t + nb_v + nb_r == 0) return cudaSuccess;
+  return launch_k(k_bwd_p2g_fem<NT>, nb_p + nb_t + nb_v + nb_r, NT, 0, stream, *w, f, nb_p, nb_t, nb_v, nb_r);
+}
+cudaError_t b3(const dt_world* w, int f, bool restore, cudaStream_t stream) {
+  switch (particle_block(w)) {
+    case 64: return b3_nt<64>(w, f, restore, stream);
+    case 256: return b3_nt<256>(w, f, restore, stream);
+    default: return b3_nt<128>(w, f, restore, stream);
+  }
+}
+
 }  // namespace
 
 extern "C" {
 
 int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t stream) {
   if (!w || f < 0 || f + 1 >= w->n_frames || stage < 0 || stage > 3) return DT_ERR_ARG;
-  const int ng = w->n_blocks < 152 * 16 ? w->n_blocks : 152 * 16;
-  const int nb_p = cdiv(w->n_particles, NT), nb_v = cdiv(w->n_verts, NT), nb_t = cdiv(w->n_tets, NT);
   cudaError_t e = cudaSuccess;
   switch (stage) {
-    case 0:
+    case 0: {
+      const int ng = w->n_blocks < 152 * 16 ? w->n_blocks : 152 * 16;
       if (ng > 0) e = launch_k(k_bwd_restore, ng, GRID_NT, 0, stream, *w, f);
       break;
+    }
     case 1:
-      if (nb_p + nb_v == 0) break;
-      if (w->scatter_mode == DT_SCATTER_TILE)
-        e = launch_k(k_bwd_g2p_fem<DT_SCATTER_TILE>, nb_p + nb_v, NT, 25 * NT * sizeof(float), stream, *w, f, nb_p,
-                     nb_v);
-      else if (w->scatter_mode == DT_SCATTER_GLOBAL)
-        e = launch_k(k_bwd_g2p_fem<DT_SCATTER_GLOBAL>, nb_p + nb_v, NT, 0, stream, *w, f, nb_p, nb_v);
-      else
-        e = launch_k(k_bwd_g2p_fem<DT_SCATTER_WARP>, nb_p + nb_v, NT, 0, stream, *w, f, nb_p, nb_v);
+      if (w->scatter_mode == DT_SCATTER_TILE) {
+        e = b1<DT_SCATTER_TILE, NT_TILE>(w, f, stream);
+      } else {
+        switch (particle_block(w)) {
+          case 64: e = w->scatter_mode == DT_SCATTER_GLOBAL ? b1<DT_SCATTER_GLOBAL, 64>(w, f, stream)
+                                                              : b1<DT_SCATTER_WARP, 64>(w, f, stream); break;
+          case 256: e = w->scatter_mode == DT_SCATTER_GLOBAL ? b1<DT_SCATTER_GLOBAL, 256>(w, f, stream)
+                                                               : b1<DT_SCATTER_WARP, 256>(w, f, stream); break;
+          default: e = w->scatter_mode == DT_SCATTER_GLOBAL ? b1<DT_SCATTER_GLOBAL, 128>(w, f, stream)
+                                                              : b1<DT_SCATTER_WARP, 128>(w, f, stream);
+        }
+      }
       break;
-    case 2:
+    case 2: {
+      const int ng = w->n_blocks < 152 * 16 ? w->n_blocks : 152 * 16;
       if (ng > 0) e = launch_k(k_bwd_grid, ng, GRID_NT, 0, stream, *w, f);
       if (e != cudaSuccess) return DT_ERR_LAUNCH;
       return dt_rope_update_bwd(w, f, stream);
+    }
     default:
-      if (nb_p + nb_t + nb_v)
-        e = launch_k(k_bwd_p2g_fem, nb_p + nb_t + nb_v, NT, 0, stream, *w, f, nb_p, nb_t, nb_v, 0);
+      e = b3(w, f, false, stream);
   }
   return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
 
 int dt_substeps_bwd(const dt_world* w, int f_hi, int f_lo, cudaStream_t stream) {
   if (!w || f_lo < 0 || f_hi <= f_lo || f_hi >= w->n_frames) return DT_ERR_ARG;
-  const int nb_p = cdiv(w->n_particles, NT), nb_v = cdiv(w->n_verts, NT), nb_t = cdiv(w->n_tets, NT);
-  const int nb_r = w->n_blocks < 152 * 4 ? cdiv(w->n_blocks, NT / 64) : 152 * 4;
   int rc = dt_substep_bwd_stage(w, f_hi - 1, 0, stream);
   for (int f = f_hi - 1; f >= f_lo && !rc; --f) {
     if ((rc = dt_substep_bwd_stage(w, f, 1, stream)) || (rc = dt_substep_bwd_stage(w, f, 2, stream))) break;
-    const int r = f > f_lo ? nb_r : 0;  // the next (lower) frame's restore rides along
-    if (nb_p + nb_t + nb_v + r &&
-        launch_k(k_bwd_p2g_fem, nb_p + nb_t + nb_v + r, NT, 0, stream, *w, f, nb_p, nb_t, nb_v, r) != cudaSuccess)
-      rc = DT_ERR_LAUNCH;
+    // the next (lower) frame's restore rides along
+    if (b3(w, f, f > f_lo, stream) != cudaSuccess) rc = DT_ERR_LAUNCH;
   }
   return rc;
 }

@@ -296,6 +296,9 @@ DT_DEV void pdl_entry() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
+// threads per CTA of the particle / tet / vertex launches (dt_world.p_block)
+inline int particle_block(const dt_world* w) { return (w->p_block == 64 || w->p_block == 256) ? w->p_block : 128; }
+
 // Opt a kernel into more than 48 KB of dynamic shared memory on the current device (the attribute
 // is per device; `cache` remembers the largest size already set on each of up to 64 devices).
 inline cudaError_t ensure_smem(const void* fn, size_t bytes, size_t (&cache)[64]) {

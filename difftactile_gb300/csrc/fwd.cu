@@ -22,7 +22,7 @@
 
 namespace {
 
-constexpr int NT = 128;           // threads per CTA for particle / tet / vertex roles
+constexpr int NT_TILE = 128;      // threads per CTA of the particle roles with the TILE scatter
 constexpr int TILE_MAX = 1728;    // shared P2G tile capacity in nodes (12^3), 27 KB of float4
 constexpr int GRID_LPN = 8;                 // lanes per node in the grid kernel's contact search
 constexpr int GRID_NT = 64 * GRID_LPN;     // one 4x4x4 node block per CTA
@@ -39,7 +39,7 @@ __device__ void mark_block(const dt_world& w, int f, int b) {
 // P2G of one CTA's particles (mpm_elastic.py:176-208 / mpm_plastic.py:222-256 / multi_obj.py:228-252):
 // contribution at node base + o is W_o (p_mass v + A (o - fx) dx) = W_o (b + o . (dx A)), with
 // A = stress + p_mass C and b = p_mass v - dx A fx precomputed once per particle.
-template <int MODE>
+template <int MODE, int NT>
 __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int* sh) {
   const int p = chunk * NT + threadIdx.x;
   const bool valid = p < w.n_particles;
@@ -182,14 +182,14 @@ __device__ void tri_centroid(const dt_world& w, int f, int t) {
   reinterpret_cast<float4*>(w.tri_cent)[t] = o;
 }
 
-template <int MODE>
+template <int MODE, int NT>
 __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
   pdl_entry();
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
-    p2g_chunk<MODE>(w, f, b, tile, sh);
+    p2g_chunk<MODE, NT>(w, f, b, tile, sh);
     return;
   }
   b -= nb_p;
@@ -377,6 +377,7 @@ __device__ void fem_integrate(const dt_world& w, int f, int i) {
   vframe(w.v_ext, w, f + 1)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+template <int NT>
 __global__ void __launch_bounds__(NT) k_fwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
   pdl_entry();
   int b = blockIdx.x;
@@ -400,22 +401,29 @@ inline int check(const dt_world* w, int f) {
 }
 inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
 
+template <int MODE, int NT>
+cudaError_t l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
+  const int nb_p = parts ? cdiv(w->n_particles, NT) : 0;
+  const int nb_t = fem ? cdiv(w->n_tets, NT) : 0;
+  const int nb_f = fem ? cdiv(w->n_tris, NT) : 0;
+  if (nb_p + nb_t + nb_f == 0) return cudaSuccess;
+  const size_t smem = MODE == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0;
+  return launch_k(k_fwd_p2g_fem<MODE, NT>, nb_p + nb_t + nb_f, NT, smem, st, *w, f, nb_p, nb_t, nb_f);
+}
+template <int MODE>
+cudaError_t l1_nt(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
+  switch (particle_block(w)) {
+    case 64: return l1<MODE, 64>(w, f, parts, fem, st);
+    case 256: return l1<MODE, 256>(w, f, parts, fem, st);
+    default: return l1<MODE, 128>(w, f, parts, fem, st);
+  }
+}
 int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
-  int nb_p = parts ? cdiv(w->n_particles, NT) : 0;
-  int nb_t = fem ? cdiv(w->n_tets, NT) : 0;
-  int nb_f = fem ? cdiv(w->n_tris, NT) : 0;
-  int tot = nb_p + nb_t + nb_f;
-  if (tot == 0) return DT_OK;
   cudaError_t e;
   switch (w->scatter_mode) {
-    case DT_SCATTER_TILE:
-      e = launch_k(k_fwd_p2g_fem<DT_SCATTER_TILE>, tot, NT, 25 * NT * sizeof(float), st, *w, f, nb_p, nb_t, nb_f);
-      break;
-    case DT_SCATTER_GLOBAL:
-      e = launch_k(k_fwd_p2g_fem<DT_SCATTER_GLOBAL>, tot, NT, 0, st, *w, f, nb_p, nb_t, nb_f);
-      break;
-    default:
-      e = launch_k(k_fwd_p2g_fem<DT_SCATTER_WARP>, tot, NT, 0, st, *w, f, nb_p, nb_t, nb_f);
+    case DT_SCATTER_TILE: e = l1<DT_SCATTER_TILE, NT_TILE>(w, f, parts, fem, st); break;
+    case DT_SCATTER_GLOBAL: e = l1_nt<DT_SCATTER_GLOBAL>(w, f, parts, fem, st); break;
+    default: e = l1_nt<DT_SCATTER_WARP>(w, f, parts, fem, st);
   }
   return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
@@ -428,11 +436,21 @@ int launch_l2(const dt_world* w, int f, cudaStream_t st) {
   if (ensure_smem((const void*)k_fwd_grid, smem, configured) != cudaSuccess) return DT_ERR_LAUNCH;
   return launch_k(k_fwd_grid, nb, GRID_NT, smem, st, *w, f, cap) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
+template <int NT>
+cudaError_t l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
+  const int nb_p = parts ? cdiv(w->n_particles, NT) : 0;
+  const int nb_v = fem ? cdiv(w->n_verts, NT) : 0;
+  if (nb_p + nb_v == 0) return cudaSuccess;
+  return launch_k(k_fwd_g2p_fem<NT>, nb_p + nb_v, NT, 0, st, *w, f, nb_p, nb_v);
+}
 int launch_l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
-  int nb_p = parts ? cdiv(w->n_particles, NT) : 0;
-  int nb_v = fem ? cdiv(w->n_verts, NT) : 0;
-  if (nb_p + nb_v == 0) return DT_OK;
-  return launch_k(k_fwd_g2p_fem, nb_p + nb_v, NT, 0, st, *w, f, nb_p, nb_v) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
+  cudaError_t e;
+  switch (particle_block(w)) {
+    case 64: e = l3<64>(w, f, parts, fem, st); break;
+    case 256: e = l3<256>(w, f, parts, fem, st); break;
+    default: e = l3<128>(w, f, parts, fem, st);
+  }
+  return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
 
 }  // namespace

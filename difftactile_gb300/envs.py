@@ -26,8 +26,12 @@ from .world import World
 
 class BatchedTactileEnv:
     def __init__(self, envs, substeps: int = 20, dt: float = 1e-4, time_limit: int = 100, n_obs_nodes: int = 32,
-                 targets=None, reward_scale: float = 1.0, device="cuda", seed: int = 0):
+                 targets=None, reward_scale: float = 1.0, device="cuda", seed: int = 0, graph: bool = False):
         self.w = World(envs, n_frames=substeps + 1, dt=dt, device=device)
+        # graph: the first step runs eagerly and records its launches (control velocities, S substeps,
+        # frame copy) as one CUDA graph that later steps replay
+        self.graph = bool(graph)
+        self._graph = None
         w = self.w
         self.n_envs = len(envs)
         self.S = int(substeps)
@@ -80,6 +84,15 @@ class BatchedTactileEnv:
         self.time_step = 0
         return self.get_observations(), {}
 
+    def _advance(self):
+        w = self.w
+        N.check(w.lib.dt_pose_control_vel_all(w.wp, self.Ab.data_ptr(), self.inv_T, 0, self.S + 1, w.stream),
+                "pose cv")
+        w.step_begin()
+        for f in range(self.S):
+            w.substep(f)
+        w.copy_frame(self.S, 0)
+
     def step(self, actions):
         """actions [n_envs, 6] (d_pos, d_ori in degrees per unit time) -> (obs, rewards, dones,
         truncated, infos), all per environment (device tensors)."""
@@ -89,12 +102,15 @@ class BatchedTactileEnv:
         M = eul2mat_zyx(a[:, 3:6] * w.dt * self.S, a[:, 0:3] * w.dt * self.S)
         D = self.TW[s] @ M @ self.TW_inv[s]
         self.Ab[s] = D[:, :3, :].reshape(self.n_envs, 12).float()
-        N.check(w.lib.dt_pose_control_vel_all(w.wp, self.Ab.data_ptr(), self.inv_T, 0, self.S + 1, w.stream),
-                "pose cv")
-        w.step_begin()
-        for f in range(self.S):
-            w.substep(f)
-        w.copy_frame(self.S, 0)
+        if self._graph is not None:
+            self._graph.replay()
+        else:
+            self._advance()
+            if self.graph:
+                torch.cuda.synchronize(w.device)
+                self._graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(self._graph):
+                    self._advance()
         self.time_step += 1
         obs = self.get_observations()
         com = obs[:, -3:]

@@ -57,10 +57,20 @@ class Trajectory:
 
     ``loss_terms``: list of (sensor, layer, target [nv,3]) marker-displacement terms read at the
     final frame.
+
+    ``graph``: the launch sequence of a forward (and of a backward) is the same on every call, so the
+    first call runs eagerly and then records it as a CUDA graph; later calls copy the new controls
+    into the recorded buffer and replay the graph (one launch from the host per rollout).  The
+    recorded graphs hold the world's and this trajectory's device pointers: state set through the
+    world's tensors in place is seen by the replays, reallocated tensors are not.
     """
 
-    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=()):
+    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=(), graph: bool = False):
         self.w = world
+        self.graph = bool(graph)
+        self._graphs = {}     # "fwd" / ("bwd", loss_bar) -> torch.cuda.CUDAGraph
+        self._graph_launches = {}
+        self._pool = None
         self.T = int(n_steps)
         self.full = int(ckpt_every) == 0
         if self.full:
@@ -146,11 +156,33 @@ class Trajectory:
         if copy_end and not self.full:
             w.copy_frame(self.S, 0)
 
-    def forward(self, actions: torch.Tensor) -> torch.Tensor:
-        """Roll out; returns the final-frame loss (device scalar)."""
-        self.actions = actions.detach().double().requires_grad_(True)
-        self.ctrl = self.controls(self.actions)
-        self.ctrl32 = self.ctrl.detach().float().contiguous()
+    # ------------------------------------------------------------------ CUDA graphs
+    def _capture(self, key, body):
+        """Record ``body``'s launches (already run once eagerly) as a CUDA graph under ``key``."""
+        if self.w.stream_override is not None:
+            raise RuntimeError("graph capture needs the world to launch on torch's current stream")
+        torch.cuda.synchronize(self.w.device)
+        g = torch.cuda.CUDAGraph()
+        n0 = self.launches
+        with torch.cuda.graph(g, pool=self._pool):
+            body()
+        self._graph_launches[key] = self.launches - n0
+        self.launches = n0
+        self._pool = g.pool()
+        self._graphs[key] = g
+
+    def _replay(self, key):
+        self._graphs[key].replay()
+        self.launches += self._graph_launches[key]
+
+    def reset_graphs(self):
+        """Drop the recorded graphs (after reallocating world tensors or changing launch settings)."""
+        self._graphs.clear()
+        self._graph_launches.clear()
+        if self.w.probe is not None:
+            self.w.probe_graph_events = []
+
+    def _forward_body(self):
         if self.full:
             self.w.step_begin()
             self.launches += 1
@@ -158,7 +190,22 @@ class Trajectory:
             if not self.full and t % self.k == 0:
                 self._save(self.ck_p, self.ck_v, self.ck_r, t // self.k)
             self._step(t)
-        return self.readout()
+        self.readout()
+
+    def forward(self, actions: torch.Tensor) -> torch.Tensor:
+        """Roll out; returns the final-frame loss (device scalar)."""
+        self.actions = actions.detach().double().requires_grad_(True)
+        self.ctrl = self.controls(self.actions)
+        c32 = self.ctrl.detach().float().contiguous()
+        if self.graph and "fwd" in self._graphs:
+            self.ctrl32.copy_(c32)
+            self._replay("fwd")
+            return self.loss
+        self.ctrl32 = c32
+        self._forward_body()
+        if self.graph:
+            self._capture("fwd", self._forward_body)
+        return self.loss
 
     def readout(self) -> torch.Tensor:
         w = self.w
@@ -179,13 +226,26 @@ class Trajectory:
     def backward(self, loss_bar: float = 1.0) -> torch.Tensor:
         """Adjoint sweep; returns d loss / d actions (float64, the actions' shape).  Initial-state
         adjoints are left in the world's frame-0 adjoint buffers, material grads in mat_adj."""
+        key = ("bwd", float(loss_bar))
+        if self.graph and key in self._graphs:
+            self._replay(key)
+        else:
+            if self.ctrl_bar is None or self.ctrl_bar.shape != self.ctrl32.shape:
+                self.ctrl_bar = torch.zeros_like(self.ctrl32)
+            self._backward_body(loss_bar)
+            if self.graph:
+                self._capture(key, lambda: self._backward_body(loss_bar))
+        (g,) = torch.autograd.grad(self.ctrl, self.actions, self.ctrl_bar.double())
+        return g
+
+    def _backward_body(self, loss_bar):
         w = self.w
         st = w.stream
         w.adj_clear()
         for s, layer, tg in self.loss_terms:
             N.check(w.lib.dt_marker_loss_bwd(w.wp, s, self.f_end, layer, tg.data_ptr(), float(loss_bar), st),
                     "loss bwd")
-        self.ctrl_bar = torch.zeros_like(self.ctrl32)
+        self.ctrl_bar.zero_()
         if self.full:
             for t in reversed(range(self.T)):
                 self._step_bwd(t)
@@ -205,16 +265,14 @@ class Trajectory:
                 if self.S & 1:  # frame 0's adjoint (buffer 0) is frame S's of the previous step (buffer 1)
                     for name in ("p_adj", "v_adj_pos", "v_adj_vel", "v_adj_vpos", "r_adj"):
                         w.t[name][1].copy_(w.t[name][0])
-        (g,) = torch.autograd.grad(self.ctrl, self.actions, self.ctrl_bar.double())
-        return g
 
 
 class PoseTrajectory(Trajectory):
     """Pose-controlled sensors (dome sensor, set_pose_control / set_control_vel): actions
     [T, n_sensors, 6] = (d_pos[3], d_ori[3] in degrees per unit time)."""
 
-    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=()):
-        super().__init__(world, n_steps, ckpt_every, loss_terms)
+    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=(), graph: bool = False):
+        super().__init__(world, n_steps, ckpt_every, loss_terms, graph)
         dev = world.device
         self.inv_T = 1.0 / (world.dt * self.S)
         self.TW, self.TW_inv = [], []
@@ -270,8 +328,9 @@ class GripperTrajectory(Trajectory):
     [T, 7] = (d_pos[3], d_ori[3] in degrees per unit time, d_gripper).  ``kin`` is a
     GripperKinematics; ``fingers`` the two sensors' indices in the world."""
 
-    def __init__(self, world: World, n_steps: int, kin, fingers=(0, 1), ckpt_every: int = 1, loss_terms=()):
-        super().__init__(world, n_steps, ckpt_every, loss_terms)
+    def __init__(self, world: World, n_steps: int, kin, fingers=(0, 1), ckpt_every: int = 1, loss_terms=(),
+                 graph: bool = False):
+        super().__init__(world, n_steps, ckpt_every, loss_terms, graph)
         self.kin = kin
         self.fingers = tuple(fingers)
         dev = world.device

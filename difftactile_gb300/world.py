@@ -56,7 +56,7 @@ class World:
 
     def __init__(self, envs: list[EnvSpec], n_frames: int, dt: float, device="cuda", tape_blocks: int | None = None,
                  grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True,
-                 svd_grad_mode: int = 0, scatter_mode: int = 2, svd_tape: bool = True):
+                 svd_grad_mode: int = 0, scatter_mode: int = 2, svd_tape: bool = True, p_block: int = 128):
         self.lib = N.load()
         self.device = torch.device(device)
         self.specs = envs
@@ -266,6 +266,7 @@ class World:
         w.svd_grad_mode = int(svd_grad_mode)
         w.max_sensor_tris = max([r.nf for r in srows], default=0)
         w.scatter_mode = int(scatter_mode)
+        w.p_block = int(p_block)
         for name in N.ROPE_PTR_FIELDS:
             setattr(w, name, t[name].data_ptr() if (self.n_ropes and t[name].numel()) else None)
         w.n_ropes, w.n_rope_particles = self.n_ropes, NR
@@ -430,49 +431,72 @@ class World:
     def step_begin(self):
         self.call("dt_step_begin")
 
-    # ``probe = ("fwd" | "bwd", stage)`` times that launch of every substep with CUDA events on the
-    # launching stream; the event pairs accumulate in ``probe_events``.
+    # ``probe = ("fwd" | "bwd", stage)`` times that launch of every ``probe_every``-th substep with
+    # CUDA events on the launching stream (the sampled substeps run as separate stage launches).
+    # Pairs recorded from the host accumulate in ``probe_events``; pairs recorded during CUDA-graph
+    # capture are graph nodes (external events) in ``probe_graph_events``, re-recorded by every replay.
     probe = None
+    probe_every = 1
+    probe_events = ()
+    probe_graph_events = ()
+
+    def _probed(self, kind, f):
+        return self.probe is not None and self.probe[0] == kind and f % self.probe_every == 0
 
     def _staged(self, name, f, n_stages, kind):
         for s in range(n_stages):
             timed = self.probe[0] == kind and self.probe[1] == s
             if timed:
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                graph = torch.cuda.is_current_stream_capturing()
+                e0 = torch.cuda.Event(enable_timing=True, external=graph)
+                e1 = torch.cuda.Event(enable_timing=True, external=graph)
                 e0.record()
             self.call(name, int(f), s)
             if timed:
                 e1.record()
-                self.probe_events.append((e0, e1))
+                (self.probe_graph_events if graph else self.probe_events).append((e0, e1))
 
     def substep(self, f):
-        if self.probe is not None and self.probe[0] == "fwd":
+        if self._probed("fwd", f):
             self._staged("dt_substep_fwd_stage", f, 3, "fwd")
         else:
             self.call("dt_substep_fwd", int(f))
 
     def substep_bwd(self, f):
-        if self.probe is not None and self.probe[0] == "bwd":
+        if self._probed("bwd", f):
             self._staged("dt_substep_bwd_stage", f, 4, "bwd")
         else:
             self.call("dt_substep_bwd", int(f))
 
+    def _substeps_bwd(self, f_hi, f_lo):
+        N.check(self.lib.dt_substeps_bwd(self.wp, int(f_hi), int(f_lo), self.stream), "dt_substeps_bwd")
+
     def substeps_bwd(self, f_hi, f_lo):
         """Adjoint substeps f_hi - 1 down to f_lo (dt_substeps_bwd: restores fused into stage 3)."""
-        if self.probe is not None and self.probe[0] == "bwd":
-            for f in reversed(range(f_lo, f_hi)):
+        if self.probe is None or self.probe[0] != "bwd":
+            self._substeps_bwd(f_hi, f_lo)
+            return
+        hi = f_hi  # fused runs between the probed frames, which run as their four stage launches
+        for f in reversed(range(f_lo, f_hi)):
+            if f % self.probe_every == 0:
+                if hi > f + 1:
+                    self._substeps_bwd(hi, f + 1)
                 self._staged("dt_substep_bwd_stage", f, 4, "bwd")
-        else:
-            N.check(self.lib.dt_substeps_bwd(self.wp, int(f_hi), int(f_lo), self.stream), "dt_substeps_bwd")
+                hi = f
+        if hi > f_lo:
+            self._substeps_bwd(hi, f_lo)
 
-    def set_probe(self, kind=None, stage=None):
+    def set_probe(self, kind=None, stage=None, every=1):
         self.probe = None if kind is None else (kind, int(stage))
+        self.probe_every = max(int(every), 1)
         self.probe_events = []
+        self.probe_graph_events = []
 
     def probe_ms(self):
-        """Mean duration (ms) of the probed launches recorded so far (synchronises)."""
+        """Mean duration (ms) of the probed launches: those recorded from the host so far and those
+        recorded in graphs (as of their latest replay).  Synchronises."""
         torch.cuda.synchronize()
-        ts = [a.elapsed_time(b) for a, b in self.probe_events]
+        ts = [a.elapsed_time(b) for a, b in self.probe_events + self.probe_graph_events]
         return (sum(ts) / len(ts)) if ts else float("nan"), len(ts)
 
     def copy_frame(self, src, dst):

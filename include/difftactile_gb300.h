@@ -50,7 +50,7 @@
 extern "C" {
 #endif
 
-#define DT_ABI_VERSION 1
+#define DT_ABI_VERSION 2
 
 #define DT_OK 0
 #define DT_ERR_ARG (-1)        /* null pointer, bad size or frame index */
@@ -201,6 +201,9 @@ typedef struct dt_world {
   float* p_svd;                  /* [n_frames][6][n_particles][4]: U, V, sigma of F_new per frame, written
                                     by the forward, read by the adjoint instead of recomputing; NULL:
                                     the adjoint recomputes the SVD */
+  /* ---- launch shape ---- */
+  int p_block;                   /* threads per CTA of the particle / tet / vertex launches: 64, 128 or
+                                    256 (any other value: 128; the TILE scatter always uses 128) */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared
@@ -231,6 +234,8 @@ size_t dt_sizeof_rope(void);
  * substep kernels (default on: each kernel waits for its predecessor's completion in-kernel, so the
  * next launch overlaps the previous kernel's tail).  Returns the previous setting. */
 int dt_set_pdl(int on);
+/* The current setting of dt_set_pdl (1 on, 0 off). */
+int dt_get_pdl(void);
 
 /* ---- step set-up ----
  * Clears the grid tape counters of every frame and prepares FEM frame 0 (velmid = vel, ext = 0).

@@ -1,0 +1,61 @@
+"""Launch-shape autotuner: the candidate set, the cache, and (GPU) a tuning pass that measures every
+candidate on a real substep, applies the fastest, and is served from the cache (in memory and from
+its JSON file) for a second world of the same shape."""
+import json
+
+import pytest
+import torch
+
+from difftactile_gb300 import autotune as AT
+
+
+def test_candidates_cover_the_shapes():
+    c = AT.candidates()
+    assert len(c) == 14
+    assert {x["p_block"] for x in c if x["scatter"] == "tile"} == {128}
+    assert {(x["scatter"], x["p_block"]) for x in c if x["scatter"] != "tile"} == \
+        {(s, b) for s in ("warp", "global") for b in (64, 128, 256)}
+    assert len({AT.label(x) for x in c}) == len(c)
+
+
+def test_cache_file_round_trip(tmp_path):
+    path = str(tmp_path / "tune.json")
+    entry = {"best": {"scatter": "warp", "p_block": 64, "pdl": 1}, "ms": {"warp/64/pdl": 0.1}}
+    AT._store(path, "k1", entry)
+    AT._store(path, "k2", dict(entry, best={"scatter": "tile", "p_block": 128, "pdl": 0}))
+    data = json.load(open(path))
+    assert data["k1"] == entry and data["k2"]["best"]["scatter"] == "tile"
+    assert AT._load(str(tmp_path / "missing.json")) == {}
+
+
+@pytest.mark.gpu
+def test_tune_substep_applies_and_caches(cuda_lib, tmp_path):
+    from difftactile_gb300.world import World
+    from tests import small_scenes as SS
+
+    env = SS.pad_over_box()
+    path = str(tmp_path / "tune.json")
+    pdl0 = cuda_lib.dt_get_pdl()
+    try:
+        w = World([env], n_frames=3, dt=1e-4)
+        w.step_begin()
+        w.substep(0)
+        w.substep(1)
+        AT._cache.clear()
+        r = AT.tune_substep(w, frame=1, reps=3, warmup=1, cache_path=path)
+        assert not r["cached"] and len(r["ms"]) == len(AT.candidates())
+        assert all(0.0 < v < 1e3 for v in r["ms"].values())
+        assert min(r["ms"], key=r["ms"].get) == AT.label(r["best"])
+        assert AT.current(w) == r["best"]
+        torch.cuda.synchronize()
+        assert w.error_word() == 0
+
+        w2 = World([env], n_frames=3, dt=1e-4)
+        r2 = AT.tune_substep(w2, frame=1, cache_path=path)
+        assert r2["cached"] and AT.current(w2) == r["best"]
+        AT._cache.clear()  # the JSON file serves it too
+        r3 = AT.tune_substep(w2, frame=1, cache_path=path)
+        assert r3["cached"] and r3["best"] == r["best"]
+    finally:
+        cuda_lib.dt_set_pdl(pdl0)
+        AT._cache.clear()

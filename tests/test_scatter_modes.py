@@ -63,3 +63,30 @@ def test_warp_runs_across_env_boundaries(cuda_lib):
     for e, env in enumerate((e0, e1)):
         st, _ = run_oracle(env, 2)
         compare(w, 2, st, env_idx=e)
+
+
+@pytest.mark.parametrize("p_block", [64, 256])
+@pytest.mark.parametrize("mode", ["warp", "global"])
+def test_particle_block_sizes(cuda_lib, mode, p_block):
+    """Particle-role CTAs of 64 and 256 threads (the autotuner's other shapes) give the oracle's
+    forward state after three substeps and its one-substep adjoint."""
+    env = SS.pad_over_box()
+    cv = [SS.control_velocity(sp) for sp in env.sensors]
+    w = World([env], n_frames=4, dt=DT, scatter_mode=MODES[mode], p_block=p_block)
+    for s, c in enumerate(cv):
+        w.set_control_velocity(s, c)
+    w.step_begin()
+    for f in range(3):
+        w.substep(f)
+    torch.cuda.synchronize()
+    assert w.error_word() == 0
+    st, _ = run_oracle(env, 3, cv)
+    compare(w, 3, st)
+    st0, cv0 = base_point(env, 7)
+    W = loss_weights(env, env.n_particles, 8)
+    g = gpu_grads(env, st0, cv0, W, 1, scatter_mode=MODES[mode], p_block=p_block)
+    o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
+    ref = o.substep_bwd({k: (v if not isinstance(v, list) else [a.copy() for a in v]) for k, v in st0.items()}, W,
+                        cv=cv0, cv1=cv0)
+    errs = {k: SS.rel_err(g[k], ref[k]) for k in ("x", "v", "C", "F")}
+    assert max(errs.values()) < 1e-3, errs
