@@ -227,7 +227,12 @@ __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w
   float4* EXT = vframe(w.v_ext, w, f);
   const int4* tris = reinterpret_cast<const int4*>(w.tris);
   int staged = -1;
-  for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
+  // a contiguous run of the active list per CTA: blocks of one environment sit together in the list
+  // (they are marked by the P2G CTAs of that environment's particles), so the CTA restages the
+  // sensor's centroids only when its run crosses into another environment
+  const int per = (cnt + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int e_end = min(cnt, ((int)blockIdx.x + 1) * per);
+  for (int e = blockIdx.x * per; e < e_end; ++e) {
     const int b = w.tape_blist[(size_t)f * w.n_blocks + e];
     const dt_env& E = w.envs[__ldg(w.blk_env + b)];
     const int lb = b - E.blk_off;
