@@ -35,6 +35,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="sensor_press", choices=["sensor_press", "batched_population"])
     ap.add_argument("--horizon", type=int, default=None, help="control steps (default: the config's)")
+    ap.add_argument("--envs", type=int, default=None, help="batched_population: the first N environments only")
     ap.add_argument("--scatter", default=None, choices=["tile", "global", "warp"],
                     help="27-node scatter strategy (default: the library's)")
     ap.add_argument("--no-pdl", action="store_true", help="launch the substep kernels without programmatic "
@@ -55,11 +56,11 @@ def parse():
     return ap.parse_args()
 
 
-def make_config(name, horizon):
+def make_config(name, horizon, envs=None):
     from difftactile_gb300 import configs
     if name == "sensor_press":
         return configs.sensor_press(n_steps=horizon or 100)
-    return configs.batched_population(n_steps=horizon or 200)
+    return configs.batched_population(n_steps=horizon or 200, n_envs=envs or 64)
 
 
 def peaks():
@@ -148,7 +149,7 @@ def run_ours(args):
         if world_size > 1:
             dist.barrier()
 
-    cfg = make_config(args.config, args.horizon)
+    cfg = make_config(args.config, args.horizon, args.envs)
     kw = {} if args.scatter is None else {"scatter_mode": {"tile": 0, "global": 1, "warp": 2}[args.scatter]}
     if args.no_svd_tape:
         kw["svd_tape"] = False
@@ -397,7 +398,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cfg = make_config(args.config, args.horizon)
+    cfg = make_config(args.config, args.horizon, args.envs)
     threads = os.cpu_count() or 1
     for _ in range(max(args.warmup, 0)):
         cpu_baseline(cfg, threads, target_s=2.0)

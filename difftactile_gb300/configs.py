@@ -117,8 +117,9 @@ def batched_population(n_envs=64, substeps=20, n_steps=200, seed=6, lo=8_000, hi
         sp = env.sensors[0]
         tg = 1e-3 * np.random.default_rng(100 + e).standard_normal(sp.verts.shape)
         terms.append((e, int(sp.layer.max()), tg))
-    # grid tape: ~14,500 of the 843,000 blocks are active per frame; 32,768 reserved
-    return Config("batched_population", envs, 1e-4, substeps, n_steps, acts, tuple(terms), tape_blocks=32768)
+    # grid tape: ~14,500 of the 843,000 blocks are active per frame for 64 environments; 32,768 reserved
+    tape = 32768 if n_envs >= 64 else max(1024, 512 * n_envs)
+    return Config("batched_population", envs, 1e-4, substeps, n_steps, acts, tuple(terms), tape_blocks=tape)
 
 
 def grasp_sphere(n_steps=1000, substeps=25, seed=4, n_grid=128, n_core=20_000, n_shell=180_000, pad=(20, 20, 5),
