@@ -206,16 +206,20 @@ __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p,
 }
 
 // ---------------------------------------------------------------------------------------------
-// L2: grid update + contact over the frame's active blocks.  256 threads per 4x4x4 block: four
+// L2: grid update + contact over the frame's active blocks.  512 threads per 4x4x4 block: eight
 // lanes per node share the node's argmin over the sensor's triangle centroids (staged in shared
-// memory), each lane scanning every fourth triangle with two independent trackers; the
-// (distance, index) pairs are combined lexicographically, which is exactly the sequential scan's
-// first-minimum-wins result.  Lane 0 of each node then does the contact force and the grid update.
+// memory, contact.cuh: closest_tri); the (distance, index) pairs are combined lexicographically,
+// which is exactly the sequential scan's first-minimum-wins result.  Then the first two warps take
+// one node per thread for the contact force and the grid update, so the serial per-node work issues
+// from 2 warps instead of from one lane in eight of all 16.
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w, int f, int smem_cap) {
   pdl_entry();
   extern __shared__ float4 scent[];
   float4* gbox = scent + smem_cap;  // 2 float4 per group of 32 centroids
+  // argmin of every node of the block per sensor slot, double-buffered over the CTA's run of blocks:
+  // the search (all lanes) fills one buffer while the node pass of the previous block reads the other
+  __shared__ int s_cid[2][DT_MAX_SENSORS_PER_ENV][64];
   const int cnt = *((volatile int*)(w.tape_bcount + f));
   const int tid = threadIdx.x;
   const int l = tid / GRID_LPN, sub = tid % GRID_LPN;
@@ -232,16 +236,40 @@ __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w
   // sensor's centroids only when its run crosses into another environment
   const int per = (cnt + (int)gridDim.x - 1) / (int)gridDim.x;
   const int e_end = min(cnt, ((int)blockIdx.x + 1) * per);
-  for (int e = blockIdx.x * per; e < e_end; ++e) {
+  int it = 0;
+  for (int e = blockIdx.x * per; e < e_end; ++e, it ^= 1) {
     const int b = w.tape_blist[(size_t)f * w.n_blocks + e];
     const dt_env& E = w.envs[__ldg(w.blk_env + b)];
     const int lb = b - E.blk_off;
     const int bk = lb % E.nb[2], bj = (lb / E.nb[2]) % E.nb[1], bi = lb / (E.nb[1] * E.nb[2]);
-    const int i = 4 * bi + (l >> 4), j = 4 * bj + ((l >> 2) & 3), k = 4 * bk + (l & 3);
-    const int g = E.node_off + (lb << 6) + l;
+    // ---- search: GRID_LPN lanes per node ----
+    {
+      const int i = 4 * bi + (l >> 4), j = 4 * bj + ((l >> 2) & 3), k = 4 * bk + (l & 3);
+      const bool occ = acc[E.node_off + (lb << 6) + l].w > E.eps;  // check_grid_occupy, mpm_elastic.py:213
+      const float px = __fmul_rn(__fadd_rn((float)i, 0.5f), E.dx), py = __fmul_rn(__fadd_rn((float)j, 0.5f), E.dx),
+                  pz = __fmul_rn(__fadd_rn((float)k, 0.5f), E.dx);
+#pragma unroll
+      for (int q = 0; q < DT_MAX_SENSORS_PER_ENV; ++q) {
+        const int si = E.s_begin + q;  // block-uniform
+        if (si >= E.s_end) break;
+        const dt_sensor& S = w.sensors[si];
+        const bool in_smem = S.nf <= smem_cap;
+        if (in_smem && staged != si) {  // block-uniform
+          stage_sensor<GRID_NT>(w, S, scent, gbox);
+          staged = si;
+        }
+        const int kk = closest_tri<GRID_LPN>(w, S, scent, gbox, in_smem, occ, px, py, pz, sub);
+        if (sub == 0) s_cid[it][q][l] = kk;
+      }
+    }
+    __syncthreads();
+    // ---- node pass: one thread per node (two warps), contact force and grid update ----
+    if (tid >= 64) continue;
+    const int i = 4 * bi + (tid >> 4), j = 4 * bj + ((tid >> 2) & 3), k = 4 * bk + (tid & 3);
+    const int g = E.node_off + (lb << 6) + tid;
     const float4 a = acc[g];
     const float m = a.w;
-    const bool occ = m > E.eps;  // check_grid_occupy, mpm_elastic.py:213
+    const bool occ = m > E.eps;
     const v3 mv = f4to3(a);
     const float me = m + E.eps;
     const v3 cur_v = v3{mv.x / me, mv.y / me, mv.z / me};
@@ -251,20 +279,15 @@ __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w
     int4 cid = make_int4(-1, -1, -1, -1);  // argmin per sensor slot (DT_MAX_SENSORS_PER_ENV = 4)
 #pragma unroll
     for (int q = 0; q < DT_MAX_SENSORS_PER_ENV; ++q) {
-      const int si = E.s_begin + q;  // block-uniform
+      const int si = E.s_begin + q;
       if (si >= E.s_end) break;
-      const dt_sensor& S = w.sensors[si];
-      const bool in_smem = S.nf <= smem_cap;
-      if (in_smem && staged != si) {  // block-uniform
-        stage_sensor<GRID_NT>(w, S, scent, gbox);
-        staged = si;
-      }
-      const int kk = closest_tri<GRID_LPN>(w, S, scent, gbox, in_smem, occ, px, py, pz, sub);
+      const int kk = s_cid[it][q][tid];
       if (q == 0) cid.x = kk;
       else if (q == 1) cid.y = kk;
       else if (q == 2) cid.z = kk;
       else cid.w = kk;
-      if (sub != 0 || !occ || kk < 0) continue;
+      if (!occ || kk < 0) continue;
+      const dt_sensor& S = w.sensors[si];
       const int4 tr = __ldg(tris + S.f_off + kk);
       SdfRes sr = find_sdf(f4to3(P[tr.x]), f4to3(P[tr.y]), f4to3(P[tr.z]), f4to3(VM[tr.x]), f4to3(VM[tr.y]),
                            f4to3(VM[tr.z]), v3{S.out_dir[0], S.out_dir[1], S.out_dir[2]}, v3{px, py, pz}, cur_v);
@@ -276,35 +299,33 @@ __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w
       red_add_v4(EXT + tr.y, fe);
       red_add_v4(EXT + tr.z, fe);
     }
-    if (sub == 0) {
-      float4 vo = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (occ) {
-        // grid_op, mpm_elastic.py:220-238
-        const float inv_m = 1.f / me;
-        v3 u = (inv_m * mv + inv_m * gf) + v3{E.dt_g[0], E.dt_g[1], E.dt_g[2]};
-        const int b_ = E.bound;
-        if (i < b_ && u.x < 0.f) u.x = 0.f;
-        if (i > E.n[0] - b_ && u.x > 0.f) u.x = 0.f;
-        if (j < b_ && u.y < 0.f) u.y = 0.f;
-        if (j > E.n[1] - b_ && u.y > 0.f) u.y = 0.f;
-        if (k < b_ && u.z < 0.f) u.z = 0.f;
-        if (k > E.n[2] - b_ && u.z > 0.f) u.z = 0.f;
-        if (E.bc == DT_BC_STICKY_FLOOR && j < b_) u = v3{0.f, 0.f, 0.f};
-        if (!finite3(u)) set_err(w, DT_DEVERR_NONFINITE);
-        vo = v3to4(u);
-      }
-      vout[g] = vo;
-      if (e < w.tape_blocks) {
-        const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + l;
-        reinterpret_cast<float4*>(w.tape_acc)[ti] = a;
-        reinterpret_cast<float4*>(w.tape_vout)[ti] = vo;
-        reinterpret_cast<int4*>(w.tape_cidx)[ti] = cid;
-      } else if (l == 0) {
-        set_err(w, DT_DEVERR_TAPE_FULL);
-      }
-      acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (l == 0) w.blk_flag[b] = 0;
+    float4 vo = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (occ) {
+      // grid_op, mpm_elastic.py:220-238
+      const float inv_m = 1.f / me;
+      v3 u = (inv_m * mv + inv_m * gf) + v3{E.dt_g[0], E.dt_g[1], E.dt_g[2]};
+      const int b_ = E.bound;
+      if (i < b_ && u.x < 0.f) u.x = 0.f;
+      if (i > E.n[0] - b_ && u.x > 0.f) u.x = 0.f;
+      if (j < b_ && u.y < 0.f) u.y = 0.f;
+      if (j > E.n[1] - b_ && u.y > 0.f) u.y = 0.f;
+      if (k < b_ && u.z < 0.f) u.z = 0.f;
+      if (k > E.n[2] - b_ && u.z > 0.f) u.z = 0.f;
+      if (E.bc == DT_BC_STICKY_FLOOR && j < b_) u = v3{0.f, 0.f, 0.f};
+      if (!finite3(u)) set_err(w, DT_DEVERR_NONFINITE);
+      vo = v3to4(u);
     }
+    vout[g] = vo;
+    if (e < w.tape_blocks) {
+      const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + tid;
+      reinterpret_cast<float4*>(w.tape_acc)[ti] = a;
+      reinterpret_cast<float4*>(w.tape_vout)[ti] = vo;
+      reinterpret_cast<int4*>(w.tape_cidx)[ti] = cid;
+    } else if (tid == 0) {
+      set_err(w, DT_DEVERR_TAPE_FULL);
+    }
+    acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tid == 0) w.blk_flag[b] = 0;
   }
 }
 
