@@ -42,8 +42,10 @@ def parse():
                     "dependent launch")
     ap.add_argument("--p-block", type=int, default=None, choices=[64, 128, 256],
                     help="threads per CTA of the particle launches")
+    ap.add_argument("--depth", type=int, default=None, choices=[0, 1, 2, 3, 4, 5],
+                    help="shuffle steps of the warp scatter's segmented reduction (0: whole runs)")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shape instead of "
-                    "the autotuner's choice (also implied by --scatter, --no-pdl or --p-block)")
+                    "the autotuner's choice (also implied by --scatter, --no-pdl, --p-block or --depth)")
     ap.add_argument("--plain", type=int, default=0,
                     help="also time the first K environments one World each (one scene per launch "
                     "sequence) and report the batched / plain ratio")
@@ -155,9 +157,11 @@ def run_ours(args):
         kw["svd_tape"] = False
     if args.p_block is not None:
         kw["p_block"] = args.p_block
+    if args.depth is not None:
+        kw["scatter_depth"] = args.depth
     w, traj = cfg.build(dev, **kw)
     w.lib.dt_set_pdl(0 if args.no_pdl else 1)
-    tune_launch = not (args.no_tune or args.scatter or args.no_pdl or args.p_block)
+    tune_launch = not (args.no_tune or args.scatter or args.no_pdl or args.p_block or args.depth is not None)
     acts = torch.as_tensor(cfg.actions, dtype=torch.float64, device=dev)
     t = w.t
     init = [t["p_state"][0].clone(), t["v_pos"][0].clone(), t["v_vel"][0].clone(), t["v_vpos"][0].clone()]
@@ -263,7 +267,7 @@ def run_ours(args):
                       "fem_tets": w.n_tets, "fem_nodes": w.n_verts, "surface_tris": w.n_tris,
                       "checkpoint_every": cfg.ckpt_every, "tape_blocks": w.tape_blocks,
                       "scatter": ["tile", "global", "warp"][w.w.scatter_mode],
-                      "p_block": int(w.w.p_block),
+                      "p_block": int(w.w.p_block), "scatter_depth": int(w.w.scatter_depth),
                       "programmatic_dependent_launch": bool(w.lib.dt_get_pdl()),
                       "launch_shape": "autotuned" if tuned else "fixed",
                       "cuda_graph": traj.graph,

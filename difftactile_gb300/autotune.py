@@ -6,6 +6,10 @@ scene (particle count and density, how many environments share the launch):
             segmented reduction before one RED per run and node ("warp"), one RED per particle and
             node ("global"), or a shared-memory gather tile per CTA ("tile", 128 threads only);
   p_block   threads per CTA of the particle / tet / vertex launches (dt_world.p_block): 64, 128, 256;
+  depth     with the warp scatter, the shuffle steps of the segmented reduction before the REDs
+            (dt_world.scatter_depth): 0 sums whole runs (fewest REDs, longest shuffle chain), 1 or 2
+            sum windows of 2 or 4 lanes (more REDs, fewer shuffles: faster when the launch is
+            throughput-bound, slower when it is latency-bound);
   pdl       programmatic dependent launch of the substep kernels (dt_set_pdl, library-wide).
 
 ``tune_substep`` times every candidate on one forward + backward substep of the world at a chosen
@@ -24,31 +28,33 @@ import statistics
 import torch
 
 SCATTERS = {"tile": 0, "global": 1, "warp": 2}
-DEFAULT = {"scatter": "warp", "p_block": 128, "pdl": 1}
+DEFAULT = {"scatter": "warp", "p_block": 128, "depth": 0, "pdl": 1}
 
 _cache: dict[str, dict] = {}
 
 
-def candidates(scatters=("warp", "global", "tile"), p_blocks=(64, 128, 256), pdl=(1, 0)):
+def candidates(scatters=("warp", "global", "tile"), p_blocks=(64, 128, 256), depths=(0, 1, 2), pdl=(1, 0)):
     out = []
     for s in scatters:
         for b in (p_blocks if s != "tile" else (128,)):
-            for p in pdl:
-                out.append({"scatter": s, "p_block": int(b), "pdl": int(p)})
+            for d in (depths if s == "warp" else (0,)):
+                for p in pdl:
+                    out.append({"scatter": s, "p_block": int(b), "depth": int(d), "pdl": int(p)})
     return out
 
 
 def apply(world, cfg: dict):
-    """Set ``cfg`` (scatter, p_block, pdl) on ``world`` (and the library's PDL switch)."""
+    """Set ``cfg`` (scatter, p_block, depth, pdl) on ``world`` (and the library's PDL switch)."""
     world.w.scatter_mode = SCATTERS[cfg["scatter"]]
     world.w.p_block = int(cfg["p_block"])
+    world.w.scatter_depth = int(cfg.get("depth", 0))
     world.lib.dt_set_pdl(int(cfg["pdl"]))  # returns the previous setting
 
 
 def current(world) -> dict:
     inv = {v: k for k, v in SCATTERS.items()}
     return {"scatter": inv.get(int(world.w.scatter_mode), "warp"), "p_block": int(world.w.p_block) or 128,
-            "pdl": int(world.lib.dt_get_pdl())}
+            "depth": int(world.w.scatter_depth), "pdl": int(world.lib.dt_get_pdl())}
 
 
 def signature(world, tag: str = "") -> str:
@@ -90,9 +96,11 @@ def _time(run, reps, warmup):
 
 
 def tune(world, run, cands=None, reps: int = 5, warmup: int = 1, tag: str = "", cache_path: str | None = None,
-         use_cache: bool = True, prepare=None) -> dict:
+         use_cache: bool = True, prepare=None, margin: float = 0.02) -> dict:
     """Time ``run()`` under every candidate launch shape (``prepare()``, untimed, before each
-    candidate's runs), apply the fastest and return {"best": cfg, "ms": {label: median ms}, "cached": bool}."""
+    candidate's runs), apply the fastest and return {"best": cfg, "ms": {label: median ms}, "cached": bool}.
+    The library default (``DEFAULT``) is kept unless a candidate beats it by more than ``margin``
+    (relative), so that timing noise between near-equal shapes does not flip the choice."""
     key = signature(world, tag)
     if use_cache:
         hit = _cache.get(key) or _load(cache_path).get(key)
@@ -113,6 +121,9 @@ def tune(world, run, cands=None, reps: int = 5, warmup: int = 1, tag: str = "", 
         times[label(c)] = ms
         if ms < best_ms:
             best, best_ms = c, ms
+    d_ms = times.get(label(DEFAULT))
+    if d_ms is not None and best_ms > (1.0 - margin) * d_ms:
+        best = dict(DEFAULT)
     apply(world, best)
     entry = {"best": best, "ms": times}
     _cache[key] = entry
@@ -140,4 +151,5 @@ def tune_substep(world, frame: int = 0, **kw) -> dict:
 
 
 def label(c: dict) -> str:
-    return f"{c['scatter']}/{c['p_block']}/{'pdl' if c['pdl'] else 'nopdl'}"
+    depth = f"/d{c.get('depth', 0)}" if c["scatter"] == "warp" else ""
+    return f"{c['scatter']}/{c['p_block']}{depth}/{'pdl' if c['pdl'] else 'nopdl'}"

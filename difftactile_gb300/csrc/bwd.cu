@@ -669,6 +669,15 @@ cudaError_t b1(const dt_world* w, int f, cudaStream_t stream) {
   return launch_k(k_bwd_g2p_fem<MODE, NT>, nb_p + nb_v, NT, smem, stream, *w, f, nb_p, nb_v);
 }
 
+template <int MODE>
+cudaError_t b1_nt(const dt_world* w, int f, cudaStream_t stream) {
+  switch (particle_block(w)) {
+    case 64: return b1<MODE, 64>(w, f, stream);
+    case 256: return b1<MODE, 256>(w, f, stream);
+    default: return b1<MODE, 128>(w, f, stream);
+  }
+}
+
 // stage 3: P2G / F adjoint (particles), tet adjoint, vertex hand-over; with `restore`, the last
 // CTAs also restore frame f - 1's grid velocities
 template <int NT>
@@ -701,17 +710,12 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
       break;
     }
     case 1:
-      if (w->scatter_mode == DT_SCATTER_TILE) {
-        e = b1<DT_SCATTER_TILE, NT_TILE>(w, f, stream);
-      } else {
-        switch (particle_block(w)) {
-          case 64: e = w->scatter_mode == DT_SCATTER_GLOBAL ? b1<DT_SCATTER_GLOBAL, 64>(w, f, stream)
-                                                              : b1<DT_SCATTER_WARP, 64>(w, f, stream); break;
-          case 256: e = w->scatter_mode == DT_SCATTER_GLOBAL ? b1<DT_SCATTER_GLOBAL, 256>(w, f, stream)
-                                                               : b1<DT_SCATTER_WARP, 256>(w, f, stream); break;
-          default: e = w->scatter_mode == DT_SCATTER_GLOBAL ? b1<DT_SCATTER_GLOBAL, 128>(w, f, stream)
-                                                              : b1<DT_SCATTER_WARP, 128>(w, f, stream);
-        }
+      switch (scatter_kind(w)) {
+        case DT_SCATTER_TILE: e = b1<DT_SCATTER_TILE, NT_TILE>(w, f, stream); break;
+        case DT_SCATTER_GLOBAL: e = b1_nt<DT_SCATTER_GLOBAL>(w, f, stream); break;
+        case DT_SCATTER_WARP + 1: e = b1_nt<DT_SCATTER_WARP + 1>(w, f, stream); break;
+        case DT_SCATTER_WARP + 2: e = b1_nt<DT_SCATTER_WARP + 2>(w, f, stream); break;
+        default: e = b1_nt<DT_SCATTER_WARP>(w, f, stream);
       }
       break;
     case 2: {

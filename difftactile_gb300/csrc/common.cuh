@@ -296,6 +296,11 @@ DT_DEV void pdl_entry() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
+// template scatter mode of the particle launches: DT_SCATTER_WARP + scatter_depth (depth 1 or 2)
+inline int scatter_kind(const dt_world* w) {
+  if (w->scatter_mode != DT_SCATTER_WARP) return w->scatter_mode == DT_SCATTER_TILE ? DT_SCATTER_TILE : DT_SCATTER_GLOBAL;
+  return DT_SCATTER_WARP + ((w->scatter_depth == 1 || w->scatter_depth == 2) ? w->scatter_depth : 0);
+}
 // threads per CTA of the particle / tet / vertex launches (dt_world.p_block)
 inline int particle_block(const dt_world* w) { return (w->p_block == 64 || w->p_block == 256) ? w->p_block : 128; }
 
@@ -637,6 +642,8 @@ struct StencilRec {
   v3 c0, c1, c2;
 };
 
+// MODE: DT_SCATTER_TILE, DT_SCATTER_GLOBAL, or DT_SCATTER_WARP + d for the warp reduction capped at
+// d shuffle steps (d = 0: whole runs; dt_world.scatter_depth selects d at launch)
 template <int NT, int TILE_MAX, int MODE, typename MarkBox, typename MarkOne>
 DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, const int base[3], const StencilRec& r,
                             float* sm, int* sh, float4* dst, const MarkBox& mark_box, const MarkOne& mark_one) {
@@ -729,7 +736,7 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
         red_add_v4(dst + g, make_float4(ax, ay, az, aw));
       }
     }
-  } else if constexpr (MODE == DT_SCATTER_WARP) {
+  } else if constexpr (MODE >= DT_SCATTER_WARP) {
     // segmented reduction over runs of lanes with the same base node (same env and cell): every
     // lane of the warp takes part in the shuffles; lanes without a particle form runs of their own
     int node_off = 0, nb1 = 1, nb2 = 1;
@@ -748,7 +755,14 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
     const unsigned after = lane == 31 ? 0u : (heads >> (lane + 1)) << (lane + 1);
     const int seg_end = after ? __ffs(after) - 1 : 32;
     const int run = __reduce_max_sync(0xffffffffu, head ? seg_end - lane : 0);
-    const int steps = run > 1 ? 32 - __clz(run - 1) : 0;
+    int steps = run > 1 ? 32 - __clz(run - 1) : 0;
+    // MODE = DT_SCATTER_WARP + depth: at most `depth` shuffle steps (0: the whole run)
+    constexpr int DEPTH = MODE - DT_SCATTER_WARP;
+    if constexpr (DEPTH > 0) steps = min(steps, DEPTH);
+    // after `steps` steps a lane holds the sum of its window of 2^steps lanes (clipped to the run);
+    // the first lane of every window issues the RED
+    const int seg_start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+    const bool issuer = ((lane - seg_start) & ((1 << steps) - 1)) == 0;
 #pragma unroll
     for (int oi = 0; oi < 3; ++oi)
 #pragma unroll
@@ -772,7 +786,7 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
               a.w += bw;
             }
           }
-          if (head && ok) {
+          if (issuer && ok) {
             const int i = base[0] + oi, j = base[1] + oj, k = base[2] + ok_;
             const int n = node_off + ((((i >> 2) * nb1 + (j >> 2)) * nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
                           ((j & 3) << 2) + (k & 3);

@@ -4,10 +4,11 @@
 //
 // A sensor's centroids are kept in contact-search order (tri_perm: groups of 32 consecutive
 // positions are compact patches of the rest surface), each carrying its original index in .w.  A CTA
-// stages them in shared memory with the bounding box of every group.  Four lanes (a quad) share one
-// query point: (1) the group with the nearest box, (2) its 32 centroids, (3) every other group
-// whose box is not farther than that distance by more than 1e-5 relative — far above the few-ulp
-// rounding of either distance, so no skipped member could win or tie — all four lanes together.
+// stages them in shared memory with the bounding box of every group.  LPN lanes (eight for grid
+// nodes, four for rope particles) share one query point: (1) the group with the nearest box, (2) its
+// 32 centroids, (3) every other group whose box is not farther than that distance by more than 1e-5
+// relative — far above the few-ulp rounding of either distance, so no skipped member could win or
+// tie — all LPN lanes together.
 // (distance, original index) pairs are combined lexicographically, which is the sequential scan's
 // first-minimum-wins result; every distance is evaluated with separately rounded operations, so the
 // argmin is bit-identical to a sequential CPU scan.
@@ -83,10 +84,27 @@ DT_DEV int closest_tri(const dt_world& w, const dt_sensor& S, const float4* scen
   if (in_smem) {
     const int Gu = (nf + 31) >> 5;  // warp-uniform trip count around the shuffles
     const int G = active ? Gu : 0;
+    // up to 32 groups: each lane keeps its groups' box distances (group sub + LPN jj) in registers
+    // for the pruning pass; beyond that the pass recomputes them
+    constexpr int KM = 32 / LPN;
+    const bool cached = Gu <= 32;  // warp-uniform
+    float bd[KM];
     Best gbest{3.4e38f, 0x7fffffff};
-    for (int gg = sub; gg < G; gg += LPN) {
-      const float lb = box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz);
-      if (lb < gbest.d) gbest = Best{lb, gg};
+    if (cached) {
+#pragma unroll
+      for (int jj = 0; jj < KM; ++jj) {
+        const int gg = sub + LPN * jj;
+        bd[jj] = 3.4e38f;
+        if (gg < G) {
+          bd[jj] = box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz);
+          if (bd[jj] < gbest.d) gbest = Best{bd[jj], gg};
+        }
+      }
+    } else {
+      for (int gg = sub; gg < G; gg += LPN) {
+        const float lb = box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz);
+        if (lb < gbest.d) gbest = Best{lb, gg};
+      }
     }
     gbest = group_min<LPN>(gbest);
     // no group is selected when every box distance is NaN (non-finite sensor positions): the
@@ -107,8 +125,16 @@ DT_DEV int closest_tri(const dt_world& w, const dt_sensor& S, const float4* scen
     for (int gc = 0; gc < Gu; gc += 64) {
       unsigned long long live = 0ull;
       const int ge = min(gc + 64, G);
-      for (int gg = gc + sub; gg < ge; gg += LPN)
-        if (gg != g0 && !(box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr)) live |= 1ull << (gg - gc);
+      if (cached) {
+#pragma unroll
+        for (int jj = 0; jj < KM; ++jj) {
+          const int gg = sub + LPN * jj;
+          if (gg < ge && gg != g0 && !(bd[jj] > thr)) live |= 1ull << gg;
+        }
+      } else {
+        for (int gg = gc + sub; gg < ge; gg += LPN)
+          if (gg != g0 && !(box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr)) live |= 1ull << (gg - gc);
+      }
 #pragma unroll
       for (int o = 1; o < LPN; o <<= 1) live |= __shfl_xor_sync(0xffffffffu, live, o);
       while (live) {

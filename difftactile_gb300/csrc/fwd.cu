@@ -446,9 +446,11 @@ cudaError_t l1_nt(const dt_world* w, int f, bool parts, bool fem, cudaStream_t s
 }
 int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   cudaError_t e;
-  switch (w->scatter_mode) {
+  switch (scatter_kind(w)) {
     case DT_SCATTER_TILE: e = l1<DT_SCATTER_TILE, NT_TILE>(w, f, parts, fem, st); break;
     case DT_SCATTER_GLOBAL: e = l1_nt<DT_SCATTER_GLOBAL>(w, f, parts, fem, st); break;
+    case DT_SCATTER_WARP + 1: e = l1_nt<DT_SCATTER_WARP + 1>(w, f, parts, fem, st); break;
+    case DT_SCATTER_WARP + 2: e = l1_nt<DT_SCATTER_WARP + 2>(w, f, parts, fem, st); break;
     default: e = l1_nt<DT_SCATTER_WARP>(w, f, parts, fem, st);
   }
   return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;

@@ -204,6 +204,10 @@ typedef struct dt_world {
   /* ---- launch shape ---- */
   int p_block;                   /* threads per CTA of the particle / tet / vertex launches: 64, 128 or
                                     256 (any other value: 128; the TILE scatter always uses 128) */
+  int scatter_depth;             /* WARP scatter: 1 or 2 caps the segmented reduction at that many
+                                    shuffle steps (runs summed in windows of 2 or 4 lanes, one RED per
+                                    window and node); any other value: the whole run, one RED per run
+                                    and node */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared

@@ -65,14 +65,15 @@ def test_warp_runs_across_env_boundaries(cuda_lib):
         compare(w, 2, st, env_idx=e)
 
 
-@pytest.mark.parametrize("p_block", [64, 256])
-@pytest.mark.parametrize("mode", ["warp", "global"])
-def test_particle_block_sizes(cuda_lib, mode, p_block):
-    """Particle-role CTAs of 64 and 256 threads (the autotuner's other shapes) give the oracle's
-    forward state after three substeps and its one-substep adjoint."""
+@pytest.mark.parametrize("mode,p_block,depth", [("warp", 64, 0), ("warp", 256, 0), ("global", 64, 0),
+                                                ("global", 256, 0), ("warp", 128, 1), ("warp", 128, 2),
+                                                ("warp", 256, 1)])
+def test_particle_block_sizes(cuda_lib, mode, p_block, depth):
+    """Particle-role CTAs of 64 and 256 threads and capped segmented reductions (the autotuner's
+    other shapes) give the oracle's forward state after three substeps and its one-substep adjoint."""
     env = SS.pad_over_box()
     cv = [SS.control_velocity(sp) for sp in env.sensors]
-    w = World([env], n_frames=4, dt=DT, scatter_mode=MODES[mode], p_block=p_block)
+    w = World([env], n_frames=4, dt=DT, scatter_mode=MODES[mode], p_block=p_block, scatter_depth=depth)
     for s, c in enumerate(cv):
         w.set_control_velocity(s, c)
     w.step_begin()
@@ -84,7 +85,7 @@ def test_particle_block_sizes(cuda_lib, mode, p_block):
     compare(w, 3, st)
     st0, cv0 = base_point(env, 7)
     W = loss_weights(env, env.n_particles, 8)
-    g = gpu_grads(env, st0, cv0, W, 1, scatter_mode=MODES[mode], p_block=p_block)
+    g = gpu_grads(env, st0, cv0, W, 1, scatter_mode=MODES[mode], p_block=p_block, scatter_depth=depth)
     o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
     ref = o.substep_bwd({k: (v if not isinstance(v, list) else [a.copy() for a in v]) for k, v in st0.items()}, W,
                         cv=cv0, cv1=cv0)
