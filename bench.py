@@ -126,7 +126,7 @@ NAMES = {("fwd", 0): "k_fwd_p2g_fem", ("fwd", 1): "k_fwd_grid", ("fwd", 2): "k_f
 
 # DRAM bytes (read + write) per launch from one ncu capture of the sensor-press workload
 # (profiles/kernels_sensor_press.md); per-launch sizes equal the full workload's
-NCU_TRAFFIC = {"sensor_press": {"k_fwd_p2g_fem": 7.875e6, "k_fwd_grid": 0.381e6, "k_bwd_p2g_fem": 18.662e6,
+NCU_TRAFFIC = {"sensor_press": {"k_fwd_p2g_fem": 7.875e6, "k_fwd_grid": 0.387e6, "k_bwd_p2g_fem": 18.662e6,
                                 "k_bwd_g2p_fem": 6.152e6}}
 
 
