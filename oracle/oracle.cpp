@@ -1,5 +1,5 @@
 // ORACLE — test infrastructure only.  CPU restatement of the DiffTactile simulation substep
-// (Taichi kernels of the reference), used as the parity checker of the CUDA path and as the
+// (Taichi kernels of the reference), used as the parity oracle of the CUDA path and as the
 // timed CPU baseline.  It is never linked into or called by the product path.
 //
 // Parity status: UNPINNED against the reference's own outputs.  The reference is Taichi 1.6.0

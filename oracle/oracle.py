@@ -1,7 +1,7 @@
 """ORACLE (test infrastructure only): ctypes wrapper of the CPU restatement in oracle.cpp.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arms use this
-module, as the checker.  Parity status: unpinned against the reference's own outputs (Taichi is
+module, to check the CUDA path's results against it.  Parity status: unpinned against the reference's own outputs (Taichi is
 not available and the reference has no tests or golden vectors); pinned by analytic known-answer
 tests and finite differences instead.
 
