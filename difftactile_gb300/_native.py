@@ -87,6 +87,7 @@ SIGNATURES = {
     "dt_sizeof_rope": (C.c_size_t, []),
     "dt_set_pdl": (C.c_int, [C.c_int]),
     "dt_get_pdl": (C.c_int, []),
+    "dt_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "dt_step_begin": (C.c_int, [_W, _P]),
     "dt_substep_fwd": (C.c_int, [_W, C.c_int, _P]),
     "dt_substep_fwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),
@@ -163,6 +164,17 @@ def load(path: str | None = None):
     return lib
 
 
+def last_error() -> tuple[int, str]:
+    """(cudaError_t code, "name: description") behind the last DT_ERR_LAUNCH on this thread; clears it."""
+    buf = C.create_string_buffer(256)
+    code = load().dt_last_error(buf, len(buf))
+    return code, buf.value.decode(errors="replace")
+
+
 def check(rc: int, what: str):
     if rc != 0:
-        raise DtError(f"{what} failed: {ERRORS.get(rc, rc)}")
+        detail = ""
+        if rc == -2 and _lib is not None:
+            code, msg = last_error()
+            detail = f" ({msg})" if code else ""
+        raise DtError(f"{what} failed: {ERRORS.get(rc, rc)}{detail}")

@@ -1,12 +1,14 @@
 // C-ABI support entry points: introspection, step set-up, frame copies, adjoint clears and the
 // centre-of-mass readout.
+#include <cstdio>
+
 #include "common.cuh"
 
 namespace {
 
 constexpr int NT = 256;
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
-inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
+inline int launched() { return launch_status(cudaGetLastError()); }
 
 // Contact.reset (grasp_plastic.py:386-392) equivalent for the per-step tape: frame counters to
 // zero, FEM frame 0 accumulators prepared.
@@ -82,6 +84,13 @@ int dt_set_pdl(int on) {
 
 int dt_get_pdl(void) { return pdl_flag(); }
 
+int dt_last_error(char* buf, size_t len) {
+  const cudaError_t e = last_cuda_error();
+  last_cuda_error() = cudaSuccess;
+  if (buf && len) snprintf(buf, len, "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+  return (int)e;
+}
+
 int dt_step_begin(const dt_world* w, cudaStream_t stream) {
   if (!w || w->n_frames < 2) return DT_ERR_ARG;
   int n = w->n_frames > w->n_verts ? w->n_frames : w->n_verts;
@@ -93,22 +102,22 @@ int dt_copy_frame(const dt_world* w, int src, int dst, cudaStream_t stream) {
   if (!w || src < 0 || dst < 0 || src >= w->n_frames || dst >= w->n_frames) return DT_ERR_ARG;
   if (src == dst) return DT_OK;
   const size_t pbytes = (size_t)6 * w->n_particles * 16;
-  if (pbytes && cudaMemcpyAsync(w->p_state + (size_t)dst * 6 * w->n_particles * 4,
+  if (pbytes && note_error(cudaMemcpyAsync(w->p_state + (size_t)dst * 6 * w->n_particles * 4,
                                 w->p_state + (size_t)src * 6 * w->n_particles * 4, pbytes, cudaMemcpyDeviceToDevice,
-                                stream) != cudaSuccess)
+                                stream)) != cudaSuccess)
     return DT_ERR_LAUNCH;
   const size_t vbytes = (size_t)w->n_verts * 16;
   float* arrs[4] = {w->v_pos, w->v_vel, w->v_vpos, w->v_cv};
   for (float* a : arrs) {
-    if (vbytes && cudaMemcpyAsync(a + (size_t)dst * w->n_verts * 4, a + (size_t)src * w->n_verts * 4, vbytes,
-                                  cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+    if (vbytes && note_error(cudaMemcpyAsync(a + (size_t)dst * w->n_verts * 4, a + (size_t)src * w->n_verts * 4, vbytes,
+                                  cudaMemcpyDeviceToDevice, stream)) != cudaSuccess)
       return DT_ERR_LAUNCH;
   }
   // rope pos, vel, travel_info (PBDRope.copy_frame, PBD_rope.py:182-187)
   const size_t rbytes = (size_t)2 * w->n_rope_particles * 16;
-  if (rbytes && cudaMemcpyAsync(w->r_state + (size_t)dst * 2 * w->n_rope_particles * 4,
+  if (rbytes && note_error(cudaMemcpyAsync(w->r_state + (size_t)dst * 2 * w->n_rope_particles * 4,
                                 w->r_state + (size_t)src * 2 * w->n_rope_particles * 4, rbytes,
-                                cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+                                cudaMemcpyDeviceToDevice, stream)) != cudaSuccess)
     return DT_ERR_LAUNCH;
   return DT_OK;
 }
@@ -133,13 +142,13 @@ int dt_adj_clear(const dt_world* w, cudaStream_t stream) {
       {w->r_extb, (size_t)w->n_rope_particles * 16},
   };
   for (auto& e : z)
-    if (e.p && e.n && cudaMemsetAsync(e.p, 0, e.n, stream) != cudaSuccess) return DT_ERR_LAUNCH;
+    if (e.p && e.n && note_error(cudaMemsetAsync(e.p, 0, e.n, stream)) != cudaSuccess) return DT_ERR_LAUNCH;
   return DT_OK;
 }
 
 int dt_com(const dt_world* w, int f, float* out, cudaStream_t stream) {
   if (!w || !out || f < 0 || f >= w->n_frames) return DT_ERR_ARG;
-  if (cudaMemsetAsync(out, 0, (size_t)w->n_envs * 16, stream) != cudaSuccess) return DT_ERR_LAUNCH;
+  if (note_error(cudaMemsetAsync(out, 0, (size_t)w->n_envs * 16, stream)) != cudaSuccess) return DT_ERR_LAUNCH;
   if (w->n_particles == 0) return DT_OK;
   k_com<<<cdiv(w->n_particles, NT), NT, 0, stream>>>(*w, f, out);
   return launched();

@@ -658,7 +658,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_bwd_p2g_fem(dt_world w, int f,
 }
 
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
-inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
+inline int launched() { return launch_status(cudaGetLastError()); }
 
 // stage 1: G2P adjoint (particles) + integration adjoint (vertices)
 template <int MODE, int NT>

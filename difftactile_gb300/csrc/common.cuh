@@ -296,6 +296,18 @@ DT_DEV void pdl_entry() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
+// The last CUDA error an entry point of the library met on this host thread (dt_last_error).
+inline cudaError_t& last_cuda_error() {
+  thread_local cudaError_t e = cudaSuccess;
+  return e;
+}
+inline cudaError_t note_error(cudaError_t e) {
+  if (e != cudaSuccess) last_cuda_error() = e;
+  return e;
+}
+// DT_OK, or DT_ERR_LAUNCH with the CUDA error kept for dt_last_error
+inline int launch_status(cudaError_t e) { return note_error(e) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
+
 // template scatter mode of the particle launches: DT_SCATTER_WARP + scatter_depth (depth 1 or 2)
 inline int scatter_kind(const dt_world* w) {
   if (w->scatter_mode != DT_SCATTER_WARP) return w->scatter_mode == DT_SCATTER_TILE ? DT_SCATTER_TILE : DT_SCATTER_GLOBAL;
@@ -311,7 +323,7 @@ inline cudaError_t ensure_smem(const void* fn, size_t bytes, size_t (&cache)[64]
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (bytes <= cache[dev]) return cudaSuccess;
-  const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  const cudaError_t e = note_error(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   if (e == cudaSuccess) cache[dev] = bytes;
   return e;
 }
@@ -331,7 +343,7 @@ inline cudaError_t launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t s
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = pdl_flag() ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+  return note_error(cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...));
 }
 
 // particle record access: plane k of frame f

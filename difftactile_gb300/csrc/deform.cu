@@ -176,7 +176,7 @@ __global__ void k_sdf_init(dt_world w, int e, float4* buf) {
   if (local < nn) buf[E.node_off + local] = make_float4(0.f, 0.f, 0.f, 1000.f);
 }
 
-inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
+inline int launched() { return launch_status(cudaGetLastError()); }
 
 }  // namespace
 

@@ -425,7 +425,7 @@ inline int check(const dt_world* w, int f) {
   if (!w || f < 0 || f + 1 >= w->n_frames) return DT_ERR_ARG;
   return DT_OK;
 }
-inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
+inline int launched() { return launch_status(cudaGetLastError()); }
 
 template <int MODE, int NT>
 cudaError_t l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {

@@ -47,7 +47,7 @@ int dt_substep_fwd_noalloc(const dt_world* w, int f, cudaStream_t stream) {
   if (!s_scratch[dev]) {
     // the symbol is a host-side stand-in: its device address must be looked up per device
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return DT_ERR_LAUNCH;
+    if (note_error(cudaGetSymbolAddress(&p, g_noalloc_scratch)) != cudaSuccess || !p) return DT_ERR_LAUNCH;
     s_scratch[dev] = static_cast<float4*>(p);
   }
   float4* S = s_scratch[dev];
@@ -80,9 +80,9 @@ int dt_substep_fwd_noalloc(const dt_world* w, int f, cudaStream_t stream) {
   v.tape_bcount = reinterpret_cast<int*>(S + NA_OFF_BCOUNT);
   v.tri_cent = reinterpret_cast<float*>(S + NA_OFF_CENT);
   // the scratch keeps the previous call's contents: clear what the substep expects to start at zero
-  if (cudaMemsetAsync(v.g_acc, 0, (size_t)w->n_nodes * sizeof(float4), stream) != cudaSuccess ||
-      cudaMemsetAsync(v.blk_flag, 0, (size_t)w->n_blocks * sizeof(int), stream) != cudaSuccess ||
-      cudaMemsetAsync(v.tape_bcount, 0, 2 * sizeof(int), stream) != cudaSuccess)
+  if (note_error(cudaMemsetAsync(v.g_acc, 0, (size_t)w->n_nodes * sizeof(float4), stream)) != cudaSuccess ||
+      note_error(cudaMemsetAsync(v.blk_flag, 0, (size_t)w->n_blocks * sizeof(int), stream)) != cudaSuccess ||
+      note_error(cudaMemsetAsync(v.tape_bcount, 0, 2 * sizeof(int), stream)) != cudaSuccess)
     return DT_ERR_LAUNCH;
   return dt_substep_fwd(&v, 0, stream);
 }

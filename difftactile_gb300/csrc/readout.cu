@@ -20,7 +20,7 @@ namespace {
 
 constexpr int NT = 256;
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
-inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
+inline int launched() { return launch_status(cudaGetLastError()); }
 
 __global__ void k_pose_cv(dt_world w, int s, const float* __restrict__ Ab, float inv_T, int f0, int nfr) {
   const dt_sensor& S = w.sensors[s];
@@ -498,7 +498,7 @@ int dt_affine_control_vel_bwd(const dt_world* w, int s, const float* src, int f0
 
 int dt_rigid_match(const dt_world* w, int e, int mat, int f, float* out, cudaStream_t stream) {
   if (!w || !out || e < 0 || e >= w->n_envs || f < 0 || f + 1 >= w->n_frames) return DT_ERR_ARG;
-  if (cudaMemsetAsync(out, 0, 20 * sizeof(float), stream) != cudaSuccess) return DT_ERR_LAUNCH;
+  if (note_error(cudaMemsetAsync(out, 0, 20 * sizeof(float), stream)) != cudaSuccess) return DT_ERR_LAUNCH;
   const int nb = cdiv(w->n_particles > 0 ? w->n_particles : 1, NT);
   k_rigid_com<<<nb, NT, 0, stream>>>(*w, e, mat, f, out);
   k_rigid_H<<<nb, NT, 0, stream>>>(*w, e, mat, f, out, out);
@@ -510,7 +510,7 @@ int dt_rigid_match_bwd(const dt_world* w, int e, int mat, int f, int part, const
   if (!w || !out || !H_b || !scratch || e < 0 || e >= w->n_envs || f < 0 || f + 1 >= w->n_frames || part < 0 ||
       part > 1)
     return DT_ERR_ARG;
-  if (cudaMemsetAsync(scratch, 0, 8 * sizeof(float), stream) != cudaSuccess) return DT_ERR_LAUNCH;
+  if (note_error(cudaMemsetAsync(scratch, 0, 8 * sizeof(float), stream)) != cudaSuccess) return DT_ERR_LAUNCH;
   const int nb = cdiv(w->n_particles > 0 ? w->n_particles : 1, NT);
   k_rigid_centred_means<<<nb, NT, 0, stream>>>(*w, e, mat, f, out, scratch);
   k_rigid_H_bwd<<<nb, NT, 0, stream>>>(*w, e, mat, f, part, out, scratch, H_b);

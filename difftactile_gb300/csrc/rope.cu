@@ -22,7 +22,7 @@ namespace {
 constexpr int RC_NT = 256;  // contact: 64 particles x 4 lanes
 constexpr int RS_NT = 256;  // solver: one CTA per rope
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
-inline int launched() { return cudaGetLastError() == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
+inline int launched() { return launch_status(cudaGetLastError()); }
 
 DT_DEV float4* rstate(const dt_world& w, int f, int plane) {
   return reinterpret_cast<float4*>(w.r_state) + ((size_t)f * 2 + plane) * w.n_rope_particles;

@@ -241,6 +241,12 @@ int dt_set_pdl(int on);
 /* The current setting of dt_set_pdl (1 on, 0 off). */
 int dt_get_pdl(void);
 
+/* No counterpart in the reference (Taichi raises Python exceptions).  The CUDA error behind the
+ * last DT_ERR_LAUNCH returned to this host thread: writes "<name>: <description>" into buf (at most len bytes, NUL-terminated),
+ * returns the cudaError_t code (0: none since the last call) and clears it.  Device-side problems
+ * are reported through dt_world.err instead. */
+int dt_last_error(char* buf, size_t len);
+
 /* ---- step set-up ----
  * Clears the grid tape counters of every frame and prepares FEM frame 0 (velmid = vel, ext = 0).
  * Call once before the substeps of a control step (the reference calls Contact.reset(),

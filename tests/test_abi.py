@@ -51,3 +51,12 @@ def test_ctypes_signatures_cover_header():
 def test_build_targets_sm103a_only():
     from difftactile_gb300 import build
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_last_error_without_a_failure(lib_path):
+    """dt_last_error reports (and clears) the CUDA error behind a DT_ERR_LAUNCH; with none recorded it
+    returns 0 and names cudaSuccess.  Host-only: no device is touched."""
+    from difftactile_gb300 import _native
+    _native.load(lib_path)
+    code, msg = _native.last_error()
+    assert code == 0 and msg.startswith("cudaSuccess")
