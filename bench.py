@@ -24,7 +24,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FALLBACK_HBM_GBS = 6800.0
-PROBE_EVERY = 10  # substeps between the timed region's event-timed launches of the dominant kernel
+PROBE_EVERY = 25  # substeps between the timed region's event-timed launches of the dominant kernel
 
 
 def parse():

@@ -109,6 +109,7 @@ SIGNATURES = {
     "dt_pose_control_vel": (C.c_int, [_W, C.c_int, _P, C.c_float, C.c_int, C.c_int, _P]),
     "dt_pose_control_vel_all": (C.c_int, [_W, _P, C.c_float, C.c_int, C.c_int, _P]),
     "dt_pose_control_vel_bwd": (C.c_int, [_W, C.c_int, _P, C.c_float, _P, C.c_int, C.c_int, _P]),
+    "dt_pose_control_vel_bwd_all": (C.c_int, [_W, _P, C.c_float, _P, C.c_int, C.c_int, _P]),
     "dt_affine_control_vel": (C.c_int, [_W, C.c_int, _P, _P, C.c_int, C.c_int, _P]),
     "dt_affine_control_vel_bwd": (C.c_int, [_W, C.c_int, _P, C.c_int, C.c_int, _P, _P]),
     "dt_grid_mass": (C.c_int, [_W, C.c_int, C.c_int, _P, _P]),

@@ -97,6 +97,80 @@ __global__ void k_pose_cv_bwd(dt_world w, int s, const float* __restrict__ Ab, f
   }
 }
 
+// every sensor at once (Ab, Ab_bar [n_sensors][12]): one thread per (frame, vertex) over all
+// vertices; vertices are sensor-contiguous, so a warp whose vertices share one sensor sums its 12
+// partial products with shuffles before its atomics, and a CTA that lies in one sensor sums its warps
+// in shared memory first
+__global__ void k_pose_cv_bwd_all(dt_world w, const float* __restrict__ Ab, float inv_T, float* Ab_bar, int f0,
+                                  int nfr) {
+  __shared__ float red[12][NT / 32];
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = f0 + blockIdx.y;
+  float g[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) g[k] = 0.f;
+  int s = -1;
+  if (v < w.n_verts) {
+    s = __ldg(w.v_sensor + v);
+    const float* A = Ab + 12 * s;
+    const v3 p = f4to3(vframe(w.v_vpos, w, f0)[v]);
+    float4* c = vframe(w.v_adj_cv, w, f) + v;  // consumed: the adjoint moves into Ab_bar and vpos_bar
+    const v3 cb = inv_T * f4to3(*c);
+    *c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (cb.x != 0.f || cb.y != 0.f || cb.z != 0.f) {
+      const float pr[4] = {p.x, p.y, p.z, 1.f};
+      const float cr[3] = {cb.x, cb.y, cb.z};
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) g[4 * r + cc] = cr[r] * pr[cc];
+      float4* ap = reinterpret_cast<float4*>(w.v_adj_vpos) + (size_t)(f0 & 1) * w.n_verts + v;
+      red_add_v4(ap, make_float4(A[0] * cb.x + A[4] * cb.y + A[8] * cb.z - cb.x,
+                                 A[1] * cb.x + A[5] * cb.y + A[9] * cb.z - cb.y,
+                                 A[2] * cb.x + A[6] * cb.y + A[10] * cb.z - cb.z, 0.f));
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // the CTA's vertices [v_first, v_last] lie in one sensor iff the two ends do (contiguous sensors)
+  const int v_first = blockIdx.x * blockDim.x;
+  const int v_last = min(v_first + (int)blockDim.x, w.n_verts) - 1;
+  const int s_cta = __ldg(w.v_sensor + v_first);
+  const bool cta_one = s_cta == __ldg(w.v_sensor + v_last);
+  const int s0 = __shfl_sync(0xffffffffu, s, 0);
+  const bool warp_one = __all_sync(0xffffffffu, s == s0 || s < 0);
+  if (warp_one) {
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      float x = g[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      g[k] = x;
+    }
+  }
+  if (cta_one) {  // block-uniform
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) red[k][wid] = g[k];  // every warp of the CTA is single-sensor here
+    }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+      float x = 0.f;
+      for (int k = 0; k < NT / 32; ++k) x += red[threadIdx.x][k];
+      if (x != 0.f) atomicAdd(Ab_bar + 12 * s_cta + threadIdx.x, x);
+    }
+  } else if (warp_one) {
+    if (lane == 0 && s0 >= 0) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k)
+        if (g[k] != 0.f) atomicAdd(Ab_bar + 12 * s0 + k, g[k]);
+    }
+  } else if (s >= 0) {
+#pragma unroll
+    for (int k = 0; k < 12; ++k)
+      if (g[k] != 0.f) atomicAdd(Ab_bar + 12 * s + k, g[k]);
+  }
+}
+
 __global__ void k_marker_loss(dt_world w, int s, int f, int layer, const float4* __restrict__ target, float* loss) {
   const dt_sensor& S = w.sensors[s];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -572,6 +646,14 @@ int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv
   if (!w || !Ab || !Ab_bar || s < 0 || s >= w->n_sensors || f0 < 0 || nfr < 1 || f0 + nfr > w->n_frames)
     return DT_ERR_ARG;
   k_pose_cv_bwd<<<dim3(cdiv(w->n_verts, NT), nfr), NT, 0, stream>>>(*w, s, Ab, inv_T, Ab_bar, f0, nfr);
+  return launched();
+}
+
+int dt_pose_control_vel_bwd_all(const dt_world* w, const float* Ab, float inv_T, float* Ab_bar, int f0, int nfr,
+                                cudaStream_t stream) {
+  if (!w || !Ab || !Ab_bar || f0 < 0 || nfr < 1 || f0 + nfr > w->n_frames) return DT_ERR_ARG;
+  if (w->n_verts == 0) return DT_OK;
+  k_pose_cv_bwd_all<<<dim3(cdiv(w->n_verts, NT), nfr), NT, 0, stream>>>(*w, Ab, inv_T, Ab_bar, f0, nfr);
   return launched();
 }
 

@@ -275,39 +275,34 @@ class PoseTrajectory(Trajectory):
         super().__init__(world, n_steps, ckpt_every, loss_terms, graph)
         dev = world.device
         self.inv_T = 1.0 / (world.dt * self.S)
-        self.TW, self.TW_inv = [], []
-        for sp in world.sensor_specs:
-            M = sp.trans_world if sp.trans_world is not None else np.eye(4)
-            self.TW.append(torch.as_tensor(M, dtype=torch.float64, device=dev))
-            self.TW_inv.append(torch.as_tensor(np.linalg.inv(M), dtype=torch.float64, device=dev))
+        Ms = [sp.trans_world if sp.trans_world is not None else np.eye(4) for sp in world.sensor_specs]
+        self.TW = torch.as_tensor(np.stack(Ms) if Ms else np.zeros((0, 4, 4)), dtype=torch.float64, device=dev)
+        self.TW_inv = torch.as_tensor(np.stack([np.linalg.inv(M) for M in Ms]) if Ms else np.zeros((0, 4, 4)),
+                                      dtype=torch.float64, device=dev)
 
     def step_transforms(self, actions: torch.Tensor) -> torch.Tensor:
-        """actions [T, n_sensors, 6] (float64) -> Ab [T, n_sensors, 12] (float64, differentiable)."""
-        S = self.S
-        out = []
-        for s in range(self.w.n_sensors):
-            a = actions[:, s]
-            M = eul2mat_zyx(a[:, 3:6] * self.w.dt * S, a[:, 0:3] * self.w.dt * S)
-            D = self.TW[s] @ M @ self.TW_inv[s]
-            out.append(D[:, :3, :].reshape(-1, 12))
-        return torch.stack(out, 1)
+        """actions [T, n_sensors, 6] (float64) -> Ab [T, n_sensors, 12] (float64, differentiable); all
+        sensors and steps in one batch of 4x4 products."""
+        k = self.w.dt * self.S
+        M = eul2mat_zyx(actions[..., 3:6] * k, actions[..., 0:3] * k)  # [T, n_sensors, 4, 4]
+        D = self.TW @ M @ self.TW_inv
+        return D[..., :3, :].reshape(actions.shape[0], actions.shape[1], 12)
 
     controls = step_transforms
 
+    # every sensor is pose-controlled: one launch for all of them (rows of ctrl32[t] are per sensor)
     def _apply(self, t, f0):
         w = self.w
-        for s in range(w.n_sensors):
-            N.check(w.lib.dt_pose_control_vel(w.wp, s, self.ctrl32[t, s].data_ptr(), self.inv_T, f0, self.S + 1,
-                                              w.stream), "pose cv")
-        self.launches += w.n_sensors
+        N.check(w.lib.dt_pose_control_vel_all(w.wp, self.ctrl32[t].data_ptr(), self.inv_T, f0, self.S + 1, w.stream),
+                "pose cv")
+        self.launches += 1
 
     def _apply_bwd(self, t, f0):
         w = self.w
-        for s in range(w.n_sensors):
-            N.check(w.lib.dt_pose_control_vel_bwd(w.wp, s, self.ctrl32[t, s].data_ptr(), self.inv_T,
-                                                  self.ctrl_bar[t, s].data_ptr(), f0, self.S + 1, w.stream),
-                    "pose cv bwd")
-        self.launches += w.n_sensors
+        N.check(w.lib.dt_pose_control_vel_bwd_all(w.wp, self.ctrl32[t].data_ptr(), self.inv_T,
+                                                  self.ctrl_bar[t].data_ptr(), f0, self.S + 1, w.stream),
+                "pose cv bwd")
+        self.launches += 1
 
     # names kept for callers of the earlier interface
     @property

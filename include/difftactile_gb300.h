@@ -345,6 +345,9 @@ int dt_pose_control_vel_all(const dt_world* w, const float* Ab, float inv_T, int
  * boundary frame: call it after the adjoint substeps of frames [f0, f0 + nfr - 1). */
 int dt_pose_control_vel_bwd(const dt_world* w, int s, const float* Ab, float inv_T, float* Ab_bar, int f0, int nfr,
                             cudaStream_t stream);
+/* dt_pose_control_vel_bwd for every sensor in one launch: Ab and Ab_bar are [n_sensors][12]. */
+int dt_pose_control_vel_bwd_all(const dt_world* w, const float* Ab, float inv_T, float* Ab_bar, int f0, int nfr,
+                                cudaStream_t stream);
 
 /* ---- action input: gripper fingers (gripper_kinematics.py:196-216, fem_sensor1/2_set_control_vel) ----
  * For k < nfr: v_cv[f0 + k][i] = D[k][:, 0:3] src_i + D[k][:, 3] for every vertex i of sensor s, with
