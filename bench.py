@@ -326,6 +326,10 @@ def run_ours(args):
         out["batched_over_plain"] = value / out["plain"]["value"]
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(cfg, threads=os.cpu_count() or 1)
+        try:
+            out["grad_check"] = grad_check(cfg, w, traj, threads=os.cpu_count() or 1)
+        except Exception as exc:  # reported in the line, not fatal to the measurement
+            out["grad_check"] = {"error": repr(exc)}
     if rank == 0:
         print(json.dumps(out))
     if world_size > 1:
@@ -394,6 +398,66 @@ def cpu_baseline(cfg, threads, target_s=15.0):
             "kind": "port",
             "sample": f"{done} substeps of env 0 of {cfg.name} ({env.n_particles} particles), forward + "
                       f"recompute + adjoint per substep, float32, {threads} OpenMP threads"}
+
+
+def grad_check(cfg, w, traj, threads):
+    """Gradient parity on the benchmark's own state: one adjoint substep of the CUDA path at a
+    mid-rollout frame, against the float64 oracle's adjoint of the same substep from the same
+    (float32) state of environment 0, the oracle serving as the reference.  Returns norm-wise
+    relative errors of the frame-f adjoints of x, v, C, F and of the sensor positions."""
+    import numpy as np
+    import torch
+
+    from oracle import oracle as O
+
+    f = traj.f_end // 2 if traj.full else traj.S // 2
+    env = cfg.envs[0]
+    n0 = env.n_particles
+    P = w.particles(f)
+    st = {k: P[k][:n0].double().cpu().numpy() for k in ("x", "v", "C", "F")}
+    sl = w.vslice(w.env_rows[0].s_begin)
+    fem = lambda name, fr: w.t[name][fr, sl, :3].double().cpu().numpy()  # noqa: E731
+    st["pos"], st["vel"], st["vpos"] = [fem("v_pos", f)], [fem("v_vel", f)], [fem("v_vpos", f)]
+    cv, cv1 = [fem("v_cv", f)], [fem("v_cv", f + 1)]
+    rng = np.random.default_rng(8)
+    Np = w.n_particles
+    W = {"x": 1e-2 * rng.standard_normal((Np, 3)), "v": 1e-2 * rng.standard_normal((Np, 3)),
+         "C": 1e-4 * rng.standard_normal((Np, 3, 3)), "F": 1e-2 * rng.standard_normal((Np, 3, 3))}
+    for k in W:
+        W[k][n0:] = 0.0
+        W[k] = W[k].astype(np.float32)
+    w.adj_clear()
+    w.set_particle_adjoint(f + 1, **W)
+    w.substep_bwd(f)
+    torch.cuda.synchronize()
+    g = {k: v[:n0].double().cpu().numpy() for k, v in w.particle_adjoint(f).items()}
+    gpos = w.t["v_adj_pos"][f & 1, sl, :3].double().cpu().numpy()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))  # noqa: E731
+    # particles on the von Mises yield surface (|delta gamma| < 1e-6, a few float32 ulps of the
+    # log-strain norm; mpm_plastic.py:151-166): the return map's branch there flips under any rounding
+    # of the forward recompute, so their F adjoint is not a precision-stable quantity (the oracle in
+    # float32 and in float64 disagree there alike)
+    m = env.materials[0]
+    keep = np.ones(n0, bool)
+    if len(env.materials) == 1 and m.model == 1 and m.yield_stress > 0:
+        Fn = (np.eye(3)[None] + cfg.dt * st["C"]) @ st["F"]
+        eps = np.log(np.maximum(np.linalg.svd(Fn, compute_uv=False), 0.05))
+        dgam = np.linalg.norm(eps - eps.mean(1, keepdims=True), axis=1) - m.yield_stress / (2.0 * m.mu_lam[0])
+        keep = np.abs(dgam) >= 1e-6
+    out = {"frame": f, "env": 0, "particles": n0, "on_yield_surface": int(n0 - keep.sum())}
+    refs = {}
+    for dtype, key in ((np.float64, "f64"), (np.float32, "f32")):
+        o = O.Oracle(env, cfg.dt, dtype, n_threads=threads, grad_clip=float(w.w.grad_clip))
+        ref = refs[key] = o.substep_bwd(st, {k: W[k][:n0].astype(np.float64) for k in W}, cv=cv, cv1=cv1)
+        errs = {k: rel(g[k], ref[k]) for k in ("x", "v", "C", "F")}
+        errs["sensor_pos"] = rel(gpos, ref["pos"][0])
+        off = {k: rel(g[k][keep], ref[k][keep]) for k in ("x", "v", "C", "F")}
+        out[key] = {"rel_err": errs, "max_rel_err": max(errs.values()), "rel_err_off_yield_surface": off,
+                    "max_rel_err_off_yield_surface": max(off.values())}
+    out["oracle_f32_vs_f64"] = {k: rel(refs["f32"][k], refs["f64"][k]) for k in ("x", "v", "C", "F")}
+    out["against"] = ("the oracle's adjoint of the same substep from the same state, in float64 and in "
+                      "float32 (the CUDA path's precision)")
+    return out
 
 
 def run_reference(args):
