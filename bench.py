@@ -268,6 +268,7 @@ def run_ours(args):
                       "checkpoint_every": cfg.ckpt_every, "tape_blocks": w.tape_blocks,
                       "scatter": ["tile", "global", "warp"][w.w.scatter_mode],
                       "p_block": int(w.w.p_block), "scatter_depth": int(w.w.scatter_depth),
+                      "contact_lanes": 4 if int(w.w.contact_lanes) == 4 else 8,
                       "programmatic_dependent_launch": bool(w.lib.dt_get_pdl()),
                       "launch_shape": "autotuned" if tuned else "fixed",
                       "cuda_graph": traj.graph,

@@ -73,7 +73,7 @@ class DtWorld(C.Structure):
                 + [("dt", C.c_float), ("grad_clip", C.c_float), ("svd_sweeps", C.c_int),
                    ("svd_grad_mode", C.c_int), ("max_sensor_tris", C.c_int), ("scatter_mode", C.c_int)]
                 + [(n, _P) for n in ROPE_PTR_FIELDS] + [(n, C.c_int) for n in ROPE_INT_FIELDS]
-                + [("p_svd", _P), ("p_block", C.c_int), ("scatter_depth", C.c_int)])
+                + [("p_svd", _P), ("p_block", C.c_int), ("scatter_depth", C.c_int), ("contact_lanes", C.c_int)])
 
 
 # entry points: name -> (restype, argtypes)

@@ -10,6 +10,9 @@ scene (particle count and density, how many environments share the launch):
             (dt_world.scatter_depth): 0 sums whole runs (fewest REDs, longest shuffle chain), 1 or 2
             sum windows of 2 or 4 lanes (more REDs, fewer shuffles: faster when the launch is
             throughput-bound, slower when it is latency-bound);
+  lanes     lanes per active grid node in the contact search (dt_world.contact_lanes): 8 shortens
+            each node's dependent chain (latency-bound launches), 4 issues fewer instructions per node
+            (throughput-bound launches);
   pdl       programmatic dependent launch of the substep kernels (dt_set_pdl, library-wide).
 
 ``tune_substep`` times every candidate on one forward + backward substep of the world at a chosen
@@ -28,18 +31,21 @@ import statistics
 import torch
 
 SCATTERS = {"tile": 0, "global": 1, "warp": 2}
-DEFAULT = {"scatter": "warp", "p_block": 128, "depth": 0, "pdl": 1}
+DEFAULT = {"scatter": "warp", "p_block": 128, "depth": 0, "lanes": 8, "pdl": 1}
 
 _cache: dict[str, dict] = {}
 
 
-def candidates(scatters=("warp", "global", "tile"), p_blocks=(64, 128, 256), depths=(0, 1, 2), pdl=(1, 0)):
+def candidates(scatters=("warp", "global", "tile"), p_blocks=(64, 128, 256), depths=(0, 1, 2), lanes=(8, 4),
+               pdl=(1, 0)):
     out = []
     for s in scatters:
         for b in (p_blocks if s != "tile" else (128,)):
             for d in (depths if s == "warp" else (0,)):
-                for p in pdl:
-                    out.append({"scatter": s, "p_block": int(b), "depth": int(d), "pdl": int(p)})
+                for ln in lanes:
+                    for p in pdl:
+                        out.append({"scatter": s, "p_block": int(b), "depth": int(d), "lanes": int(ln),
+                                    "pdl": int(p)})
     return out
 
 
@@ -48,13 +54,15 @@ def apply(world, cfg: dict):
     world.w.scatter_mode = SCATTERS[cfg["scatter"]]
     world.w.p_block = int(cfg["p_block"])
     world.w.scatter_depth = int(cfg.get("depth", 0))
+    world.w.contact_lanes = int(cfg.get("lanes", 8))
     world.lib.dt_set_pdl(int(cfg["pdl"]))  # returns the previous setting
 
 
 def current(world) -> dict:
     inv = {v: k for k, v in SCATTERS.items()}
     return {"scatter": inv.get(int(world.w.scatter_mode), "warp"), "p_block": int(world.w.p_block) or 128,
-            "depth": int(world.w.scatter_depth), "pdl": int(world.lib.dt_get_pdl())}
+            "depth": int(world.w.scatter_depth), "lanes": 4 if int(world.w.contact_lanes) == 4 else 8,
+            "pdl": int(world.lib.dt_get_pdl())}
 
 
 def signature(world, tag: str = "") -> str:
@@ -152,4 +160,4 @@ def tune_substep(world, frame: int = 0, **kw) -> dict:
 
 def label(c: dict) -> str:
     depth = f"/d{c.get('depth', 0)}" if c["scatter"] == "warp" else ""
-    return f"{c['scatter']}/{c['p_block']}{depth}/{'pdl' if c['pdl'] else 'nopdl'}"
+    return f"{c['scatter']}/{c['p_block']}{depth}/l{c.get('lanes', 8)}/{'pdl' if c['pdl'] else 'nopdl'}"

@@ -24,8 +24,9 @@ namespace {
 
 constexpr int NT_TILE = 128;      // threads per CTA of the particle roles with the TILE scatter
 constexpr int TILE_MAX = 1728;    // shared P2G tile capacity in nodes (12^3), 27 KB of float4
-constexpr int GRID_LPN = 8;                 // lanes per node in the grid kernel's contact search
-constexpr int GRID_NT = 64 * GRID_LPN;     // one 4x4x4 node block per CTA
+// lanes per node in the grid kernel's contact search (dt_world.contact_lanes): 8 (shorter chains,
+// for launches with few active blocks) or 4 (fewer issued instructions per node); one 4x4x4 node
+// block per CTA of 64 * lanes threads
 constexpr int SMEM_CENT_MAX = 12288;  // triangle centroids staged in shared memory (192 KB)
 
 __device__ void mark_block(const dt_world& w, int f, int b) {
@@ -213,6 +214,7 @@ __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p,
 // one node per thread for the contact force and the grid update, so the serial per-node work issues
 // from 2 warps instead of from one lane in eight of all 16.
 // ---------------------------------------------------------------------------------------------
+template <int GRID_LPN, int GRID_NT = 64 * GRID_LPN>
 __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w, int f, int smem_cap) {
   pdl_entry();
   extern __shared__ float4 scent[];
@@ -455,14 +457,18 @@ int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   }
   return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
-int launch_l2(const dt_world* w, int f, cudaStream_t st) {
+template <int LPN>
+int l2(const dt_world* w, int f, cudaStream_t st) {
   int nb = w->n_blocks < 152 * 8 ? w->n_blocks : 152 * 8;
   if (nb <= 0) return DT_OK;
   const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
   const size_t smem = stage_bytes(cap);
   static size_t configured[64] = {};
-  if (ensure_smem((const void*)k_fwd_grid, smem, configured) != cudaSuccess) return DT_ERR_LAUNCH;
-  return launch_k(k_fwd_grid, nb, GRID_NT, smem, st, *w, f, cap) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
+  if (ensure_smem((const void*)k_fwd_grid<LPN>, smem, configured) != cudaSuccess) return DT_ERR_LAUNCH;
+  return launch_status(launch_k(k_fwd_grid<LPN>, nb, 64 * LPN, smem, st, *w, f, cap));
+}
+int launch_l2(const dt_world* w, int f, cudaStream_t st) {
+  return w->contact_lanes == 4 ? l2<4>(w, f, st) : l2<8>(w, f, st);
 }
 template <int NT>
 cudaError_t l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {

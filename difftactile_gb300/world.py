@@ -57,7 +57,7 @@ class World:
     def __init__(self, envs: list[EnvSpec], n_frames: int, dt: float, device="cuda", tape_blocks: int | None = None,
                  grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True,
                  svd_grad_mode: int = 0, scatter_mode: int = 2, svd_tape: bool = True, p_block: int = 128,
-                 scatter_depth: int = 0):
+                 scatter_depth: int = 0, contact_lanes: int = 8):
         self.lib = N.load()
         self.device = torch.device(device)
         self.specs = envs
@@ -269,6 +269,7 @@ class World:
         w.scatter_mode = int(scatter_mode)
         w.p_block = int(p_block)
         w.scatter_depth = int(scatter_depth)
+        w.contact_lanes = int(contact_lanes)
         for name in N.ROPE_PTR_FIELDS:
             setattr(w, name, t[name].data_ptr() if (self.n_ropes and t[name].numel()) else None)
         w.n_ropes, w.n_rope_particles = self.n_ropes, NR

@@ -208,6 +208,8 @@ typedef struct dt_world {
                                     shuffle steps (runs summed in windows of 2 or 4 lanes, one RED per
                                     window and node); any other value: the whole run, one RED per run
                                     and node */
+  int contact_lanes;             /* lanes per active grid node in the contact search: 4 or 8 (any other
+                                    value: 8) */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared

@@ -11,7 +11,8 @@ from difftactile_gb300 import autotune as AT
 
 def test_candidates_cover_the_shapes():
     c = AT.candidates()
-    assert len(c) == 3 * 3 * 2 + 3 * 2 + 2
+    assert len(c) == 2 * (3 * 3 * 2 + 3 * 2 + 2)
+    assert {x["lanes"] for x in c} == {8, 4}
     assert {x["p_block"] for x in c if x["scatter"] == "tile"} == {128}
     assert {(x["scatter"], x["p_block"]) for x in c if x["scatter"] != "tile"} == \
         {(s, b) for s in ("warp", "global") for b in (64, 128, 256)}

@@ -17,8 +17,8 @@ pytestmark = pytest.mark.gpu
 DT = 1e-4
 
 
-def run_gpu(envs, n_sub, cvs=None):
-    w = World(envs, n_frames=n_sub + 1, dt=DT)
+def run_gpu(envs, n_sub, cvs=None, **world_kw):
+    w = World(envs, n_frames=n_sub + 1, dt=DT, **world_kw)
     if cvs is not None:
         for s, cv in enumerate(cvs):
             w.set_control_velocity(s, cv)
@@ -66,10 +66,11 @@ def test_one_substep_elastic_cube(cuda_lib, model):
     compare(w, 1, st)
 
 
-def test_one_substep_pad_contact_and_grid(cuda_lib):
+@pytest.mark.parametrize("lanes", [8, 4])
+def test_one_substep_pad_contact_and_grid(cuda_lib, lanes):
     env = SS.pad_over_box()
     cv = [SS.control_velocity(sp) for sp in env.sensors]
-    w = run_gpu([env], 1, cv)
+    w = run_gpu([env], 1, cv, contact_lanes=lanes)
     st, dbg = run_oracle(env, 1, cv)
     assert w.error_word() == 0
     compare(w, 1, st)
@@ -159,12 +160,13 @@ def test_oob_particle_sets_error_and_is_skipped(cuda_lib):
     assert w.error_word() == 0
 
 
+@pytest.mark.parametrize("lanes", [8, 4])
 @pytest.mark.parametrize("maker", [SS.aligned_pad_over_box, SS.dome_over_box])
-def test_contact_argmin_ties_and_unordered_meshes(cuda_lib, maker):
+def test_contact_argmin_ties_and_unordered_meshes(cuda_lib, maker, lanes):
     """Exact first-minimum argmin on exact ties (grid-aligned pad) and on a spatially unordered
-    triangle list (Delaunay dome), against the oracle's sequential scan."""
+    triangle list (Delaunay dome), against the oracle's sequential scan, with 8 and 4 lanes per node."""
     env = maker()
-    w = run_gpu([env], 1)
+    w = run_gpu([env], 1, contact_lanes=lanes)
     _, dbg = run_oracle(env, 1)
     g = w.dense_grid(0)
     occ = dbg[0]["grid_m"] > env.eps
