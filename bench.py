@@ -4,8 +4,15 @@ GB300 (replicas on N GPUs under torchrun).
 One bench step = one training iteration of the sensor-press task: 100 control steps x 20 substeps
 forward (every frame kept on the device), then the backward sweep (adjoint substeps straight down
 the tape) down to the action gradients.  The batched-population workload keeps a device checkpoint
-of every step start instead and recomputes each step's substep tape in the backward sweep.  The unit counts each particle
-advanced one substep forward and back-propagated once: n_particles x 100 x 20 per bench step.
+of every step start instead and recomputes each step's substep tape in the backward sweep.  The
+unit counts each particle advanced one substep forward and back-propagated once: n_particles x 100
+x 20 per bench step.
+
+Before timing, the autotuner picks the launch shape on a mid-rollout substep and the rollout is
+recorded as CUDA graphs (the timed iterations replay them).  The line carries the dominant kernel's
+roofline (CUDA events around every 25th of its launches), the end-to-end rate through the public API
+with host buffers, the oracle on the host cores as the CPU baseline, and a full-size gradient check
+against the oracle's adjoint of one mid-rollout substep.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
 """
