@@ -72,20 +72,64 @@ DT_DEV void stage_sensor(const dt_world& w, const dt_sensor& S, float4* scent, f
   __syncthreads();
 }
 
+// Largest and smallest Euclidean distance between two axis-aligned boxes.
+DT_DEV float box_box_max(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+  const float dx = fmaxf(fabsf(ahi.x - blo.x), fabsf(bhi.x - alo.x));
+  const float dy = fmaxf(fabsf(ahi.y - blo.y), fabsf(bhi.y - alo.y));
+  const float dz = fmaxf(fabsf(ahi.z - blo.z), fabsf(bhi.z - alo.z));
+  return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+DT_DEV float box_box_min(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+  const float dx = fmaxf(fmaxf(blo.x - ahi.x, alo.x - bhi.x), 0.f);
+  const float dy = fmaxf(fmaxf(blo.y - ahi.y, alo.y - bhi.y), 0.f);
+  const float dz = fmaxf(fmaxf(blo.z - ahi.z, alo.z - bhi.z), 0.f);
+  return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
+// Groups that can hold the nearest centroid of any query point inside the box [qlo, qhi] (used for
+// sensors of more than 32 groups): every centroid of group g lies within box_box_max(q, g) of every
+// query, so no query's nearest centroid is farther than U = min_g box_box_max(q, g), and a group
+// whose box is farther than U from the query box (with a 1e-4 relative margin, far above rounding)
+// holds neither the nearest centroid nor one tied with it.  Writes the group indices, in no
+// particular order, to cand and returns their number; `sh` is 2 ints of shared scratch; every
+// thread of the CTA calls it (barriers inside).
+template <int NTH>
+DT_DEV int block_candidates(const float4* gbox, int G, float4 qlo, float4 qhi, int* cand, int* sh) {
+  const int tid = threadIdx.x;
+  __syncthreads();  // cand and sh may still be read by the previous query box's search
+  if (tid == 0) {
+    sh[0] = f2ord(3.4e38f);
+    sh[1] = 0;
+  }
+  __syncthreads();
+  float u = 3.4e38f;
+  for (int g = tid; g < G; g += NTH) u = fminf(u, box_box_max(qlo, qhi, gbox[2 * g], gbox[2 * g + 1]));
+  u = ord_min(u);
+  if ((tid & 31) == 0) atomicMin(sh, f2ord(u));
+  __syncthreads();
+  const float U = ord2f(sh[0]) * (1.f + 1e-4f);
+  for (int g = tid; g < G; g += NTH)
+    if (!(box_box_min(qlo, qhi, gbox[2 * g], gbox[2 * g + 1]) > U)) cand[atomicAdd(sh + 1, 1)] = g;
+  __syncthreads();
+  return sh[1];
+}
+
 // Argmin for the query point (px, py, pz) shared by LPN consecutive lanes (`sub` = lane index within
 // them, LPN in {4, 8}); all 32 lanes of the warp call it, `active` false for lane groups without a
 // query.  Returns the local triangle index (original order) or -1, in every lane of the group.
-// in_smem: S staged by stage_sensor; otherwise a direct scan of global centroids.
+// in_smem: S staged by stage_sensor; otherwise a direct scan of global centroids.  cand / nc: the
+// groups to search (block_candidates of a box holding the query), or null for all of them.
 template <int LPN>
 DT_DEV int closest_tri(const dt_world& w, const dt_sensor& S, const float4* scent, const float4* gbox, bool in_smem,
-                       bool active, float px, float py, float pz, int sub) {
+                       bool active, float px, float py, float pz, int sub, const int* cand = nullptr, int nc = 0) {
   const int nf = S.nf;
   Best bb{100.f, -1};
   if (in_smem) {
-    const int Gu = (nf + 31) >> 5;  // warp-uniform trip count around the shuffles
+    const int Gu = cand ? nc : (nf + 31) >> 5;  // groups searched; warp-uniform trip count around the shuffles
     const int G = active ? Gu : 0;
-    // up to 32 groups: each lane keeps its groups' box distances (group sub + LPN jj) in registers
-    // for the pruning pass; beyond that the pass recomputes them
+    auto grp = [&](int c) { return cand ? cand[c] : c; };  // group of search position c
+    // up to 32 groups: each lane keeps its groups' box distances (position sub + LPN jj) in
+    // registers for the pruning pass; beyond that the pass recomputes them
     constexpr int KM = 32 / LPN;
     const bool cached = Gu <= 32;  // warp-uniform
     float bd[KM];
@@ -93,23 +137,24 @@ DT_DEV int closest_tri(const dt_world& w, const dt_sensor& S, const float4* scen
     if (cached) {
 #pragma unroll
       for (int jj = 0; jj < KM; ++jj) {
-        const int gg = sub + LPN * jj;
+        const int c = sub + LPN * jj;
         bd[jj] = 3.4e38f;
-        if (gg < G) {
+        if (c < G) {
+          const int gg = grp(c);
           bd[jj] = box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz);
-          if (bd[jj] < gbest.d) gbest = Best{bd[jj], gg};
+          gbest = lexmin(gbest, Best{bd[jj], gg});
         }
       }
     } else {
-      for (int gg = sub; gg < G; gg += LPN) {
-        const float lb = box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz);
-        if (lb < gbest.d) gbest = Best{lb, gg};
+      for (int c = sub; c < G; c += LPN) {
+        const int gg = grp(c);
+        gbest = lexmin(gbest, Best{box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz), gg});
       }
     }
     gbest = group_min<LPN>(gbest);
     // no group is selected when every box distance is NaN (non-finite sensor positions): the
     // sentinel must not be used as an index; the pruned scan below then covers every group
-    const int g0 = gbest.i < G ? gbest.i : -1;
+    const int g0 = gbest.i != 0x7fffffff ? gbest.i : -1;
     if (g0 >= 0) {
 #pragma unroll
       for (int jj = 0; jj < 32 / LPN; ++jj) {
@@ -128,17 +173,19 @@ DT_DEV int closest_tri(const dt_world& w, const dt_sensor& S, const float4* scen
       if (cached) {
 #pragma unroll
         for (int jj = 0; jj < KM; ++jj) {
-          const int gg = sub + LPN * jj;
-          if (gg < ge && gg != g0 && !(bd[jj] > thr)) live |= 1ull << gg;
+          const int c = sub + LPN * jj;
+          if (c < ge && grp(c) != g0 && !(bd[jj] > thr)) live |= 1ull << c;
         }
       } else {
-        for (int gg = gc + sub; gg < ge; gg += LPN)
-          if (gg != g0 && !(box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr)) live |= 1ull << (gg - gc);
+        for (int c = gc + sub; c < ge; c += LPN) {
+          const int gg = grp(c);
+          if (gg != g0 && !(box_dist(gbox[2 * gg], gbox[2 * gg + 1], px, py, pz) > thr)) live |= 1ull << (c - gc);
+        }
       }
 #pragma unroll
       for (int o = 1; o < LPN; o <<= 1) live |= __shfl_xor_sync(0xffffffffu, live, o);
       while (live) {
-        const int gg = gc + __ffsll((long long)live) - 1;
+        const int gg = grp(gc + __ffsll((long long)live) - 1);
         live &= live - 1ull;
 #pragma unroll
         for (int jj = 0; jj < 32 / LPN; ++jj) {

@@ -214,7 +214,8 @@ __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p,
 // one node per thread for the contact force and the grid update, so the serial per-node work issues
 // from 2 warps instead of from one lane in eight of all 16.
 // ---------------------------------------------------------------------------------------------
-template <int GRID_LPN, int GRID_NT = 64 * GRID_LPN>
+// CAND: sensors of more than 32 groups of centroids are searched over per-block candidate groups
+template <int GRID_LPN, bool CAND, int GRID_NT = 64 * GRID_LPN>
 __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w, int f, int smem_cap) {
   pdl_entry();
   extern __shared__ float4 scent[];
@@ -222,6 +223,8 @@ __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w
   // argmin of every node of the block per sensor slot, double-buffered over the CTA's run of blocks:
   // the search (all lanes) fills one buffer while the node pass of the previous block reads the other
   __shared__ int s_cid[2][DT_MAX_SENSORS_PER_ENV][64];
+  __shared__ int s_cand[CAND ? SMEM_CENT_MAX / 32 : 1];  // candidate groups of the block
+  __shared__ int s_csh[2];
   const int cnt = *((volatile int*)(w.tape_bcount + f));
   const int tid = threadIdx.x;
   const int l = tid / GRID_LPN, sub = tid % GRID_LPN;
@@ -260,7 +263,20 @@ __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w
           stage_sensor<GRID_NT>(w, S, scent, gbox);
           staged = si;
         }
-        const int kk = closest_tri<GRID_LPN>(w, S, scent, gbox, in_smem, occ, px, py, pz, sub);
+        const int Gall = (S.nf + 31) >> 5;
+        int nc = 0;
+        const int* cand = nullptr;
+        if (CAND && in_smem && Gall > 32) {  // block-uniform: the groups any node of this block can need
+          const float4 qlo = make_float4(__fmul_rn(__fadd_rn((float)(4 * bi), 0.5f), E.dx),
+                                         __fmul_rn(__fadd_rn((float)(4 * bj), 0.5f), E.dx),
+                                         __fmul_rn(__fadd_rn((float)(4 * bk), 0.5f), E.dx), 0.f);
+          const float4 qhi = make_float4(__fmul_rn(__fadd_rn((float)(4 * bi + 3), 0.5f), E.dx),
+                                         __fmul_rn(__fadd_rn((float)(4 * bj + 3), 0.5f), E.dx),
+                                         __fmul_rn(__fadd_rn((float)(4 * bk + 3), 0.5f), E.dx), 0.f);
+          nc = block_candidates<GRID_NT>(gbox, Gall, qlo, qhi, s_cand, s_csh);
+          cand = s_cand;
+        }
+        const int kk = closest_tri<GRID_LPN>(w, S, scent, gbox, in_smem, occ, px, py, pz, sub, cand, nc);
         if (sub == 0) s_cid[it][q][l] = kk;
       }
     }
@@ -457,18 +473,20 @@ int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   }
   return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }
-template <int LPN>
+template <int LPN, bool CAND>
 int l2(const dt_world* w, int f, cudaStream_t st) {
   int nb = w->n_blocks < 152 * 8 ? w->n_blocks : 152 * 8;
   if (nb <= 0) return DT_OK;
   const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
   const size_t smem = stage_bytes(cap);
   static size_t configured[64] = {};
-  if (ensure_smem((const void*)k_fwd_grid<LPN>, smem, configured) != cudaSuccess) return DT_ERR_LAUNCH;
-  return launch_status(launch_k(k_fwd_grid<LPN>, nb, 64 * LPN, smem, st, *w, f, cap));
+  if (ensure_smem((const void*)k_fwd_grid<LPN, CAND>, smem, configured) != cudaSuccess) return DT_ERR_LAUNCH;
+  return launch_status(launch_k(k_fwd_grid<LPN, CAND>, nb, 64 * LPN, smem, st, *w, f, cap));
 }
 int launch_l2(const dt_world* w, int f, cudaStream_t st) {
-  return w->contact_lanes == 4 ? l2<4>(w, f, st) : l2<8>(w, f, st);
+  const bool big = w->max_sensor_tris > 32 * 32;  // some sensor has more than 32 groups
+  if (w->contact_lanes == 4) return big ? l2<4, true>(w, f, st) : l2<4, false>(w, f, st);
+  return big ? l2<8, true>(w, f, st) : l2<8, false>(w, f, st);
 }
 template <int NT>
 cudaError_t l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {

@@ -21,6 +21,7 @@ namespace {
 
 constexpr int RC_NT = 256;  // contact: 64 particles x 4 lanes
 constexpr int RS_NT = 256;  // solver: one CTA per rope
+constexpr int SMEM_CENT_MAX = 12288;  // triangle centroids staged in shared memory (192 KB)
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 inline int launched() { return launch_status(cudaGetLastError()); }
 
@@ -53,10 +54,14 @@ DT_DEV int rope_of_particle(const dt_world& w, int p) {
 }
 
 // ------------------------------------------------------------------------------- forward
+// CAND: sensors of more than 32 groups of centroids are searched over per-CTA candidate groups
+template <bool CAND>
 __global__ void __launch_bounds__(RC_NT) k_rope_contact(dt_world w, int f, int smem_cap) {
   pdl_entry();
   extern __shared__ float4 scent[];
   float4* gbox = scent + smem_cap;
+  __shared__ int s_cand[CAND ? SMEM_CENT_MAX / 32 : 1];  // candidate groups of the CTA
+  __shared__ int s_box[8];
   const int r = rope_of_block(w, blockIdx.x);
   const dt_rope& R = w.ropes[r];
   const int lp = (blockIdx.x - R.blk_off) * (RC_NT / 4) + (threadIdx.x >> 2), sub = threadIdx.x & 3;
@@ -81,7 +86,33 @@ __global__ void __launch_bounds__(RC_NT) k_rope_contact(dt_world w, int f, int s
     const dt_sensor& S = w.sensors[si];
     const bool in_smem = S.nf <= smem_cap;
     if (in_smem) stage_sensor<RC_NT>(w, S, scent, gbox);
-    const int kk = closest_tri<4>(w, S, scent, gbox, in_smem, active, x.x, x.y, x.z, sub);
+    const int Gall = (S.nf + 31) >> 5;
+    int nc = 0;
+    const int* cand = nullptr;
+    if (CAND && in_smem && Gall > 32) {  // block-uniform: the groups any particle of this CTA can need
+      if (threadIdx.x == 0) {
+        s_box[0] = s_box[1] = s_box[2] = f2ord(3.4e38f);
+        s_box[3] = s_box[4] = s_box[5] = f2ord(-3.4e38f);
+      }
+      __syncthreads();
+      const float big = 3.4e38f;
+      const float lx = ord_min(active ? x.x : big), ly = ord_min(active ? x.y : big), lz = ord_min(active ? x.z : big);
+      const float hx = ord_max(active ? x.x : -big), hy = ord_max(active ? x.y : -big), hz = ord_max(active ? x.z : -big);
+      if ((threadIdx.x & 31) == 0) {
+        atomicMin(s_box + 0, f2ord(lx));
+        atomicMin(s_box + 1, f2ord(ly));
+        atomicMin(s_box + 2, f2ord(lz));
+        atomicMax(s_box + 3, f2ord(hx));
+        atomicMax(s_box + 4, f2ord(hy));
+        atomicMax(s_box + 5, f2ord(hz));
+      }
+      __syncthreads();
+      const float4 qlo = make_float4(ord2f(s_box[0]), ord2f(s_box[1]), ord2f(s_box[2]), 0.f);
+      const float4 qhi = make_float4(ord2f(s_box[3]), ord2f(s_box[4]), ord2f(s_box[5]), 0.f);
+      nc = block_candidates<RC_NT>(gbox, Gall, qlo, qhi, s_cand, s_box + 6);
+      cand = s_cand;
+    }
+    const int kk = closest_tri<4>(w, S, scent, gbox, in_smem, active, x.x, x.y, x.z, sub, cand, nc);
     if (q == 0) cid.x = kk;
     else if (q == 1) cid.y = kk;
     else if (q == 2) cid.z = kk;
@@ -292,7 +323,6 @@ int set_smem(const void* fn, size_t bytes, size_t (&configured)[64]) {
   return ensure_smem(fn, bytes, configured) == cudaSuccess ? DT_OK : DT_ERR_CAPACITY;
 }
 
-constexpr int SMEM_CENT_MAX = 12288;
 
 }  // namespace
 
@@ -307,10 +337,15 @@ int dt_rope_update(const dt_world* w, int f, cudaStream_t stream) {
   int rc;
   const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
   const size_t smem = stage_bytes(cap);
-  static size_t conf_c[64] = {}, conf_s[64] = {};
-  if ((rc = set_smem((const void*)k_rope_contact, smem, conf_c))) return rc;
+  static size_t conf_c[64] = {}, conf_cc[64] = {}, conf_s[64] = {};
+  const bool big = w->max_sensor_tris > 32 * 32;  // some sensor has more than 32 groups
+  if ((rc = set_smem(big ? (const void*)k_rope_contact<true> : (const void*)k_rope_contact<false>, smem,
+                     big ? conf_cc : conf_c)))
+    return rc;
   if ((rc = set_smem((const void*)k_rope_solve, solve_smem, conf_s))) return rc;
-  if (w->rope_blocks > 0 && launch_k(k_rope_contact, w->rope_blocks, RC_NT, smem, stream, *w, f, cap) != cudaSuccess)
+  if (w->rope_blocks > 0 &&
+      launch_k(big ? k_rope_contact<true> : k_rope_contact<false>, w->rope_blocks, RC_NT, smem, stream, *w, f, cap) !=
+          cudaSuccess)
     return DT_ERR_LAUNCH;
   return launch_k(k_rope_solve, w->n_ropes, RS_NT, solve_smem, stream, *w, f) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
 }

@@ -173,3 +173,21 @@ def test_contact_argmin_ties_and_unordered_meshes(cuda_lib, maker, lanes):
     assert occ.sum() > 100
     ci = g["cidx"].cpu().numpy()[..., 0]
     assert np.array_equal(ci[occ], dbg[0]["cidx"][..., 0][occ])
+
+
+@pytest.mark.parametrize("lanes", [8, 4])
+def test_contact_argmin_large_pad(cuda_lib, lanes):
+    """A 40x40 pad (3,200 surface triangles, 100 groups of centroids) over a box: the grid kernel
+    searches per-block candidate groups; the argmin stays bit-exact with the oracle's scan."""
+    env = SS.pad_over_box(n=64, box_cells=(16, 4, 16), pad=(40, 40, 2))
+    assert len(env.sensors[0].tris) > 32 * 32
+    cv = [SS.control_velocity(sp) for sp in env.sensors]
+    w = run_gpu([env], 1, cv, contact_lanes=lanes)
+    st, dbg = run_oracle(env, 1, cv)
+    assert w.error_word() == 0
+    compare(w, 1, st)
+    g = w.dense_grid(0)
+    occ = dbg[0]["grid_m"] > env.eps
+    assert occ.sum() > 1000
+    ci = g["cidx"].cpu().numpy()[..., 0]
+    assert np.array_equal(ci[occ], dbg[0]["cidx"][..., 0][occ])

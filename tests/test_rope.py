@@ -118,3 +118,19 @@ def test_rope_adjoint_matches_oracle(cuda_lib):
             "pos": SS.rel_err(w.t["v_adj_pos"][0, sl, :3].cpu().numpy(), ref["pos"][0]),
             "vel": SS.rel_err(w.t["v_adj_vel"][0, sl, :3].cpu().numpy(), ref["vel"][0])}
     assert max(errs.values()) < 1e-3, errs
+
+
+def test_rope_argmin_on_a_large_pad(cuda_lib):
+    """A 40x40 pad (3,200 surface triangles, 100 groups of centroids: the per-CTA candidate search)
+    over a 48-particle rope: argmin bit-exact and state as the oracle's."""
+    env = SS.rope_under_pad(n_rope=48, pad=(40, 40, 2))
+    assert len(env.sensors[0].tris) > 32 * 32
+    cv = [SS.control_velocity(sp, scale=0.02, down=-0.05) for sp in env.sensors]
+    n_sub = 2
+    w = run_gpu([env], n_sub, cv)
+    st, dbgs = oracle_run(env, n_sub, cv)
+    for f, d in enumerate(dbgs):
+        cid = w.t["r_cidx"][f, :, 0].cpu().numpy()
+        assert np.array_equal(cid, d["rope_cidx"][0][:, 0]), f
+    rs = {k: v.cpu().numpy() for k, v in w.rope_state(n_sub, 0).items()}
+    assert SS.rel_err(rs["pos"], st["rpos"][0]) < 1e-5
