@@ -146,17 +146,15 @@ def run_ours(args):
     import torch
     import torch.distributed as dist
 
-    world_size = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from difftactile_gb300 import replicas
+
+    rank, world_size, local = replicas.rank_info()
     if world_size > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    def barrier():
-        if world_size > 1:
-            dist.barrier()
+    barrier = replicas.barrier
 
     cfg = make_config(args.config, args.horizon, args.envs)
     kw = {} if args.scatter is None else {"scatter_mode": {"tile": 0, "global": 1, "warp": 2}[args.scatter]}
@@ -248,12 +246,9 @@ def run_ours(args):
     traj.reset_graphs()  # the end-to-end iterations record their own graphs, without the event pairs
     launches_per_iter = traj.launches // max(args.steps, 1) + 2  # + loss readout/adjoint seeds
     ms = sum(times) / len(times)
-    if world_size > 1:
-        tm = torch.tensor([ms], device=dev)
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-        ms = float(tm.item())
+    ms = replicas.slowest(ms, dev)  # the step of the whole job lasts as long as its slowest rank
     units = cfg.n_particles * cfg.n_steps * cfg.substeps
-    value = units * world_size / (ms / 1e3)
+    value = replicas.total(units, dev) / (ms / 1e3)
 
     # ---- roofline of the dominant kernel ----
     used = t["tape_bcount"][: traj.f_end]
@@ -321,11 +316,8 @@ def run_ours(args):
             if i > 0:
                 e2e.append(t1 - t0)
         e_ms = 1e3 * sum(e2e) / len(e2e)
-        if world_size > 1:
-            tm = torch.tensor([e_ms], device=dev)
-            dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-            e_ms = float(tm.item())
-        out["e2e"] = {"value": units * world_size / (e_ms / 1e3), "unit": "particle-substeps/s",
+        e_ms = replicas.slowest(e_ms, dev)
+        out["e2e"] = {"value": replicas.total(units, dev) / (e_ms / 1e3), "unit": "particle-substeps/s",
                       "ms_per_step": e_ms,
                       "h2d_bytes_per_step": int(h_act.numel() * 4 + h_x.numel() * 4 + h_v.numel() * 4),
                       "d2h_bytes_per_step": int(res.numel() * 8)}
