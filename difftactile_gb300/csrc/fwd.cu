@@ -207,12 +207,12 @@ __global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p,
 }
 
 // ---------------------------------------------------------------------------------------------
-// L2: grid update + contact over the frame's active blocks.  512 threads per 4x4x4 block: eight
-// lanes per node share the node's argmin over the sensor's triangle centroids (staged in shared
-// memory, contact.cuh: closest_tri); the (distance, index) pairs are combined lexicographically,
-// which is exactly the sequential scan's first-minimum-wins result.  Then the first two warps take
-// one node per thread for the contact force and the grid update, so the serial per-node work issues
-// from 2 warps instead of from one lane in eight of all 16.
+// L2: grid update + contact over the frame's active blocks.  64 x GRID_LPN threads per 4x4x4 block:
+// GRID_LPN (8 or 4) lanes per node share the node's argmin over the sensor's triangle centroids
+// (staged in shared memory, contact.cuh: closest_tri); the (distance, index) pairs are combined
+// lexicographically, which is exactly the sequential scan's first-minimum-wins result.  Then the
+// first two warps take one node per thread for the contact force and the grid update, so the serial
+// per-node work issues from 2 warps instead of from one lane in GRID_LPN of every warp.
 // ---------------------------------------------------------------------------------------------
 // CAND: sensors of more than 32 groups of centroids are searched over per-block candidate groups
 template <int GRID_LPN, bool CAND, int GRID_NT = 64 * GRID_LPN>
