@@ -383,10 +383,13 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) A.a[i][j] = E.stress_k * s.cauchy.a[i][j] + pm * r.C.a[i][j];
-  // gather the grid adjoint
+  // gather the grid adjoint.  With m_o the momentum adjoint of node o, W_o its weight and
+  // dp_o = (o - fx) dx:  v_bar = p_mass S0,  A_bar = dx (S1 - S0 fx^T)  with  S0 = sum W_o m_o and
+  // S1 = sum W_o m_o o^T,  and  fx_bar_d = sum dW_o/dfx_d Wb_o - dx (A^T S0)_d  with
+  // Wb_o = m_o . (p_mass v + A dp_o) + p_mass mass_bar_o  — the per-node work is two moments and Wb_o
   const float4* aacc = reinterpret_cast<const float4*>(w.g_adj_acc);
-  v3 vb = v3{0.f, 0.f, 0.f};
-  m3 Ab = mzero();
+  v3 S0 = v3{0.f, 0.f, 0.f};
+  m3 S1 = mzero();
   float fxb[3] = {0.f, 0.f, 0.f};
   float wts[3][3], dws[3][3];
 #pragma unroll
@@ -396,6 +399,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
       wts[i][d] = bsw(i, fx[d]);
       dws[i][d] = bsdw(i, fx[d]);
     }
+  const v3 pmv = pm * r.v;
 #pragma unroll
   for (int oi = 0; oi < 3; ++oi)
 #pragma unroll
@@ -405,22 +409,36 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
         const float4 gb = __ldg(aacc + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok));
         const v3 mvb = f4to3(gb);
         const float W = (wts[oi][0] * wts[oj][1]) * wts[ok][2];
-        const v3 dp = v3{((float)oi - fx[0]) * dx, ((float)oj - fx[1]) * dx, ((float)ok - fx[2]) * dx};
-        const v3 Adp = mvec(A, dp);
-        vb = vb + (W * pm) * mvb;
+        const v3 Wm = W * mvb;
+        S0 = S0 + Wm;
+        const float o[3] = {(float)oi, (float)oj, (float)ok};
 #pragma unroll
-        for (int rr = 0; rr < 3; ++rr) {
-          const float mr = rr == 0 ? mvb.x : (rr == 1 ? mvb.y : mvb.z);
-          Ab.a[rr][0] += W * mr * dp.x;
-          Ab.a[rr][1] += W * mr * dp.y;
-          Ab.a[rr][2] += W * mr * dp.z;
+        for (int c = 0; c < 3; ++c) {
+          if (o[c] == 0.f) continue;  // resolved at compile time
+          S1.a[0][c] += o[c] * Wm.x;
+          S1.a[1][c] += o[c] * Wm.y;
+          S1.a[2][c] += o[c] * Wm.z;
         }
-        const float Wb = dot(mvb, pm * r.v + Adp) + pm * gb.w;
-        const v3 Atm = mTvec(A, mvb);  // dpos adjoint / W
-        fxb[0] += Wb * (dws[oi][0] * wts[oj][1] * wts[ok][2]) - dx * W * Atm.x;
-        fxb[1] += Wb * (wts[oi][0] * dws[oj][1] * wts[ok][2]) - dx * W * Atm.y;
-        fxb[2] += Wb * (wts[oi][0] * wts[oj][1] * dws[ok][2]) - dx * W * Atm.z;
+        const v3 dp = v3{(o[0] - fx[0]) * dx, (o[1] - fx[1]) * dx, (o[2] - fx[2]) * dx};
+        const float Wb = dot(mvb, pmv + mvec(A, dp)) + pm * gb.w;
+        fxb[0] += Wb * (dws[oi][0] * wts[oj][1] * wts[ok][2]);
+        fxb[1] += Wb * (wts[oi][0] * dws[oj][1] * wts[ok][2]);
+        fxb[2] += Wb * (wts[oi][0] * wts[oj][1] * dws[ok][2]);
       }
+  const v3 vb = pm * S0;
+  m3 Ab;
+#pragma unroll
+  for (int rr = 0; rr < 3; ++rr) {
+    const float s0 = rr == 0 ? S0.x : (rr == 1 ? S0.y : S0.z);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Ab.a[rr][c] = dx * (S1.a[rr][c] - s0 * fx[c]);
+  }
+  {
+    const v3 AtS0 = mTvec(A, S0);
+    fxb[0] -= dx * AtS0.x;
+    fxb[1] -= dx * AtS0.y;
+    fxb[2] -= dx * AtS0.z;
+  }
   // affine = stress_k * cauchy + p_mass * C
   m3 Cb = mscale(pm, Ab);
   const m3 G = mscale(E.stress_k, Ab);  // cauchy adjoint
