@@ -367,9 +367,11 @@ __device__ void g2p_particle(const dt_world& w, int f, int p) {
     q3n[2] = q3.z;
     return;
   }
+  // new v = sum W_o v_o; new C = g2p_k sum W_o v_o (o - fx)^T = g2p_k (S1 - v fx^T) with
+  // S1 = sum W_o v_o o^T: per node one product W v_o and the moment's nonzero columns
   const float4* vout = reinterpret_cast<const float4*>(w.g_vout);
   v3 nv = v3{0.f, 0.f, 0.f};
-  m3 nC = mzero();
+  m3 S1 = mzero();
   float wts[3][3];
 #pragma unroll
   for (int d = 0; d < 3; ++d)
@@ -383,16 +385,24 @@ __device__ void g2p_particle(const dt_world& w, int f, int p) {
       for (int ok = 0; ok < 3; ++ok) {
         const v3 gv = f4to3(__ldg(vout + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok)));
         const float W = (wts[oi][0] * wts[oj][1]) * wts[ok][2];
-        const float kw = E.g2p_k * W;
-        const float d[3] = {(float)oi - fx[0], (float)oj - fx[1], (float)ok - fx[2]};
-        nv = nv + W * gv;
+        const v3 Wg = W * gv;
+        nv = nv + Wg;
+        const float o[3] = {(float)oi, (float)oj, (float)ok};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          nC.a[0][c] += kw * (gv.x * d[c]);
-          nC.a[1][c] += kw * (gv.y * d[c]);
-          nC.a[2][c] += kw * (gv.z * d[c]);
+          if (o[c] == 0.f) continue;  // resolved at compile time
+          S1.a[0][c] += o[c] * Wg.x;
+          S1.a[1][c] += o[c] * Wg.y;
+          S1.a[2][c] += o[c] * Wg.z;
         }
       }
+  m3 nC;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    nC.a[0][c] = E.g2p_k * (S1.a[0][c] - nv.x * fx[c]);
+    nC.a[1][c] = E.g2p_k * (S1.a[1][c] - nv.y * fx[c]);
+    nC.a[2][c] = E.g2p_k * (S1.a[2][c] - nv.z * fx[c]);
+  }
   const v3 nx = x + w.dt * nv;
   if (!finite3(nx)) set_err(w, DT_DEVERR_NONFINITE);
   pplane(w, f + 1, 0)[p] = make_float4(nx.x, nx.y, nx.z, nv.x);
