@@ -132,29 +132,43 @@ __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile,
         dws[i][1] = bsdw(i, fx[1]);
         dws[i][2] = bsdw(i, fx[2]);
       }
+      // With v_o the grid velocity of node o:  Wb_o = v_o . (vnb + g2p_k C_bar (o - fx)) = v_o . u_o,
+      // u_o = u_0 + sum_c o_c k_c  (u_0 = vnb - g2p_k C_bar fx, k_c = g2p_k C_bar column c), and the
+      // weight-independent part of fx_bar, -g2p_k sum_o W_o C_bar^T v_o, is -g2p_k C_bar^T S0 with
+      // S0 = sum W_o v_o, applied after the loop
+      const float gk = E.g2p_k;
+      const v3 k0 = gk * mcol(Cb, 0), k1 = gk * mcol(Cb, 1), k2 = gk * mcol(Cb, 2);
+      const v3 u0 = vnb - ((fx[0] * k0 + fx[1] * k1) + fx[2] * k2);
+      v3 S0 = v3{0.f, 0.f, 0.f};
+      v3 ui = u0;  // u_o built up along the loops: + k0 per step of oi, + k1 of oj, + k2 of ok
 #pragma unroll
-      for (int oi = 0; oi < 3; ++oi)
+      for (int oi = 0; oi < 3; ++oi, ui = ui + k0) {
+        v3 uij = ui;
 #pragma unroll
-        for (int oj = 0; oj < 3; ++oj)
+        for (int oj = 0; oj < 3; ++oj, uij = uij + k1) {
+          v3 u = uij;
 #pragma unroll
-          for (int ok_ = 0; ok_ < 3; ++ok_) {
+          for (int ok_ = 0; ok_ < 3; ++ok_, u = u + k2) {
             const v3 gv = f4to3(__ldg(vout + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok_)));
             const float W = (wx[oi] * wy[oj]) * wz[ok_];
-            const float kw = E.g2p_k * W;
-            const v3 d = v3{(float)oi - fx[0], (float)oj - fx[1], (float)ok_ - fx[2]};
-            const v3 Ctg = mTvec(Cb, gv);  // C_bar^T gv
-            const float Wb = dot(gv, vnb) + E.g2p_k * dot(Ctg, d);
-            fxb[0] += Wb * (dws[oi][0] * wy[oj] * wz[ok_]) - kw * Ctg.x;
-            fxb[1] += Wb * (wx[oi] * dws[oj][1] * wz[ok_]) - kw * Ctg.y;
-            fxb[2] += Wb * (wx[oi] * wy[oj] * dws[ok_][2]) - kw * Ctg.z;
+            const float Wb = dot(gv, u);
+            S0 = S0 + W * gv;
+            fxb[0] += Wb * (dws[oi][0] * wy[oj] * wz[ok_]);
+            fxb[1] += Wb * (wx[oi] * dws[oj][1] * wz[ok_]);
+            fxb[2] += Wb * (wx[oi] * wy[oj] * dws[ok_][2]);
           }
+        }
+      }
+      const v3 CtS0 = mTvec(Cb, S0);
+      fxb[0] -= gk * CtS0.x;
+      fxb[1] -= gk * CtS0.y;
+      fxb[2] -= gk * CtS0.z;
       const v3 xb = xb1 + E.inv_dx * v3{fxb[0], fxb[1], fxb[2]};
       *out0 = make_float4(xb.x, xb.y, xb.z, 0.f);
-      const float gk = E.g2p_k;
-      c0 = gk * mcol(Cb, 0);
-      c1 = gk * mcol(Cb, 1);
-      c2 = gk * mcol(Cb, 2);
-      q = vnb - ((fx[0] * c0 + fx[1] * c1) + fx[2] * c2);
+      c0 = k0;
+      c1 = k1;
+      c2 = k2;
+      q = u0;
     }
   }
   StencilRec rec;
