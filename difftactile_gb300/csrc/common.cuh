@@ -213,30 +213,13 @@ DT_DEV void qr_givens(float B[3][3], float U[3][3], int i, int j, int col) {
   }
 }
 
-// V0: optional starting rotation (the previous substep's V, whose columns nearly diagonalize
-// A^T A already): the sweeps then start from V0^T A^T A V0 = (A V0)^T (A V0)
-DT_DEV void svd3(const m3& A, m3& U, v3& sv, m3& V, int sweeps, const m3* V0 = nullptr) {
+DT_DEV void svd3(const m3& A, m3& U, v3& sv, m3& V, int sweeps) {
   float S[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) S[i][j] = A.a[0][i] * A.a[0][j] + A.a[1][i] * A.a[1][j] + A.a[2][i] * A.a[2][j];
   float Vm[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
-  if (V0 != nullptr) {
-    float B0[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        B0[i][j] = A.a[i][0] * V0->a[0][j] + A.a[i][1] * V0->a[1][j] + A.a[i][2] * V0->a[2][j];
-        Vm[i][j] = V0->a[i][j];
-      }
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) S[i][j] = B0[0][i] * B0[0][j] + B0[1][i] * B0[1][j] + B0[2][i] * B0[2][j];
-  } else {
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) S[i][j] = A.a[0][i] * A.a[0][j] + A.a[1][i] * A.a[1][j] + A.a[2][i] * A.a[2][j];
-  }
   for (int it = 0; it < sweeps; ++it) {
     // converged once the off-diagonal is below fp32 resolution of the diagonal
     const float off = S[0][1] * S[0][1] + S[0][2] * S[0][2] + S[1][2] * S[1][2];
@@ -485,7 +468,7 @@ DT_DEV void load_svd(const dt_world& w, int f, int p, m3& U, v3& sg, m3& V) {
 // mpm_plastic.py:151-166,228-235).  svd_src: frame whose tape holds the SVD of this F_new (the
 // backward re-reading the forward's), or -1 to compute it.  Neo-Hookean stress needs no SVD.
 DT_DEV void constitutive(const m3& C, const m3& F, float dt, const dt_material& M, int sweeps, Stress& s,
-                         const dt_world* w = nullptr, int svd_src = -1, int p = 0, int warm_src = -1) {
+                         const dt_world* w = nullptr, int svd_src = -1, int p = 0) {
   m3 A = meye();
 #pragma unroll
   for (int i = 0; i < 3; ++i)
@@ -498,21 +481,6 @@ DT_DEV void constitutive(const m3& C, const m3& F, float dt, const dt_material& 
     s.sig = v3{1.f, 1.f, 1.f};
   } else if (w != nullptr && svd_src >= 0) {
     load_svd(*w, svd_src, p, s.U, s.sig, s.V);
-  } else if (w != nullptr && warm_src >= 0) {
-    // warm start from the SVD tape of frame warm_src (the previous substep) when its V is a rotation
-    // (a frame never written holds zeros): F changes little in one substep, so one sweep mostly suffices
-    const float4 c = svd_plane(*w, warm_src, 2)[p], d = svd_plane(*w, warm_src, 3)[p], e = svd_plane(*w, warm_src, 4)[p];
-    m3 V0;
-    V0.a[0][0] = c.y; V0.a[0][1] = c.z; V0.a[0][2] = c.w;
-    V0.a[1][0] = d.x; V0.a[1][1] = d.y; V0.a[1][2] = d.z;
-    V0.a[2][0] = d.w; V0.a[2][1] = e.x; V0.a[2][2] = e.y;
-    bool unit = true;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float n2 = V0.a[0][k] * V0.a[0][k] + V0.a[1][k] * V0.a[1][k] + V0.a[2][k] * V0.a[2][k];
-      unit = unit && fabsf(n2 - 1.f) < 1e-3f;
-    }
-    svd3(s.Fn, s.U, s.sig, s.V, sweeps, unit ? &V0 : nullptr);
   } else {
     svd3(s.Fn, s.U, s.sig, s.V, sweeps);
   }

@@ -64,7 +64,7 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
     if (!ok) set_err(w, DT_DEVERR_PARTICLE_OOB);
     if (ok) {
       const dt_material M = w.materials[__ldg(w.p_mat + p)];
-      constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s, &w, -1, p, w.p_svd && f > 0 ? f - 1 : -1);
+      constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s);
       if (w.p_svd && M.model != DT_MODEL_NEOHOOKEAN) store_svd(w, f, p, s.U, s.sig, s.V);  // for the adjoint
       pm = E.p_mass;
       const float dx = E.dx, sk = E.stress_k;
