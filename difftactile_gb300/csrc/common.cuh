@@ -213,6 +213,26 @@ DT_DEV void qr_givens(float B[3][3], float U[3][3], int i, int j, int col) {
   }
 }
 
+// columns of M made orthonormal in order (modified Gram-Schmidt); a rotation stays a rotation
+DT_DEV void orthonormalize(float M[3][3]) {
+  float n0 = rsqrtf(M[0][0] * M[0][0] + M[1][0] * M[1][0] + M[2][0] * M[2][0]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) M[i][0] *= n0;
+  float d01 = M[0][0] * M[0][1] + M[1][0] * M[1][1] + M[2][0] * M[2][1];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) M[i][1] -= d01 * M[i][0];
+  float n1 = rsqrtf(M[0][1] * M[0][1] + M[1][1] * M[1][1] + M[2][1] * M[2][1]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) M[i][1] *= n1;
+  float d02 = M[0][0] * M[0][2] + M[1][0] * M[1][2] + M[2][0] * M[2][2];
+  float d12 = M[0][1] * M[0][2] + M[1][1] * M[1][2] + M[2][1] * M[2][2];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) M[i][2] -= d02 * M[i][0] + d12 * M[i][1];
+  float n2 = rsqrtf(M[0][2] * M[0][2] + M[1][2] * M[1][2] + M[2][2] * M[2][2]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) M[i][2] *= n2;
+}
+
 DT_DEV void svd3(const m3& A, m3& U, v3& sv, m3& V, int sweeps) {
   float S[3][3];
 #pragma unroll
@@ -244,6 +264,11 @@ DT_DEV void svd3(const m3& A, m3& U, v3& sv, m3& V, int sweeps) {
   qr_givens(B, Um, 0, 2, 0);
   qr_givens(B, Um, 1, 2, 1);
   sv = v3{B[0][0], B[1][1], B[2][2]};
+  // one Gram-Schmidt pass on both factors: the rotations' approximate reciprocals leave columns
+  // ~1e-6 off orthonormal, which the SVD adjoint's 1 / (s_j^2 - s_i^2) factors amplify wherever two
+  // singular values nearly coincide; the pass brings them to rounding (~1e-7)
+  orthonormalize(Um);
+  orthonormalize(Vm);
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
