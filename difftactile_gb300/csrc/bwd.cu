@@ -24,6 +24,16 @@ DT_DEV float clampg(float a, float c) { return c > 0.f ? fminf(fmaxf(a, -c), c) 
 DT_DEV v3 clampg(v3 a, float c) { return v3{clampg(a.x, c), clampg(a.y, c), clampg(a.z, c)}; }
 DT_DEV float4 ld4(const float4* p) { return *p; }
 
+// (y^p - x^p) / (y - x) for x, y > 0, with its series in t = (y - x) / x where the two are within 1%
+// (the direct quotient would cancel): p x^(p-1) (1 + q t / 2 + q (q-1) t^2 / 6 + q (q-1) (q-2) t^3 / 24),
+// q = p - 1, truncation below 1e-8 there
+DT_DEV float pow_dd(float x, float y, float p) {
+  const float h = y - x;
+  if (fabsf(h) > 1e-2f * fmaxf(x, y)) return (powf(y, p) - powf(x, p)) / h;
+  const float t = h / x, q = p - 1.f;
+  return p * powf(x, q) * (1.f + t * (0.5f * q + t * (q * (q - 1.f) / 6.f + t * (q * (q - 1.f) * (q - 2.f) / 24.f))));
+}
+
 // the reference's clamp of the singular-value gap (mpm_elastic.py:150-155)
 DT_DEV float gap_clamp(float a) { return a >= 0.f ? fmaxf(a, 1e-8f) : fminf(a, -1e-8f); }
 
@@ -457,6 +467,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   m3 Cb = mscale(pm, Ab);
   const m3 G = mscale(E.stress_k, Ab);  // cauchy adjoint
   m3 Ub = mzero(), Vb = mzero(), Rb = mzero();
+  m3 Frm = mzero();  // the return map's rotation-part adjoint when formed directly (von Mises)
   v3 sb = v3{0.f, 0.f, 0.f};
   float Jb;
   if (M.model == DT_MODEL_NEOHOOKEAN) {
@@ -498,16 +509,38 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
 #pragma unroll
       for (int d = 0; d < 3; ++d) ex[d] = expf(ep[d] - rr * eh[d]);
       const m3 UtFV = mmul(mTmul(s.U, Fpb), s.V);
-      m3 Ue = s.U, Ve = s.V;
+      if (w.svd_grad_mode != DT_SVDGRAD_REFERENCE && sg[0] > 0.05f && sg[1] > 0.05f && sg[2] > 0.05f) {
+        // e_k = c s_k^a (a = 1 - rr, c = exp(rr mean)): the rotation part of the SVD adjoint of
+        // Fp = U diag(e) V^T has, for i != j and M = U^T Fp_bar V, the entries
+        //   M_ij (e_j s_j - e_i s_i) / (s_j^2 - s_i^2) + M_ji (s_i e_j - e_i s_j) / (s_j^2 - s_i^2)
+        // = M_ij c dd(a+1) / (s_i + s_j) + M_ji c s_i s_j dd(a-1) / (s_i + s_j),  dd(p) the divided
+        // difference of x^p at (s_i, s_j): finite where singular values coincide, unlike the generic
+        // formula's 1 / (s_j^2 - s_i^2)
+        const float a = 1.f - rr, c = expf(rr * mean);
+        m3 inner = mzero();
 #pragma unroll
-      for (int i = 0; i < 3; ++i)
+        for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          Ue.a[i][d] *= ex[d];
-          Ve.a[i][d] *= ex[d];
-        }
-      Ub = madd(Ub, mmul(Fpb, Ve));   // Fpb V diag(e)
-      Vb = madd(Vb, mTmul(Fpb, Ue));  // Fpb^T U diag(e)
+          for (int j = 0; j < 3; ++j) {
+            if (i == j) continue;
+            const float sum = sg[i] + sg[j];
+            const float A = c * pow_dd(sg[i], sg[j], a + 1.f) / sum;
+            const float B = c * (sg[i] * sg[j]) * pow_dd(sg[i], sg[j], a - 1.f) / sum;
+            inner.a[i][j] = UtFV.a[i][j] * A + UtFV.a[j][i] * B;
+          }
+        Frm = mmulT(mmul(s.U, inner), s.V);
+      } else {
+        m3 Ue = s.U, Ve = s.V;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            Ue.a[i][d] *= ex[d];
+            Ve.a[i][d] *= ex[d];
+          }
+        Ub = madd(Ub, mmul(Fpb, Ve));   // Fpb V diag(e)
+        Vb = madd(Vb, mTmul(Fpb, Ue));  // Fpb^T U diag(e)
+      }
       float epb[3], ehb[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) epb[d] = UtFV.a[d][d] * ex[d];
@@ -535,7 +568,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
       Fnb = Fpb;
     }
   }
-  if (M.model != DT_MODEL_NEOHOOKEAN) Fnb = madd(Fnb, svd_grad(s.U, s.sig, s.V, Ub, sb, Vb, Rb, w.svd_grad_mode));
+  if (M.model != DT_MODEL_NEOHOOKEAN) Fnb = madd(madd(Fnb, Frm), svd_grad(s.U, s.sig, s.V, Ub, sb, Vb, Rb, w.svd_grad_mode));
   // F_new = (I + dt C) F
   m3 Ad = meye();
 #pragma unroll

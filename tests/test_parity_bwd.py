@@ -185,3 +185,45 @@ def test_multi_substep_backward_equals_substep_sequence(cuda_lib):
     for k in ("x", "v", "C", "F"):
         spread = SS.rel_err(outs[1][k], outs[0][k])
         assert SS.rel_err(outs[2][k], outs[0][k]) <= max(10 * spread, 1e-6), (k, spread)
+
+
+def test_adjoint_mid_rollout_plastic_state(cuda_lib):
+    """One adjoint substep from a mid-rollout state of compressed plastic material (the pad pressing
+    a box of yield stress 2 for 16 substeps: every particle yielding, most with two singular values
+    of F_new within 0.1% of each other) against the float64 oracle's adjoint of the same substep from
+    the same float32 state.  The CUDA return-map adjoint forms the rotation part with divided
+    differences, so it stays precise where the generic SVD adjoint's 1 / (s_j^2 - s_i^2) would
+    amplify float32 rounding; only particles within 1e-6 of the yield surface (whose branch flips
+    under rounding) are excepted.  Tolerance 1e-3 relative on every adjoint."""
+    env = SS.pad_over_box(yield_stress=2.0)
+    cv = [SS.control_velocity(sp, down=-0.3) for sp in env.sensors]
+    n = 16
+    w = World([env], n_frames=n + 2, dt=DT, grad_clip=0.0)
+    for s, c in enumerate(cv):
+        w.set_control_velocity(s, c)
+    w.step_begin()
+    for f in range(n + 1):
+        w.substep(f)
+    f = n
+    P = w.particles(f)
+    st = {k: P[k].double().cpu().numpy() for k in ("x", "v", "C", "F")}
+    sl = w.vslice(0)
+    fem = lambda name, fr: w.t[name][fr, sl, :3].double().cpu().numpy()  # noqa: E731
+    st["pos"], st["vel"], st["vpos"] = [fem("v_pos", f)], [fem("v_vel", f)], [fem("v_vpos", f)]
+    W = {k: v.astype(np.float32) for k, v in loss_weights(env, env.n_particles, 31).items() if k in ("x", "v", "C", "F")}
+    w.adj_clear()
+    w.set_particle_adjoint(f + 1, **W)
+    w.substep_bwd(f)
+    torch.cuda.synchronize()
+    assert w.error_word() == 0
+    g = {k: v.double().cpu().numpy() for k, v in w.particle_adjoint(f).items()}
+    o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
+    ref = o.substep_bwd(st, {k: W[k].astype(np.float64) for k in W}, cv=[fem("v_cv", f)], cv1=[fem("v_cv", f + 1)])
+    m = env.materials[0]
+    Fn = (np.eye(3)[None] + DT * st["C"]) @ st["F"]
+    eps = np.log(np.maximum(np.linalg.svd(Fn, compute_uv=False), 0.05))
+    dgam = np.linalg.norm(eps - eps.mean(1, keepdims=True), axis=1) - m.yield_stress / (2.0 * m.mu_lam[0])
+    assert (dgam > 0).mean() > 0.5, "the state should be mostly yielding"
+    keep = np.abs(dgam) >= 1e-6
+    errs = {k: SS.rel_err(g[k][keep], ref[k][keep]) for k in ("x", "v", "C", "F")}
+    assert max(errs.values()) < 1e-3, errs
