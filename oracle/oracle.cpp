@@ -905,6 +905,14 @@ template <typename T>
 inline T clampg(T a, T c) {
   return c > T(0) ? std::min(std::max(a, -c), c) : a;
 }
+// (y^p - x^p) / (y - x) for x, y > 0, by its series in t = (y - x) / x where the two are within 1%
+template <typename T>
+inline T pow_dd(T x, T y, T p) {
+  const T h = y - x;
+  if (std::fabs(h) > T(1e-2) * std::max(x, y)) return (std::pow(y, p) - std::pow(x, p)) / h;
+  const T t = h / x, q = p - T(1);
+  return p * std::pow(x, q) * (T(1) + t * (T(0.5) * q + t * (q * (q - T(1)) / T(6) + t * (q * (q - T(1)) * (q - T(2)) / T(24)))));
+}
 template <typename T>
 inline T gap_clamp(T a) {
   return a >= T(0) ? std::max(a, T(1e-8)) : std::min(a, T(-1e-8));
@@ -1466,6 +1474,7 @@ static int substep_bwd_impl(const orc_scene* sc, const T* x, const T* v, const T
           fxb[2] += Wb * (o.w[i][0] * o.w[j][1] * o.dw[k][2]) - dx * W * Atm[2];
         }
     M3<T> Cbp, G, Fpb, Ub = mzero<T>(), Vb = mzero<T>(), Rb = mzero<T>();
+    M3<T> Frm = mzero<T>();  // the return map's rotation-part adjoint when formed directly
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {
         Cbp.a[i][j] = pm * Ab.a[i][j];
@@ -1522,17 +1531,35 @@ static int substep_bwd_impl(const orc_scene* sc, const T* x, const T* v, const T
         T ex[3];
         for (int d = 0; d < 3; ++d) ex[d] = std::exp(ep[d] - rr * eh[d]);
         M3<T> UtFV = mmul(mmul(mT(o.U), Fpb), o.V), Ue = o.U, Ve = o.V;
-        for (int i = 0; i < 3; ++i)
-          for (int d = 0; d < 3; ++d) {
-            Ue.a[i][d] *= ex[d];
-            Ve.a[i][d] *= ex[d];
-          }
-        M3<T> a1 = mmul(Fpb, Ve), a2 = mmul(mT(Fpb), Ue);
-        for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 3; ++j) {
-            Ub.a[i][j] += a1.a[i][j];
-            Vb.a[i][j] += a2.a[i][j];
-          }
+        if (svd_grad_mode != 1 && o.sig[0] > T(0.05) && o.sig[1] > T(0.05) && o.sig[2] > T(0.05)) {
+          // stable form (not in the reference): with e_k = c s_k^a the rotation part of the SVD
+          // adjoint of Fp = U diag(e) V^T is, off the diagonal,
+          // M_ij c dd(a+1) / (s_i + s_j) + M_ji c s_i s_j dd(a-1) / (s_i + s_j), dd the divided
+          // difference of x^p; equal to the generic formula below wherever that one is finite
+          const T a = T(1) - rr, c = std::exp(rr * mean);
+          M3<T> inner = mzero<T>();
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+              if (i == j) continue;
+              const T sum = o.sig[i] + o.sig[j];
+              const T A = c * pow_dd(o.sig[i], o.sig[j], a + T(1)) / sum;
+              const T B = c * (o.sig[i] * o.sig[j]) * pow_dd(o.sig[i], o.sig[j], a - T(1)) / sum;
+              inner.a[i][j] = UtFV.a[i][j] * A + UtFV.a[j][i] * B;
+            }
+          Frm = mmul(mmul(o.U, inner), mT(o.V));
+        } else {
+          for (int i = 0; i < 3; ++i)
+            for (int d = 0; d < 3; ++d) {
+              Ue.a[i][d] *= ex[d];
+              Ve.a[i][d] *= ex[d];
+            }
+          M3<T> a1 = mmul(Fpb, Ve), a2 = mmul(mT(Fpb), Ue);
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+              Ub.a[i][j] += a1.a[i][j];
+              Vb.a[i][j] += a2.a[i][j];
+            }
+        }
         T epb[3], ehb[3], rrb = T(0);
         for (int d = 0; d < 3; ++d) epb[d] = UtFV.a[d][d] * ex[d];
         for (int d = 0; d < 3; ++d) {
@@ -1555,7 +1582,7 @@ static int substep_bwd_impl(const orc_scene* sc, const T* x, const T* v, const T
     if (o.model != MODEL_NEOHOOKEAN) {
       M3<T> gsv = svd_grad(o.U, o.sig, o.V, Ub, sb, Vb, Rb, svd_grad_mode);
       for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) Fnb.a[i][j] += gsv.a[i][j];
+        for (int j = 0; j < 3; ++j) Fnb.a[i][j] += gsv.a[i][j] + Frm.a[i][j];
     }
     M3<T> Ad = meye<T>();
     for (int i = 0; i < 3; ++i)

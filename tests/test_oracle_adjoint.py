@@ -37,3 +37,31 @@ def test_oracle_multithreaded_forward_matches_sequential():
     sb, _ = b.substep(b.initial_state(), cv=cv, cv1=cv)
     for k in ("x", "v", "C", "F"):
         assert SS.rel_err(sb[k], sa[k]) < 1e-12
+
+
+def test_return_map_adjoint_is_stable_at_coinciding_singular_values():
+    """Compressed plastic material (a pad pressing a box of yield stress 2 for 16 substeps: most
+    particles have two singular values of F_new within 0.1% of each other): with the divided-
+    difference form of the return map's rotation adjoint (svd_grad_mode 0) the float32 adjoint
+    agrees with the float64 one to 1e-4; the reference's generic formula (mode 1) amplifies float32
+    rounding there by orders of magnitude more."""
+    from oracle import oracle as O
+    from tests.test_parity_bwd import loss_weights
+    dt = 1e-4
+    env = SS.pad_over_box(yield_stress=2.0)
+    cv = [SS.control_velocity(sp, down=-0.3) for sp in env.sensors]
+    o32 = O.Oracle(env, dt, np.float32, grad_clip=0.0)
+    st = o32.initial_state()
+    for _ in range(16):
+        st, _ = o32.substep(st, cv=cv, cv1=cv)
+    st = {k: (v.astype(np.float64) if not isinstance(v, list) else [a.astype(np.float64) for a in v])
+          for k, v in st.items()}
+    W = {k: v.astype(np.float32).astype(np.float64)
+         for k, v in loss_weights(env, env.n_particles, 31).items() if k in ("x", "v", "C", "F")}
+    err = {}
+    for mode in (0, 1):
+        r64 = O.Oracle(env, dt, np.float64, grad_clip=0.0).substep_bwd(st, W, cv=cv, cv1=cv, svd_grad_mode=mode)
+        r32 = O.Oracle(env, dt, np.float32, grad_clip=0.0).substep_bwd(st, W, cv=cv, cv1=cv, svd_grad_mode=mode)
+        err[mode] = SS.rel_err(r32["F"], r64["F"])
+    assert err[0] < 1e-4, err
+    assert err[1] > 10 * err[0], err
