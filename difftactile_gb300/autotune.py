@@ -66,7 +66,7 @@ def current(world) -> dict:
 
 
 def signature(world, tag: str = "") -> str:
-    name = torch.cuda.get_device_name(world.device)
+    name = torch.cuda.get_device_name(world.device) if torch.cuda.is_available() else "no-device"
     return "|".join(str(x) for x in (name, tag, world.n_envs, world.n_particles, world.n_verts, world.n_tets,
                                      world.n_tris, world.n_blocks, world.n_rope_particles))
 
@@ -104,11 +104,12 @@ def _time(run, reps, warmup):
 
 
 def tune(world, run, cands=None, reps: int = 5, warmup: int = 1, tag: str = "", cache_path: str | None = None,
-         use_cache: bool = True, prepare=None, margin: float = 0.02) -> dict:
+         use_cache: bool = True, prepare=None, margin: float = 0.02, timer=None) -> dict:
     """Time ``run()`` under every candidate launch shape (``prepare()``, untimed, before each
     candidate's runs), apply the fastest and return {"best": cfg, "ms": {label: median ms}, "cached": bool}.
     The library default (``DEFAULT``) is kept unless a candidate beats it by more than ``margin``
-    (relative), so that timing noise between near-equal shapes does not flip the choice."""
+    (relative), so that timing noise between near-equal shapes does not flip the choice.  ``timer``
+    replaces the CUDA-event timing (called as timer(run, reps, warmup) -> ms)."""
     key = signature(world, tag)
     if use_cache:
         hit = _cache.get(key) or _load(cache_path).get(key)
@@ -123,7 +124,7 @@ def tune(world, run, cands=None, reps: int = 5, warmup: int = 1, tag: str = "", 
         apply(world, c)
         if prepare is not None:
             prepare()
-        ms = _time(run, reps, warmup)
+        ms = (timer or _time)(run, reps, warmup)
         if world.error_word():
             raise RuntimeError(f"device error word {world.error_word()} while tuning {c}")
         times[label(c)] = ms

@@ -66,3 +66,64 @@ def test_tune_substep_applies_and_caches(cuda_lib, tmp_path):
     finally:
         cuda_lib.dt_set_pdl(pdl0)
         AT._cache.clear()
+
+
+class _FakeLib:
+    def __init__(self):
+        self.pdl = 1
+
+    def dt_set_pdl(self, on):
+        old, self.pdl = self.pdl, int(on)
+        return old
+
+    def dt_get_pdl(self):
+        return self.pdl
+
+
+class _FakeWorld:
+    """The fields the tuner sets, without a device: the 'time' of a shape is a fixed function of it."""
+    def __init__(self, n_particles=1000):
+        import types
+        self.w = types.SimpleNamespace(scatter_mode=2, p_block=128, scatter_depth=0, contact_lanes=8)
+        self.lib = _FakeLib()
+        self.device = "cpu"
+        self.n_envs, self.n_particles, self.n_verts, self.n_tets, self.n_tris = 1, n_particles, 10, 10, 10
+        self.n_blocks, self.n_rope_particles = 100, 0
+
+    def error_word(self):
+        return 0
+
+
+def _timer_for(costs):
+    def timer(run, reps, warmup):
+        run()
+        return costs(run.world)
+    return timer
+
+
+def test_tuner_picks_the_fastest_shape_and_keeps_the_default_within_the_margin():
+    AT._cache.clear()
+    world = _FakeWorld()
+
+    def run():
+        pass
+    run.world = world
+    cur = lambda w: AT.current(w)  # noqa: E731
+    # a shape 10% faster than the default wins
+    fast = {"scatter": "warp", "p_block": 256, "depth": 1, "lanes": 4, "pdl": 1}
+    cost = lambda w: 0.9 if cur(w) == fast else 1.0  # noqa: E731
+    r = AT.tune(world, run, timer=_timer_for(cost), use_cache=False)
+    assert r["best"] == fast and AT.current(world) == fast and not r["cached"]
+    # a shape only 1% faster does not displace the default
+    cost2 = lambda w: 0.99 if cur(w) == fast else 1.0  # noqa: E731
+    r2 = AT.tune(world, run, timer=_timer_for(cost2), use_cache=False)
+    assert r2["best"] == AT.DEFAULT and AT.current(world) == AT.DEFAULT
+    # the result is cached per world shape; a different shape is tuned afresh
+    r3 = AT.tune(world, run, timer=_timer_for(cost), tag="t")
+    r4 = AT.tune(world, run, timer=lambda *a: 1 / 0, tag="t")  # served from the cache, no timing
+    assert r4["cached"] and r4["best"] == r3["best"] == fast
+    other = _FakeWorld(n_particles=2000)
+    run.world = other
+    r5 = AT.tune(other, run, timer=_timer_for(cost2), tag="t")
+    assert not r5["cached"]
+    AT._cache.clear()
