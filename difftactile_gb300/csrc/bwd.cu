@@ -24,14 +24,14 @@ DT_DEV float clampg(float a, float c) { return c > 0.f ? fminf(fmaxf(a, -c), c) 
 DT_DEV v3 clampg(v3 a, float c) { return v3{clampg(a.x, c), clampg(a.y, c), clampg(a.z, c)}; }
 DT_DEV float4 ld4(const float4* p) { return *p; }
 
-// (y^p - x^p) / (y - x) for x, y > 0, with its series in t = (y - x) / x where the two are within 1%
-// (the direct quotient would cancel): p x^(p-1) (1 + q t / 2 + q (q-1) t^2 / 6 + q (q-1) (q-2) t^3 / 24),
-// q = p - 1, truncation below 1e-8 there
-DT_DEV float pow_dd(float x, float y, float p) {
+// c (y^p - x^p) / (y - x) for x, y > 0 from the values fx = c x^p, fy = c y^p and gx = c x^(p-1):
+// the quotient itself, or where x and y are within 1% (the quotient would cancel) its series in
+// t = (y - x) / x, p gx (1 + q t / 2 + q (q-1) t^2 / 6 + q (q-1) (q-2) t^3 / 24) with q = p - 1
+DT_DEV float cdd(float x, float y, float fx, float fy, float gx, float p) {
   const float h = y - x;
-  if (fabsf(h) > 1e-2f * fmaxf(x, y)) return (powf(y, p) - powf(x, p)) / h;
+  if (fabsf(h) > 1e-2f * fmaxf(x, y)) return (fy - fx) / h;
   const float t = h / x, q = p - 1.f;
-  return p * powf(x, q) * (1.f + t * (0.5f * q + t * (q * (q - 1.f) / 6.f + t * (q * (q - 1.f) * (q - 2.f) / 24.f))));
+  return p * gx * (1.f + t * (0.5f * q + t * (q * (q - 1.f) / 6.f + t * (q * (q - 1.f) * (q - 2.f) / 24.f))));
 }
 
 // the reference's clamp of the singular-value gap (mpm_elastic.py:150-155)
@@ -516,17 +516,20 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
         // = M_ij c dd(a+1) / (s_i + s_j) + M_ji c s_i s_j dd(a-1) / (s_i + s_j),  dd(p) the divided
         // difference of x^p at (s_i, s_j): finite where singular values coincide, unlike the generic
         // formula's 1 / (s_j^2 - s_i^2)
-        const float a = 1.f - rr, c = expf(rr * mean);
+        // (the powers come from e itself: c s^(a+1) = e s, c s^(a-1) = e / s, c s^(a-2) = e / s^2;
+        // both factors are symmetric in i, j)
+        const float a = 1.f - rr;
         m3 inner = mzero();
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            if (i == j) continue;
+          for (int j = i + 1; j < 3; ++j) {
             const float sum = sg[i] + sg[j];
-            const float A = c * pow_dd(sg[i], sg[j], a + 1.f) / sum;
-            const float B = c * (sg[i] * sg[j]) * pow_dd(sg[i], sg[j], a - 1.f) / sum;
+            const float A = cdd(sg[i], sg[j], ex[i] * sg[i], ex[j] * sg[j], ex[i], a + 1.f) / sum;
+            const float B = (sg[i] * sg[j]) *
+                            cdd(sg[i], sg[j], ex[i] / sg[i], ex[j] / sg[j], ex[i] / (sg[i] * sg[i]), a - 1.f) / sum;
             inner.a[i][j] = UtFV.a[i][j] * A + UtFV.a[j][i] * B;
+            inner.a[j][i] = UtFV.a[j][i] * A + UtFV.a[i][j] * B;
           }
         Frm = mmulT(mmul(s.U, inner), s.V);
       } else {

@@ -905,13 +905,14 @@ template <typename T>
 inline T clampg(T a, T c) {
   return c > T(0) ? std::min(std::max(a, -c), c) : a;
 }
-// (y^p - x^p) / (y - x) for x, y > 0, by its series in t = (y - x) / x where the two are within 1%
+// c (y^p - x^p) / (y - x) for x, y > 0 from fx = c x^p, fy = c y^p, gx = c x^(p-1): the quotient,
+// or its series in t = (y - x) / x where the two are within 1%
 template <typename T>
-inline T pow_dd(T x, T y, T p) {
+inline T cdd(T x, T y, T fx, T fy, T gx, T p) {
   const T h = y - x;
-  if (std::fabs(h) > T(1e-2) * std::max(x, y)) return (std::pow(y, p) - std::pow(x, p)) / h;
+  if (std::fabs(h) > T(1e-2) * std::max(x, y)) return (fy - fx) / h;
   const T t = h / x, q = p - T(1);
-  return p * std::pow(x, q) * (T(1) + t * (T(0.5) * q + t * (q * (q - T(1)) / T(6) + t * (q * (q - T(1)) * (q - T(2)) / T(24)))));
+  return p * gx * (T(1) + t * (T(0.5) * q + t * (q * (q - T(1)) / T(6) + t * (q * (q - T(1)) * (q - T(2)) / T(24)))));
 }
 template <typename T>
 inline T gap_clamp(T a) {
@@ -1536,15 +1537,17 @@ static int substep_bwd_impl(const orc_scene* sc, const T* x, const T* v, const T
           // adjoint of Fp = U diag(e) V^T is, off the diagonal,
           // M_ij c dd(a+1) / (s_i + s_j) + M_ji c s_i s_j dd(a-1) / (s_i + s_j), dd the divided
           // difference of x^p; equal to the generic formula below wherever that one is finite
-          const T a = T(1) - rr, c = std::exp(rr * mean);
+          // the powers from e itself: c s^(a+1) = e s, c s^(a-1) = e / s, c s^(a-2) = e / s^2
+          const T a = T(1) - rr;
+          const T* sg = o.sig;
           M3<T> inner = mzero<T>();
           for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) {
-              if (i == j) continue;
-              const T sum = o.sig[i] + o.sig[j];
-              const T A = c * pow_dd(o.sig[i], o.sig[j], a + T(1)) / sum;
-              const T B = c * (o.sig[i] * o.sig[j]) * pow_dd(o.sig[i], o.sig[j], a - T(1)) / sum;
+            for (int j = i + 1; j < 3; ++j) {
+              const T sum = sg[i] + sg[j];
+              const T A = cdd(sg[i], sg[j], ex[i] * sg[i], ex[j] * sg[j], ex[i], a + T(1)) / sum;
+              const T B = (sg[i] * sg[j]) * cdd(sg[i], sg[j], ex[i] / sg[i], ex[j] / sg[j], ex[i] / (sg[i] * sg[i]), a - T(1)) / sum;
               inner.a[i][j] = UtFV.a[i][j] * A + UtFV.a[j][i] * B;
+              inner.a[j][i] = UtFV.a[j][i] * A + UtFV.a[i][j] * B;
             }
           Frm = mmul(mmul(o.U, inner), mT(o.V));
         } else {
