@@ -58,8 +58,11 @@ class World:
                  grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True,
                  svd_grad_mode: int = 0, scatter_mode: int = 2, svd_tape: bool = True, p_block: int = 128,
                  scatter_depth: int = 0, contact_lanes: int = 8):
-        self.lib = N.load()
         self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError(f"World buffers must live on a CUDA device (the kernels take device pointers), "
+                             f"got {self.device}")
+        self.lib = N.load()
         self.specs = envs
         self.n_frames = int(n_frames)
         self.dt = float(dt)

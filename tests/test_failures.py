@@ -33,6 +33,12 @@ def test_argument_errors_are_status_codes_without_a_device():
         N.check(lib.dt_substep_fwd(wp, 7, None), "dt_substep_fwd")
 
 
+def test_world_on_host_memory_is_refused():
+    from difftactile_gb300.world import World
+    with pytest.raises(ValueError, match="CUDA device"):
+        World([SS.pad_over_box()], n_frames=3, dt=DT, device="cpu")
+
+
 @pytest.mark.gpu
 def test_out_of_range_frame_raises_before_launch(cuda_lib):
     from difftactile_gb300.world import World
