@@ -32,6 +32,7 @@ sys.path.insert(0, ROOT)
 
 FALLBACK_HBM_GBS = 6800.0
 PROBE_EVERY = 25  # substeps between the timed region's event-timed launches of the dominant kernel
+METRIC, UNIT = "fwd+bwd particle-substeps/s", "particle-substeps/s"  # both arms report these
 
 
 def parse():
@@ -260,7 +261,7 @@ def run_ours(args):
     ab = algo_bytes(dom, unit_counts)
     achieved = ab / (dom_ms / 1e3) / 1e9
 
-    out = {"metric": "fwd+bwd particle-substeps/s", "value": value, "unit": "particle-substeps/s",
+    out = {"metric": METRIC, "value": value, "unit": UNIT,
            "n_gpus": world_size, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded scene generators)",
@@ -317,7 +318,7 @@ def run_ours(args):
                 e2e.append(t1 - t0)
         e_ms = 1e3 * sum(e2e) / len(e2e)
         e_ms = replicas.slowest(e_ms, dev)
-        out["e2e"] = {"value": replicas.total(units, dev) / (e_ms / 1e3), "unit": "particle-substeps/s",
+        out["e2e"] = {"value": replicas.total(units, dev) / (e_ms / 1e3), "unit": UNIT,
                       "ms_per_step": e_ms,
                       "h2d_bytes_per_step": int(h_act.numel() * 4 + h_x.numel() * 4 + h_v.numel() * 4),
                       "d2h_bytes_per_step": int(res.numel() * 8)}
@@ -370,7 +371,7 @@ def time_plain(cfg, args, dev, flush, tune_launch):
         total_ms += e0.elapsed_time(e1)
         units += cfg.envs[e].n_particles * cfg.n_steps * cfg.substeps
         del w, traj
-    return {"value": units / (total_ms / 1e3), "unit": "particle-substeps/s", "envs": k, "ms": total_ms,
+    return {"value": units / (total_ms / 1e3), "unit": UNIT, "envs": k, "ms": total_ms,
             "path": "one World per environment, launched one after the other"}
 
 
@@ -394,7 +395,7 @@ def cpu_baseline(cfg, threads, target_s=15.0):
         st = st1
         done += 1
     dt_ = time.perf_counter() - t0
-    return {"value": env.n_particles * done / dt_, "unit": "particle-substeps/s", "cores": threads,
+    return {"value": env.n_particles * done / dt_, "unit": UNIT, "cores": threads,
             "kind": "port",
             "sample": f"{done} substeps of env 0 of {cfg.name} ({env.n_particles} particles), forward + "
                       f"recompute + adjoint per substep, float32, {threads} OpenMP threads"}
@@ -473,14 +474,14 @@ def run_reference(args):
     vals = [cpu_baseline(cfg, threads, target_s=10.0) for _ in range(max(args.steps, 1))]
     v = sum(x["value"] for x in vals) / len(vals)
     units = cfg.n_particles * cfg.n_steps * cfg.substeps
-    out = {"impl": "reference", "metric": "fwd+bwd particle-substeps/s", "value": v, "unit": "particle-substeps/s",
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": units / v * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded scene generators)",
            "config": {"workload": cfg.name, "particles": cfg.n_particles, "control_steps": cfg.n_steps,
                       "substeps": cfg.substeps},
            "cpu_baseline": dict(vals[-1], value=v),
-           "e2e": {"value": v, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
 
