@@ -1647,6 +1647,23 @@ void orc_svd3_f64(int n, const double* A, double* U, double* s, double* V, int s
   }
 }
 
+// Standalone SVD adjoint (svd_grad, mpm_elastic.py:145-173, for finite-difference tests) in float64:
+// U, V, Ub, Vb, Rb, Fb [n][9], s, sb [n][3]; Rb is the adjoint of R = U V^T (mode 1 folds it into Ub
+// and Vb as the reference does, any other mode uses the divided form).
+void orc_svd_grad_f64(int n, const double* U, const double* s, const double* V, const double* Ub,
+                      const double* sb, const double* Vb, const double* Rb, int mode, double* Fb) {
+  for (int i = 0; i < n; ++i) {
+    M3<double> u, v, ub, vb, rb;
+    std::memcpy(u.a, U + 9 * i, sizeof(u.a));
+    std::memcpy(v.a, V + 9 * i, sizeof(v.a));
+    std::memcpy(ub.a, Ub + 9 * i, sizeof(ub.a));
+    std::memcpy(vb.a, Vb + 9 * i, sizeof(vb.a));
+    std::memcpy(rb.a, Rb + 9 * i, sizeof(rb.a));
+    M3<double> g = svd_grad(u, s + 3 * i, v, ub, sb + 3 * i, vb, rb, mode);
+    std::memcpy(Fb + 9 * i, g.a, sizeof(g.a));
+  }
+}
+
 // Standalone argmin (find_closest) over one sensor for a list of query points [nq][3].
 void orc_find_closest_f32(const orc_sensor* s, const float* pos, int nq, const float* q, int* out) {
   for (int i = 0; i < nq; ++i) out[i] = find_closest(*s, pos, q + 3 * i);

@@ -65,6 +65,8 @@ def lib():
             fn = getattr(L, name)
             fn.restype = None
             fn.argtypes = [I, P, P, P, P, I]
+        L.orc_svd_grad_f64.restype = None
+        L.orc_svd_grad_f64.argtypes = [I] + [P] * 7 + [I, P]
         L.orc_find_closest_f32.restype = None
         L.orc_find_closest_f32.argtypes = [P, P, I, P, P]
         for name in ("orc_substep_bwd_f32", "orc_substep_bwd_f64"):
@@ -275,6 +277,17 @@ def svd3(A, dtype=np.float32, sweeps=None):
     fn = lib().orc_svd3_f32 if T == np.float32 else lib().orc_svd3_f64
     fn(C.c_int(n), _ptr(A), _ptr(U), _ptr(s), _ptr(V), C.c_int(sweeps if sweeps else (4 if T == np.float32 else 12)))
     return U, s, V
+
+
+def svd_grad(U, s, V, Ub, sb, Vb, Rb, mode=0):
+    """Standalone SVD adjoint of the oracle in float64 (svd_grad, mpm_elastic.py:145-173): the adjoint
+    of F = U diag(s) V^T from the adjoints of U, s, V and of R = U V^T.  All [n,3,3] / [n,3]."""
+    a = [np.ascontiguousarray(x, np.float64).reshape(-1, 3, 3) for x in (U, V, Ub, Vb, Rb)]
+    ss = [np.ascontiguousarray(x, np.float64).reshape(-1, 3) for x in (s, sb)]
+    Fb = np.zeros_like(a[0])
+    lib().orc_svd_grad_f64(C.c_int(len(Fb)), _ptr(a[0]), _ptr(ss[0]), _ptr(a[1]), _ptr(a[2]), _ptr(ss[1]),
+                           _ptr(a[3]), _ptr(a[4]), C.c_int(mode), _ptr(Fb))
+    return Fb
 
 
 def find_closest(sensor, pos, queries):

@@ -30,6 +30,43 @@ def test_svd_convention_and_accuracy(dtype, tol):
     assert (s[neg, 2] < 0).all()  # inverted elements keep the sign in the last singular value
 
 
+def _svd_loss(A, W, sb, Rb):
+    """sum_i <W_i, u_i v_i^T> + <sb, s> + <Rb, U V^T>: unchanged when the SVD flips the signs of a
+    pair of matching columns, so central differences through svd3 are well defined."""
+    U, s, V = O.svd3(A, np.float64)
+    L = np.einsum("nkab,nak,nbk->n", W, U, V) + (sb * s).sum(1) + np.einsum("nab,nak,nbk->n", Rb, U, V)
+    return L, U, s, V
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("det_sign", [1.0, -1.0])
+def test_svd_adjoint_matches_finite_differences(mode, det_sign):
+    """The SVD adjoint (svd_grad, mpm_elastic.py:145-173) on random F away from degeneracy (singular
+    values at least 0.2 apart in magnitude), both the reference's form (mode 1, the R = U V^T adjoint
+    folded into the U and V adjoints) and the divided form (mode 0), for det F > 0 and for inverted F
+    (negative last singular value)."""
+    rng = np.random.default_rng(3 + mode)
+    n = 200
+    Q1 = np.linalg.qr(rng.standard_normal((n, 3, 3)))[0]
+    Q2 = np.linalg.qr(rng.standard_normal((n, 3, 3)))[0]
+    sig = np.sort(rng.uniform(0.3, 2.0, (n, 3)), 1)[:, ::-1] + np.array([0.4, 0.2, 0.0])
+    sig[:, 2] *= det_sign * np.sign(np.linalg.det(Q1) * np.linalg.det(Q2))
+    A = np.einsum("nij,nj,nkj->nik", Q1, sig, Q2)
+    W = rng.standard_normal((n, 3, 3, 3))     # W[:, k] weighs u_k v_k^T
+    sb = rng.standard_normal((n, 3))
+    Rb = rng.standard_normal((n, 3, 3))
+    _, U, s, V = _svd_loss(A, W, sb, Rb)
+    assert np.all(np.sign(np.linalg.det(A)) == det_sign)
+    Ub = np.einsum("nkab,nbk->nak", W, V)      # d/du_k of <W_k, u_k v_k^T> = W_k v_k
+    Vb = np.einsum("nkab,nak->nbk", W, U)      # d/dv_k = W_k^T u_k
+    Fb = O.svd_grad(U, s, V, Ub, sb, Vb, Rb, mode)
+    D = rng.standard_normal((n, 3, 3))
+    eps = 1e-6
+    fd = (_svd_loss(A + eps * D, W, sb, Rb)[0] - _svd_loss(A - eps * D, W, sb, Rb)[0]) / (2 * eps)
+    pred = (Fb * D).sum((1, 2))
+    assert np.abs(pred - fd).max() < 1e-6 * np.abs(fd).max()
+
+
 def _cube(n=32, v=(0.0, 0.0, 0.0), gravity=(0, 0, 0), eps=1e-20, model=S.MODEL_COROTATED):
     x = S.cube_particles([0.5, 0.55, 0.45], 0.25, 1.0 / n, 8, 0)
     return S.EnvSpec(x=x, v=np.asarray(v, np.float32), materials=[S.Material(5e3, 0.3, 50.0, model)],
