@@ -194,6 +194,8 @@ class Trajectory:
 
     def forward(self, actions: torch.Tensor) -> torch.Tensor:
         """Roll out; returns the final-frame loss (device scalar)."""
+        if actions.shape[0] != self.T:
+            raise ValueError(f"actions hold {actions.shape[0]} control steps, the trajectory {self.T}")
         self.actions = actions.detach().double().requires_grad_(True)
         self.ctrl = self.controls(self.actions)
         c32 = self.ctrl.detach().float().contiguous()

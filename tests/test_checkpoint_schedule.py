@@ -210,3 +210,12 @@ def test_probed_adjoint_runs_cover_each_frame_once(f_hi, f_lo, every):
     calls.clear()
     w.substeps_bwd(f_hi, f_lo)
     assert calls == [("run", f_hi, f_lo)]            # unprobed: one fused run
+
+
+def test_actions_of_another_horizon_are_refused_before_any_step():
+    sys = System()
+    w = FakeWorld(Trajectory.frames_needed(4, 3, 1), sys)
+    tr = LinearTrajectory(w, 4, ckpt_every=1)
+    with pytest.raises(ValueError, match="control steps"):
+        tr.forward(torch.zeros(3, NC, dtype=torch.float64))
+    assert float(w.cv.abs().max()) == 0.0 and w.calls == []
