@@ -1,0 +1,175 @@
+"""Golden substeps computed by the reference's own simulation methods.
+
+The reference's substep is Taichi code (taichi is absent here and not installable), so its methods
+are read out of the reference source with `ast` and run, in float64, on numpy fields through the
+stand-in `ti` module of this folder (ti_numpy.py, which lists the semantics it takes for Taichi's
+primitives).  Two cases, one substep each, on seeded states:
+
+  corotated_cube  MPMObj of object_model/mpm_elastic.py (compute_new_F, svd, p2g, check_grid_occupy,
+                  grid_op, g2p; :134-260), a fixed-corotated cube falling into the floor band of a 16^3
+                  grid (wall rule of grid_op);
+  plastic_pads    Contact.update of tasks/grasp_plastic.py:151-164 (check_collision, collision,
+                  calculate_contact_force; :205-299) over MPMObj of object_model/mpm_plastic.py (the
+                  von Mises p2g; :140-310) and two FEMDomeSensor pads of sensor_model/fem_sensor.py
+                  (init_pos, find_closest, find_sdf, update_contact_force, update, update2; :325-457),
+                  a plastic box pressed by two hex pads (half of its particles beyond the yield surface).
+
+The scenes come from tests/small_scenes.py (the parity scenes); states, constants and the outputs
+(particles, the grid at occupied nodes, contact indices, the sensors' forces and next frame) go to
+tests/golden/substep_ref.npz.
+
+    python tests/golden/make_substep.py [REFERENCE_ROOT]
+"""
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from tests import small_scenes as SS  # noqa: E402
+from tests.golden import ti_numpy as ti  # noqa: E402
+
+DT = 1e-4
+PKG = None  # the reference's package folder, set by main()
+
+
+def scenes():
+    """The two parity scenes (also rebuilt by tests/test_golden_substep.py)."""
+    cube = SS.elastic_cube(n=16, side_cells=4, center=(0.5, 3.5 / 16, 0.5), v=(0.0, -0.5, 0.0))
+    pads = SS.pad_over_box(two_pads=True, box_cells=(4, 3, 4), yield_stress=2.0)
+    return {"corotated_cube": cube, "plastic_pads": pads}
+
+
+def seeded_state(env, seed):
+    rng = np.random.default_rng(seed)
+    N = env.n_particles
+    r32 = lambda a: np.asarray(a, np.float32).astype(np.float64)  # noqa: E731
+    F = np.eye(3) + 0.05 * rng.standard_normal((N, 3, 3))
+    F[1::2] = (np.eye(3) + 1e-4 * rng.standard_normal((N, 3, 3)))[1::2]  # inside the yield surface
+    st = {"x": r32(env.x), "v": r32(env.v if env.v is not None else np.zeros((N, 3))),
+          "C": r32(0.3 * rng.standard_normal((N, 3, 3))), "F": r32(F)}
+    dx = env.dx
+    st["pos"] = [r32(sp.verts + 0.02 * dx * rng.standard_normal(sp.verts.shape)) for sp in env.sensors]
+    st["vel"] = [r32(0.01 * rng.standard_normal(sp.verts.shape)) for sp in env.sensors]
+    st["vpos"] = [r32(sp.verts) for sp in env.sensors]
+    st["cv"] = [r32(SS.control_velocity(sp, seed=11 + i)) for i, sp in enumerate(env.sensors)]
+    return st
+
+
+def mpm_object(env, st, src, plastic):
+    n = env.n_grid[0]
+    N = env.n_particles
+    m = env.materials[0]
+    mu, lam = m.mu_lam
+    o = types.SimpleNamespace(
+        n_particles=N, n_grid=n, dim=3, bound=env.bound, dt=DT, dx_0=env.dx, inv_dx_0=1.0 / env.dx,
+        p_vol=env.volume, p_mass=env.p_mass, eps=env.eps, dtype=ti.f32, gravity=ti.Vector(list(env.gravity)),
+        mu_0=ti.scalar(mu), lambda_0=ti.scalar(lam), yield_stress=ti.scalar(m.yield_stress))
+    for k, e in (("x_0", (3,)), ("v_0", (3,)), ("C_0", (3, 3)), ("F_new", (3, 3)), ("F_0", (3, 3)),
+                 ("U_svd", (3, 3)), ("V_svd", (3, 3)), ("S_svd", (3, 3))):
+        setattr(o, k, ti.Field((2, N), e))
+    for k, e in (("grid_v_in", (3,)), ("grid_v_out", (3,)), ("grid_m", ()), ("grid_f", (3,))):
+        setattr(o, k, ti.Field((2, n, n, n), e))
+    o.grid_occupy = ti.Field((2, n, n, n), (), np.int64)
+    o.x_0.a[0], o.v_0.a[0], o.C_0.a[0], o.F_0.a[0] = st["x"], st["v"], st["C"], st["F"]
+    names = ["compute_new_F", "svd", "p2g", "check_grid_occupy", "grid_op", "g2p", "update_contact_force"]
+    if plastic:
+        names += ["norm", "make_matrix_from_diag", "compute_von_mises"]
+    return ti.methods(src, "MPMObj", names, o)
+
+
+def sensor_object(sp, pos, vel, vpos, cv, src):
+    V, T = len(sp.verts), len(sp.tets)
+    mu, lam = sp.lame()
+    M = np.eye(4) if sp.trans_world is None else np.asarray(sp.trans_world, np.float64)
+    s = types.SimpleNamespace(n_verts=V, n_cells=T, num_triangles=len(sp.tris), dt=DT, mass=float(sp.mass), eps=1e-10,
+                              mu=ti.scalar(mu), lam=ti.scalar(lam), trans_h=ti.Field((), (4, 4)),
+                              rot_h=ti.Field((), (3, 3)), out_direction=ti.Field((), (3,)))
+    s.trans_h[None] = np.eye(4)
+    s.rot_h[None] = M[:3, :3]
+    s.init_x = ti.Field((V,), (3,))
+    s.init_x.a[:] = np.asarray(sp.verts, np.float64)
+    for k in ("pos", "vel", "virtual_pos", "external_force_field"):
+        setattr(s, k, ti.Field((2, V), (3,)))
+    s.control_vel = ti.Field((V,), (3,))
+    s.B = ti.Field((T,), (3, 3))
+    s.f2v = ti.Field((T,), (4,), np.int64)
+    s.f2v.a[:] = sp.tets
+    s.contact_seg = ti.Field((len(sp.tris),), (3,), np.int64)
+    s.contact_seg.a[:] = sp.tris
+    s.layer_id = ti.Field((V,), (), np.int64)
+    s.layer_id.a[:] = sp.layer
+    ti.methods(src, "FEMDomeSensor", ["init_pos", "find_closest", "find_sdf", "update_contact_force", "update",
+                                      "update2"], s)
+    s.init_pos()  # rest-shape inverses B from the rest positions, out_direction = rot_h e_y
+    s.pos.a[0], s.vel.a[0], s.virtual_pos.a[0] = pos, vel, vpos
+    s.control_vel.a[:] = cv
+    return s
+
+
+def occupied(o):
+    occ = np.argwhere(o.grid_occupy.a[0] == 1)
+    i, j, k = occ.T
+    return occ, o.grid_m.a[0][i, j, k], o.grid_v_in.a[0][i, j, k], o.grid_v_out.a[0][i, j, k], o.grid_f.a[0][i, j, k]
+
+
+def run_cube(env, st):
+    o = mpm_object(env, st, os.path.join(PKG, "object_model", "mpm_elastic.py"), plastic=False)
+    for name in ("compute_new_F", "svd", "p2g", "check_grid_occupy", "grid_op", "g2p"):
+        getattr(o, name)(0)
+    return o, []
+
+
+def run_pads(env, st):
+    o = mpm_object(env, st, os.path.join(PKG, "object_model", "mpm_plastic.py"), plastic=True)
+    sens = [sensor_object(sp, st["pos"][i], st["vel"][i], st["vpos"][i], st["cv"][i],
+                          os.path.join(PKG, "sensor_model", "fem_sensor.py")) for i, sp in enumerate(env.sensors)]
+    n = env.n_grid[0]
+    c = types.SimpleNamespace(mpm_object=o, gripper=types.SimpleNamespace(fem_sensor1=sens[0], fem_sensor2=sens[1]),
+                              kn=ti.scalar(env.kn), kd=ti.scalar(env.kd), kt=ti.scalar(env.kt),
+                              friction_coeff=ti.scalar(env.mu_t), norm_eps=1e-11,
+                              contact_idx=ti.Field((2, n, n, n), (2,), np.int64))
+    ti.methods(os.path.join(PKG, "tasks", "grasp_plastic.py"), "Contact",
+               ["update", "check_collision", "collision", "calculate_contact_force"], c)
+    c.update(0)
+    return o, sens, c
+
+
+def main():
+    global PKG
+    PKG = os.path.join(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", "difftactile")
+    out = {}
+    for name, env in scenes().items():
+        st = seeded_state(env, seed=5 if name == "corotated_cube" else 6)
+        if name == "corotated_cube":
+            o, sens = run_cube(env, st)
+        else:
+            o, sens, c = run_pads(env, st)
+        occ, gm, gvi, gvo, gf = occupied(o)
+        f32 = lambda a: np.asarray(a, np.float32)  # noqa: E731 - the inputs are float32 values
+        rec = {"x": f32(st["x"]), "v": f32(st["v"]), "C": f32(st["C"]), "F": f32(st["F"]),
+               "x1": o.x_0.a[1], "v1": o.v_0.a[1], "C1": o.C_0.a[1], "F1": o.F_0.a[1],
+               "occ": occ.astype(np.int32), "grid_m": gm, "grid_v_in": gvi, "grid_v_out": gvo, "grid_f": gf,
+               "consts": np.array([DT, env.dx, env.volume, env.p_mass, env.eps, env.bound, *env.materials[0].mu_lam,
+                                   env.materials[0].yield_stress, env.kn, env.kd, env.kt, env.mu_t])}
+        if name != "corotated_cube":
+            i, j, k = occ.T
+            rec["cidx"] = c.contact_idx.a[0][i, j, k].astype(np.int32)
+            for s, so in enumerate(sens):
+                for key, val in (("pos", f32(st["pos"][s])), ("vel", f32(st["vel"][s])),
+                                 ("vpos", f32(st["vpos"][s])), ("cv", f32(st["cv"][s])), ("B", so.B.a), ("vel_mid", so.vel.a[0]),
+                                 ("ext", so.external_force_field.a[0]), ("pos1", so.pos.a[1]),
+                                 ("vel1", so.vel.a[1]), ("vpos1", so.virtual_pos.a[1])):
+                    rec[f"s{s}_{key}"] = val
+        out.update({f"{name}/{k}": v for k, v in rec.items()})
+        print(name, env.n_particles, "particles,", len(occ), "occupied nodes",
+              "" if name == "corotated_cube" else f", contacts {int((rec['s0_ext'] != 0).any(1).sum())}"
+              f" + {int((rec['s1_ext'] != 0).any(1).sum())} sensor vertices")
+    np.savez_compressed(os.path.join(HERE, "substep_ref.npz"), **out)
+
+
+if __name__ == "__main__":
+    main()
