@@ -2,13 +2,16 @@
 // (Taichi kernels of the reference), used as the parity oracle of the CUDA path and as the
 // timed CPU baseline.  It is never linked into or called by the product path.
 //
-// Parity status: UNPINNED against the reference's own outputs.  The reference is Taichi 1.6.0
-// code (un-vendored third-party JIT, not importable in this image) and ships no tests, golden
-// vectors or fixtures for this path, so nothing the reference produced can be compared here.
-// The restatement is pinned instead by analytic known-answer tests (rest state, rigid
-// translation, partition of unity, momentum conservation, FEM rest/dilation, contact force,
-// argmin vs brute force) in tests/test_oracle_kat.py, and its adjoint by central finite
-// differences in double precision.
+// Parity status: the forward substep is pinned against the reference's own simulation methods.
+// The reference is Taichi 1.6.0 code (un-vendored third-party JIT, not importable in this image)
+// and ships no tests, golden vectors or fixtures for this path; tests/golden/make_substep.py runs
+// its MPMObj (mpm_elastic.py, mpm_plastic.py), FEMDomeSensor (fem_sensor.py) and Contact.update
+// (grasp_plastic.py) methods, read from the reference source, in float64 on a numpy stand-in for
+// the Taichi primitives, and tests/test_golden_substep.py finds this restatement within 1e-11 of
+// them (particles, grid, contact argmin, sensor forces and next frame).  The rope, the gripper's
+// update2 variant and the adjoints (Taichi autodiff) are pinned by analytic known-answer tests
+// (tests/test_oracle_kat.py, test_oracle_rope.py) and by central finite differences in double
+// precision.
 //
 // Structure follows the reference kernel by kernel, on a dense per-frame grid in (i, j, k)
 // row-major order exactly like the Taichi fields, processing particles/nodes/tets in index
