@@ -7,11 +7,11 @@
 // and ships no tests, golden vectors or fixtures for this path; tests/golden/make_substep.py runs
 // its MPMObj (mpm_elastic.py, mpm_plastic.py), FEMDomeSensor (fem_sensor.py) and Contact.update
 // (grasp_plastic.py) methods, read from the reference source, in float64 on a numpy stand-in for
-// the Taichi primitives, and tests/test_golden_substep.py finds this restatement within 1e-11 of
-// them (particles, grid, contact argmin, sensor forces and next frame).  The rope, the gripper's
-// update2 variant and the adjoints (Taichi autodiff) are pinned by analytic known-answer tests
-// (tests/test_oracle_kat.py, test_oracle_rope.py) and by central finite differences in double
-// precision.
+// the Taichi primitives, and tests/test_golden_substep.py finds this restatement within 2e-15 of
+// them (particles, grid, contact argmin, sensor forces and next frame; the rope and the gripper's
+// update2 through the cable task's Contact.update).  The adjoints (Taichi autodiff) are pinned by
+// analytic known-answer tests (tests/test_oracle_kat.py, test_oracle_rope.py) and by central
+// finite differences in double precision.
 //
 // Structure follows the reference kernel by kernel, on a dense per-frame grid in (i, j, k)
 // row-major order exactly like the Taichi fields, processing particles/nodes/tets in index

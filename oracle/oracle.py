@@ -3,8 +3,8 @@
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arms use this
 module, to check the CUDA path's results against it.  Parity status: the forward substep is pinned
 against golden substeps of the reference's own methods run on a numpy stand-in for Taichi
-(tests/golden/make_substep.py, tests/test_golden_substep.py: within 1e-11); the rope and the
-adjoints by analytic known-answer tests and finite differences.
+(tests/golden/make_substep.py, tests/test_golden_substep.py: MPM, FEM sensors, contact and rope
+within 2e-15); the adjoints by analytic known-answer tests and finite differences.
 
 Arrays are numpy in the reference layout: x, v [N,3]; C, F [N,3,3]; per sensor pos/vel/vpos/cv
 [V,3]; dense grids [n0,n1,n2(,3)].

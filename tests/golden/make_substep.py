@@ -12,7 +12,12 @@ primitives).  Two cases, one substep each, on seeded states:
                   calculate_contact_force; :205-299) over MPMObj of object_model/mpm_plastic.py (the
                   von Mises p2g; :140-310) and two FEMDomeSensor pads of sensor_model/fem_sensor.py
                   (init_pos, find_closest, find_sdf, update_contact_force, update, update2; :325-457),
-                  a plastic box pressed by two hex pads (half of its particles beyond the yield surface).
+                  a plastic box pressed by two hex pads (half of its particles beyond the yield surface);
+  rope_pads       Contact.update of tasks/cable_straightening.py:166-173 (check_collision, collision and
+                  its calculate_contact_force variant; :212-319) over PBDRope of object_model/PBD_rope.py
+                  (update, update_contact_force; :108-180) and two FEMDomeSensor pads of
+                  sensor_model/gripper_fem.py (per-frame control velocities, the carry term of update2),
+                  a rope pressed by a pad along ten of its sixteen particles.
 
 The scenes come from tests/small_scenes.py (the parity scenes); states, constants and the outputs
 (particles, the grid at occupied nodes, contact indices, the sensors' forces and next frame) go to
@@ -20,6 +25,7 @@ tests/golden/substep_ref.npz.
 
     python tests/golden/make_substep.py [REFERENCE_ROOT]
 """
+import dataclasses
 import os
 import sys
 import types
@@ -37,13 +43,20 @@ PKG = None  # the reference's package folder, set by main()
 
 
 def scenes():
-    """The two parity scenes (also rebuilt by tests/test_golden_substep.py)."""
+    """The parity scenes (also rebuilt by tests/test_golden_substep.py)."""
+    from difftactile_gb300 import scene as S
     cube = SS.elastic_cube(n=16, side_cells=4, center=(0.5, 3.5 / 16, 0.5), v=(0.0, -0.5, 0.0))
     pads = SS.pad_over_box(two_pads=True, box_cells=(4, 3, 4), yield_stress=2.0)
-    return {"corotated_cube": cube, "plastic_pads": pads}
+    rope = SS.rope_under_pad(pad=(16, 4, 2), press=0.5)  # 11 of the 16 rope particles under the pad
+    # the cable task's two gripper pads (control-velocity carry of gripper_fem.update2): the parity
+    # scene's pad pressing the rope, and a second one well above it
+    far = S.hex_pad_sensor([0.5, 0.3, 0.5], nx=4, nz=4, ny=2, h=0.012)
+    rope = rope.replace(sensors=[dataclasses.replace(rope.sensors[0], carry=1), dataclasses.replace(far, carry=1)])
+    return {"corotated_cube": cube, "plastic_pads": pads, "rope_pads": rope}
 
 
-def seeded_state(env, seed):
+def seeded_state(env, seed, jitter):
+    """Seeded float32 state; sensor vertices displaced by ``jitter`` x N(0, 1) from rest."""
     rng = np.random.default_rng(seed)
     N = env.n_particles
     r32 = lambda a: np.asarray(a, np.float32).astype(np.float64)  # noqa: E731
@@ -51,11 +64,14 @@ def seeded_state(env, seed):
     F[1::2] = (np.eye(3) + 1e-4 * rng.standard_normal((N, 3, 3)))[1::2]  # inside the yield surface
     st = {"x": r32(env.x), "v": r32(env.v if env.v is not None else np.zeros((N, 3))),
           "C": r32(0.3 * rng.standard_normal((N, 3, 3))), "F": r32(F)}
-    dx = env.dx
-    st["pos"] = [r32(sp.verts + 0.02 * dx * rng.standard_normal(sp.verts.shape)) for sp in env.sensors]
+    st["pos"] = [r32(sp.verts + jitter * rng.standard_normal(sp.verts.shape)) for sp in env.sensors]
     st["vel"] = [r32(0.01 * rng.standard_normal(sp.verts.shape)) for sp in env.sensors]
     st["vpos"] = [r32(sp.verts) for sp in env.sensors]
     st["cv"] = [r32(SS.control_velocity(sp, seed=11 + i)) for i, sp in enumerate(env.sensors)]
+    st["cv1"] = [r32(c + 0.01 * rng.standard_normal(c.shape)) for c in st["cv"]]  # frame f + 1 (gripper)
+    st["rpos"] = [r32(rp.init_positions()) for rp in env.ropes]
+    st["rvel"] = [r32(0.01 * rng.standard_normal((rp.n, 3))) for rp in env.ropes]
+    st["rtrav"] = [r32(rng.integers(0, 2, rp.n)) for rp in env.ropes]
     return st
 
 
@@ -81,7 +97,7 @@ def mpm_object(env, st, src, plastic):
     return ti.methods(src, "MPMObj", names, o)
 
 
-def sensor_object(sp, pos, vel, vpos, cv, src):
+def sensor_object(sp, pos, vel, vpos, cv, src, cls="FEMDomeSensor"):
     V, T = len(sp.verts), len(sp.tets)
     mu, lam = sp.lame()
     M = np.eye(4) if sp.trans_world is None else np.asarray(sp.trans_world, np.float64)
@@ -102,12 +118,39 @@ def sensor_object(sp, pos, vel, vpos, cv, src):
     s.contact_seg.a[:] = sp.tris
     s.layer_id = ti.Field((V,), (), np.int64)
     s.layer_id.a[:] = sp.layer
-    ti.methods(src, "FEMDomeSensor", ["init_pos", "find_closest", "find_sdf", "update_contact_force", "update",
-                                      "update2"], s)
+    ti.methods(src, cls, ["init_pos", "find_closest", "find_sdf", "update_contact_force", "update", "update2"], s)
     s.init_pos()  # rest-shape inverses B from the rest positions, out_direction = rot_h e_y
+    s.B.a[:] = s.B.a.astype(np.float32)  # B is a float32 field in the reference (and on the device)
     s.pos.a[0], s.vel.a[0], s.virtual_pos.a[0] = pos, vel, vpos
     s.control_vel.a[:] = cv
     return s
+
+
+def gripper_sensor_object(sp, pos, vel, vpos, cv, cv1, src):
+    """A gripper pad (sensor_model/gripper_fem.py: per-frame control velocities)."""
+    s = sensor_object(sp, pos, vel, vpos, cv, src, cls="FEMDomeSensor")
+    s.control_vel = ti.Field((2, len(sp.verts)), (3,))
+    s.control_vel.a[0], s.control_vel.a[1] = cv, cv1
+    return s
+
+
+def rope_object(rp, pos, vel, trav, src):
+    n = rp.n
+    cs, cb = rp.compliance
+    o = types.SimpleNamespace(n_particles=n, n_segments=n - 1, dt=DT, p_rad=rp.rad, p_mass=rp.mass,
+                              invM=1.0 / rp.mass, gravity=ti.Vector(list(rp.gravity)), eps=1e-10,
+                              table_height=rp.table_h, rest_length=rp.rest, bending_length=rp.bend,
+                              stretch_compliance=ti.scalar(cs), bending_compliance=ti.scalar(cb),
+                              stretch_relaxation=ti.scalar(rp.stretch_relax),
+                              bending_relaxation=ti.scalar(rp.bend_relax), floor_friction=rp.friction,
+                              floor_normal=ti.Field((), (3,)), init_pos=ti.Field((n,), (3,)),
+                              travel_info=ti.Field((2, n), (1,)))
+    o.floor_normal[None] = [0.0, 1.0, 0.0]
+    o.init_pos.a[:] = rp.init_positions()
+    for k in ("tmp_pos", "tmp_vel", "dpos", "pos", "vel", "ext_f"):
+        setattr(o, k, ti.Field((2, n), (3,)))
+    o.pos.a[0], o.vel.a[0], o.travel_info.a[0, :, 0] = pos, vel, trav
+    return ti.methods(src, "PBDRope", ["update", "update_contact_force"], o)
 
 
 def occupied(o):
@@ -138,36 +181,58 @@ def run_pads(env, st):
     return o, sens, c
 
 
+def run_rope(env, st):
+    fem = os.path.join(PKG, "sensor_model", "gripper_fem.py")
+    sens = [gripper_sensor_object(sp, st["pos"][i], st["vel"][i], st["vpos"][i], st["cv"][i], st["cv1"][i], fem)
+            for i, sp in enumerate(env.sensors)]
+    rp = env.ropes[0]
+    ro = rope_object(rp, st["rpos"][0], st["rvel"][0], st["rtrav"][0], os.path.join(PKG, "object_model", "PBD_rope.py"))
+    c = types.SimpleNamespace(rope_object=ro, gripper=types.SimpleNamespace(fem_sensor1=sens[0], fem_sensor2=sens[1]),
+                              kn=ti.scalar(rp.kn), kd=ti.scalar(rp.kd), kt=ti.scalar(rp.kt),
+                              friction_coeff=ti.scalar(rp.mu_t), norm_eps=1e-11,
+                              contact_idx=ti.Field((2, rp.n), (2,), np.int64),
+                              contact_flag=ti.Field((2, rp.n), (), np.int64))
+    ti.methods(os.path.join(PKG, "tasks", "cable_straightening.py"), "Contact",
+               ["update", "check_collision", "collision", "calculate_contact_force"], c)
+    c.update(0)
+    return ro, sens, c
+
+
 def main():
     global PKG
     PKG = os.path.join(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", "difftactile")
+    f32 = lambda a: np.asarray(a, np.float32)  # noqa: E731 - the inputs are float32 values
     out = {}
     for name, env in scenes().items():
-        st = seeded_state(env, seed=5 if name == "corotated_cube" else 6)
-        if name == "corotated_cube":
-            o, sens = run_cube(env, st)
-        else:
-            o, sens, c = run_pads(env, st)
-        occ, gm, gvi, gvo, gf = occupied(o)
-        f32 = lambda a: np.asarray(a, np.float32)  # noqa: E731 - the inputs are float32 values
-        rec = {"x": f32(st["x"]), "v": f32(st["v"]), "C": f32(st["C"]), "F": f32(st["F"]),
-               "x1": o.x_0.a[1], "v1": o.v_0.a[1], "C1": o.C_0.a[1], "F1": o.F_0.a[1],
-               "occ": occ.astype(np.int32), "grid_m": gm, "grid_v_in": gvi, "grid_v_out": gvo, "grid_f": gf,
-               "consts": np.array([DT, env.dx, env.volume, env.p_mass, env.eps, env.bound, *env.materials[0].mu_lam,
+        st = seeded_state(env, seed={"corotated_cube": 5, "plastic_pads": 6, "rope_pads": 7}[name],
+                          jitter=0.02 * (0.012 if name == "rope_pads" else env.dx))  # 2% of a hex edge
+        rec = {"consts": np.array([DT, env.dx, env.volume, env.p_mass, env.eps, env.bound, *env.materials[0].mu_lam,
                                    env.materials[0].yield_stress, env.kn, env.kd, env.kt, env.mu_t])}
-        if name != "corotated_cube":
-            i, j, k = occ.T
-            rec["cidx"] = c.contact_idx.a[0][i, j, k].astype(np.int32)
-            for s, so in enumerate(sens):
-                for key, val in (("pos", f32(st["pos"][s])), ("vel", f32(st["vel"][s])),
-                                 ("vpos", f32(st["vpos"][s])), ("cv", f32(st["cv"][s])), ("B", so.B.a), ("vel_mid", so.vel.a[0]),
-                                 ("ext", so.external_force_field.a[0]), ("pos1", so.pos.a[1]),
-                                 ("vel1", so.vel.a[1]), ("vpos1", so.virtual_pos.a[1])):
-                    rec[f"s{s}_{key}"] = val
+        if name == "rope_pads":
+            ro, sens, c = run_rope(env, st)
+            rec.update(rpos=f32(st["rpos"][0]), rvel=f32(st["rvel"][0]), rtrav=f32(st["rtrav"][0]),
+                       rpos1=ro.pos.a[1], rvel1=ro.vel.a[1], rtrav1=ro.travel_info.a[1, :, 0], rext=ro.ext_f.a[0],
+                       rcidx=c.contact_idx.a[0].astype(np.int32))
+            summary = f"{env.ropes[0].n} rope particles, {int((ro.ext_f.a[0] != 0).any(1).sum())} in contact"
+        else:
+            o, sens, c = run_cube(env, st) + (None,) if name == "corotated_cube" else run_pads(env, st)
+            occ, gm, gvi, gvo, gf = occupied(o)
+            rec.update(x=f32(st["x"]), v=f32(st["v"]), C=f32(st["C"]), F=f32(st["F"]), x1=o.x_0.a[1], v1=o.v_0.a[1],
+                       C1=o.C_0.a[1], F1=o.F_0.a[1], occ=occ.astype(np.int32), grid_m=gm, grid_v_in=gvi,
+                       grid_v_out=gvo, grid_f=gf)
+            if c is not None:
+                i, j, k = occ.T
+                rec["cidx"] = c.contact_idx.a[0][i, j, k].astype(np.int32)
+            summary = f"{env.n_particles} particles, {len(occ)} occupied nodes"
+        for s, so in enumerate(sens):
+            for key, val in (("pos", f32(st["pos"][s])), ("vel", f32(st["vel"][s])), ("vpos", f32(st["vpos"][s])),
+                             ("cv", f32(st["cv"][s])), ("cv1", f32(st["cv1"][s])), ("B", so.B.a),
+                             ("vel_mid", so.vel.a[0]), ("ext", so.external_force_field.a[0]), ("pos1", so.pos.a[1]),
+                             ("vel1", so.vel.a[1]), ("vpos1", so.virtual_pos.a[1])):
+                rec[f"s{s}_{key}"] = val
+            summary += f", sensor {s}: {int((so.external_force_field.a[0] != 0).any(1).sum())} vertices in contact"
         out.update({f"{name}/{k}": v for k, v in rec.items()})
-        print(name, env.n_particles, "particles,", len(occ), "occupied nodes",
-              "" if name == "corotated_cube" else f", contacts {int((rec['s0_ext'] != 0).any(1).sum())}"
-              f" + {int((rec['s1_ext'] != 0).any(1).sum())} sensor vertices")
+        print(name + ":", summary)
     np.savez_compressed(os.path.join(HERE, "substep_ref.npz"), **out)
 
 

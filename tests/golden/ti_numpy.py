@@ -6,7 +6,8 @@ scripts of this folder (make_substep.py), which read the methods out of a refere
 Semantics taken for the Taichi primitives (the documented behaviour of Taichi 1.6):
   - a kernel's outermost loop runs its iterations; `+=` on a field element accumulates (Taichi makes
     it atomic; sequential execution here only fixes the summation order);
-  - reading a field element gives a copy; `x.cast(int)` truncates toward zero;
+  - reading a field element gives a copy (`field[k][i] = x` still writes the field);
+    `x.cast(int)` truncates toward zero;
   - `v.norm(eps) = sqrt(v.v + eps)`, `v.normalized(eps) = v / (|v| + eps)`;
   - `ti.math.sign(0) = +1` (never reached by the fixtures' inputs);
   - `ti.svd(F) = (U, diag(s), V)` with det U = det V = +1, the last singular value carrying the sign
@@ -58,6 +59,24 @@ class Arr(np.ndarray):
         return np.linalg.inv(np.asarray(self, np.float64)).view(Arr)
 
 
+class Elem(Arr):
+    """A field element as read: a copy (arithmetic and `+=` on it stay local, as in Taichi), except
+    that a component assignment made straight through the read, `field[k][i] = x`, also writes the
+    field, which is what that form does in Taichi.  (The reference methods run here never assign a
+    component of an element they stored in a local name.)"""
+
+    _home = None
+
+    def __array_finalize__(self, obj):
+        self._home = None
+
+    def __setitem__(self, i, v):
+        super().__setitem__(i, v)
+        if self._home is not None:
+            a, k = self._home
+            a[k][i] = v
+
+
 class Field:
     """A Taichi field: ``shape`` indices, each element a scalar or an ``elem``-shaped value."""
 
@@ -81,8 +100,13 @@ class Field:
         return tuple(out)
 
     def __getitem__(self, key):
-        v = self.a[self._key(key)]
-        return v.copy().view(Arr) if isinstance(v, np.ndarray) else v.item()
+        k = self._key(key)
+        v = self.a[k]
+        if not isinstance(v, np.ndarray):
+            return v.item()
+        e = v.copy().view(Elem)
+        e._home = (self.a, k)
+        return e
 
     def __setitem__(self, key, val):
         self.a[self._key(key)] = np.asarray(val)

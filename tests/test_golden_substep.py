@@ -1,9 +1,11 @@
 """The oracle's substep against golden substeps of the reference's own simulation methods
 (tests/golden/make_substep.py runs MPMObj of mpm_elastic.py / mpm_plastic.py, FEMDomeSensor of
-fem_sensor.py and Contact.update of grasp_plastic.py, taken out of the reference source, in float64
-on numpy fields).  Same states, same constants, one substep: particles, the grid at every occupied
-node, the contact argmin, the sensors' elastic velocities, contact forces and next frame agree to
-float64 rounding (1e-9 relative, norm-wise), and the rest-shape inverses B to 1e-12."""
+fem_sensor.py / gripper_fem.py, PBDRope of PBD_rope.py and Contact.update of grasp_plastic.py and
+cable_straightening.py, taken out of the reference source, in float64 on numpy fields).  Same
+states, same constants, one substep: particles, the grid at every occupied node, the contact argmin,
+the sensors' elastic velocities, contact forces and next frame, and the rope's next frame, contact
+impulses, contact indices and travel flags agree to float64 rounding (1e-9 relative, norm-wise);
+the rest-shape inverses B (float32 fields in the reference) are equal."""
 import os
 
 import numpy as np
@@ -26,6 +28,42 @@ def _case(g, name):
     return {k.split("/", 1)[1]: g[k] for k in g.files if k.startswith(name + "/")}
 
 
+def _sensors_agree(r, out, dbg, NS):
+    for s in range(NS):
+        assert SS.rel_err(dbg["vel_mid"][s], r[f"s{s}_vel_mid"]) < TOL, s
+        assert SS.rel_err(dbg["ext"][s], r[f"s{s}_ext"]) < TOL, s
+        assert SS.rel_err(out["pos"][s], r[f"s{s}_pos1"]) < TOL, s
+        assert SS.rel_err(out["vel"][s], r[f"s{s}_vel1"]) < TOL, s
+        assert SS.rel_err(out["vpos"][s], r[f"s{s}_vpos1"]) < TOL, s
+
+
+def _sensor_state(env, r):
+    NS = len(env.sensors)
+    f64 = lambda k: [r[f"s{s}_{k}"].astype(np.float64) for s in range(NS)]  # noqa: E731
+    for s, sp in enumerate(env.sensors):  # float32 fields in the reference and on the device alike
+        assert np.array_equal(sp.rest_inverse().astype(np.float64), r[f"s{s}_B"])
+    return {"pos": f64("pos"), "vel": f64("vel"), "vpos": f64("vpos")}, f64("cv"), f64("cv1")
+
+
+def test_oracle_rope_substep_matches_reference_methods(golden):
+    """Contact.update of tasks/cable_straightening.py:166-173 (two gripper pads of gripper_fem.py with
+    per-frame control velocities; PBDRope.update of PBD_rope.py:112-180; the rope collision
+    :288-319 with its contact-force variant :212-224)."""
+    env = scenes()["rope_pads"]
+    r = _case(golden, "rope_pads")
+    st, cv, cv1 = _sensor_state(env, r)
+    st.update(x=np.zeros((0, 3)), v=np.zeros((0, 3)), C=np.zeros((0, 3, 3)), F=np.zeros((0, 3, 3)),
+              rpos=[r["rpos"].astype(np.float64)], rvel=[r["rvel"].astype(np.float64)],
+              rtrav=[r["rtrav"].astype(np.float64)])
+    out, dbg = O.Oracle(env, DT, np.float64, grad_clip=0.0).substep(st, cv=cv, cv1=cv1)
+    assert np.array_equal(dbg["rope_cidx"][0][:, :2], r["rcidx"])
+    assert (r["rext"] != 0).any() and np.array_equal(out["rtrav"][0], r["rtrav1"])
+    assert SS.rel_err(dbg["rope_ext"][0], r["rext"]) < TOL
+    assert SS.rel_err(out["rpos"][0], r["rpos1"]) < TOL
+    assert SS.rel_err(out["rvel"][0], r["rvel1"]) < TOL
+    _sensors_agree(r, out, dbg, 2)
+
+
 @pytest.mark.parametrize("name", ["corotated_cube", "plastic_pads"])
 def test_oracle_substep_matches_reference_methods(golden, name):
     env = scenes()[name]
@@ -35,13 +73,8 @@ def test_oracle_substep_matches_reference_methods(golden, name):
               env.kt, env.mu_t]
     assert np.allclose(r["consts"], consts, rtol=1e-15, atol=0)  # the scene builders still build these scenes
     NS = len(env.sensors)
-    st = {k: r[k].astype(np.float64) for k in ("x", "v", "C", "F")}
-    st["pos"] = [r[f"s{s}_pos"].astype(np.float64) for s in range(NS)]
-    st["vel"] = [r[f"s{s}_vel"].astype(np.float64) for s in range(NS)]
-    st["vpos"] = [r[f"s{s}_vpos"].astype(np.float64) for s in range(NS)]
-    cv = [r[f"s{s}_cv"].astype(np.float64) for s in range(NS)]
-    for s, sp in enumerate(env.sensors):
-        assert SS.rel_err(sp.rest_inverse().astype(np.float64), r[f"s{s}_B"]) < 1e-12
+    st, cv, _ = _sensor_state(env, r)
+    st.update({k: r[k].astype(np.float64) for k in ("x", "v", "C", "F")})
     o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
     out, dbg = o.substep(st, cv=cv if NS else None, cv1=cv if NS else None)
     for a, b in (("x1", "x"), ("v1", "v"), ("C1", "C"), ("F1", "F")):
@@ -54,12 +87,7 @@ def test_oracle_substep_matches_reference_methods(golden, name):
         return
     assert np.array_equal(dbg["cidx"][i, j, k, :NS], r["cidx"])
     assert float(np.abs(r["grid_f"]).max()) > 0 and all((r[f"s{s}_ext"] != 0).any() for s in range(NS))
-    for s in range(NS):
-        assert SS.rel_err(dbg["vel_mid"][s], r[f"s{s}_vel_mid"]) < TOL, s
-        assert SS.rel_err(dbg["ext"][s], r[f"s{s}_ext"]) < TOL, s
-        assert SS.rel_err(out["pos"][s], r[f"s{s}_pos1"]) < TOL, s
-        assert SS.rel_err(out["vel"][s], r[f"s{s}_vel1"]) < TOL, s
-        assert SS.rel_err(out["vpos"][s], r[f"s{s}_vpos1"]) < TOL, s
+    _sensors_agree(r, out, dbg, NS)
 
 
 def test_fixture_exercises_both_return_map_branches(golden):
