@@ -1,8 +1,9 @@
 """ORACLE (test infrastructure only): float64 numpy restatement of the shape-target loss
 (difftactile/tasks/deform_loss.py:8-146) and the mass-only P2G it reads
-(compute_grid_m_kernel, difftactile/object_model/mpm_plastic.py:169-178).  Parity unpinned against
-the reference's outputs (Taichi not available); pinned by the known answers in
-tests/test_oracle_deform.py."""
+(compute_grid_m_kernel, difftactile/object_model/mpm_plastic.py:169-178).  Pinned against the
+reference's own methods run on a numpy stand-in for Taichi (tests/golden/make_deform.py,
+tests/test_golden_deform.py: grid mass, distance field and loss to float64 rounding) and by the
+known answers in tests/test_oracle_deform.py; the gradient by finite differences."""
 from __future__ import annotations
 
 import numpy as np

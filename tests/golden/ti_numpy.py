@@ -135,7 +135,19 @@ def static(x):
 
 
 def ndrange(*ns):
-    return itertools.product(*[range(n) for n in ns])
+    return itertools.product(*[range(*n) if isinstance(n, tuple) else range(n) for n in ns])
+
+
+def grouped(x):
+    """Index vectors of a field's shape or of an ndrange."""
+    it = ndrange(*x.shape) if isinstance(x, Field) else x
+    return (Arr(i, np.int64) for i in it)
+
+
+def cast(x, dtype):
+    if dtype in (int, i32):
+        return np.trunc(np.asarray(x, np.float64)).astype(np.int64).view(Arr)
+    return np.asarray(x, np.float64).view(Arr) if isinstance(x, np.ndarray) else float(x)
 
 
 # ---- values ----
