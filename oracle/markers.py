@@ -1,10 +1,11 @@
 """ORACLE (test infrastructure only): float64 numpy restatement of the marker readout
 (extract_markers, difftactile/sensor_model/fem_sensor.py:161-187) with the fisheye projection
 project_3d_2d (difftactile/sensor_model/fisheye_model.py:12-30), and the summed contact force
-(compute_contact_force, difftactile/tasks/grasp_plastic.py:218-229).  The projection is pinned
-against golden vectors of the reference's numpy projection (tests/golden/fisheye_ref.npz, made by
-tests/golden/make_fisheye.py from the reference source); the rest is unpinned against the
-reference's outputs (Taichi not available) and pinned by analytic known answers in
+(compute_contact_force, difftactile/tasks/grasp_plastic.py:218-229).  Pinned against the
+reference's own code: the numpy projection (tests/golden/fisheye_ref.npz, tests/golden/
+make_fisheye.py), the marker set-up and readout (tests/golden/markers_ref.npz: init_cam_model and
+extract_markers run on a numpy stand-in for Taichi by tests/golden/make_markers.py) and the force
+sum (tests/golden/substep_ref.npz, compute_contact_force); also by analytic known answers in
 tests/test_oracle_readout.py."""
 from __future__ import annotations
 

@@ -9,7 +9,8 @@ primitives).  Two cases, one substep each, on seeded states:
                   grid_op, g2p; :134-260), a fixed-corotated cube falling into the floor band of a 16^3
                   grid (wall rule of grid_op);
   plastic_pads    Contact.update of tasks/grasp_plastic.py:151-164 (check_collision, collision,
-                  calculate_contact_force; :205-299) over MPMObj of object_model/mpm_plastic.py (the
+                  calculate_contact_force; :205-299) and its readouts compute_contact_force and
+                  compute_obj_pos (:218-229, :259-261) over MPMObj of object_model/mpm_plastic.py (the
                   von Mises p2g; :140-310) and two FEMDomeSensor pads of sensor_model/fem_sensor.py
                   (init_pos, find_closest, find_sdf, update_contact_force, update, update2; :325-457),
                   a plastic box pressed by two hex pads (half of its particles beyond the yield surface);
@@ -175,9 +176,13 @@ def run_pads(env, st):
                               kn=ti.scalar(env.kn), kd=ti.scalar(env.kd), kt=ti.scalar(env.kt),
                               friction_coeff=ti.scalar(env.mu_t), norm_eps=1e-11,
                               contact_idx=ti.Field((2, n, n, n), (2,), np.int64))
+    c.contact_force1, c.contact_force2, c.predict_obj_pos = ti.Field((), (3,)), ti.Field((), (3,)), ti.Field((), (3,))
     ti.methods(os.path.join(PKG, "tasks", "grasp_plastic.py"), "Contact",
-               ["update", "check_collision", "collision", "calculate_contact_force"], c)
+               ["update", "check_collision", "collision", "calculate_contact_force", "compute_contact_force",
+                "compute_obj_pos"], c)
     c.update(0)
+    c.compute_contact_force(0)  # the readouts of the grasp task's losses (:218-229, :259-261)
+    c.compute_obj_pos(1)
     return o, sens, c
 
 
@@ -223,6 +228,8 @@ def main():
             if c is not None:
                 i, j, k = occ.T
                 rec["cidx"] = c.contact_idx.a[0][i, j, k].astype(np.int32)
+                rec["contact_force"] = np.stack([c.contact_force1.a, c.contact_force2.a])
+                rec["com1"] = c.predict_obj_pos.a
             summary = f"{env.n_particles} particles, {len(occ)} occupied nodes"
         for s, so in enumerate(sens):
             for key, val in (("pos", f32(st["pos"][s])), ("vel", f32(st["vel"][s])), ("vpos", f32(st["vpos"][s])),

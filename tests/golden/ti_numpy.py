@@ -202,6 +202,8 @@ exp = _ew(np.exp)
 sqrt = _ew(np.sqrt)
 cos = _ew(np.cos)
 sin = _ew(np.sin)
+acos = _ew(np.arccos)
+atan2 = _ew(np.arctan2)
 
 
 def svd(F):
@@ -221,22 +223,39 @@ math = types.SimpleNamespace(
     sign=lambda x: 1.0 if x >= 0 else -1.0,
     radians=lambda x: (np.asarray(x, np.float64) * (np.pi / 180.0)).view(Arr),
     clamp=lambda x, lo, hi: _ew(np.clip)(x, lo, hi),
+    pi=np.pi,
 )
 
 
-def methods(path, cls_name, names, obj):
+def _defs(path, body, names, extra):
+    import ast
+
+    defs = [n for n in body if isinstance(n, ast.FunctionDef) and n.name in names]
+    missing = set(names) - {d.name for d in defs}
+    if missing:
+        raise KeyError(f"{path} has no {sorted(missing)}")
+    ns = {"ti": sys.modules[__name__], "np": np, **(extra or {})}
+    exec(compile(ast.Module(body=defs, type_ignores=[]), path, "exec"), ns)
+    return ns
+
+
+def functions(path, names, extra=None):
+    """The module-level functions ``names`` of the source file ``path``, executed with this module
+    as ``ti`` (and the names of ``extra`` in scope)."""
+    import ast
+
+    ns = _defs(path, ast.parse(open(path).read(), path).body, names, extra)
+    return {n: ns[n] for n in names}
+
+
+def methods(path, cls_name, names, obj, extra=None):
     """Bind the methods ``names`` of class ``cls_name`` in the source file ``path`` to ``obj``, their
-    source executed with this module as ``ti``."""
+    source executed with this module as ``ti`` (and the names of ``extra`` in scope)."""
     import ast
 
     tree = ast.parse(open(path).read(), path)
     cls = next(n for n in tree.body if isinstance(n, ast.ClassDef) and n.name == cls_name)
-    defs = [n for n in cls.body if isinstance(n, ast.FunctionDef) and n.name in names]
-    missing = set(names) - {d.name for d in defs}
-    if missing:
-        raise KeyError(f"{cls_name} in {path} has no {sorted(missing)}")
-    ns = {"ti": sys.modules[__name__], "np": np}
-    exec(compile(ast.Module(body=defs, type_ignores=[]), path, "exec"), ns)
+    ns = _defs(path, cls.body, names, extra)
     for n in names:
         setattr(obj, n, types.MethodType(ns[n], obj))
     return obj

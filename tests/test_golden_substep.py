@@ -11,6 +11,7 @@ import os
 import numpy as np
 import pytest
 
+from oracle import markers as OM
 from oracle import oracle as O
 from tests import small_scenes as SS
 from tests.golden.make_substep import DT, scenes
@@ -88,6 +89,10 @@ def test_oracle_substep_matches_reference_methods(golden, name):
     assert np.array_equal(dbg["cidx"][i, j, k, :NS], r["cidx"])
     assert float(np.abs(r["grid_f"]).max()) > 0 and all((r[f"s{s}_ext"] != 0).any() for s in range(NS))
     _sensors_agree(r, out, dbg, NS)
+    # the grasp task's readouts: summed surface force of each pad, centre of mass of the next frame
+    for s, sp in enumerate(env.sensors):
+        assert SS.rel_err(OM.contact_force_sum(dbg["ext"][s], sp.tris), r["contact_force"][s]) < TOL, s
+    assert SS.rel_err(out["x"].mean(0), r["com1"]) < TOL
 
 
 def test_fixture_exercises_both_return_map_branches(golden):
