@@ -171,7 +171,7 @@ class _Matrix:
         return Arr(np.zeros((n, m)))
 
     @staticmethod
-    def identity(dtype, n):
+    def identity(dtype=None, n=None, dt=None):
         return Arr(np.eye(n))
 
     @staticmethod
