@@ -206,7 +206,7 @@ acos = _ew(np.arccos)
 atan2 = _ew(np.arctan2)
 
 
-def svd(F):
+def svd(F, dt=None):
     U, s, Vt = np.linalg.svd(np.asarray(F, np.float64))
     V = Vt.T.copy()
     if np.linalg.det(U) < 0:
