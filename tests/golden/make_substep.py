@@ -3,7 +3,7 @@
 The reference's substep is Taichi code (taichi is absent here and not installable), so its methods
 are read out of the reference source with `ast` and run, in float64, on numpy fields through the
 stand-in `ti` module of this folder (ti_numpy.py, which lists the semantics it takes for Taichi's
-primitives).  Two cases, one substep each, on seeded states:
+primitives).  Four cases, one substep each, on seeded states:
 
   corotated_cube  MPMObj of object_model/mpm_elastic.py (compute_new_F, svd, p2g, check_grid_occupy,
                   grid_op, g2p; :134-260), a fixed-corotated cube falling into the floor band of a 16^3
@@ -14,6 +14,8 @@ primitives).  Two cases, one substep each, on seeded states:
                   von Mises p2g; :140-310) and two FEMDomeSensor pads of sensor_model/fem_sensor.py
                   (init_pos, find_closest, find_sdf, update_contact_force, update, update2; :325-457),
                   a plastic box pressed by two hex pads (half of its particles beyond the yield surface);
+  multi_material_cube  MultiObj of object_model/multi_obj.py (per-particle Lame parameters by material
+                  tag in p2g; :168-305), a cube of three material layers;
   rope_pads       Contact.update of tasks/cable_straightening.py:166-173 (check_collision, collision and
                   its calculate_contact_force variant; :212-319) over PBDRope of object_model/PBD_rope.py
                   (update, update_contact_force; :108-180) and two FEMDomeSensor pads of
@@ -53,7 +55,12 @@ def scenes():
     # scene's pad pressing the rope, and a second one well above it
     far = S.hex_pad_sensor([0.5, 0.3, 0.5], nx=4, nz=4, ny=2, h=0.012)
     rope = rope.replace(sensors=[dataclasses.replace(rope.sensors[0], carry=1), dataclasses.replace(far, carry=1)])
-    return {"corotated_cube": cube, "plastic_pads": pads, "rope_pads": rope}
+    # three materials by particle (MultiObj's lower / middle / upper parts, E 4e5 / 4e1 / 4e3, nu 0.4)
+    mats = [S.Material(4e5, 0.4), S.Material(4e1, 0.4), S.Material(4e3, 0.4)]
+    tri = SS.elastic_cube(n=16, side_cells=4, center=(0.5, 0.5, 0.5), v=(0.0, 0.0, 0.0), seed=2)
+    layer = np.digitize(tri.x[:, 1], np.quantile(tri.x[:, 1], [1 / 3, 2 / 3])).astype(np.int32)
+    tri = tri.replace(materials=mats, mat=layer)
+    return {"corotated_cube": cube, "plastic_pads": pads, "rope_pads": rope, "multi_material_cube": tri}
 
 
 def seeded_state(env, seed, jitter):
@@ -76,7 +83,7 @@ def seeded_state(env, seed, jitter):
     return st
 
 
-def mpm_object(env, st, src, plastic):
+def mpm_object(env, st, src, plastic, cls="MPMObj"):
     n = env.n_grid[0]
     N = env.n_particles
     m = env.materials[0]
@@ -95,7 +102,7 @@ def mpm_object(env, st, src, plastic):
     names = ["compute_new_F", "svd", "p2g", "check_grid_occupy", "grid_op", "g2p", "update_contact_force"]
     if plastic:
         names += ["norm", "make_matrix_from_diag", "compute_von_mises"]
-    return ti.methods(src, "MPMObj", names, o)
+    return ti.methods(src, cls, names, o)
 
 
 def sensor_object(sp, pos, vel, vpos, cv, src, cls="FEMDomeSensor"):
@@ -167,6 +174,18 @@ def run_cube(env, st):
     return o, []
 
 
+def run_multi(env, st):
+    o = mpm_object(env, st, os.path.join(PKG, "object_model", "multi_obj.py"), plastic=False, cls="MultiObj")
+    mu, lam = zip(*[m.mu_lam for m in env.materials])
+    o.mu_0, o.lamda_0 = ti.Field((len(mu),)), ti.Field((len(mu),))
+    o.mu_0.a[:], o.lamda_0.a[:] = mu, lam
+    o.titles = ti.Field((env.n_particles,), (), np.int64)
+    o.titles.a[:] = env.mat
+    for name in ("compute_new_F", "svd", "p2g", "check_grid_occupy", "grid_op", "g2p"):
+        getattr(o, name)(0)
+    return o, []
+
+
 def run_pads(env, st):
     o = mpm_object(env, st, os.path.join(PKG, "object_model", "mpm_plastic.py"), plastic=True)
     sens = [sensor_object(sp, st["pos"][i], st["vel"][i], st["vpos"][i], st["cv"][i],
@@ -209,7 +228,7 @@ def main():
     f32 = lambda a: np.asarray(a, np.float32)  # noqa: E731 - the inputs are float32 values
     out = {}
     for name, env in scenes().items():
-        st = seeded_state(env, seed={"corotated_cube": 5, "plastic_pads": 6, "rope_pads": 7}[name],
+        st = seeded_state(env, seed={"corotated_cube": 5, "plastic_pads": 6, "rope_pads": 7, "multi_material_cube": 8}[name],
                           jitter=0.02 * (0.012 if name == "rope_pads" else env.dx))  # 2% of a hex edge
         rec = {"consts": np.array([DT, env.dx, env.volume, env.p_mass, env.eps, env.bound, *env.materials[0].mu_lam,
                                    env.materials[0].yield_stress, env.kn, env.kd, env.kt, env.mu_t])}
@@ -220,7 +239,8 @@ def main():
                        rcidx=c.contact_idx.a[0].astype(np.int32))
             summary = f"{env.ropes[0].n} rope particles, {int((ro.ext_f.a[0] != 0).any(1).sum())} in contact"
         else:
-            o, sens, c = run_cube(env, st) + (None,) if name == "corotated_cube" else run_pads(env, st)
+            run = {"corotated_cube": run_cube, "multi_material_cube": run_multi}.get(name)
+            o, sens, c = run(env, st) + (None,) if run else run_pads(env, st)
             occ, gm, gvi, gvo, gf = occupied(o)
             rec.update(x=f32(st["x"]), v=f32(st["v"]), C=f32(st["C"]), F=f32(st["F"]), x1=o.x_0.a[1], v1=o.v_0.a[1],
                        C1=o.C_0.a[1], F1=o.F_0.a[1], occ=occ.astype(np.int32), grid_m=gm, grid_v_in=gvi,

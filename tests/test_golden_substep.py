@@ -1,5 +1,6 @@
 """The oracle's substep against golden substeps of the reference's own simulation methods
-(tests/golden/make_substep.py runs MPMObj of mpm_elastic.py / mpm_plastic.py, FEMDomeSensor of
+(tests/golden/make_substep.py runs MPMObj of mpm_elastic.py / mpm_plastic.py, MultiObj of
+multi_obj.py, FEMDomeSensor of
 fem_sensor.py / gripper_fem.py, PBDRope of PBD_rope.py and Contact.update of grasp_plastic.py and
 cable_straightening.py, taken out of the reference source, in float64 on numpy fields).  Same
 states, same constants, one substep: particles, the grid at every occupied node, the contact argmin,
@@ -65,7 +66,7 @@ def test_oracle_rope_substep_matches_reference_methods(golden):
     _sensors_agree(r, out, dbg, 2)
 
 
-@pytest.mark.parametrize("name", ["corotated_cube", "plastic_pads"])
+@pytest.mark.parametrize("name", ["corotated_cube", "plastic_pads", "multi_material_cube"])
 def test_oracle_substep_matches_reference_methods(golden, name):
     env = scenes()[name]
     r = _case(golden, name)
