@@ -3,7 +3,7 @@
 The reference's substep is Taichi code (taichi is absent here and not installable), so its methods
 are read out of the reference source with `ast` and run, in float64, on numpy fields through the
 stand-in `ti` module of this folder (ti_numpy.py, which lists the semantics it takes for Taichi's
-primitives).  Four cases, one substep each, on seeded states:
+primitives).  Five cases on seeded states, one substep each except the chained one:
 
   corotated_cube  MPMObj of object_model/mpm_elastic.py (compute_new_F, svd, p2g, check_grid_occupy,
                   grid_op, g2p; :134-260), a fixed-corotated cube falling into the floor band of a 16^3
@@ -16,6 +16,8 @@ primitives).  Four cases, one substep each, on seeded states:
                   a plastic box pressed by two hex pads (half of its particles beyond the yield surface);
   multi_material_cube  MultiObj of object_model/multi_obj.py (per-particle Lame parameters by material
                   tag in p2g; :168-305), a cube of three material layers;
+  plastic_pads_chain  the plastic_pads scene over five substeps of the grasp task's Contact.update
+                  (frame-to-frame carry of particles, sensor state and per-frame grids);
   rope_pads       Contact.update of tasks/cable_straightening.py:166-173 (check_collision, collision and
                   its calculate_contact_force variant; :212-319) over PBDRope of object_model/PBD_rope.py
                   (update, update_contact_force; :108-180) and two FEMDomeSensor pads of
@@ -42,6 +44,7 @@ from tests import small_scenes as SS  # noqa: E402
 from tests.golden import ti_numpy as ti  # noqa: E402
 
 DT = 1e-4
+CHAIN = 5   # substeps of the chained case
 PKG = None  # the reference's package folder, set by main()
 
 
@@ -60,7 +63,8 @@ def scenes():
     tri = SS.elastic_cube(n=16, side_cells=4, center=(0.5, 0.5, 0.5), v=(0.0, 0.0, 0.0), seed=2)
     layer = np.digitize(tri.x[:, 1], np.quantile(tri.x[:, 1], [1 / 3, 2 / 3])).astype(np.int32)
     tri = tri.replace(materials=mats, mat=layer)
-    return {"corotated_cube": cube, "plastic_pads": pads, "rope_pads": rope, "multi_material_cube": tri}
+    return {"corotated_cube": cube, "plastic_pads": pads, "rope_pads": rope, "multi_material_cube": tri,
+            "plastic_pads_chain": pads}
 
 
 def seeded_state(env, seed, jitter):
@@ -83,7 +87,7 @@ def seeded_state(env, seed, jitter):
     return st
 
 
-def mpm_object(env, st, src, plastic, cls="MPMObj"):
+def mpm_object(env, st, src, plastic, cls="MPMObj", frames=2):
     n = env.n_grid[0]
     N = env.n_particles
     m = env.materials[0]
@@ -94,10 +98,10 @@ def mpm_object(env, st, src, plastic, cls="MPMObj"):
         mu_0=ti.scalar(mu), lambda_0=ti.scalar(lam), yield_stress=ti.scalar(m.yield_stress))
     for k, e in (("x_0", (3,)), ("v_0", (3,)), ("C_0", (3, 3)), ("F_new", (3, 3)), ("F_0", (3, 3)),
                  ("U_svd", (3, 3)), ("V_svd", (3, 3)), ("S_svd", (3, 3))):
-        setattr(o, k, ti.Field((2, N), e))
+        setattr(o, k, ti.Field((frames, N), e))
     for k, e in (("grid_v_in", (3,)), ("grid_v_out", (3,)), ("grid_m", ()), ("grid_f", (3,))):
-        setattr(o, k, ti.Field((2, n, n, n), e))
-    o.grid_occupy = ti.Field((2, n, n, n), (), np.int64)
+        setattr(o, k, ti.Field((frames, n, n, n), e))
+    o.grid_occupy = ti.Field((frames, n, n, n), (), np.int64)
     o.x_0.a[0], o.v_0.a[0], o.C_0.a[0], o.F_0.a[0] = st["x"], st["v"], st["C"], st["F"]
     names = ["compute_new_F", "svd", "p2g", "check_grid_occupy", "grid_op", "g2p", "update_contact_force"]
     if plastic:
@@ -105,7 +109,7 @@ def mpm_object(env, st, src, plastic, cls="MPMObj"):
     return ti.methods(src, cls, names, o)
 
 
-def sensor_object(sp, pos, vel, vpos, cv, src, cls="FEMDomeSensor"):
+def sensor_object(sp, pos, vel, vpos, cv, src, cls="FEMDomeSensor", frames=2):
     V, T = len(sp.verts), len(sp.tets)
     mu, lam = sp.lame()
     M = np.eye(4) if sp.trans_world is None else np.asarray(sp.trans_world, np.float64)
@@ -117,7 +121,7 @@ def sensor_object(sp, pos, vel, vpos, cv, src, cls="FEMDomeSensor"):
     s.init_x = ti.Field((V,), (3,))
     s.init_x.a[:] = np.asarray(sp.verts, np.float64)
     for k in ("pos", "vel", "virtual_pos", "external_force_field"):
-        setattr(s, k, ti.Field((2, V), (3,)))
+        setattr(s, k, ti.Field((frames, V), (3,)))
     s.control_vel = ti.Field((V,), (3,))
     s.B = ti.Field((T,), (3, 3))
     s.f2v = ti.Field((T,), (4,), np.int64)
@@ -186,20 +190,23 @@ def run_multi(env, st):
     return o, []
 
 
-def run_pads(env, st):
-    o = mpm_object(env, st, os.path.join(PKG, "object_model", "mpm_plastic.py"), plastic=True)
+def run_pads(env, st, n_sub=1):
+    fr = n_sub + 1
+    o = mpm_object(env, st, os.path.join(PKG, "object_model", "mpm_plastic.py"), plastic=True, frames=fr)
     sens = [sensor_object(sp, st["pos"][i], st["vel"][i], st["vpos"][i], st["cv"][i],
-                          os.path.join(PKG, "sensor_model", "fem_sensor.py")) for i, sp in enumerate(env.sensors)]
+                          os.path.join(PKG, "sensor_model", "fem_sensor.py"), frames=fr)
+            for i, sp in enumerate(env.sensors)]
     n = env.n_grid[0]
     c = types.SimpleNamespace(mpm_object=o, gripper=types.SimpleNamespace(fem_sensor1=sens[0], fem_sensor2=sens[1]),
                               kn=ti.scalar(env.kn), kd=ti.scalar(env.kd), kt=ti.scalar(env.kt),
                               friction_coeff=ti.scalar(env.mu_t), norm_eps=1e-11,
-                              contact_idx=ti.Field((2, n, n, n), (2,), np.int64))
+                              contact_idx=ti.Field((fr, n, n, n), (2,), np.int64))
     c.contact_force1, c.contact_force2, c.predict_obj_pos = ti.Field((), (3,)), ti.Field((), (3,)), ti.Field((), (3,))
     ti.methods(os.path.join(PKG, "tasks", "grasp_plastic.py"), "Contact",
                ["update", "check_collision", "collision", "calculate_contact_force", "compute_contact_force",
                 "compute_obj_pos"], c)
-    c.update(0)
+    for f in range(n_sub):
+        c.update(f)
     c.compute_contact_force(0)  # the readouts of the grasp task's losses (:218-229, :259-261)
     c.compute_obj_pos(1)
     return o, sens, c
@@ -228,10 +235,25 @@ def main():
     f32 = lambda a: np.asarray(a, np.float32)  # noqa: E731 - the inputs are float32 values
     out = {}
     for name, env in scenes().items():
-        st = seeded_state(env, seed={"corotated_cube": 5, "plastic_pads": 6, "rope_pads": 7, "multi_material_cube": 8}[name],
+        seed = {"corotated_cube": 5, "plastic_pads": 6, "rope_pads": 7, "multi_material_cube": 8,
+                "plastic_pads_chain": 9}[name]
+        st = seeded_state(env, seed=seed,
                           jitter=0.02 * (0.012 if name == "rope_pads" else env.dx))  # 2% of a hex edge
         rec = {"consts": np.array([DT, env.dx, env.volume, env.p_mass, env.eps, env.bound, *env.materials[0].mu_lam,
                                    env.materials[0].yield_stress, env.kn, env.kd, env.kt, env.mu_t])}
+        if name == "plastic_pads_chain":
+            o, sens, c = run_pads(env, st, n_sub=CHAIN)
+            rec.update(x=f32(st["x"]), v=f32(st["v"]), C=f32(st["C"]), F=f32(st["F"]),
+                       xN=o.x_0.a[CHAIN], vN=o.v_0.a[CHAIN], CN=o.C_0.a[CHAIN], FN=o.F_0.a[CHAIN])
+            for s_, so in enumerate(sens):
+                for key, val in (("pos", f32(st["pos"][s_])), ("vel", f32(st["vel"][s_])),
+                                 ("vpos", f32(st["vpos"][s_])), ("cv", f32(st["cv"][s_])), ("cv1", f32(st["cv1"][s_])),
+                                 ("B", so.B.a), ("posN", so.pos.a[CHAIN]), ("velN", so.vel.a[CHAIN]),
+                                 ("vposN", so.virtual_pos.a[CHAIN])):
+                    rec[f"s{s_}_{key}"] = val
+            out.update({f"{name}/{k}": v for k, v in rec.items()})
+            print(name + ":", f"{CHAIN} substeps")
+            continue
         if name == "rope_pads":
             ro, sens, c = run_rope(env, st)
             rec.update(rpos=f32(st["rpos"][0]), rvel=f32(st["rvel"][0]), rtrav=f32(st["rtrav"][0]),

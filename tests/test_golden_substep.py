@@ -96,6 +96,24 @@ def test_oracle_substep_matches_reference_methods(golden, name):
     assert SS.rel_err(out["x"].mean(0), r["com1"]) < TOL
 
 
+def test_oracle_chain_matches_reference_methods(golden):
+    """Five substeps of the grasp task's Contact.update, each oracle substep fed the previous one's
+    output: the particles and both pads at the last frame."""
+    from tests.golden.make_substep import CHAIN
+    env = scenes()["plastic_pads_chain"]
+    r = _case(golden, "plastic_pads_chain")
+    st, cv, _ = _sensor_state(env, r)
+    st.update({k: r[k].astype(np.float64) for k in ("x", "v", "C", "F")})
+    o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
+    for _ in range(CHAIN):
+        st, _ = o.substep(st, cv=cv, cv1=cv)
+    for a, b in (("xN", "x"), ("vN", "v"), ("CN", "C"), ("FN", "F")):
+        assert SS.rel_err(st[b], r[a]) < TOL, a
+    for s in range(len(env.sensors)):
+        for a, b in (("posN", "pos"), ("velN", "vel"), ("vposN", "vpos")):
+            assert SS.rel_err(st[b][s], r[f"s{s}_{a}"]) < TOL, (s, a)
+
+
 def test_fixture_exercises_both_return_map_branches(golden):
     """Half of the plastic box's particles start beyond the von Mises yield surface, half inside."""
     r = _case(golden, "plastic_pads")
