@@ -96,6 +96,23 @@ def test_oracle_substep_matches_reference_methods(golden, name):
     assert SS.rel_err(out["x"].mean(0), r["com1"]) < TOL
 
 
+@pytest.mark.parametrize("name", ["corotated_cube", "plastic_pads", "multi_material_cube"])
+def test_float32_oracle_is_within_the_one_substep_tolerance(golden, name):
+    """In float32 (the CUDA path's arithmetic) the oracle's substep stays within 1e-5 relative of the
+    reference's float64 step for x, v, C, F and the sensors' positions (worst 4e-6: v and C of the
+    three-material cube, whose stiffest layer has E = 4e5)."""
+    env = scenes()[name]
+    r = _case(golden, name)
+    st, cv, _ = _sensor_state(env, r)
+    st.update({k: r[k].astype(np.float64) for k in ("x", "v", "C", "F")})
+    NS = len(env.sensors)
+    out, _ = O.Oracle(env, DT, np.float32, grad_clip=0.0).substep(st, cv=cv if NS else None, cv1=cv if NS else None)
+    for a, b in (("x1", "x"), ("v1", "v"), ("C1", "C"), ("F1", "F")):
+        assert SS.rel_err(out[b].astype(np.float64), r[a]) < 1e-5, a
+    for s in range(NS):
+        assert SS.rel_err(out["pos"][s].astype(np.float64), r[f"s{s}_pos1"]) < 1e-5, s
+
+
 def test_oracle_chain_matches_reference_methods(golden):
     """Five substeps of the grasp task's Contact.update, each oracle substep fed the previous one's
     output: the particles and both pads at the last frame."""
