@@ -22,7 +22,8 @@ primitives).  Five cases on seeded states, one substep each except the chained o
                   its calculate_contact_force variant; :212-319) over PBDRope of object_model/PBD_rope.py
                   (update, update_contact_force; :108-180) and two FEMDomeSensor pads of
                   sensor_model/gripper_fem.py (per-frame control velocities, the carry term of update2),
-                  a rope pressed by a pad along ten of its sixteen particles.
+                  a rope pressed by a pad along ten of its sixteen particles;
+  rope_pads_chain the rope_pads scene over five substeps, the pads' control velocities ramping.
 
 The scenes come from tests/small_scenes.py (the parity scenes); states, constants and the outputs
 (particles, the grid at occupied nodes, contact indices, the sensors' forces and next frame) go to
@@ -64,7 +65,7 @@ def scenes():
     layer = np.digitize(tri.x[:, 1], np.quantile(tri.x[:, 1], [1 / 3, 2 / 3])).astype(np.int32)
     tri = tri.replace(materials=mats, mat=layer)
     return {"corotated_cube": cube, "plastic_pads": pads, "rope_pads": rope, "multi_material_cube": tri,
-            "plastic_pads_chain": pads}
+            "plastic_pads_chain": pads, "rope_pads_chain": rope}
 
 
 def seeded_state(env, seed, jitter):
@@ -138,15 +139,15 @@ def sensor_object(sp, pos, vel, vpos, cv, src, cls="FEMDomeSensor", frames=2):
     return s
 
 
-def gripper_sensor_object(sp, pos, vel, vpos, cv, cv1, src):
-    """A gripper pad (sensor_model/gripper_fem.py: per-frame control velocities)."""
-    s = sensor_object(sp, pos, vel, vpos, cv, src, cls="FEMDomeSensor")
-    s.control_vel = ti.Field((2, len(sp.verts)), (3,))
-    s.control_vel.a[0], s.control_vel.a[1] = cv, cv1
+def gripper_sensor_object(sp, pos, vel, vpos, cvs, src):
+    """A gripper pad (sensor_model/gripper_fem.py: per-frame control velocities ``cvs`` [frames][V][3])."""
+    s = sensor_object(sp, pos, vel, vpos, cvs[0], src, cls="FEMDomeSensor", frames=len(cvs))
+    s.control_vel = ti.Field((len(cvs), len(sp.verts)), (3,))
+    s.control_vel.a[:] = cvs
     return s
 
 
-def rope_object(rp, pos, vel, trav, src):
+def rope_object(rp, pos, vel, trav, src, frames=2):
     n = rp.n
     cs, cb = rp.compliance
     o = types.SimpleNamespace(n_particles=n, n_segments=n - 1, dt=DT, p_rad=rp.rad, p_mass=rp.mass,
@@ -156,11 +157,11 @@ def rope_object(rp, pos, vel, trav, src):
                               stretch_relaxation=ti.scalar(rp.stretch_relax),
                               bending_relaxation=ti.scalar(rp.bend_relax), floor_friction=rp.friction,
                               floor_normal=ti.Field((), (3,)), init_pos=ti.Field((n,), (3,)),
-                              travel_info=ti.Field((2, n), (1,)))
+                              travel_info=ti.Field((frames, n), (1,)))
     o.floor_normal[None] = [0.0, 1.0, 0.0]
     o.init_pos.a[:] = rp.init_positions()
     for k in ("tmp_pos", "tmp_vel", "dpos", "pos", "vel", "ext_f"):
-        setattr(o, k, ti.Field((2, n), (3,)))
+        setattr(o, k, ti.Field((frames, n), (3,)))
     o.pos.a[0], o.vel.a[0], o.travel_info.a[0, :, 0] = pos, vel, trav
     return ti.methods(src, "PBDRope", ["update", "update_contact_force"], o)
 
@@ -212,20 +213,24 @@ def run_pads(env, st, n_sub=1):
     return o, sens, c
 
 
-def run_rope(env, st):
+def run_rope(env, st, n_sub=1):
     fem = os.path.join(PKG, "sensor_model", "gripper_fem.py")
-    sens = [gripper_sensor_object(sp, st["pos"][i], st["vel"][i], st["vpos"][i], st["cv"][i], st["cv1"][i], fem)
+    fr = n_sub + 1
+    cvs = [np.stack([st["cv"][i] + f * (st["cv1"][i] - st["cv"][i]) for f in range(fr)]) for i in range(len(env.sensors))]
+    sens = [gripper_sensor_object(sp, st["pos"][i], st["vel"][i], st["vpos"][i], cvs[i], fem)
             for i, sp in enumerate(env.sensors)]
     rp = env.ropes[0]
-    ro = rope_object(rp, st["rpos"][0], st["rvel"][0], st["rtrav"][0], os.path.join(PKG, "object_model", "PBD_rope.py"))
+    ro = rope_object(rp, st["rpos"][0], st["rvel"][0], st["rtrav"][0], os.path.join(PKG, "object_model", "PBD_rope.py"),
+                     frames=fr)
     c = types.SimpleNamespace(rope_object=ro, gripper=types.SimpleNamespace(fem_sensor1=sens[0], fem_sensor2=sens[1]),
                               kn=ti.scalar(rp.kn), kd=ti.scalar(rp.kd), kt=ti.scalar(rp.kt),
                               friction_coeff=ti.scalar(rp.mu_t), norm_eps=1e-11,
-                              contact_idx=ti.Field((2, rp.n), (2,), np.int64),
-                              contact_flag=ti.Field((2, rp.n), (), np.int64))
+                              contact_idx=ti.Field((fr, rp.n), (2,), np.int64),
+                              contact_flag=ti.Field((fr, rp.n), (), np.int64))
     ti.methods(os.path.join(PKG, "tasks", "cable_straightening.py"), "Contact",
                ["update", "check_collision", "collision", "calculate_contact_force"], c)
-    c.update(0)
+    for f in range(n_sub):
+        c.update(f)
     return ro, sens, c
 
 
@@ -236,7 +241,7 @@ def main():
     out = {}
     for name, env in scenes().items():
         seed = {"corotated_cube": 5, "plastic_pads": 6, "rope_pads": 7, "multi_material_cube": 8,
-                "plastic_pads_chain": 9}[name]
+                "plastic_pads_chain": 9, "rope_pads_chain": 10}[name]
         st = seeded_state(env, seed=seed,
                           jitter=0.02 * (0.012 if name == "rope_pads" else env.dx))  # 2% of a hex edge
         rec = {"consts": np.array([DT, env.dx, env.volume, env.p_mass, env.eps, env.bound, *env.materials[0].mu_lam,
@@ -253,6 +258,19 @@ def main():
                     rec[f"s{s_}_{key}"] = val
             out.update({f"{name}/{k}": v for k, v in rec.items()})
             print(name + ":", f"{CHAIN} substeps")
+            continue
+        if name == "rope_pads_chain":  # control velocities ramp linearly: frame f = cv + f (cv1 - cv)
+            ro, sens, c = run_rope(env, st, n_sub=CHAIN)
+            rec.update(rpos=f32(st["rpos"][0]), rvel=f32(st["rvel"][0]), rtrav=f32(st["rtrav"][0]),
+                       rposN=ro.pos.a[CHAIN], rvelN=ro.vel.a[CHAIN], rtravN=ro.travel_info.a[CHAIN, :, 0])
+            for s_, so in enumerate(sens):
+                for key, val in (("pos", f32(st["pos"][s_])), ("vel", f32(st["vel"][s_])),
+                                 ("vpos", f32(st["vpos"][s_])), ("cv", f32(st["cv"][s_])), ("cv1", f32(st["cv1"][s_])),
+                                 ("B", so.B.a), ("posN", so.pos.a[CHAIN]), ("velN", so.vel.a[CHAIN]),
+                                 ("vposN", so.virtual_pos.a[CHAIN])):
+                    rec[f"s{s_}_{key}"] = val
+            out.update({f"{name}/{k}": v for k, v in rec.items()})
+            print(name + ":", f"{CHAIN} substeps, {int(ro.travel_info.a[CHAIN, :, 0].sum())} rope particles travelled")
             continue
         if name == "rope_pads":
             ro, sens, c = run_rope(env, st)

@@ -96,6 +96,27 @@ def test_oracle_substep_matches_reference_methods(golden, name):
     assert SS.rel_err(out["x"].mean(0), r["com1"]) < TOL
 
 
+def test_oracle_rope_chain_matches_reference_methods(golden):
+    """Five substeps of the cable task's Contact.update with ramping control velocities (frame f:
+    cv + f (cv1 - cv)), each oracle substep fed the previous one's output: rope and pads at the end."""
+    from tests.golden.make_substep import CHAIN
+    env = scenes()["rope_pads_chain"]
+    r = _case(golden, "rope_pads_chain")
+    st, cv, cv1 = _sensor_state(env, r)
+    st.update(x=np.zeros((0, 3)), v=np.zeros((0, 3)), C=np.zeros((0, 3, 3)), F=np.zeros((0, 3, 3)),
+              rpos=[r["rpos"].astype(np.float64)], rvel=[r["rvel"].astype(np.float64)],
+              rtrav=[r["rtrav"].astype(np.float64)])
+    o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
+    ramp = lambda f: [a + f * (b - a) for a, b in zip(cv, cv1)]  # noqa: E731
+    for f in range(CHAIN):
+        st, _ = o.substep(st, cv=ramp(f), cv1=ramp(f + 1))
+    assert np.array_equal(st["rtrav"][0], r["rtravN"]) and r["rtravN"].sum() > r["rtrav"].sum()
+    assert SS.rel_err(st["rpos"][0], r["rposN"]) < TOL and SS.rel_err(st["rvel"][0], r["rvelN"]) < TOL
+    for s in range(len(env.sensors)):
+        for a, b in (("posN", "pos"), ("velN", "vel"), ("vposN", "vpos")):
+            assert SS.rel_err(st[b][s], r[f"s{s}_{a}"]) < TOL, (s, a)
+
+
 @pytest.mark.parametrize("name", ["corotated_cube", "plastic_pads", "multi_material_cube"])
 def test_float32_oracle_is_within_the_one_substep_tolerance(golden, name):
     """In float32 (the CUDA path's arithmetic) the oracle's substep stays within 1e-5 relative of the
