@@ -9,9 +9,11 @@
 // (grasp_plastic.py) methods, read from the reference source, in float64 on a numpy stand-in for
 // the Taichi primitives, and tests/test_golden_substep.py finds this restatement within 2e-15 of
 // them (particles, grid, contact argmin, sensor forces and next frame; the rope and the gripper's
-// update2 through the cable task's Contact.update).  The adjoints (Taichi autodiff) are pinned by
-// analytic known-answer tests (tests/test_oracle_kat.py, test_oracle_rope.py) and by central
-// finite differences in double precision.
+// update2 through the cable task's Contact.update).  The adjoints (Taichi autodiff in the
+// reference) are checked against central differences of the reference's own substep
+// (tests/golden/make_gradient.py, tests/test_golden_gradient.py), against the reference's
+// hand-written SVD adjoint (tests/test_golden_svdgrad.py), by analytic known-answer tests and by
+// central differences of this restatement in double precision.
 //
 // Structure follows the reference kernel by kernel, on a dense per-frame grid in (i, j, k)
 // row-major order exactly like the Taichi fields, processing particles/nodes/tets in index
