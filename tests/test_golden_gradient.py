@@ -35,3 +35,22 @@ def test_oracle_adjoint_matches_reference_derivatives():
         if abs(pred - ref) > 1e-5 * abs(ref):
             bad.append((gr, pred, ref))
     assert not bad, bad
+
+
+def test_oracle_rope_adjoint_matches_reference_derivatives():
+    """The cable task's substep (PBD rope under a gripper pad, both frames' control velocities)."""
+    from tests.golden.make_gradient import ROPE_GROUPS, rope_base, rope_directions
+    fd = np.load(GOLDEN)["fd_rope"]
+    env, st, W = rope_base()
+    z3, z33 = np.zeros((0, 3)), np.zeros((0, 3, 3))
+    s = {"x": z3, "v": z3, "C": z33, "F": z33, **{k: st[k] for k in ("pos", "vel", "vpos", "rpos", "rvel", "rtrav")}}
+    adj1 = {"x": z3, "v": z3, "C": z33, "F": z33, **W}
+    adj = O.Oracle(env, DT, np.float64, grad_clip=0.0).substep_bwd(s, adj1, cv=st["cv"], cv1=st["cv1"])
+    ds = rope_directions(st, seed=400)
+    assert len(ds) == len(fd)
+    bad = []
+    for (gr, d), ref in zip(ds, fd):
+        pred = sum(float((a * b).sum()) for k in ROPE_GROUPS for a, b in zip(adj[k], d[k]))
+        if abs(pred - ref) > 1e-5 * abs(ref):
+            bad.append((gr, pred, ref))
+    assert not bad, bad
