@@ -40,17 +40,21 @@ class Config:
 
 
 def _press_env(n_grid=96, box_cells=20, pad=(20, 20, 5), pad_h=0.0125, seed=1, yield_stress=50.0, E=5e3, nu=0.3,
-               center=(0.5, 0.5)):
+               center=(0.5, 0.5), gap_cells=0.37):
     dx = 1.0 / n_grid
     cx, cz = center
     lo = np.array([cx * n_grid - box_cells / 2, 4.0, cz * n_grid - box_cells / 2]) * dx
     hi = lo + box_cells * dx
     x = S.box_particles(lo, hi, dx, 8, seed)
-    # pad density scaled so that node masses stay those of the 0.0125 m pad: the explicit penalty
-    # contact (stiffness 1e4 per node) needs k dt^2 / m well below 1 on the pad's vertices too
-    rho_pad = 1000.0 * (0.0125 / pad_h) ** 3
-    sp = S.hex_pad_sensor([cx, hi[1] + 0.37 * dx, cz], nx=pad[0], nz=pad[1], ny=pad[2], h=pad_h, E=1.5e5, nu=0.45,
-                          rho=rho_pad)
+    # pad density scaled as h^-2: a tet's stiffness grows as E h and a node's mass as rho h^3, so the
+    # pad keeps the stiffness-to-mass ratio, and with it the explicit stability margin at dt = 1e-4,
+    # of the 0.0125 m pad (the elastomer has no damping; with node masses held fixed instead, pads
+    # of 0.023 m hexes oscillate with growing amplitude and turn non-finite within 170 control
+    # steps).  Node masses then grow in proportion to h, and the penalty contact (stiffness 1e4 per
+    # node) keeps k dt^2 / m below 0.2 down to the smallest pads of the population (0.005 m)
+    rho_pad = 1000.0 * (0.0125 / pad_h) ** 2
+    sp = S.hex_pad_sensor([cx, hi[1] + gap_cells * dx, cz], nx=pad[0], nz=pad[1], ny=pad[2], h=pad_h, E=1.5e5,
+                          nu=0.45, rho=rho_pad)
     env = S.EnvSpec(x=x, materials=[S.Material(E, nu, yield_stress, S.MODEL_VON_MISES)],
                     n_grid=(n_grid, n_grid, n_grid), dx=dx, rho=1000.0, sensors=[sp],
                     kn=1e4, kd=100.0, kt=100.0, mu_t=0.5)
@@ -58,11 +62,13 @@ def _press_env(n_grid=96, box_cells=20, pad=(20, 20, 5), pad_h=0.0125, seed=1, y
 
 
 def press_actions(n_steps, n_sensors=1, seed=2, press=0.15, slide=0.1, noise=0.01):
-    """Press for the first 60% of the steps, then slide along +x; N(0, noise) on all 6 DoF."""
+    """Press for the first 60% of the steps, then slide along +x; N(0, noise) on all 6 DoF.  Pose actions
+    act in the sensor's own frame (set_pose_control, fem_sensor.py:229-245), whose +y is the pad's
+    out-direction, towards the object: the press is +y.  ``press`` is a speed (m/s) or one per sensor."""
     rng = np.random.default_rng(seed)
     a = noise * rng.standard_normal((n_steps, n_sensors, 6))
     n_press = int(0.6 * n_steps)
-    a[:n_press, :, 1] -= press
+    a[:n_press, :, 1] += np.broadcast_to(np.asarray(press, np.float64), (n_sensors,))
     a[n_press:, :, 0] += slide
     return a
 
@@ -99,9 +105,18 @@ def elastic_cube(substeps=200, seed=0) -> Config:
 
 def batched_population(n_envs=64, substeps=20, n_steps=200, seed=6, lo=8_000, hi=128_000) -> Config:
     """Config 4: independent environments with particle counts log-uniform in [8k, 128k], grids
-    48^3..128^3 sized to the object, per-env materials, one config-2 pad each."""
+    48^3..128^3 sized to the object, per-env materials, one config-2 pad each.
+
+    Each pad starts 2.07 cells above its box, clear of the grid nodes the box occupies (a pad started
+    inside that band takes a penalty impulse on its first substep which, with no damping in the
+    elastomer, rings on for the whole rollout and drives pads of some environments to non-finite
+    values within 200 steps), and presses at a speed that takes it through the gap and 25% of the
+    box's height by the end of the press phase (the boxes, yield stress 20-100 Pa, also slump under
+    gravity)."""
     rng = np.random.default_rng(seed)
-    envs = []
+    envs, press = [], []
+    gap = 2.07
+    n_press = int(0.6 * n_steps)
     for e in range(n_envs):
         n_p = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
         cells = max(4, int(round((n_p / 8) ** (1 / 3))))
@@ -109,9 +124,10 @@ def batched_population(n_envs=64, substeps=20, n_steps=200, seed=6, lo=8_000, hi
         n_grid = int(np.clip(max(need, 4 * int(rng.uniform(48, 128) / 4)), 48, 128))
         Ev = float(np.exp(rng.uniform(np.log(2e3), np.log(2e4))))
         env, _ = _press_env(n_grid=n_grid, box_cells=cells, pad=(20, 20, 5), pad_h=cells / n_grid / 16,
-                            seed=seed * 1000 + e, E=Ev, yield_stress=float(rng.uniform(20, 100)))
+                            seed=seed * 1000 + e, E=Ev, yield_stress=float(rng.uniform(20, 100)), gap_cells=gap)
         envs.append(env)
-    acts = press_actions(n_steps, n_envs)
+        press.append((gap + 0.25 * cells) / n_grid / (max(n_press, 1) * 1e-4 * substeps))
+    acts = press_actions(n_steps, n_envs, press=np.array(press))
     terms = []
     for e, env in enumerate(envs):
         sp = env.sensors[0]
@@ -145,7 +161,7 @@ def grasp_sphere(n_steps=1000, substeps=25, seed=4, n_grid=128, n_core=20_000, n
     grip = 0.5 * (0.3 - 2 * R) + 0.1 * h  # pads start just inside the sphere's silhouette
     kin = GripperKinematics([0.0, 0.0, 0.0], [0.5, c[1] + 0.12, 0.5], grip, 1e-4, base_height=0.02, base_width=0.3,
                             finger_height=0.1)
-    pads = [S.finger_pad_sensor(f.numpy(), nx=pad[0], nz=pad[1], ny=pad[2], h=h, rho=1000.0 * (0.0125 / h) ** 3,
+    pads = [S.finger_pad_sensor(f.numpy(), nx=pad[0], nz=pad[1], ny=pad[2], h=h, rho=1000.0 * (0.0125 / h) ** 2,
                                 shift=(0.13 * dx, -0.21 * dx))
             for f in kin.finger_poses0()]
     env = S.EnvSpec(x=x, materials=mats, mat=core.astype(np.int32), n_grid=(n_grid,) * 3, dx=dx, rho=1000.0,
@@ -184,7 +200,7 @@ def rope_pads(n_envs=16, n_steps=500, substeps=20, seed=5, n_rope=2000, pad=(40,
                           kn=kn, kd=0.01 * kn * dt, kt=0.01 * kn, mu_t=0.5)
         h = min(1.2 * rope_len, 0.9) / pad[0]
         sp = S.hex_pad_sensor([0.5 + 0.13 * dx, top + 1.7 * rad, 0.5 - 0.21 * dx], nx=pad[0], nz=pad[1], ny=pad[2],
-                              h=h, rho=1000.0 * (0.0125 / h) ** 3)
+                              h=h, rho=1000.0 * (0.0125 / h) ** 2)
         envs.append(S.EnvSpec(x=x, materials=[S.Material(5e3, 0.3)], n_grid=(n_grid,) * 3, dx=dx, rho=1000.0,
                               sensors=[sp], ropes=[rope], kn=1e4, kd=100.0, kt=100.0, mu_t=0.5))
     return Config("rope_pads", envs, dt, substeps, n_steps, press_actions(n_steps, n_envs), ())

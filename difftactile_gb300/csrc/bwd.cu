@@ -143,22 +143,22 @@ __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile,
         dws[i][2] = bsdw(i, fx[2]);
       }
       // With v_o the grid velocity of node o:  Wb_o = v_o . (vnb + g2p_k C_bar (o - fx)) = v_o . u_o,
-      // u_o = u_0 + sum_c o_c k_c  (u_0 = vnb - g2p_k C_bar fx, k_c = g2p_k C_bar column c), and the
-      // weight-independent part of fx_bar, -g2p_k sum_o W_o C_bar^T v_o, is -g2p_k C_bar^T S0 with
-      // S0 = sum W_o v_o, applied after the loop
+      // u_o = u_1 + sum_c (o_c - 1) k_c  (u_1 = vnb + g2p_k C_bar (1 - fx), the middle node's;
+      // k_c = g2p_k C_bar column c), and the weight-independent part of fx_bar,
+      // -g2p_k sum_o W_o C_bar^T v_o, is -g2p_k C_bar^T S0 with S0 = sum W_o v_o, applied after the loop
       const float gk = E.g2p_k;
       const v3 k0 = gk * mcol(Cb, 0), k1 = gk * mcol(Cb, 1), k2 = gk * mcol(Cb, 2);
-      const v3 u0 = vnb - ((fx[0] * k0 + fx[1] * k1) + fx[2] * k2);
+      const v3 u1 = vnb + mvec(Cb, v3{(1.f - fx[0]) * gk, (1.f - fx[1]) * gk, (1.f - fx[2]) * gk});
       v3 S0 = v3{0.f, 0.f, 0.f};
-      v3 ui = u0;  // u_o built up along the loops: + k0 per step of oi, + k1 of oj, + k2 of ok
 #pragma unroll
-      for (int oi = 0; oi < 3; ++oi, ui = ui + k0) {
-        v3 uij = ui;
+      for (int oi = 0; oi < 3; ++oi) {
+        const v3 ui = oi == 0 ? u1 - k0 : (oi == 1 ? u1 : u1 + k0);  // offsets about the middle node
 #pragma unroll
-        for (int oj = 0; oj < 3; ++oj, uij = uij + k1) {
-          v3 u = uij;
+        for (int oj = 0; oj < 3; ++oj) {
+          const v3 uij = oj == 0 ? ui - k1 : (oj == 1 ? ui : ui + k1);
 #pragma unroll
-          for (int ok_ = 0; ok_ < 3; ++ok_, u = u + k2) {
+          for (int ok_ = 0; ok_ < 3; ++ok_) {
+            const v3 u = ok_ == 0 ? uij - k2 : (ok_ == 1 ? uij : uij + k2);
             const v3 gv = f4to3(__ldg(vout + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok_)));
             const float W = (wx[oi] * wy[oj]) * wz[ok_];
             const float Wb = dot(gv, u);
@@ -178,7 +178,7 @@ __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile,
       c0 = k0;
       c1 = k1;
       c2 = k2;
-      q = u0;
+      q = u1;
     }
   }
   StencilRec rec;
@@ -408,8 +408,9 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
 #pragma unroll
     for (int j = 0; j < 3; ++j) A.a[i][j] = E.stress_k * s.cauchy.a[i][j] + pm * r.C.a[i][j];
   // gather the grid adjoint.  With m_o the momentum adjoint of node o, W_o its weight and
-  // dp_o = (o - fx) dx:  v_bar = p_mass S0,  A_bar = dx (S1 - S0 fx^T)  with  S0 = sum W_o m_o and
-  // S1 = sum W_o m_o o^T,  and  fx_bar_d = sum dW_o/dfx_d Wb_o - dx (A^T S0)_d  with
+  // dp_o = (o - fx) dx:  v_bar = p_mass S0,  A_bar = dx (S1 - S0 (fx - 1)^T)  with  S0 = sum W_o m_o and
+  // S1 = sum W_o m_o (o - 1)^T (the moment about the stencil's middle node),  and
+  // fx_bar_d = sum dW_o/dfx_d Wb_o - dx (A^T S0)_d  with
   // Wb_o = m_o . (p_mass v + A dp_o) + p_mass mass_bar_o  — the per-node work is two moments and Wb_o
   const float4* aacc = reinterpret_cast<const float4*>(w.g_adj_acc);
   v3 S0 = v3{0.f, 0.f, 0.f};
@@ -435,7 +436,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
         const float W = (wts[oi][0] * wts[oj][1]) * wts[ok][2];
         const v3 Wm = W * mvb;
         S0 = S0 + Wm;
-        const float o[3] = {(float)oi, (float)oj, (float)ok};
+        const float o[3] = {(float)(oi - 1), (float)(oj - 1), (float)(ok - 1)};  // about the middle node
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           if (o[c] == 0.f) continue;  // resolved at compile time
@@ -443,7 +444,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
           S1.a[1][c] += o[c] * Wm.y;
           S1.a[2][c] += o[c] * Wm.z;
         }
-        const v3 dp = v3{(o[0] - fx[0]) * dx, (o[1] - fx[1]) * dx, (o[2] - fx[2]) * dx};
+        const v3 dp = v3{((float)oi - fx[0]) * dx, ((float)oj - fx[1]) * dx, ((float)ok - fx[2]) * dx};
         const float Wb = dot(mvb, pmv + mvec(A, dp)) + pm * gb.w;
         fxb[0] += Wb * (dws[oi][0] * wts[oj][1] * wts[ok][2]);
         fxb[1] += Wb * (wts[oi][0] * dws[oj][1] * wts[ok][2]);
@@ -455,7 +456,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   for (int rr = 0; rr < 3; ++rr) {
     const float s0 = rr == 0 ? S0.x : (rr == 1 ? S0.y : S0.z);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) Ab.a[rr][c] = dx * (S1.a[rr][c] - s0 * fx[c]);
+    for (int c = 0; c < 3; ++c) Ab.a[rr][c] = dx * (S1.a[rr][c] - s0 * (fx[c] - 1.f));
   }
   {
     const v3 AtS0 = mTvec(A, S0);

@@ -467,17 +467,18 @@ DT_DEV void von_mises(Stress& s, float mu, float ys) {
 }
 
 // the SVD of F_new as stored on the tape: 6 float4 planes per particle and frame,
-// (U00 U01 U02 U10) (U11 U12 U20 U21) (U22 V00 V01 V02) (V10 V11 V12 V20) (V21 V22 s0 s1) (s2 0 0 0)
+// (U00 U01 U02 U10) (U11 U12 U20 U21) (U22 V00 V01 V02) (V10 V11 V12 V20) (V21 V22 s0 s1) (s2 y 0 0)
+// with y = 1 where the von Mises return map yielded (the branch its adjoint differentiates), else 0
 DT_DEV float4* svd_plane(const dt_world& w, int f, int k) {
   return reinterpret_cast<float4*>(w.p_svd) + ((size_t)f * 6 + k) * w.n_particles;
 }
-DT_DEV void store_svd(const dt_world& w, int f, int p, const m3& U, v3 sg, const m3& V) {
+DT_DEV void store_svd(const dt_world& w, int f, int p, const m3& U, v3 sg, const m3& V, bool yield) {
   svd_plane(w, f, 0)[p] = make_float4(U.a[0][0], U.a[0][1], U.a[0][2], U.a[1][0]);
   svd_plane(w, f, 1)[p] = make_float4(U.a[1][1], U.a[1][2], U.a[2][0], U.a[2][1]);
   svd_plane(w, f, 2)[p] = make_float4(U.a[2][2], V.a[0][0], V.a[0][1], V.a[0][2]);
   svd_plane(w, f, 3)[p] = make_float4(V.a[1][0], V.a[1][1], V.a[1][2], V.a[2][0]);
   svd_plane(w, f, 4)[p] = make_float4(V.a[2][1], V.a[2][2], sg.x, sg.y);
-  svd_plane(w, f, 5)[p] = make_float4(sg.z, 0.f, 0.f, 0.f);
+  svd_plane(w, f, 5)[p] = make_float4(sg.z, yield ? 1.f : 0.f, 0.f, 0.f);
 }
 DT_DEV void load_svd(const dt_world& w, int f, int p, m3& U, v3& sg, m3& V) {
   const float4 a = svd_plane(w, f, 0)[p], b = svd_plane(w, f, 1)[p], c = svd_plane(w, f, 2)[p],
@@ -664,7 +665,10 @@ DT_DEV void tri_geom_bwd(v3 p1, v3 p2, v3 p3, v3 od, v3 p, v3 n, float sdfb, v3 
 // ------------------------------------------------------------------------------------------
 // Privatised 27-node scatter of one CTA's particles (P2G and the G2P adjoint), without atomics on
 // the chunk's own overlaps.  Both scatters have the form
-//     value(node base + o) = W_o (q + o_x c0 + o_y c1 + o_z c2),  W_o = wx[o_x] wy[o_y] wz[o_z].
+//     value(node base + o) = W_o (q + (o_x - 1) c0 + (o_y - 1) c1 + (o_z - 1) c2),  W_o = wx[o_x] wy[o_y] wz[o_z],
+// q the affine part at the middle node of the stencil (expanding about it keeps the offsets in
+// {-1, 0, 1} and the cancellation between q and the c terms small when the c terms dominate, as the
+// stress does for stiff materials).
 // The CTA's consecutive particles (spatially sorted) are reduced to the bounding box of their base
 // cells.  If the box holds at most TILE_MAX nodes and one environment, every particle writes its
 // stencil record (base, 9 weights, q, c0, c1, c2) to shared memory and each thread owns nodes of
@@ -759,7 +763,7 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
         const int ok_ = nc - __float_as_int(rec[2 * NT + p]);
         if ((unsigned)oi <= 2u && (unsigned)oj <= 2u && (unsigned)ok_ <= 2u) {
           const float W = (rec[(3 + oi) * NT + p] * rec[(6 + oj) * NT + p]) * rec[(9 + ok_) * NT + p];
-          const float fi = (float)oi, fj = (float)oj, fk = (float)ok_;
+          const float fi = (float)(oi - 1), fj = (float)(oj - 1), fk = (float)(ok_ - 1);
           ax += W * (((rec[12 * NT + p] + fi * rec[16 * NT + p]) + fj * rec[19 * NT + p]) + fk * rec[22 * NT + p]);
           ay += W * (((rec[13 * NT + p] + fi * rec[17 * NT + p]) + fj * rec[20 * NT + p]) + fk * rec[23 * NT + p]);
           az += W * (((rec[14 * NT + p] + fi * rec[18 * NT + p]) + fj * rec[21 * NT + p]) + fk * rec[24 * NT + p]);
@@ -807,7 +811,7 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
 #pragma unroll
         for (int ok_ = 0; ok_ < 3; ++ok_) {
           const float W = ok ? (r.wx[oi] * r.wy[oj]) * r.wz[ok_] : 0.f;
-          const float fi = (float)oi, fj = (float)oj, fk = (float)ok_;
+          const float fi = (float)(oi - 1), fj = (float)(oj - 1), fk = (float)(ok_ - 1);
           const v3 t = ((v3{r.q.x, r.q.y, r.q.z} + fi * r.c0) + fj * r.c1) + fk * r.c2;
           float4 a = make_float4(W * t.x, W * t.y, W * t.z, W * r.q.w);
           for (int s = 0; s < steps; ++s) {
@@ -844,7 +848,7 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
           const int n = node_off + ((((i >> 2) * nb1 + (j >> 2)) * nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
                         ((j & 3) << 2) + (k & 3);
           const float W = (r.wx[oi] * r.wy[oj]) * r.wz[ok_];
-          const float fi = (float)oi, fj = (float)oj, fk = (float)ok_;
+          const float fi = (float)(oi - 1), fj = (float)(oj - 1), fk = (float)(ok_ - 1);
           const v3 t = ((v3{r.q.x, r.q.y, r.q.z} + fi * r.c0) + fj * r.c1) + fk * r.c2;
           red_add_v4(dst + n, make_float4(W * t.x, W * t.y, W * t.z, W * r.q.w));
         }

@@ -38,8 +38,8 @@ __device__ void mark_block(const dt_world& w, int f, int b) {
 }
 
 // P2G of one CTA's particles (mpm_elastic.py:176-208 / mpm_plastic.py:222-256 / multi_obj.py:228-252):
-// contribution at node base + o is W_o (p_mass v + A (o - fx) dx) = W_o (b + o . (dx A)), with
-// A = stress + p_mass C and b = p_mass v - dx A fx precomputed once per particle.
+// contribution at node base + o is W_o (p_mass v + A (o - fx) dx) = W_o (b + (o - 1) . (dx A)), with
+// A = stress + p_mass C and b = p_mass v + A (1 - fx) dx (the middle node's) precomputed once per particle.
 template <int MODE, int NT>
 __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int* sh) {
   const int p = chunk * NT + threadIdx.x;
@@ -65,7 +65,7 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
     if (ok) {
       const dt_material M = w.materials[__ldg(w.p_mat + p)];
       constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s);
-      if (w.p_svd && M.model != DT_MODEL_NEOHOOKEAN) store_svd(w, f, p, s.U, s.sig, s.V);  // for the adjoint
+      if (w.p_svd && M.model != DT_MODEL_NEOHOOKEAN) store_svd(w, f, p, s.U, s.sig, s.V, s.yield);  // for the adjoint
       pm = E.p_mass;
       const float dx = E.dx, sk = E.stress_k;
       m3 A;
@@ -76,7 +76,8 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
       c0 = dx * mcol(A, 0);
       c1 = dx * mcol(A, 1);
       c2 = dx * mcol(A, 2);
-      b = pm * r.v - ((fx[0] * c0 + fx[1] * c1) + fx[2] * c2);
+      // the affine momentum at the middle node of the stencil, (1 - fx) dx from the particle
+      b = pm * r.v + mvec(A, v3{(1.f - fx[0]) * dx, (1.f - fx[1]) * dx, (1.f - fx[2]) * dx});
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         wx[i] = bsw(i, fx[0]);
@@ -367,8 +368,10 @@ __device__ void g2p_particle(const dt_world& w, int f, int p) {
     q3n[2] = q3.z;
     return;
   }
-  // new v = sum W_o v_o; new C = g2p_k sum W_o v_o (o - fx)^T = g2p_k (S1 - v fx^T) with
-  // S1 = sum W_o v_o o^T: per node one product W v_o and the moment's nonzero columns
+  // new v = sum W_o v_o; new C = g2p_k sum W_o v_o (o - fx)^T = g2p_k (S1 - v (fx - 1)^T) with
+  // S1 = sum W_o v_o (o - 1)^T, the moment about the stencil's middle node (offsets in {-1, 0, 1}: no
+  // cancellation of a large moment against v fx^T): per node one product W v_o and the moment's
+  // nonzero columns
   const float4* vout = reinterpret_cast<const float4*>(w.g_vout);
   v3 nv = v3{0.f, 0.f, 0.f};
   m3 S1 = mzero();
@@ -387,7 +390,7 @@ __device__ void g2p_particle(const dt_world& w, int f, int p) {
         const float W = (wts[oi][0] * wts[oj][1]) * wts[ok][2];
         const v3 Wg = W * gv;
         nv = nv + Wg;
-        const float o[3] = {(float)oi, (float)oj, (float)ok};
+        const float o[3] = {(float)(oi - 1), (float)(oj - 1), (float)(ok - 1)};  // about the middle node
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           if (o[c] == 0.f) continue;  // resolved at compile time
@@ -399,9 +402,10 @@ __device__ void g2p_particle(const dt_world& w, int f, int p) {
   m3 nC;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    nC.a[0][c] = E.g2p_k * (S1.a[0][c] - nv.x * fx[c]);
-    nC.a[1][c] = E.g2p_k * (S1.a[1][c] - nv.y * fx[c]);
-    nC.a[2][c] = E.g2p_k * (S1.a[2][c] - nv.z * fx[c]);
+    const float d = fx[c] - 1.f;
+    nC.a[0][c] = E.g2p_k * (S1.a[0][c] - nv.x * d);
+    nC.a[1][c] = E.g2p_k * (S1.a[1][c] - nv.y * d);
+    nC.a[2][c] = E.g2p_k * (S1.a[2][c] - nv.z * d);
   }
   const v3 nx = x + w.dt * nv;
   if (!finite3(nx)) set_err(w, DT_DEVERR_NONFINITE);
@@ -423,6 +427,7 @@ __device__ void fem_integrate(const dt_world& w, int f, int i) {
   const v3 vel1 = S.carry ? vo + (cvn - cvf) : vo;
   const v3 pos1 = f4to3(vframe(w.v_pos, w, f)[i]) + w.dt * vo;
   const v3 vp1 = f4to3(vframe(w.v_vpos, w, f)[i]) + w.dt * cvf;
+  if (!finite3(vel1) || !finite3(pos1)) set_err(w, DT_DEVERR_NONFINITE);
   vframe(w.v_vel, w, f + 1)[i] = v3to4(vel1);
   vframe(w.v_pos, w, f + 1)[i] = v3to4(pos1);
   vframe(w.v_vpos, w, f + 1)[i] = v3to4(vp1);

@@ -9,6 +9,8 @@
 // dt_substep_fwd_noalloc keeps that scratch in one file-scope static device array of fixed size
 // (every GPU that loads the library holds it until the process exits) and otherwise runs exactly
 // dt_substep_fwd.
+#include <atomic>
+
 #include "common.cuh"
 
 namespace {
@@ -32,7 +34,12 @@ constexpr size_t NA_TOTAL = NA_OFF_CENT + NA_TRIS;                   // float4 u
 static __device__ __align__(256) float4 g_noalloc_scratch[NA_TOTAL];
 
 constexpr int NA_MAX_DEVICES = 64;
-float4* s_scratch[NA_MAX_DEVICES] = {nullptr};
+// The array's device address per device, looked up once (cudaGetSymbolAddress) by the first call on
+// that device.  Several host threads may race to fill an entry: each stores the same address, and
+// the atomic makes the store and the loads well-defined.  The address belongs to the device's
+// primary context; after cudaDeviceReset the cached address is stale, so a process that resets a
+// device must not call this entry point again (restart the process instead).
+std::atomic<float4*> s_scratch[NA_MAX_DEVICES];
 
 }  // namespace
 
@@ -44,13 +51,21 @@ int dt_substep_fwd_noalloc(const dt_world* w, int f, cudaStream_t stream) {
     return DT_ERR_CAPACITY;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return DT_ERR_LAUNCH;
-  if (!s_scratch[dev]) {
+  if (stream != nullptr) {
+    // the scratch address looked up below is the current device's: a stream of another device
+    // would run the kernels there against this device's address
+    int sdev = -1;
+    if (note_error(cudaStreamGetDevice(stream, &sdev)) != cudaSuccess) return DT_ERR_LAUNCH;
+    if (sdev != dev) return DT_ERR_ARG;
+  }
+  float4* S = s_scratch[dev].load(std::memory_order_acquire);
+  if (!S) {
     // the symbol is a host-side stand-in: its device address must be looked up per device
     void* p = nullptr;
     if (note_error(cudaGetSymbolAddress(&p, g_noalloc_scratch)) != cudaSuccess || !p) return DT_ERR_LAUNCH;
-    s_scratch[dev] = static_cast<float4*>(p);
+    S = static_cast<float4*>(p);
+    s_scratch[dev].store(S, std::memory_order_release);
   }
-  float4* S = s_scratch[dev];
   // frames f, f+1 of the caller become frames 0, 1 of a two-frame view; scratch comes from S
   dt_world v = *w;
   const size_t P = (size_t)6 * w->n_particles * 4, Vv = (size_t)w->n_verts * 4;

@@ -240,6 +240,54 @@ class Trajectory:
         (g,) = torch.autograd.grad(self.ctrl, self.actions, self.ctrl_bar.double())
         return g
 
+    def adjoint_at(self, t: int, f: int, loss_bar: float = 1.0) -> int:
+        """Run the backward sweep of the last forward from the loss down to frame ``f`` + 1 of step
+        ``t`` (host-launched, no graph) and stop there: the step's forward tape (frames of step t, its
+        grid tape) is valid and the adjoint of its frame f + 1 is in the world's adjoint buffers
+        ((f + 1) & 1).  Returns the world frame index of step t's frame f.  For inspecting gradients
+        mid-rollout (the adjoint of one substep from a real loss); a following backward() starts over."""
+        if not (0 <= t < self.T and 0 <= f < self.S):
+            raise ValueError(f"(t, f) = ({t}, {f}) outside [0, {self.T}) x [0, {self.S})")
+        w = self.w
+        w.adj_clear()
+        for s, layer, tg in self.loss_terms:
+            N.check(w.lib.dt_marker_loss_bwd(w.wp, s, self.f_end, layer, tg.data_ptr(), float(loss_bar), w.stream),
+                    "loss bwd")
+        if self.ctrl_bar is None or self.ctrl_bar.shape != self.ctrl32.shape:
+            self.ctrl_bar = torch.zeros_like(self.ctrl32)
+        self.ctrl_bar.zero_()
+
+        def stop(tt):
+            f0 = self._f0(tt)
+            w.substeps_bwd(f0 + self.S, f0 + f + 1)
+            return f0 + f
+
+        if self.full:
+            for tt in reversed(range(t + 1, self.T)):
+                self._step_bwd(tt)
+            return stop(t)
+        for seg in reversed(range(self.n_ck)):
+            t0, t1 = seg * self.k, min((seg + 1) * self.k, self.T)
+            if t1 <= t:
+                break
+            self._load(self.ck_p, self.ck_v, self.ck_r, seg)
+            if self.k > 1:
+                for tt in range(t0, t1):
+                    self._save(self.seg_p, self.seg_v, self.seg_r, tt - t0)
+                    if tt + 1 < t1:
+                        self._step(tt)
+            for tt in reversed(range(max(t0, t), t1)):
+                if self.k > 1:
+                    self._load(self.seg_p, self.seg_v, self.seg_r, tt - t0)
+                self._step(tt, copy_end=False)
+                if tt == t:
+                    return stop(tt)
+                self._step_bwd(tt)
+                if self.S & 1:
+                    for name in ("p_adj", "v_adj_pos", "v_adj_vel", "v_adj_vpos", "r_adj"):
+                        w.t[name][1].copy_(w.t[name][0])
+        raise AssertionError("unreachable")
+
     def _backward_body(self, loss_bar):
         w = self.w
         st = w.stream

@@ -366,6 +366,14 @@ class World:
         return {"x": rec[:, 0:3], "v": rec[:, 3:6], "C": rec[:, 6:15].reshape(-1, 3, 3),
                 "F": rec[:, 15:24].reshape(-1, 3, 3)}
 
+    def yield_flags(self, frame):
+        """Per particle (user order) whether the von Mises return map yielded in the forward substep
+        ``frame`` -> ``frame`` + 1, as recorded on the SVD tape (the branch the adjoint differentiates);
+        needs the SVD tape."""
+        if self.t["p_svd"] is None:
+            raise RuntimeError("the yield flags are recorded on the SVD tape (World(svd_tape=True))")
+        return self.t["p_svd"][frame, 5, :, 1][self._inv_perm_t] > 0.5
+
     def particle_adjoint(self, frame):
         rec = self.t["p_adj"][frame & 1].permute(1, 0, 2).reshape(self.n_particles, 24)[self._inv_perm_t]
         return {"x": rec[:, 0:3], "v": rec[:, 3:6], "C": rec[:, 6:15].reshape(-1, 3, 3),
@@ -504,6 +512,30 @@ class World:
         torch.cuda.synchronize()
         ts = [a.elapsed_time(b) for a, b in self.probe_events + self.probe_graph_events]
         return (sum(ts) / len(ts)) if ts else float("nan"), len(ts)
+
+    def stage_breakdown(self, frame: int, reps: int = 10, warmup: int = 2) -> dict:
+        """Median CUDA-event time (ms) of each launch of one forward + backward substep, replayed on
+        the state of ``frame`` (which must be valid): {("fwd", 0..2) | ("bwd", 0..3): ms}.  Frame + 1,
+        the tape counters and the grid tape of ``frame`` and the adjoint buffers are overwritten."""
+        if not 0 <= frame < self.n_frames - 1:
+            raise ValueError(f"frame {frame} outside [0, {self.n_frames - 1})")
+        keys = [("fwd", s) for s in range(3)] + [("bwd", s) for s in range(4)]
+        times = {k: [] for k in keys}
+        self.adj_clear()
+        for it in range(warmup + reps):
+            self.step_begin()
+            ev = []
+            for kind, s in keys:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                self.call("dt_substep_fwd_stage" if kind == "fwd" else "dt_substep_bwd_stage", int(frame), s)
+                e1.record()
+                ev.append((e0, e1))
+            torch.cuda.synchronize()
+            if it >= warmup:
+                for k, (e0, e1) in zip(keys, ev):
+                    times[k].append(e0.elapsed_time(e1))
+        return {k: float(np.median(v)) for k, v in times.items()}
 
     def copy_frame(self, src, dst):
         self.call("dt_copy_frame", int(src), int(dst))

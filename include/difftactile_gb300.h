@@ -60,7 +60,7 @@ extern "C" {
 /* device error bits, OR-ed into err[0] */
 #define DT_DEVERR_PARTICLE_OOB 1   /* a particle's B-spline stencil left the grid: it was skipped */
 #define DT_DEVERR_TAPE_FULL    2   /* more active grid blocks than tape_blocks in one frame */
-#define DT_DEVERR_NONFINITE    4   /* NaN/Inf met in a grid node or a particle */
+#define DT_DEVERR_NONFINITE    4   /* NaN/Inf met in a grid node, a particle or a sensor vertex */
 
 #define DT_MAX_SENSORS_PER_ENV 4
 #define DT_BLOCK_NODES 64
@@ -200,7 +200,9 @@ typedef struct dt_world {
   /* ---- optional SVD tape ---- */
   float* p_svd;                  /* [n_frames][6][n_particles][4]: U, V, sigma of F_new per frame, written
                                     by the forward, read by the adjoint instead of recomputing; NULL:
-                                    the adjoint recomputes the SVD */
+                                    the adjoint recomputes the SVD.  Planes (U00 U01 U02 U10)
+                                    (U11 U12 U20 U21) (U22 V00 V01 V02) (V10 V11 V12 V20) (V21 V22 s0 s1)
+                                    (s2 y 0 0), y = 1 where the von Mises return map yielded */
   /* ---- launch shape ---- */
   int p_block;                   /* threads per CTA of the particle / tet / vertex launches: 64, 128 or
                                     256 (any other value: 128; the TILE scatter always uses 128) */
@@ -273,6 +275,8 @@ int dt_substep_fwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
  * process exits); w's scratch pointers are ignored and may be NULL.  Limits: n_nodes <= 64^3,
  * n_blocks <= 4096, n_tris <= 8192, else DT_ERR_CAPACITY.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The stream must belong to the current device (else DT_ERR_ARG).  The looked-up address is kept
+ * for the life of the process: after cudaDeviceReset do not call this entry point again.
  * All calls share the array: calls that overlap on the GPU (other streams, other threads) race.
  * The grid tape written here is scratch, so dt_substep_bwd cannot follow this call; it allocates
  * nothing (no cudaMalloc, cudaFree or allocating library routine). */

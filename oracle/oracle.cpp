@@ -114,6 +114,10 @@ typedef struct orc_scene {
   int pad2_;
   const orc_rope* ropes;
   orc_rope_io* rope_io;  // [n_ropes]
+  // optional [n_particles] branch of the von Mises return map: -1 decided by the yield test, 0 elastic,
+  // 1 yielding (a comparison pins the branch another implementation took for particles on the yield
+  // surface, where the test's outcome depends on rounding); NULL: every particle decided by the test
+  const signed char* yield_branch;
 } orc_scene;
 
 }  // extern "C"
@@ -344,15 +348,16 @@ inline size_t gidx(const int* n, int i, int j, int k) { return (size_t(i) * n[1]
 // von Mises return mapping, mpm_plastic.py:151-166.  Returns F unchanged when not yielding.
 template <typename T>
 M3<T> von_mises(const M3<T>& F, const M3<T>& U, const T sig[3], const M3<T>& V, T mu, T yield_stress,
-                bool* yielded = nullptr) {
+                bool* yielded = nullptr, int branch = -1) {
   T eps[3];
   for (int d = 0; d < 3; ++d) eps[d] = std::log(std::max(sig[d], T(0.05)));
   T mean = ((eps[0] + eps[1]) + eps[2]) / T(3);
   T eh[3] = {eps[0] - mean, eps[1] - mean, eps[2] - mean};
   T nrm = std::sqrt(((eh[0] * eh[0] + eh[1] * eh[1]) + eh[2] * eh[2]) + T(1e-8));
   T dg = nrm - yield_stress / (T(2) * mu);
-  if (yielded) *yielded = dg > T(0);
-  if (dg > T(0)) {
+  const bool yield = branch < 0 ? dg > T(0) : branch == 1;
+  if (yielded) *yielded = yield;
+  if (yield) {
     T e[3];
     for (int d = 0; d < 3; ++d) e[d] = std::exp(eps[d] - (dg / nrm) * eh[d]);
     M3<T> r;
@@ -544,7 +549,7 @@ void p2g_particle(const orc_scene* sc, const Consts<T>& K, const Particle<T>& q,
   o.yield = false;
   o.R = mmul(o.U, mT(o.V));
   if (o.model == MODEL_VON_MISES) {
-    o.Fp = von_mises(o.Fn, o.U, o.sig, o.V, o.mu, o.ys, &o.yield);
+    o.Fp = von_mises(o.Fn, o.U, o.sig, o.V, o.mu, o.ys, &o.yield, sc->yield_branch ? int(sc->yield_branch[p]) : -1);
     o.J = mdet(o.Fp);
   } else if (o.model == MODEL_NEOHOOKEAN) {
     o.Fp = o.Fn;

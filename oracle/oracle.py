@@ -49,7 +49,7 @@ class OrcScene(C.Structure):
                 ("mat_mu", C.c_void_p), ("mat_lam", C.c_void_p), ("mat_yield", C.c_void_p), ("mat_model", C.c_void_p),
                 ("p_mat", C.c_void_p), ("sensors", C.c_void_p), ("svd_sweeps", C.c_int), ("n_threads", C.c_int),
                 ("grad_clip", C.c_double), ("n_ropes", C.c_int), ("pad2_", C.c_int), ("ropes", C.c_void_p),
-                ("rope_io", C.c_void_p)]
+                ("rope_io", C.c_void_p), ("yield_branch", C.c_void_p)]
 
 
 def lib():
@@ -89,7 +89,10 @@ def _ptr_array(arrs):
 class Oracle:
     """CPU restatement of one environment's substep (float32 or float64)."""
 
-    def __init__(self, env, dt, dtype=np.float32, svd_sweeps=None, n_threads=1, grad_clip=1000.0):
+    def __init__(self, env, dt, dtype=np.float32, svd_sweeps=None, n_threads=1, grad_clip=1000.0, yield_branch=None):
+        """``yield_branch``: optional [n_particles] branch of the von Mises return map per particle (-1
+        decided by the yield test, 0 elastic, 1 yielding), to evaluate the substep on the branch another
+        implementation took where the yield test's outcome depends on rounding."""
         self.env = env
         self.dtype = np.dtype(dtype)
         self.dt = float(dt)
@@ -153,6 +156,12 @@ class Oracle:
         sc.ropes = C.cast(rr, C.c_void_p)
         sc.rope_io = C.cast(self.rope_io, C.c_void_p)
         self.ropes = ropes
+        if yield_branch is not None:
+            yb = np.ascontiguousarray(yield_branch, np.int8)
+            if yb.shape != (env.n_particles,):
+                raise ValueError(f"yield_branch: {yb.shape}, expected ({env.n_particles},)")
+            self.keep.append(yb)
+            sc.yield_branch = _ptr(yb)
         self.sc = sc
         self.fn = lib().orc_substep_f32 if self.dtype == np.float32 else lib().orc_substep_f64
         self.fn.restype = C.c_int

@@ -1,7 +1,8 @@
-"""The benchmark's reference arm on the host (no GPU): `bench.py --impl reference` times the oracle on
-the host cores over bounded samples of the sensor-press scene and prints one JSON line with our arm's
-metric, unit and direction, the CPU-baseline description and an end-to-end entry without device
-copies; under torchrun only rank 0 prints."""
+"""The benchmark's reference arm on the host (no GPU): `bench.py --impl reference` rolls environment 0
+forward with the oracle, times bounded samples of whole substeps of the training iteration on the host
+cores (all threads per step, then one thread) and prints one JSON line with our arm's metric, unit and
+direction, the CPU-baseline description and an end-to-end entry without device copies; under torchrun
+only rank 0 prints."""
 import json
 import types
 
@@ -15,14 +16,14 @@ def _args(**kw):
 
 
 def _short(monkeypatch):
-    real = bench.cpu_baseline
+    real = bench.cpu_sample
     calls = []
 
-    def short(cfg, threads, target_s=15.0):
-        calls.append(target_s)
-        return real(cfg, min(threads, 4), target_s=0.05)
+    def short(env, dt, st, adj1, cv, cv1, threads, target_s, max_sub):
+        calls.append((threads, target_s))
+        return real(env, dt, st, adj1, cv, cv1, min(threads, 4), 0.01, 1)
 
-    monkeypatch.setattr(bench, "cpu_baseline", short)
+    monkeypatch.setattr(bench, "cpu_sample", short)
     return calls
 
 
@@ -39,11 +40,14 @@ def test_reference_arm_prints_one_line(monkeypatch, capsys):
     assert out["config"]["workload"] == "sensor_press" and out["config"]["particles"] == 64_000
     cb = out["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and "substeps" in cb["sample"] and cb["value"] == out["value"]
+    assert cb["value_1thread"] > 0
     assert out["e2e"] == {"value": out["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0,
                           "d2h_bytes_per_step": 0}
     # units of one bench step / the measured rate
     assert abs(out["ms_per_step"] - 64_000 * 1 * 20 / out["value"] * 1e3) <= 1e-6 * out["ms_per_step"]
-    assert calls == [2.0, 10.0, 10.0]  # one short warm-up sample, then one bounded sample per step
+    n = cb["cores"]
+    # one short warm-up sample, one bounded sample per step on all threads, then one on a single thread
+    assert calls == [(n, 1.0), (n, 10.0), (n, 10.0), (1, 5.0)]
 
 
 def test_reference_arm_is_silent_off_rank_0(monkeypatch, capsys):

@@ -64,7 +64,8 @@ def oracle_loss(env, st0, cv, W, n_sub, mu_lam=None):
 
 
 def gpu_grads(env, st0, cv, W, n_sub, **world_kw):
-    w = World([env], n_frames=n_sub + 1, dt=DT, grad_clip=0.0, **world_kw)
+    world_kw.setdefault("grad_clip", 0.0)
+    w = World([env], n_frames=n_sub + 1, dt=DT, **world_kw)
     w.set_particles(0, x=st0["x"], v=st0["v"], C=st0["C"], F=st0["F"])
     for s in range(len(env.sensors)):
         sl = w.vslice(s)
@@ -155,6 +156,29 @@ def test_adjoint_matches_oracle_adjoint(cuda_lib, model, ys):
     errs["mu"] = abs(g["mu"] - ref["mat"][0, 0]) / abs(ref["mat"][0, 0])
     errs["lam"] = abs(g["lam"] - ref["mat"][0, 1]) / abs(ref["mat"][0, 1])
     assert max(errs.values()) < 1e-3, errs
+
+
+def test_clamp_grid_fires_and_matches_oracle(cuda_lib):
+    """The grasp task's clamp_grid (grasp_plastic.py:192-202: grid_m.grad and the sensors' pos / vel
+    grads clipped to +-c in the backward pass) with a clip small enough to fire on most nodes and
+    vertices: the clipped CUDA adjoint of one substep against the oracle's float64 adjoint with the same
+    clip (norm-wise 1e-3), and far from the unclipped one (the clip changed the result)."""
+    env = SS.pad_over_box(n=40, box_cells=(10, 6, 10), pad=(10, 10, 3), model=S.MODEL_VON_MISES, yield_stress=2.0)
+    st0, cv = base_point(env, 7)
+    W = loss_weights(env, env.n_particles, 8)
+    clip = 0.05
+    g = gpu_grads(env, st0, cv, W, 1, grad_clip=clip)
+    g0 = gpu_grads(env, st0, cv, W, 1, grad_clip=0.0)
+    copy = lambda: {k: (v if not isinstance(v, list) else [a.copy() for a in v]) for k, v in st0.items()}  # noqa: E731
+    ref = O.Oracle(env, DT, np.float64, grad_clip=clip).substep_bwd(copy(), W, cv=cv, cv1=cv)
+    errs = {k: SS.rel_err(g[k], ref[k]) for k in ("x", "v", "C", "F")}
+    for k in ("pos", "vel", "vpos"):
+        errs[k] = SS.rel_err(g[k][0], ref[k][0])
+    changed = {"x": SS.rel_err(g["x"], g0["x"])}
+    changed["pos"] = SS.rel_err(g["pos"][0], g0["pos"][0])
+    print("clipped vs oracle", errs, "clipped vs unclipped", changed)
+    assert max(errs.values()) < 1e-3, errs
+    assert min(changed.values()) > 1e-2, changed
 
 
 def test_multi_substep_backward_equals_substep_sequence(cuda_lib):

@@ -1,8 +1,9 @@
 """Forward-substep parity of the CUDA path (through the C ABI) against the CPU oracle.
 
-Tolerances (fp32, norm-wise relative): state after one substep within 1e-5 (x, F, sensor pos)
-and 1e-4 for v, C (sums of 27 atomically accumulated contributions, order-dependent); the contact
-argmin is compared bit-exactly; drift after 100 substeps is bounded by 1e-3.
+Tolerances (fp32, norm-wise relative): state after one substep within 1e-5 (x, v, F, sensor pos)
+and 1e-4 for C and the sensor velocities (sums of 27 atomically accumulated, partly cancelling
+contributions whose order the atomics choose); the contact argmin is compared bit-exactly; drift
+after 100 substeps is bounded by 1e-3.  Each comparison prints its measured errors (pytest -s).
 """
 import numpy as np
 import pytest
@@ -43,7 +44,7 @@ def sensor_state(w, f, s):
     return {k: w.sensor_frame(n, f, s).cpu().numpy() for k, n in (("pos", "v_pos"), ("vel", "v_vel"), ("vpos", "v_vpos"))}
 
 
-def compare(w, f, st, env_idx=0, sensor_base=0, tol_x=1e-5, tol_v=1e-4):
+def compare(w, f, st, env_idx=0, sensor_base=0, tol_x=1e-5, tol_v=1e-5, tol_c=1e-4):
     got = {k: v.cpu().numpy() for k, v in w.particles(f).items()}
     row = w.env_rows[env_idx]
     sl = slice(row.p_begin, row.p_end)
@@ -52,7 +53,12 @@ def compare(w, f, st, env_idx=0, sensor_base=0, tol_x=1e-5, tol_v=1e-4):
         ss = sensor_state(w, f, sensor_base + s)
         errs[f"pos{s}"] = SS.rel_err(ss["pos"], st["pos"][s])
         errs[f"vel{s}"] = SS.rel_err(ss["vel"], st["vel"][s])
-    bad = {k: e for k, e in errs.items() if e > (tol_x if k in ("x", "F") or k.startswith("pos") else tol_v)}
+    def tol(k):
+        if k in ("x", "F") or k.startswith("pos"):
+            return tol_x
+        return tol_v if k == "v" else tol_c
+    print("parity", {k: f"{e:.2e}" for k, e in errs.items()})
+    bad = {k: e for k, e in errs.items() if e > tol(k)}
     assert not bad, f"parity errors {errs}"
     return errs
 
@@ -143,7 +149,7 @@ def test_drift_after_100_substeps(cuda_lib):
     w = run_gpu([env], n, cv)
     st, _ = run_oracle(env, n, cv)
     assert w.error_word() == 0
-    errs = compare(w, n, st, tol_x=1e-3, tol_v=1e-3)
+    errs = compare(w, n, st, tol_x=1e-3, tol_v=1e-3, tol_c=1e-3)
     print("drift after 100 substeps:", errs)
 
 
