@@ -63,8 +63,10 @@ def parse():
                     help="threads per CTA of the particle launches")
     ap.add_argument("--depth", type=int, default=None, choices=[0, 1, 2, 3, 4, 5],
                     help="shuffle steps of the warp scatter's segmented reduction (0: whole runs)")
+    ap.add_argument("--lanes", type=int, default=None, choices=[4, 8],
+                    help="lanes per active grid node in the contact search")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shape instead of "
-                    "the autotuner's choice (also implied by --scatter, --no-pdl, --p-block or --depth)")
+                    "the autotuner's choice (also implied by --scatter, --no-pdl, --p-block, --depth or --lanes)")
     ap.add_argument("--no-svd-tape", action="store_true", help="the adjoint recomputes the SVD instead of "
                     "reading the forward's from the tape")
     ap.add_argument("--no-graph", action="store_true", help="launch every substep from the host instead of "
@@ -168,11 +170,14 @@ def build(cfg, dev, args, **extra):
         kw["p_block"] = args.p_block
     if args.depth is not None:
         kw["scatter_depth"] = args.depth
+    if args.lanes is not None:
+        kw["contact_lanes"] = args.lanes
     return cfg.build(dev, **kw)
 
 
 def tune_launch(args):
-    return not (args.no_tune or args.scatter or args.no_pdl or args.p_block or args.depth is not None)
+    return not (args.no_tune or args.scatter or args.no_pdl or args.p_block or args.depth is not None
+                or args.lanes is not None)
 
 
 def mid_frame(traj):

@@ -73,7 +73,8 @@ class DtWorld(C.Structure):
                 + [("dt", C.c_float), ("grad_clip", C.c_float), ("svd_sweeps", C.c_int),
                    ("svd_grad_mode", C.c_int), ("max_sensor_tris", C.c_int), ("scatter_mode", C.c_int)]
                 + [(n, _P) for n in ROPE_PTR_FIELDS] + [(n, C.c_int) for n in ROPE_INT_FIELDS]
-                + [("p_svd", _P), ("p_block", C.c_int), ("scatter_depth", C.c_int), ("contact_lanes", C.c_int)])
+                + [("p_svd", _P), ("p_block", C.c_int), ("scatter_depth", C.c_int), ("contact_lanes", C.c_int),
+                   ("skip_tape", C.c_int)])
 
 
 # entry points: name -> (restype, argtypes)
@@ -159,7 +160,7 @@ def load(path: str | None = None):
         n = getattr(lib, f"dt_sizeof_{name}")()
         if n != C.sizeof(cls):
             raise ImportError(f"ABI mismatch: sizeof(dt_{name}) = {n} in the library, {C.sizeof(cls)} in ctypes")
-    if lib.dt_abi_version() != 2:
+    if lib.dt_abi_version() != 3:
         raise ImportError("ABI version mismatch")
     _lib = lib
     return lib

@@ -111,12 +111,13 @@ def batched_population(n_envs=64, substeps=20, n_steps=200, seed=6, lo=8_000, hi
     inside that band takes a penalty impulse on its first substep which, with no damping in the
     elastomer, rings on for the whole rollout and drives pads of some environments to non-finite
     values within 200 steps), and presses at a speed that takes it through the gap and 25% of the
-    box's height by the end of the press phase (the boxes, yield stress 20-100 Pa, also slump under
-    gravity)."""
+    box's height by the end of the press phase of the 200-step rollout (120 steps; the boxes, yield
+    stress 20-100 Pa, also slump under gravity).  Shorter rollouts keep these speeds, so their steps
+    are the first steps of the full one."""
     rng = np.random.default_rng(seed)
     envs, press = [], []
     gap = 2.07
-    n_press = int(0.6 * n_steps)
+    n_press = 120
     for e in range(n_envs):
         n_p = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
         cells = max(4, int(round((n_p / 8) ** (1 / 3))))
@@ -126,7 +127,7 @@ def batched_population(n_envs=64, substeps=20, n_steps=200, seed=6, lo=8_000, hi
         env, _ = _press_env(n_grid=n_grid, box_cells=cells, pad=(20, 20, 5), pad_h=cells / n_grid / 16,
                             seed=seed * 1000 + e, E=Ev, yield_stress=float(rng.uniform(20, 100)), gap_cells=gap)
         envs.append(env)
-        press.append((gap + 0.25 * cells) / n_grid / (max(n_press, 1) * 1e-4 * substeps))
+        press.append((gap + 0.25 * cells) / n_grid / (n_press * 1e-4 * substeps))
     acts = press_actions(n_steps, n_envs, press=np.array(press))
     terms = []
     for e, env in enumerate(envs):

@@ -150,13 +150,15 @@ DT_DEV v3 mTvec(const m3& m, v3 v) {
 // of 3x3 matrices with minimal branching and elementary floating point operations") with exact
 // rotation angles.
 // ------------------------------------------------------------------------------------------
+// Correctly rounded divisions and square roots in the rotations: with approximate reciprocals the
+// factors reconstruct F only to ~2e-7, which the corotated stress 2 mu (F - R) F^T of a stiff material
+// near F = I amplifies (E = 4e5, F - R ~ 0.05: 1e-5 relative in the grid momentum; 6e-6 with these)
 DT_DEV void jacobi_rot(float S[3][3], float V[3][3], int p, int q) {
   float apq = S[p][q];
   if (apq == 0.f) return;
-  // reciprocal-based: the rotation only has to be orthogonal to rounding, not correctly rounded
-  float tau = __fdividef(S[q][q] - S[p][p], 2.f * apq);
-  float t = __fdividef(tau >= 0.f ? 1.f : -1.f, fabsf(tau) + sqrtf(fmaf(tau, tau, 1.f)));
-  float c = rsqrtf(fmaf(t, t, 1.f));
+  float tau = (S[q][q] - S[p][p]) / (2.f * apq);
+  float t = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.f)));
+  float c = 1.f / sqrtf(fmaf(t, t, 1.f));
   float s = t * c;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -195,7 +197,7 @@ DT_DEV void qr_givens(float B[3][3], float U[3][3], int i, int j, int col) {
   float r2 = a * a + b * b;
   float c = 1.f, s = 0.f;
   if (r2 > 1e-30f) {
-    const float ir = rsqrtf(r2);
+    const float ir = 1.f / sqrtf(r2);
     c = a * ir;
     s = b * ir;
   }

@@ -65,7 +65,8 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
     if (ok) {
       const dt_material M = w.materials[__ldg(w.p_mat + p)];
       constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s);
-      if (w.p_svd && M.model != DT_MODEL_NEOHOOKEAN) store_svd(w, f, p, s.U, s.sig, s.V, s.yield);  // for the adjoint
+      if (w.p_svd && !w.skip_tape && M.model != DT_MODEL_NEOHOOKEAN)
+        store_svd(w, f, p, s.U, s.sig, s.V, s.yield);  // for the adjoint
       pm = E.p_mass;
       const float dx = E.dx, sk = E.stress_k;
       m3 A;
@@ -335,7 +336,9 @@ __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w
       vo = v3to4(u);
     }
     vout[g] = vo;
-    if (e < w.tape_blocks) {
+    if (w.skip_tape) {
+      // a forward whose tape no backward reads
+    } else if (e < w.tape_blocks) {
       const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + tid;
       reinterpret_cast<float4*>(w.tape_acc)[ti] = a;
       reinterpret_cast<float4*>(w.tape_vout)[ti] = vo;

@@ -143,15 +143,21 @@ class Trajectory:
     def _f0(self, t):
         return t * self.S if self.full else 0
 
-    def _step(self, t, copy_end=True):
+    def _step(self, t, copy_end=True, tape=True):
+        """Control step t.  ``tape`` = False: its substeps write no grid or SVD tape (a checkpointed
+        rollout's forward pass, whose backward sweep recomputes the step with its tape)."""
         w = self.w
         f0 = self._f0(t)
         self._apply(t, f0)
         if not self.full:
             w.step_begin()
             self.launches += 1
-        for f in range(f0, f0 + self.S):
-            w.substep(f)
+        w.set_tape(tape)
+        try:
+            for f in range(f0, f0 + self.S):
+                w.substep(f)
+        finally:
+            w.set_tape(True)
         self.launches += 3 * self.S
         if copy_end and not self.full:
             w.copy_frame(self.S, 0)
@@ -189,7 +195,7 @@ class Trajectory:
         for t in range(self.T):
             if not self.full and t % self.k == 0:
                 self._save(self.ck_p, self.ck_v, self.ck_r, t // self.k)
-            self._step(t)
+            self._step(t, tape=self.full)  # checkpointed: the backward sweep recomputes each step's tape
         self.readout()
 
     def forward(self, actions: torch.Tensor) -> torch.Tensor:
@@ -275,7 +281,7 @@ class Trajectory:
                 for tt in range(t0, t1):
                     self._save(self.seg_p, self.seg_v, self.seg_r, tt - t0)
                     if tt + 1 < t1:
-                        self._step(tt)
+                        self._step(tt, tape=False)
             for tt in reversed(range(max(t0, t), t1)):
                 if self.k > 1:
                     self._load(self.seg_p, self.seg_v, self.seg_r, tt - t0)
@@ -306,7 +312,7 @@ class Trajectory:
                 for t in range(t0, t1):
                     self._save(self.seg_p, self.seg_v, self.seg_r, t - t0)
                     if t + 1 < t1:
-                        self._step(t)
+                        self._step(t, tape=False)
             for t in reversed(range(t0, t1)):
                 if self.k > 1:
                     self._load(self.seg_p, self.seg_v, self.seg_r, t - t0)

@@ -470,6 +470,12 @@ class World:
                 e1.record()
                 (self.probe_graph_events if graph else self.probe_events).append((e0, e1))
 
+    def set_tape(self, on: bool):
+        """Whether the forward substeps write the grid and SVD tapes that a backward substep of the same
+        frame reads (dt_world.skip_tape); off for a forward pass whose frames are recomputed before any
+        backward reads them."""
+        self.w.skip_tape = 0 if on else 1
+
     def substep(self, f):
         if self._probed("fwd", f):
             self._staged("dt_substep_fwd_stage", f, 3, "fwd")

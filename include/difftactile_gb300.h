@@ -50,7 +50,7 @@
 extern "C" {
 #endif
 
-#define DT_ABI_VERSION 2
+#define DT_ABI_VERSION 3
 
 #define DT_OK 0
 #define DT_ERR_ARG (-1)        /* null pointer, bad size or frame index */
@@ -212,6 +212,11 @@ typedef struct dt_world {
                                     and node */
   int contact_lanes;             /* lanes per active grid node in the contact search: 4 or 8 (any other
                                     value: 8) */
+  int skip_tape;                 /* 1: the forward substeps write neither the grid tape (tape_acc,
+                                    tape_vout, tape_cidx) nor the SVD tape, for a forward whose tape no
+                                    backward reads (the first pass of a checkpointed rollout, whose
+                                    backward sweep recomputes each step); the active-block lists are
+                                    still kept.  0: both are written */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared

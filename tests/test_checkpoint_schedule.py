@@ -78,6 +78,7 @@ class FakeWorld:
         self.adj_cv = torch.zeros((n_frames, NC))
         self.lib = FakeLib(self)
         self.calls = []
+        self.taped = [False] * n_frames
 
     def z(self, f):
         return torch.cat([self.t[k][f].reshape(-1) for k in STATE])
@@ -99,17 +100,24 @@ class FakeWorld:
             self.t[k][b].copy_(a[o:o + n].reshape(self.t[k][b].shape))
             o += n
 
+    tape_on = True
+
     def step_begin(self):
         self.calls.append("begin")
 
+    def set_tape(self, on):
+        self.tape_on = bool(on)
+
     def substep(self, f):
         assert 0 <= f < self.n_frames - 1
+        self.taped[f] = self.tape_on  # whether the substep's tape (read by its adjoint) was written
         self.set_z(f + 1, self.sys.step(self.z(f).double(), self.cv[f].double()))
 
     def substeps_bwd(self, f_hi, f_lo):
         assert 0 <= f_lo < f_hi < self.n_frames
         W = self.sys.W
         for f in reversed(range(f_lo, f_hi)):
+            assert self.taped[f], f"adjoint of frame {f} whose forward substep wrote no tape"
             a = self.adj((f + 1) & 1).double()
             th = torch.tanh(W @ self.z(f).double())
             self.adj_cv[f] += (H * (self.sys.B.T @ a)).float()

@@ -72,11 +72,6 @@ ONE = {"x": 1e-5, "v": 1e-5, "F": 1e-5, "C": 1e-4, "pos": 1e-5, "vel": 1e-4, "vp
        "rpos": 1e-5, "rvel": 1e-4, "rext": 1e-4}
 
 
-# the three-material cube's stiffest layer (E = 4e5, F - R ~ 0.05) turns the rotation's float32 rounding into
-# the momentum's: the float32 oracle itself is 3.8e-6 from the fixture there, the CUDA path 1.1e-5
-STIFF = {"multi_material_cube": dict(ONE, v=2e-5)}
-
-
 @pytest.mark.parametrize("name", ["corotated_cube", "plastic_pads", "multi_material_cube"])
 def test_cuda_substep_matches_reference_fixture(cuda_lib, golden, name):
     env = scenes()[name]
@@ -114,7 +109,7 @@ def test_cuda_substep_matches_reference_fixture(cuda_lib, golden, name):
             cf.append(out[:3].double().cpu().numpy())
         errs["contact_force"] = SS.rel_err(np.stack(cf), r["contact_force"])
         errs["com"] = SS.rel_err(w.com(1)[0].double().cpu().numpy(), r["com1"])
-    _check(errs, STIFF.get(name, ONE))
+    _check(errs, ONE)
 
 
 def test_cuda_rope_substep_matches_reference_fixture(cuda_lib, golden):
