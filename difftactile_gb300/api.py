@@ -262,13 +262,26 @@ class SubstepSegment(torch.autograd.Function):
     """Substeps f0 .. f0 + n - 1 of a World as one differentiable torch op.
 
     Inputs: particle x, v, C, F (user order, [N,3] / [N,3,3]) and the sensors' pos, vel, vpos
-    ([V,3], all sensors flattened) of frame f0.  Outputs the same quantities at frame f0 + n.  The
-    world's control velocities and materials are constants here.  Backward seeds the world's adjoint
-    buffers of frame f0 + n with the output gradients and runs dt_substep_bwd down to f0."""
+    ([V,3], all sensors flattened) of frame f0, and optionally the materials' Lame parameters
+    ``lame`` [n_materials, 2] (mu, lambda; mpm_elastic.py:64-71, multi_obj.py:65-74), written into the
+    world's material table.  Outputs the same state quantities at frame f0 + n.  The world's control
+    velocities are constants here.  Backward seeds the world's adjoint buffers of frame f0 + n with the
+    output gradients, runs dt_substep_bwd down to f0 and returns the adjoints of frame f0 and, for
+    ``lame``, the material adjoint the substeps accumulated (dt_world.mat_adj).
+
+    The backward reads the frames and grid tape the forward left in the world.  If any of frames
+    f0 .. f0 + n was rewritten in between (another segment, a rollout, set_particles, a step_begin) or
+    the material table changed, the backward raises instead of returning another rollout's gradient."""
 
     @staticmethod
-    def forward(ctx, world: World, f0: int, n: int, x, v, C, F, pos, vel, vpos):
+    def forward(ctx, world: World, f0: int, n: int, x, v, C, F, pos, vel, vpos, lame=None):
         w = world
+        if lame is not None:
+            lt = lame.detach().double().cpu()
+            if lt.shape != (w.n_materials, 2):
+                raise ValueError(f"lame: {tuple(lt.shape)}, expected ({w.n_materials}, 2)")
+            for m in range(w.n_materials):
+                w.set_material(m, mu=float(lt[m, 0]), lam=float(lt[m, 1]))
         w.set_particles(f0, x=x.detach(), v=v.detach(), C=C.detach(), F=F.detach())
         for name, a in (("v_pos", pos), ("v_vel", vel), ("v_vpos", vpos)):
             w.t[name][f0, :, :3] = a.detach().to(torch.float32)
@@ -281,6 +294,9 @@ class SubstepSegment(torch.autograd.Function):
         for f in range(f0, f0 + n):
             w.substep(f)
         ctx.world, ctx.f0, ctx.n = w, f0, n
+        ctx.gen = w.frame_gen[f0:f0 + n + 1].copy()
+        ctx.mgen = w.material_gen
+        ctx.lame = None if lame is None else (lame.dtype, lame.device)
         out = w.particles(f0 + n)
         return (out["x"], out["v"], out["C"], out["F"], w.t["v_pos"][f0 + n, :, :3].clone(),
                 w.t["v_vel"][f0 + n, :, :3].clone(), w.t["v_vpos"][f0 + n, :, :3].clone())
@@ -289,6 +305,9 @@ class SubstepSegment(torch.autograd.Function):
     def backward(ctx, gx, gv, gC, gF, gpos, gvel, gvpos):
         w, f0, n = ctx.world, ctx.f0, ctx.n
         fe = f0 + n
+        if not np.array_equal(w.frame_gen[f0:fe + 1], ctx.gen) or w.material_gen != ctx.mgen:
+            raise RuntimeError(f"frames {f0}..{fe} of the world (or its material table) were rewritten after this "
+                               "segment's forward; its backward would differentiate another rollout")
         w.adj_clear()
         z = lambda g, shape: torch.zeros(shape, device=w.device) if g is None else g  # noqa: E731
         Np, V = w.n_particles, w.n_verts
@@ -300,10 +319,13 @@ class SubstepSegment(torch.autograd.Function):
             w.substep_bwd(f)
         a = w.particle_adjoint(f0)
         b0 = f0 & 1
+        glame = None
+        if ctx.lame is not None:
+            glame = w.material_adjoint().to(dtype=ctx.lame[0], device=ctx.lame[1])
         return (None, None, None, a["x"], a["v"], a["C"], a["F"], w.t["v_adj_pos"][b0, :, :3].clone(),
-                w.t["v_adj_vel"][b0, :, :3].clone(), w.t["v_adj_vpos"][b0, :, :3].clone())
+                w.t["v_adj_vel"][b0, :, :3].clone(), w.t["v_adj_vpos"][b0, :, :3].clone(), glame)
 
 
-def simulate(world: World, f0: int, n: int, x, v, C, F, pos, vel, vpos):
+def simulate(world: World, f0: int, n: int, x, v, C, F, pos, vel, vpos, lame=None):
     """Functional form of SubstepSegment (see there)."""
-    return SubstepSegment.apply(world, f0, n, x, v, C, F, pos, vel, vpos)
+    return SubstepSegment.apply(world, f0, n, x, v, C, F, pos, vel, vpos, lame)

@@ -24,6 +24,15 @@ def lame(E: float, nu: float) -> tuple[float, float]:
     return E / 2 / (1 + nu), E * nu / (1 + nu) / (1 - 2 * nu)
 
 
+def lame_grad_to_E_nu(E: float, nu: float, g_mu, g_lam):
+    """Chain rule of lame(): gradients with respect to (mu, lambda) -> gradients with respect to
+    (E, nu).  mu = E / (2 (1 + nu)), lambda = E nu / ((1 + nu)(1 - 2 nu)) (mpm_elastic.py:70-71)."""
+    a, b = 1.0 + nu, 1.0 - 2.0 * nu
+    dmu_dE, dmu_dnu = 1.0 / (2.0 * a), -E / (2.0 * a * a)
+    dlam_dE, dlam_dnu = nu / (a * b), E * (1.0 + 2.0 * nu * nu) / (a * b) ** 2
+    return g_mu * dmu_dE + g_lam * dlam_dE, g_mu * dmu_dnu + g_lam * dlam_dnu
+
+
 @dataclass
 class Material:
     E: float

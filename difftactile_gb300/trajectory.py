@@ -178,6 +178,7 @@ class Trajectory:
         self._graphs[key] = g
 
     def _replay(self, key):
+        self.w.touch()  # the replay rewrites the world's frames
         self._graphs[key].replay()
         self.launches += self._graph_launches[key]
 
@@ -245,6 +246,23 @@ class Trajectory:
                 self._capture(key, lambda: self._backward_body(loss_bar))
         (g,) = torch.autograd.grad(self.ctrl, self.actions, self.ctrl_bar.double())
         return g
+
+    def material_grad(self) -> torch.Tensor:
+        """d loss / d (mu, lambda) of every material of the world, [n_materials, 2] float64, from the
+        last backward (the adjoint substeps accumulate it over the whole rollout)."""
+        return self.w.material_adjoint()
+
+    def material_grad_E_nu(self) -> torch.Tensor:
+        """d loss / d (E, nu) of every material, [n_materials, 2] float64, by the chain rule of
+        mu(E, nu), lambda(E, nu) (mpm_elastic.py:70-71) applied to material_grad(); for materials
+        given by E and nu (not by explicit Lame parameters)."""
+        from .scene import lame_grad_to_E_nu
+        g = self.material_grad()
+        out = torch.zeros_like(g)
+        for m, mat in enumerate(self.w.materials):
+            gE, gnu = lame_grad_to_E_nu(float(mat.E), float(mat.nu), g[m, 0], g[m, 1])
+            out[m, 0], out[m, 1] = gE, gnu
+        return out
 
     def adjoint_at(self, t: int, f: int, loss_bar: float = 1.0) -> int:
         """Run the backward sweep of the last forward from the loss down to frame ``f`` + 1 of step

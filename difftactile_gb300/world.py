@@ -209,7 +209,8 @@ class World:
             mu, lam = m.mu_lam
             r.mu, r.lam, r.yield_stress, r.model = mu, lam, m.yield_stress, m.model
             mat_rows.append(r)
-        self.materials = mats
+        self.materials = list(mats)
+        self._mat_rows = mat_rows
         self.n_materials = len(mats)
         t["envs"] = struct_tensor(env_rows, N.DtEnv)
         t["sensors"] = struct_tensor(srows, N.DtSensor)
@@ -282,6 +283,13 @@ class World:
         self.w = w
         self.wp = C.pointer(w)
 
+        # write generations: every call that rewrites a frame's state or tape (or the material table)
+        # bumps its counter, so that a differentiable segment can check in its backward that the frames
+        # its forward left are still the ones it computed (writes through the tensors in ``t`` are not
+        # tracked)
+        self.frame_gen = np.zeros(self.n_frames, np.int64)
+        self.material_gen = 0
+
         # FEM rest state in frame 0
         if V:
             vp = torch.zeros((V, 4), dtype=F32, device=dev)
@@ -324,12 +332,55 @@ class World:
         st = self.t["r_state"][f]
         return {"pos": st[0, sl, :3], "vel": st[1, sl, :3], "trav": st[0, sl, 3]}
 
+    def touch(self, frames=None):
+        """Mark frames (default: all) as rewritten (see frame_gen)."""
+        if frames is None:
+            self.frame_gen += 1
+        else:
+            self.frame_gen[frames] += 1
+
+    def set_material(self, m, mu=None, lam=None, yield_stress=None, E=None, nu=None):
+        """Change material m's parameters in the device table (in place: recorded graphs see it).  Lame
+        parameters directly (``mu``, ``lam``) or from ``E``, ``nu`` (mpm_elastic.py:70-71)."""
+        from .scene import Material, lame
+        old = self.materials[m]
+        if E is not None or nu is not None:
+            E_ = old.E if E is None else float(E)
+            nu_ = old.nu if nu is None else float(nu)
+            new = Material(E_, nu_, old.yield_stress, old.model)
+            mu, lam = lame(E_, nu_)
+        else:
+            mu = old.mu_lam[0] if mu is None else float(mu)
+            lam = old.mu_lam[1] if lam is None else float(lam)
+            new = Material(old.E, old.nu, old.yield_stress, old.model, mu=mu, lam=lam)
+        if yield_stress is not None:
+            new.yield_stress = float(yield_stress)
+        row = self._mat_rows[m]
+        row.mu, row.lam, row.yield_stress = mu, lam, new.yield_stress
+        self.materials[m] = new
+        buf = bytearray(C.sizeof(N.DtMaterial) * len(self._mat_rows))
+        for i, r_ in enumerate(self._mat_rows):
+            C.memmove(C.addressof(C.c_char.from_buffer(buf, i * C.sizeof(N.DtMaterial))), C.addressof(r_),
+                      C.sizeof(N.DtMaterial))
+        self.t["materials"].copy_(torch.frombuffer(buf, dtype=torch.uint8))
+        self.material_gen += 1
+
+    def lame_table(self) -> torch.Tensor:
+        """[n_materials, 2] (mu, lambda) of the device table, float64 on the world's device."""
+        return torch.tensor([m.mu_lam for m in self.materials], dtype=torch.float64, device=self.device)
+
+    def material_adjoint(self) -> torch.Tensor:
+        """[n_materials, 2] (d/dmu, d/dlambda) accumulated by the backward substeps since the last
+        adj_clear, float64."""
+        return self.t["mat_adj"][: self.n_materials, :2].double().clone()
+
     def set_rope_state(self, f, r, pos=None, vel=None, trav=None):
         st = self.rope_state(f, r)
         for k, a in (("pos", pos), ("vel", vel), ("trav", trav)):
             if a is not None:
                 st[k].copy_(torch.as_tensor(np.asarray(a, np.float32) if not torch.is_tensor(a) else a,
                                             dtype=F32, device=self.device).reshape(st[k].shape))
+        self.touch(f)
 
     def rope_adjoint(self, f, r):
         """Adjoint of rope r's frame f, held in buffer f & 1 during a backward sweep."""
@@ -359,6 +410,7 @@ class World:
         if F is not None:
             rec[:, 15:24] = put(F).reshape(-1, 9)[self._perm_t]
         self.t["p_state"][frame].copy_(rec.reshape(self.n_particles, 6, 4).permute(1, 0, 2))
+        self.touch(frame)
 
     def particles(self, frame):
         """dict of torch tensors x [N,3], v [N,3], C [N,3,3], F [N,3,3] of ``frame`` in user order."""
@@ -443,6 +495,7 @@ class World:
 
     # ---- C-ABI wrappers ----
     def step_begin(self):
+        self.touch()  # clears every frame's tape counters
         self.call("dt_step_begin")
 
     # ``probe = ("fwd" | "bwd", stage)`` times that launch of every ``probe_every``-th substep with
@@ -481,6 +534,7 @@ class World:
             self._staged("dt_substep_fwd_stage", f, 3, "fwd")
         else:
             self.call("dt_substep_fwd", int(f))
+        self.touch([f, f + 1])  # frame f's grid tape, frame f + 1's state
 
     def substep_bwd(self, f):
         if self._probed("bwd", f):
@@ -545,6 +599,7 @@ class World:
 
     def copy_frame(self, src, dst):
         self.call("dt_copy_frame", int(src), int(dst))
+        self.touch(dst)
 
     def adj_clear(self):
         self.call("dt_adj_clear")
