@@ -45,6 +45,37 @@ class Simulation:
         self.sensors = [FEMDomeSensor(self, s) for s in range(self.world.n_sensors)]
         self.ropes = [PBDRope(self, r) for r in range(self.world.n_ropes)]
 
+    @classmethod
+    def from_objects(cls, mpm_object, sensors=(), ropes=(), *, kn=34.53, kd=269.44, kt=154.78, friction=53.85,
+                     device="cuda", **world_kw):
+        """The device world of objects made the reference's way (MPMObj(...).init(...),
+        FEMDomeSensor(...).init(...), PBDRope(...).init(...)), as a task's Contact holds them
+        (tasks/grasp_plastic.py:31-150): one environment, the object's 64^3 grid, the sensors in the given
+        order, the contact parameters of the grasp task (kn, kd, kt, friction coefficient; :61-64).  The
+        objects become views of the returned simulation, so their reference methods run on the device.
+        The world holds ``sub_steps`` frames, as the reference's fields do."""
+        from .scene import EnvSpec
+        mo = mpm_object
+        if mo.x_init is None:
+            raise RuntimeError("call mpm_object.init(position, orientation, velocity) first")
+        for sp in sensors:
+            if sp.spec is None:
+                raise RuntimeError("place every sensor first (init)")
+        env = EnvSpec(x=mo.x_init, v=mo.v_init, materials=[mo.material()], n_grid=(mo.n_grid,) * 3, dx=mo.dx_0,
+                      p_vol=mo.p_vol, rho=mo.rho, gravity=mo.gravity, bound=mo.bound, eps=mo.eps,
+                      sensors=[sp.spec for sp in sensors], ropes=[r.spec for r in ropes], kn=kn, kd=kd, kt=kt,
+                      mu_t=friction)
+        sim = cls([env], n_frames=mo.sub_steps, dt=mo.dt, device=device, **world_kw)
+        mo.sim = sim
+        sim.mpm_object = mo
+        for i, sp in enumerate(sensors):
+            sp.sim, sp.s = sim, i
+        for i, r in enumerate(ropes):
+            r.sim, r.r = sim, i
+        sim.sensors = list(sensors)
+        sim.ropes = list(ropes)
+        return sim
+
     # ---- fused launches, once per frame between resets ----
     def _once(self, key, f, name):
         if (key, f) in self._done:
@@ -114,11 +145,71 @@ class Simulation:
         self.world.adj_clear()
 
 
-class MPMObj:
-    """MPM object methods (object_model/mpm_elastic.py:117-344)."""
+def _rotvec_deg(r) -> np.ndarray:
+    """Rotation matrix of a rotation vector given in degrees (scipy's Rotation.from_rotvec of the
+    radians, as the reference's init methods: mpm_elastic.py:95-96, fem_sensor.py:113-114)."""
+    from scipy.spatial.transform import Rotation
+    return Rotation.from_rotvec(np.deg2rad(np.asarray(r, np.float64))).as_matrix()
 
-    def __init__(self, sim: Simulation):
-        self.sim = sim
+
+class MPMObj:
+    """MPM object (object_model/mpm_elastic.py, mpm_plastic.py).  Two ways to make one:
+
+    - as the reference does, ``MPMObj(dt, sub_steps, obj_name, space_scale, obj_scale, density, rho)``
+      (mpm_elastic.py:19): a 64^3 grid of spacing space_scale / 64, the object's particles sampled from
+      ``obj_name`` (a mesh file, see meshes.object_particles) at particle_density = 64 density
+      obj_scale / space_scale and scaled by obj_scale, p_vol = (dx obj_scale)^3, rho = rho obj_scale,
+      E = 4e3 space_scale, nu = 0.4, grid-mass epsilon 1e-5; ``plastic=True`` gives mpm_plastic.py's
+      von Mises object (yield stress 1000).  Then ``init(position, orientation, velocity)``, and
+      ``Simulation.from_objects`` builds the device world around it;
+    - as a view of a built ``Simulation`` (``MPMObj(sim)``).
+    Once bound to a simulation the reference's methods (p2g, grid_op, g2p, ...) run on the device."""
+
+    def __init__(self, dt=5e-5, sub_steps=80, obj_name=None, space_scale=1.0, obj_scale=1.0, density=2, rho=1, *,
+                 plastic=False, n_grid=64):
+        self.particles = None
+        if hasattr(dt, "world"):  # a view of a built simulation
+            self.sim = dt
+            return
+        from . import meshes
+        from .scene import MODEL_COROTATED, MODEL_VON_MISES
+        self.sim = None
+        self.dt, self.sub_steps = float(dt), int(sub_steps)
+        self.n_grid, self.bound, self.dim = int(n_grid), 3, 3
+        self.space_scale, self.obj_scale = float(space_scale), float(obj_scale)
+        self.rho = rho * self.obj_scale
+        self.particle_density = self.n_grid * density * self.obj_scale / self.space_scale
+        self.obj_name = obj_name
+        self.particles = meshes.object_particles(obj_name, int(self.particle_density)) * np.float32(self.obj_scale)
+        self.n_particles = len(self.particles)
+        self.dx_0 = float(self.space_scale / self.n_grid)
+        self.inv_dx_0 = 1.0 / self.dx_0
+        self.p_vol = (self.dx_0 * self.obj_scale) ** 3
+        self.p_mass = self.p_vol * self.rho
+        self.eps = 1e-5
+        self.gravity = (0.0, -9.8, 0.0)
+        self.E_0, self.nu_0 = 4e3 * self.space_scale, 0.4
+        self.yield_stress = 1000.0 if plastic else 0.0
+        self.model = MODEL_VON_MISES if plastic else MODEL_COROTATED
+        self.x_init = self.v_init = None
+
+    @property
+    def mu_0(self):
+        return self.E_0 / 2 / (1 + self.nu_0)
+
+    @property
+    def lambda_0(self):
+        return self.E_0 * self.nu_0 / (1 + self.nu_0) / (1 - 2 * self.nu_0)
+
+    def set_material_params(self, E, nu):
+        """Young's modulus and Poisson's ratio (mu_0, lambda_0 follow, mpm_elastic.py:64-71)."""
+        self.E_0, self.nu_0 = float(E), float(nu)
+        if self.sim is not None:
+            self.sim.world.set_material(0, E=self.E_0, nu=self.nu_0)
+
+    def material(self):
+        from .scene import Material
+        return Material(self.E_0, self.nu_0, self.yield_stress, self.model)
 
     def compute_new_F(self, f):
         """F_new = (I + dt C) F; fused into p2g."""
@@ -164,16 +255,89 @@ class MPMObj:
     def state(self, f):
         return self.sim.world.particles(int(f))
 
-    def init(self, x, v=None):
-        self.sim.world.set_particles(0, x=x, v=np.zeros_like(x) if v is None else v)
+    def init(self, *args):
+        """``init(position, orientation, velocity)`` (mpm_elastic.py:90-114): x = R(orientation) p +
+        position for the object's particles p, v = velocity, F = I, of frame 0.  A view of a simulation
+        built from environment specs (no particles of its own) takes ``init(x, v=None)`` with the
+        particles' positions instead."""
+        if self.particles is not None and len(args) == 3 and np.asarray(args[0]).shape == (3,):
+            position, orientation, velocity = args
+            R = _rotvec_deg(orientation)
+            self.x_init = (self.particles.astype(np.float64) @ R.T + np.asarray(position, np.float64)).astype(np.float32)
+            self.v_init = np.broadcast_to(np.asarray(velocity, np.float32), self.x_init.shape).copy()
+            x, v = self.x_init, self.v_init
+        else:
+            x = np.asarray(args[0], np.float32)
+            v = np.zeros_like(x) if len(args) < 2 or args[1] is None else np.asarray(args[1], np.float32)
+        if self.sim is not None:
+            n = len(x)
+            self.sim.world.set_particles(0, x=x, v=v, C=np.zeros((n, 3, 3), np.float32),
+                                         F=np.broadcast_to(np.eye(3, dtype=np.float32), (n, 3, 3)))
 
 
 class FEMDomeSensor:
-    """FEM sensor methods (sensor_model/fem_sensor.py:212-521, gripper_fem.py)."""
+    """FEM dome sensor (sensor_model/fem_sensor.py).  Two ways to make one:
 
-    def __init__(self, sim: Simulation, s: int):
-        self.sim, self.s = sim, s
+    - as the reference does, ``FEMDomeSensor(dt, sub_steps, init_img_path)`` (fem_sensor.py:20): the
+      dome elastomer (fibonacci hemisphere layers, Delaunay tets; N_node 200, N_t 4, t_res 0.25, inner
+      radius 0.75), node mass 2 pi r^2 / N_node t_res rho with rho 2000, E 0.8e4, nu 0.43; then
+      ``init(rot_x, rot_y, rot_z, t_dx, t_dy, t_dz)`` places it (fem_sensor.py:112-128) and
+      ``Simulation.from_objects`` builds the device world.  ``init_img_path`` (the camera image whose
+      marker blobs OpenCV detects) is not read: markers.MarkerModel holds a stored marker set;
+    - as a view of sensor ``s`` of a built ``Simulation`` (``FEMDomeSensor(sim, s)``)."""
+
+    carry = 0  # control-velocity carry of the gripper pads' update2 (gripper_fem.py:415)
+
+    def __init__(self, dt=5e-5, sub_steps=50, init_img_path=None):
         self.dtrans = None
+        self.spec = None
+        if hasattr(dt, "world"):  # a view of a built simulation
+            self.sim, self.s = dt, int(sub_steps)
+            return
+        from .scene import dome_mesh
+        self.sim, self.s = None, None
+        self.dt, self.sub_steps = float(dt), int(sub_steps)
+        self.N_node, self.N_t, self.t_res, self.inner_radius = 200, 4, 0.25, 0.75
+        self.all_nodes, self.all_f2v, self.surface_f2v, self.layer_idxs = dome_mesh(
+            self.N_node, self.N_t, self.t_res, self.inner_radius)
+        self.n_verts, self.n_cells, self.num_triangles = len(self.all_nodes), len(self.all_f2v), len(self.surface_f2v)
+        self.dx = 2 * np.pi * self.inner_radius ** 2 / self.N_node
+        self.vol = self.dx * self.t_res
+        self.rho = 2000.0
+        self.mass = self.vol * self.rho
+        self.E_init, self.nu_init = 0.8e4, 0.43
+        self.trans_world = None
+
+    @property
+    def mu(self):
+        return self.E_init / 2 / (1 + self.nu_init)
+
+    @property
+    def lam(self):
+        return self.E_init * self.nu_init / (1 + self.nu_init) / (1 - 2 * self.nu_init)
+
+    def set_material_params(self, E, nu):
+        """Young's modulus and Poisson's ratio of the elastomer (fem_sensor.py:190-193)."""
+        self.E_init, self.nu_init = float(E), float(nu)
+
+    def init(self, rot_x, rot_y, rot_z, t_dx, t_dy, t_dz):
+        """Place the sensor: trans_world = [R | t] with R the rotation vector (rot_x, rot_y, rot_z) in
+        degrees (fem_sensor.py:112-128); the rest positions are trans_world applied to the dome."""
+        M = np.eye(4)
+        M[:3, :3] = _rotvec_deg([rot_x, rot_y, rot_z])
+        M[:3, 3] = [t_dx, t_dy, t_dz]
+        self._place(M)
+
+    def _place(self, M):
+        from .scene import SensorSpec
+        if self.sim is not None:
+            raise RuntimeError("the sensor is already part of a simulation; place it before Simulation.from_objects")
+        self.trans_world = np.asarray(M, np.float64)
+        world = (self.trans_world[:3, :3] @ self.all_nodes.T).T + self.trans_world[:3, 3]
+        out_dir = self.trans_world[:3, :3] @ np.array([0.0, 1.0, 0.0])
+        self.spec = SensorSpec(verts=world.astype(np.float32), tets=self.all_f2v, tris=self.surface_f2v,
+                               layer=self.layer_idxs, mass=self.mass, E=self.E_init, nu=self.nu_init,
+                               out_dir=tuple(out_dir), carry=self.carry, trans_world=self.trans_world)
 
     def update(self, f):
         self.sim._once("fem", f, "dt_fem_update")
@@ -235,11 +399,45 @@ class FEMDomeSensor:
         self.sim.memory_from_cache(t)
 
 
-class PBDRope:
-    """PBD rope methods (object_model/PBD_rope.py:112-258)."""
+class GripperFEMSensor(FEMDomeSensor):
+    """A gripper finger's dome sensor (sensor_model/gripper_fem.py): the same elastomer, placed by
+    ``init(matrix)`` (gripper_fem.py:102-108, the finger's 4x4 pose) and integrated with the control
+    velocity carried over between frames (update2, gripper_fem.py:404-418)."""
 
-    def __init__(self, sim: Simulation, r: int):
-        self.sim, self.r = sim, r
+    carry = 1
+
+    def init(self, matrix):
+        self._place(np.asarray(matrix, np.float64))
+
+
+class PBDRope:
+    """PBD rope (object_model/PBD_rope.py).  Two ways to make one:
+
+    - as the reference does, ``PBDRope(dt, sub_steps, p_rad, p_rho, n_particles, table_height,
+      rest_length)`` (PBD_rope.py:16-60) then ``init(pos, ori)`` (:74-87), and
+      ``Simulation.from_objects``;
+    - as a view of rope ``r`` of a built ``Simulation`` (``PBDRope(sim, r)``)."""
+
+    def __init__(self, dt=5e-5, sub_steps=80, p_rad=0.05, p_rho=1.0, n_particles=10, table_height=0.0,
+                 rest_length=None):
+        if hasattr(dt, "world"):  # a view of a built simulation
+            self.sim, self.r = dt, int(sub_steps)
+            self.spec = None
+            return
+        from .scene import RopeSpec
+        self.sim, self.r = None, None
+        self.dt, self.sub_steps = float(dt), int(sub_steps)
+        self.spec = RopeSpec(n=int(n_particles), rad=float(p_rad), rho=float(p_rho), rest_length=rest_length,
+                             table_h=float(table_height))
+        self.n_particles = int(n_particles)
+
+    def init(self, pos, ori):
+        """Node 0 at ``pos`` (pinned), the others along ``ori`` at the rest length (PBD_rope.py:74-87)."""
+        self.spec = self.spec.replace(pos=tuple(float(c) for c in pos), ori=tuple(float(c) for c in ori))
+        if self.sim is not None:
+            self.sim.world.set_rope_state(0, self.r, pos=self.spec.init_positions(),
+                                          vel=np.zeros((self.spec.n, 3), np.float32),
+                                          trav=np.zeros(self.spec.n, np.float32))
 
     def update(self, f):
         self.sim._once("rope", f, "dt_rope_update")

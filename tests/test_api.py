@@ -83,3 +83,79 @@ def test_substep_segment_gradients_match_oracle_adjoint(cuda_lib):
     for k, g in zip(names, grads):
         r = ref[k][0] if isinstance(ref[k], list) else ref[k]
         assert SS.rel_err(g.cpu().numpy(), r) < 1e-3, k
+
+
+def _sphere_obj(path, n_lat=16, n_lon=32):
+    """A closed latitude-longitude sphere of radius 1 as an OBJ file."""
+    V = [[0.0, 1.0, 0.0]]
+    for i in range(1, n_lat):
+        th = np.pi * i / n_lat
+        for j in range(n_lon):
+            ph = 2 * np.pi * j / n_lon
+            V.append([np.sin(th) * np.cos(ph), np.cos(th), np.sin(th) * np.sin(ph)])
+    V.append([0.0, -1.0, 0.0])
+    F, last = [], len(V) - 1
+    for j in range(n_lon):
+        F.append([0, 1 + (j + 1) % n_lon, 1 + j])
+    for i in range(n_lat - 2):
+        for j in range(n_lon):
+            a, b = 1 + i * n_lon + j, 1 + i * n_lon + (j + 1) % n_lon
+            F += [[a, b, b + n_lon], [a, b + n_lon, a + n_lon]]
+    for j in range(n_lon):
+        F.append([last, 1 + (n_lat - 2) * n_lon + j, 1 + (n_lat - 2) * n_lon + (j + 1) % n_lon])
+    with open(path, "w") as fh:
+        fh.writelines(f"v {x} {y} {z}\n" for x, y, z in V)
+        fh.writelines(f"f {a + 1} {b + 1} {c + 1}\n" for a, b, c in F)
+
+
+def test_reference_shaped_construction_runs_the_task_loop(cuda_lib, tmp_path):
+    """Objects made as a reference task makes them (tasks/grasp_plastic.py:31-48, 118-136):
+    MPMObj(dt, sub_steps, obj_name, space_scale, obj_scale, density, rho).init(position, orientation,
+    velocity), FEMDomeSensor(dt, sub_steps).init(rot_x, rot_y, rot_z, t_dx, t_dy, t_dz), set_pose_control /
+    set_control_vel, then the reference's Contact.update call sequence for every substep and
+    Contact.update_grad back down: the same frames as a World of the equivalent scene stepped with the
+    fused substep, and finite adjoints."""
+    from difftactile_gb300.api import FEMDomeSensor, MPMObj
+    from difftactile_gb300.scene import EnvSpec
+    obj = str(tmp_path / "ball.obj")
+    _sphere_obj(obj)
+    dt, S = 5e-5, 5
+    mo = MPMObj(dt=dt, sub_steps=S, obj_name=obj, space_scale=10.0, obj_scale=4.0, density=1.5, rho=4.0, plastic=True)
+    assert mo.n_particles > 10_000 and abs(mo.dx_0 - 10.0 / 64) < 1e-12 and abs(mo.p_vol - (mo.dx_0 * 4.0) ** 3) < 1e-12
+    mo.init([5.5, 2.3, 5.8], [-90.0, 0.0, 0.0], [0.0, 0.0, 0.0])
+    top = float(mo.x_init[:, 1].max())
+    s = FEMDomeSensor(dt=dt, sub_steps=S)
+    s.init(180.0, 0.0, 0.0, 5.5, top + 1.5 + 0.05, 5.8)  # apex down, just above the ball
+    sim = Simulation.from_objects(mo, [s])
+    w = sim.world
+    assert w.n_particles == mo.n_particles and w.n_sensors == 1
+    assert np.allclose(mo.state(0)["x"].cpu().numpy(), mo.x_init)
+    s.set_pose_control([0.0, 8.0, 0.0], [0.0, 0.0, 0.0])  # +y: the dome's out-direction, into the ball
+    s.set_control_vel(0)
+    # the same scene as specs, stepped with the fused substep
+    env = EnvSpec(x=mo.x_init, v=mo.v_init, materials=[mo.material()], n_grid=(64,) * 3, dx=mo.dx_0, p_vol=mo.p_vol,
+                  rho=mo.rho, sensors=[s.spec], kn=34.53, kd=269.44, kt=154.78, mu_t=53.85)
+    ref = World([env], n_frames=S, dt=dt)
+    ref.t["v_cv"].copy_(w.t["v_cv"])
+    sim.reset()
+    ref.step_begin()
+    for f in range(S - 1):
+        grasp_sequence(sim, f)
+        ref.substep(f)
+    torch.cuda.synchronize()
+    assert w.error_word() == 0
+    assert float(w.t["v_ext"][: S - 1, :, :3].abs().sum()) > 0  # the dome touched the ball
+    a, b = w.particles(S - 1), ref.particles(S - 1)
+    for k in ("x", "v", "C", "F"):
+        assert SS.rel_err(a[k].cpu().numpy(), b[k].cpu().numpy()) < 1e-6, k
+    assert SS.rel_err(s.pos(S - 1).cpu().numpy(), ref.sensor_frame("v_pos", S - 1, 0).cpu().numpy()) < 1e-6
+    # Contact.update_grad down the frames from a centre-of-mass loss
+    sim.clear_all_grad()
+    gb = torch.zeros((1, 4), device=w.device)
+    gb[0, 1] = 1.0
+    assert w.lib.dt_com_bwd(w.wp, S - 1, gb.data_ptr(), w.stream) == 0
+    for f in reversed(range(S - 1)):
+        sim.update_grad(f)
+    torch.cuda.synchronize()
+    g = w.particle_adjoint(0)
+    assert all(torch.isfinite(g[k]).all() for k in g) and float(g["v"].abs().sum()) > 0
