@@ -3,7 +3,9 @@
 Physical parameters the configuration text leaves open are fixed here (and only here):
 object density 1000 kg/m^3 (so that the reference's absolute grid-mass epsilon of 1e-5 stays far
 below node masses and the penalty contact of stiffness 1e4 N/m per node stays explicit-stable at
-dt = 1e-4), contact damping 100, tangential stiffness 100, friction coefficient 0.5.
+dt = 1e-4), contact damping 100, friction coefficient 0.5, and the tangential stiffness kt of the
+friction (calculate_contact_force, grasp_plastic.py:205-216) per environment from the mass of a grid
+node of one cell, kt = 0.2 rho dx^3 / dt (``friction_stiffness``).
 """
 from __future__ import annotations
 
@@ -12,6 +14,16 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import scene as S
+
+
+def friction_stiffness(rho, dx, dt=1e-4, gain=0.2):
+    """Tangential stiffness of the contact friction for grid nodes of mass ~ rho dx^3.  While a contact
+    sticks (kt |v_t| below the Coulomb cap) the explicit friction removes kt dt / m of the relative
+    tangential velocity per substep; above 1 it overshoots.  The forward stays bounded by the cap, but
+    the adjoint runs through the sticking branch's Jacobian with gain |1 - kt dt / m| per substep: with
+    kt = 100 on nodes of ~1e-3 kg (gain ~ 9) the 25,000-substep adjoint of the grasp rollout overflows
+    float32.  ``gain`` = kt dt / m for a node of one cell's mass."""
+    return gain * rho * dx ** 3 / dt
 
 
 @dataclass
@@ -57,7 +69,7 @@ def _press_env(n_grid=96, box_cells=20, pad=(20, 20, 5), pad_h=0.0125, seed=1, y
                           nu=0.45, rho=rho_pad)
     env = S.EnvSpec(x=x, materials=[S.Material(E, nu, yield_stress, S.MODEL_VON_MISES)],
                     n_grid=(n_grid, n_grid, n_grid), dx=dx, rho=1000.0, sensors=[sp],
-                    kn=1e4, kd=100.0, kt=100.0, mu_t=0.5)
+                    kn=1e4, kd=100.0, kt=friction_stiffness(1000.0, dx), mu_t=0.5)
     return env, sp
 
 
@@ -166,7 +178,8 @@ def grasp_sphere(n_steps=1000, substeps=25, seed=4, n_grid=128, n_core=20_000, n
                                 shift=(0.13 * dx, -0.21 * dx))
             for f in kin.finger_poses0()]
     env = S.EnvSpec(x=x, materials=mats, mat=core.astype(np.int32), n_grid=(n_grid,) * 3, dx=dx, rho=1000.0,
-                    sensors=pads, kn=1e4, kd=100.0, kt=100.0, mu_t=0.5, bc=S.BC_STICKY_FLOOR)
+                    sensors=pads, kn=1e4, kd=100.0, kt=friction_stiffness(1000.0, dx), mu_t=0.5,
+                    bc=S.BC_STICKY_FLOOR)
     acts = np.zeros((n_steps, 7))
     acts[: n_steps // 2, 6] = 0.05
     acts[n_steps // 2:, 1] = 0.05
@@ -198,10 +211,11 @@ def rope_pads(n_envs=16, n_steps=500, substeps=20, seed=5, n_rope=2000, pad=(40,
         kn = 0.2 * mass / dt ** 2
         rope = S.RopeSpec(n=n_rope, rad=rad, rho=1000.0, rest_length=rest, pos=tuple(xs[0]), ori=(1.0, 0.0, 0.0),
                           table_h=top, x=xs.astype(np.float32), stretch_compliance=1e-6, bend_compliance=1e-6,
-                          kn=kn, kd=0.01 * kn * dt, kt=0.01 * kn, mu_t=0.5)
+                          kn=kn, kd=0.01 * kn * dt, kt=0.2 * mass / dt, mu_t=0.5)
         h = min(1.2 * rope_len, 0.9) / pad[0]
         sp = S.hex_pad_sensor([0.5 + 0.13 * dx, top + 1.7 * rad, 0.5 - 0.21 * dx], nx=pad[0], nz=pad[1], ny=pad[2],
                               h=h, rho=1000.0 * (0.0125 / h) ** 2)
         envs.append(S.EnvSpec(x=x, materials=[S.Material(5e3, 0.3)], n_grid=(n_grid,) * 3, dx=dx, rho=1000.0,
-                              sensors=[sp], ropes=[rope], kn=1e4, kd=100.0, kt=100.0, mu_t=0.5))
+                              sensors=[sp], ropes=[rope], kn=1e4, kd=100.0, kt=friction_stiffness(1000.0, dx),
+                              mu_t=0.5))
     return Config("rope_pads", envs, dt, substeps, n_steps, press_actions(n_steps, n_envs), ())

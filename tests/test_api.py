@@ -145,9 +145,17 @@ def test_reference_shaped_construction_runs_the_task_loop(cuda_lib, tmp_path):
     torch.cuda.synchronize()
     assert w.error_word() == 0
     assert float(w.t["v_ext"][: S - 1, :, :3].abs().sum()) > 0  # the dome touched the ball
-    a, b = w.particles(S - 1), ref.particles(S - 1)
+    # a second fused run gives the atomic-ordering spread (C of a ball nearly at rest is mostly that noise)
+    ref2 = World([env], n_frames=S, dt=dt)
+    ref2.t["v_cv"].copy_(w.t["v_cv"])
+    ref2.step_begin()
+    for f in range(S - 1):
+        ref2.substep(f)
+    torch.cuda.synchronize()
+    a, b, c = w.particles(S - 1), ref.particles(S - 1), ref2.particles(S - 1)
     for k in ("x", "v", "C", "F"):
-        assert SS.rel_err(a[k].cpu().numpy(), b[k].cpu().numpy()) < 1e-6, k
+        spread = SS.rel_err(c[k].cpu().numpy(), b[k].cpu().numpy())
+        assert SS.rel_err(a[k].cpu().numpy(), b[k].cpu().numpy()) <= max(10 * spread, 1e-6), (k, spread)
     assert SS.rel_err(s.pos(S - 1).cpu().numpy(), ref.sensor_frame("v_pos", S - 1, 0).cpu().numpy()) < 1e-6
     # Contact.update_grad down the frames from a centre-of-mass loss
     sim.clear_all_grad()
