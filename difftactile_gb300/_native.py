@@ -38,7 +38,8 @@ class DtRope(C.Structure):
                 ("mass", C.c_float), ("inv_m", C.c_float), ("rad", C.c_float), ("rest", C.c_float),
                 ("bend", C.c_float), ("alpha_s", C.c_float), ("alpha_b", C.c_float), ("relax_s", C.c_float),
                 ("relax_b", C.c_float), ("table_h", C.c_float), ("friction", C.c_float), ("dt_g", C.c_float * 3),
-                ("pin", C.c_float * 3), ("kn", C.c_float), ("kd", C.c_float), ("kt", C.c_float), ("mu_t", C.c_float)]
+                ("pin", C.c_float * 3), ("kn", C.c_float), ("kd", C.c_float), ("kt", C.c_float), ("mu_t", C.c_float),
+                ("iters", C.c_int)]
 
 
 class DtFisheye(C.Structure):
@@ -74,7 +75,7 @@ class DtWorld(C.Structure):
                    ("svd_grad_mode", C.c_int), ("max_sensor_tris", C.c_int), ("scatter_mode", C.c_int)]
                 + [(n, _P) for n in ROPE_PTR_FIELDS] + [(n, C.c_int) for n in ROPE_INT_FIELDS]
                 + [("p_svd", _P), ("p_block", C.c_int), ("scatter_depth", C.c_int), ("contact_lanes", C.c_int),
-                   ("skip_tape", C.c_int)])
+                   ("skip_tape", C.c_int), ("r_work", _P), ("max_rope_iters", C.c_int)])
 
 
 # entry points: name -> (restype, argtypes)
@@ -129,7 +130,8 @@ SIGNATURES = {
 }
 
 ERRORS = {0: "DT_OK", -1: "DT_ERR_ARG", -2: "DT_ERR_LAUNCH", -3: "DT_ERR_CAPACITY"}
-DEVERR = {1: "particle left the grid's safe band", 2: "grid tape capacity exceeded", 4: "non-finite value"}
+DEVERR = {1: "particle left the grid's safe band", 2: "grid tape capacity exceeded", 4: "non-finite value",
+          8: "rope iterations beyond the adjoint workspace"}
 
 
 class DtError(RuntimeError):
@@ -160,7 +162,7 @@ def load(path: str | None = None):
         n = getattr(lib, f"dt_sizeof_{name}")()
         if n != C.sizeof(cls):
             raise ImportError(f"ABI mismatch: sizeof(dt_{name}) = {n} in the library, {C.sizeof(cls)} in ctypes")
-    if lib.dt_abi_version() != 3:
+    if lib.dt_abi_version() != 4:
         raise ImportError("ABI version mismatch")
     _lib = lib
     return lib

@@ -37,6 +37,7 @@ class Config:
     loss_terms: tuple = ()
     ckpt_every: int = 1        # 0: full tape (every frame kept, no recompute)
     tape_blocks: int | None = None  # grid-tape capacity per frame (active 4^3-node blocks)
+    rope_terms: tuple = ()     # (rope, target [3]): squared distance of the rope's tip from the target
 
     @property
     def n_particles(self):
@@ -48,7 +49,7 @@ class Config:
         from .world import World
         nf = PoseTrajectory.frames_needed(self.n_steps, self.substeps, self.ckpt_every)
         w = World(self.envs, n_frames=nf, dt=self.dt, device=device, tape_blocks=self.tape_blocks, **world_kw)
-        return w, PoseTrajectory(w, self.n_steps, self.ckpt_every, self.loss_terms)
+        return w, PoseTrajectory(w, self.n_steps, self.ckpt_every, self.loss_terms, rope_terms=self.rope_terms)
 
 
 def _press_env(n_grid=96, box_cells=20, pad=(20, 20, 5), pad_h=0.0125, seed=1, yield_stress=50.0, E=5e3, nu=0.3,
@@ -187,21 +188,31 @@ def grasp_sphere(n_steps=1000, substeps=25, seed=4, n_grid=128, n_core=20_000, n
     return Config("grasp_sphere", [env], 1e-4, substeps, n_steps, acts, (), ckpt_every), kin
 
 
-def rope_pads(n_envs=16, n_steps=500, substeps=20, seed=5, n_rope=2000, pad=(40, 40, 5), n_particles=32_000,
-              n_grid=160, rope_len=0.6) -> Config:
+def rope_pads(n_envs=16, n_steps=500, substeps=20, seed=5, n_rope=2000, pad=(40, 40, 5), n_particles=512_000,
+              n_grid=160, rope_len=0.6, iters=50, ckpt_every=10, yield_stress=50.0) -> Config:
     """Config 5: ``n_envs`` environments, each a 40x40x5 hex pad (10,086 nodes, 48,000 tets) pressing a
-    PBD rope of ``n_rope`` particles (``rope_len`` long, compliance 1e-6) lying on an elastic slab of
-    ``n_particles`` MPM particles (4 cells thick) on an ``n_grid``^3 grid; ``n_steps`` x ``substeps``.
-    The rope-pad contact stiffness is scaled to the rope particles' mass (k dt^2 / m = 0.2) so that the
-    explicit penalty contact stays stable for thin ropes."""
+    PBD rope of ``n_rope`` particles (``rope_len`` long, compliance 1e-6, ``iters`` stretch + bending pass
+    pairs per substep) into an elastoplastic slab (von Mises, yield stress 50) of ``n_particles`` MPM
+    particles (4 cells thick) on an ``n_grid``^3 grid; ``n_steps`` x ``substeps``, a checkpoint every
+    ``ckpt_every`` steps (16 x 512k particles: 786 MB per frame).  The loss is the squared distance of
+    each rope's tip from a seeded target.
+
+    Each pad starts 2.07 cells above the slab, clear of the grid nodes it occupies (see
+    batched_population), and presses at a speed that takes its surface one cell below the slab's top
+    by the end of the press phase of the 500-step rollout (300 steps); shorter rollouts keep that
+    speed.  The rope-pad contact stiffness is scaled to the rope particles' mass (k dt^2 / m = 0.2) so
+    that the explicit penalty contact stays stable for thin ropes."""
     rng = np.random.default_rng(seed)
     envs = []
     dx = 1.0 / n_grid
     dt = 1e-4
+    gap = 2.07
+    press = (gap + 1.0) * dx / (300 * dt * substeps)
     for e in range(n_envs):
-        side = max(2, int(round(np.sqrt(n_particles / 8 / 4))))
-        lo = np.array([0.5 - side * dx / 2, 4 * dx, 0.5 - side * dx / 2])
-        x = S.box_particles(lo, lo + np.array([side, 4, side]) * dx, dx, 8, seed * 100 + e)
+        sx = max(2, int(round(np.sqrt(n_particles / 8 / 4))))   # cells of a 4-cell-thick slab, 8 per cell
+        sz = max(2, int(round(n_particles / 8 / 4 / sx)))
+        lo = np.array([0.5 - sx * dx / 2, 4 * dx, 0.5 - sz * dx / 2])
+        x = S.box_particles(lo, lo + np.array([sx, 4, sz]) * dx, dx, 8, seed * 100 + e)
         top = float(x[:, 1].max())
         rest = rope_len / max(n_rope - 1, 1)
         rad = rest / 1.6
@@ -211,11 +222,16 @@ def rope_pads(n_envs=16, n_steps=500, substeps=20, seed=5, n_rope=2000, pad=(40,
         kn = 0.2 * mass / dt ** 2
         rope = S.RopeSpec(n=n_rope, rad=rad, rho=1000.0, rest_length=rest, pos=tuple(xs[0]), ori=(1.0, 0.0, 0.0),
                           table_h=top, x=xs.astype(np.float32), stretch_compliance=1e-6, bend_compliance=1e-6,
-                          kn=kn, kd=0.01 * kn * dt, kt=0.2 * mass / dt, mu_t=0.5)
+                          kn=kn, kd=0.01 * kn * dt, kt=0.2 * mass / dt, mu_t=0.5, iters=iters)
         h = min(1.2 * rope_len, 0.9) / pad[0]
-        sp = S.hex_pad_sensor([0.5 + 0.13 * dx, top + 1.7 * rad, 0.5 - 0.21 * dx], nx=pad[0], nz=pad[1], ny=pad[2],
+        sp = S.hex_pad_sensor([0.5 + 0.13 * dx, top + gap * dx, 0.5 - 0.21 * dx], nx=pad[0], nz=pad[1], ny=pad[2],
                               h=h, rho=1000.0 * (0.0125 / h) ** 2)
-        envs.append(S.EnvSpec(x=x, materials=[S.Material(5e3, 0.3)], n_grid=(n_grid,) * 3, dx=dx, rho=1000.0,
-                              sensors=[sp], ropes=[rope], kn=1e4, kd=100.0, kt=friction_stiffness(1000.0, dx),
-                              mu_t=0.5))
-    return Config("rope_pads", envs, dt, substeps, n_steps, press_actions(n_steps, n_envs), ())
+        envs.append(S.EnvSpec(x=x, materials=[S.Material(5e3, 0.3, yield_stress, S.MODEL_VON_MISES)],
+                              n_grid=(n_grid,) * 3, dx=dx, rho=1000.0, sensors=[sp], ropes=[rope], kn=1e4, kd=100.0,
+                              kt=friction_stiffness(1000.0, dx), mu_t=0.5))
+    rope_terms = tuple((e, xs_tip) for e, xs_tip in enumerate(
+        [np.asarray(env.ropes[0].x[-1], np.float64) + np.array([0.0, 0.0, 0.05]) for env in envs]))
+    # grid tape: a 512k-particle slab touches ~3,000 of the 64,000 blocks of its 160^3 grid per frame
+    tape = 8192 * n_envs
+    return Config("rope_pads", envs, dt, substeps, n_steps, press_actions(n_steps, n_envs, press=press), (),
+                  ckpt_every=ckpt_every, tape_blocks=tape, rope_terms=rope_terms)

@@ -6,15 +6,17 @@
 //                  (cable_straightening.py:212-224); the rope gets ext * dt (PBD_rope.py:104-105), the
 //                  triangle's vertices -ext / 3 (fem_sensor.py:402-406); travel_info set on contact.
 //   rope solver    PBDRope.update, PBD_rope.py:112-180: external impulse and gravity, floor (normal
-//                  velocity removed, tangential scaled by the friction factor), one Jacobi stretch
-//                  pass and one Jacobi bending pass with compliance alpha = c / dt^2 and relaxation,
-//                  node 0 pinned, velocity from the position change.
+//                  velocity removed, tangential scaled by the friction factor), a Jacobi stretch
+//                  pass and a Jacobi bending pass with compliance alpha = c / dt^2 and relaxation
+//                  (dt_rope.iters pairs of them; the reference runs one), node 0 pinned, velocity
+//                  from the position change.
 //
 // One CTA per rope holds the rope in shared memory for the solver (a Jacobi pass is a gather of the
 // per-constraint corrections, no atomics); the contact search runs four lanes per particle over
-// CTAs of 64 particles.  The adjoint recomputes the solver's intermediate positions, runs the two
-// passes backwards, applies clamp_grid (cable_straightening.py:196-199) and then the contact adjoint
-// with the argmin held from the tape.
+// CTAs of 64 particles.  The adjoint recomputes the solver's intermediate positions (in shared memory
+// for one pass pair, in the dt_world.r_work workspace for more), runs the passes backwards, applies
+// clamp_grid (cable_straightening.py:196-199) and then the contact adjoint with the argmin held from
+// the tape.
 #include "contact.cuh"
 
 namespace {
@@ -182,8 +184,11 @@ __global__ void __launch_bounds__(RS_NT) k_rope_solve(dt_world w, int f) {
     tp[i] = rope_integrate(R, dt, rstate(w, f, 0)[p], rstate(w, f, 1)[p], rext(w, f)[p]);
   }
   __syncthreads();
-  rope_pass<RS_NT>(tp, cd, n, 1, R.rest, R.alpha_s, R.relax_s, R.inv_m);
-  rope_pass<RS_NT>(tp, cd, n, 2, R.bend, R.alpha_b, R.relax_b, R.inv_m);
+  const int iters = R.iters > 1 ? R.iters : 1;
+  for (int it = 0; it < iters; ++it) {
+    rope_pass<RS_NT>(tp, cd, n, 1, R.rest, R.alpha_s, R.relax_s, R.inv_m);
+    rope_pass<RS_NT>(tp, cd, n, 2, R.bend, R.alpha_b, R.relax_b, R.inv_m);
+  }
   for (int i = threadIdx.x; i < n; i += RS_NT) {
     const int p = R.p_off + i;
     const float4 s0 = rstate(w, f, 0)[p];
@@ -231,6 +236,11 @@ __global__ void __launch_bounds__(RS_NT) k_rope_solve_bwd(dt_world w, int f) {
   float4* cd = sm + 3 * M;
   const float dt = w.dt;
   const int b1 = (f + 1) & 1, b0 = f & 1;
+  const int iters = R.iters > 1 ? R.iters : 1;
+  if (iters > 1 && (w.r_work == nullptr || iters > w.max_rope_iters)) {  // no room for the pass inputs
+    if (threadIdx.x == 0) set_err(w, DT_DEVERR_ROPE_ITERS);
+    return;
+  }
   for (int i = threadIdx.x; i < n; i += RS_NT) {
     const int p = R.p_off + i;
     const float4 t = rope_integrate(R, dt, rstate(w, f, 0)[p], rstate(w, f, 1)[p], rext(w, f)[p]);
@@ -241,9 +251,27 @@ __global__ void __launch_bounds__(RS_NT) k_rope_solve_bwd(dt_world w, int f) {
     tpb[i] = i == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : v3to4(pb1 + vb1 / dt);
   }
   __syncthreads();
-  rope_pass<RS_NT>(tp1, cd, n, 1, R.rest, R.alpha_s, R.relax_s, R.inv_m);
-  rope_pass_bwd<RS_NT>(tp1, tpb, cd, n, 2, R.bend, R.alpha_b, R.relax_b, R.inv_m);
-  rope_pass_bwd<RS_NT>(tp0, tpb, cd, n, 1, R.rest, R.alpha_s, R.relax_s, R.inv_m);
+  if (iters == 1) {  // the pass inputs fit in shared memory: tp0 (stretch), tp1 (bending)
+    rope_pass<RS_NT>(tp1, cd, n, 1, R.rest, R.alpha_s, R.relax_s, R.inv_m);
+    rope_pass_bwd<RS_NT>(tp1, tpb, cd, n, 2, R.bend, R.alpha_b, R.relax_b, R.inv_m);
+    rope_pass_bwd<RS_NT>(tp0, tpb, cd, n, 1, R.rest, R.alpha_s, R.relax_s, R.inv_m);
+  } else {
+    // every pass's input positions into the workspace (pass k of this rope at r_work[k][p_off ..]),
+    // then the passes backwards
+    const size_t NR = (size_t)w.n_rope_particles;
+    float4* work = reinterpret_cast<float4*>(w.r_work) + R.p_off;
+    for (int k = 0; k < 2 * iters; ++k) {
+      for (int i = threadIdx.x; i < n; i += RS_NT) work[k * NR + i] = tp1[i];
+      // each pass ends with __syncthreads(), which also orders these writes before the backward
+      // passes read them from other threads of the CTA
+      if (k & 1) rope_pass<RS_NT>(tp1, cd, n, 2, R.bend, R.alpha_b, R.relax_b, R.inv_m);
+      else rope_pass<RS_NT>(tp1, cd, n, 1, R.rest, R.alpha_s, R.relax_s, R.inv_m);
+    }
+    for (int it = iters - 1; it >= 0; --it) {
+      rope_pass_bwd<RS_NT>(work + (2 * it + 1) * NR, tpb, cd, n, 2, R.bend, R.alpha_b, R.relax_b, R.inv_m);
+      rope_pass_bwd<RS_NT>(work + (2 * it) * NR, tpb, cd, n, 1, R.rest, R.alpha_s, R.relax_s, R.inv_m);
+    }
+  }
   const float clip = w.grad_clip;
   for (int i = threadIdx.x; i < n; i += RS_NT) {
     const int p = R.p_off + i;

@@ -95,6 +95,7 @@ class RopeSpec:
     bend_compliance: float | None = None     # default 1e-5 / rho
     stretch_relax: float = 0.3
     bend_relax: float = 0.1
+    iters: int = 1                     # stretch + bending pass pairs per substep (the reference: one)
     friction: float = 0.995
     gravity: tuple = (0.0, -9.8, 0.0)
     kn: float = 1e4

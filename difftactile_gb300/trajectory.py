@@ -56,7 +56,8 @@ class Trajectory:
     gradient tape would do if it fitted in memory; on a 280 GB device it does for the tasks here.
 
     ``loss_terms``: list of (sensor, layer, target [nv,3]) marker-displacement terms read at the
-    final frame.
+    final frame; ``rope_terms``: list of (rope, target [3]) terms |tip - target|^2 of the rope's last
+    particle at the final frame (the cable task's tip-position loss).
 
     ``graph``: the launch sequence of a forward (and of a backward) is the same on every call, so the
     first call runs eagerly and then records it as a CUDA graph; later calls copy the new controls
@@ -65,7 +66,8 @@ class Trajectory:
     world's tensors in place is seen by the replays, reallocated tensors are not.
     """
 
-    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=(), graph: bool = False):
+    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=(), graph: bool = False,
+                 rope_terms=()):
         self.w = world
         self.graph = bool(graph)
         self._graphs = {}     # "fwd" / ("bwd", loss_bar) -> torch.cuda.CUDAGraph
@@ -99,6 +101,11 @@ class Trajectory:
             tg = torch.zeros((world.sensor_rows[s].nv, 4), device=dev)
             tg[:, :3] = torch.as_tensor(np.asarray(target), dtype=torch.float32, device=dev)
             self.loss_terms.append((s, int(layer), tg))
+        self.rope_terms = []
+        for r, target in rope_terms:
+            row = world.rope_rows[r]
+            self.rope_terms.append((row.p_off + row.n - 1,
+                                    torch.as_tensor(np.asarray(target), dtype=torch.float32, device=dev).reshape(3)))
         self.loss = torch.zeros(1, device=dev)
         self.ctrl = None
         self.ctrl_bar = None
@@ -223,7 +230,16 @@ class Trajectory:
         for s, layer, tg in self.loss_terms:
             N.check(w.lib.dt_marker_loss(w.wp, s, f, layer, tg.data_ptr(), self.loss.data_ptr(), w.stream), "loss")
             self.launches += 1
+        for tip, tg in self.rope_terms:
+            self.loss += ((w.t["r_state"][f, 0, tip, :3] - tg) ** 2).sum()
         return self.loss
+
+    def _seed_rope_terms(self, loss_bar):
+        """Adjoint of the rope-tip terms into the rope adjoint of the final frame."""
+        w = self.w
+        for tip, tg in self.rope_terms:
+            w.t["r_adj"][self.f_end & 1, 0, tip, :3] += (2.0 * float(loss_bar)) * (
+                w.t["r_state"][self.f_end, 0, tip, :3] - tg)
 
     def _step_bwd(self, t):
         w = self.w
@@ -277,6 +293,7 @@ class Trajectory:
         for s, layer, tg in self.loss_terms:
             N.check(w.lib.dt_marker_loss_bwd(w.wp, s, self.f_end, layer, tg.data_ptr(), float(loss_bar), w.stream),
                     "loss bwd")
+        self._seed_rope_terms(loss_bar)
         if self.ctrl_bar is None or self.ctrl_bar.shape != self.ctrl32.shape:
             self.ctrl_bar = torch.zeros_like(self.ctrl32)
         self.ctrl_bar.zero_()
@@ -319,6 +336,7 @@ class Trajectory:
         for s, layer, tg in self.loss_terms:
             N.check(w.lib.dt_marker_loss_bwd(w.wp, s, self.f_end, layer, tg.data_ptr(), float(loss_bar), st),
                     "loss bwd")
+        self._seed_rope_terms(loss_bar)
         self.ctrl_bar.zero_()
         if self.full:
             for t in reversed(range(self.T)):
@@ -345,8 +363,9 @@ class PoseTrajectory(Trajectory):
     """Pose-controlled sensors (dome sensor, set_pose_control / set_control_vel): actions
     [T, n_sensors, 6] = (d_pos[3], d_ori[3] in degrees per unit time)."""
 
-    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=(), graph: bool = False):
-        super().__init__(world, n_steps, ckpt_every, loss_terms, graph)
+    def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=(), graph: bool = False,
+                 rope_terms=()):
+        super().__init__(world, n_steps, ckpt_every, loss_terms, graph, rope_terms)
         dev = world.device
         self.inv_T = 1.0 / (world.dt * self.S)
         Ms = [sp.trans_world if sp.trans_world is not None else np.eye(4) for sp in world.sensor_specs]
@@ -398,8 +417,8 @@ class GripperTrajectory(Trajectory):
     GripperKinematics; ``fingers`` the two sensors' indices in the world."""
 
     def __init__(self, world: World, n_steps: int, kin, fingers=(0, 1), ckpt_every: int = 1, loss_terms=(),
-                 graph: bool = False):
-        super().__init__(world, n_steps, ckpt_every, loss_terms, graph)
+                 graph: bool = False, rope_terms=()):
+        super().__init__(world, n_steps, ckpt_every, loss_terms, graph, rope_terms)
         self.kin = kin
         self.fingers = tuple(fingers)
         dev = world.device

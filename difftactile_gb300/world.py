@@ -180,6 +180,7 @@ class World:
                 x0 = rp.init_positions()
                 row.pin[:] = [float(c) for c in x0[0]]
                 row.kn, row.kd, row.kt, row.mu_t = rp.kn, rp.kd, rp.kt, rp.mu_t
+                row.iters = max(int(getattr(rp, "iters", 1)), 1)
                 rope_rows.append(row)
                 r_x.append(x0)
                 r_v.append(np.zeros((rp.n, 3), np.float32) if rp.v is None else np.asarray(rp.v, np.float32))
@@ -258,6 +259,9 @@ class World:
         t["r_cidx"] = zeros((Fn, NR, 4), I32)
         t["r_adj"] = zeros((2, 2, NR, 4))
         t["r_extb"] = zeros((NR, 4))
+        max_iters = max([r.iters for r in rope_rows], default=1)
+        # the adjoint of more than one pass pair recomputes every pass's input positions into here
+        t["r_work"] = zeros((2 * max_iters, NR, 4)) if (max_iters > 1 and NR) else None
         # the forward's SVD per frame, so that the adjoint need not recompute it (96 B per particle-frame)
         t["p_svd"] = zeros((Fn, 6, Np, 4)) if (svd_tape and Np) else None
 
@@ -279,6 +283,8 @@ class World:
         w.n_ropes, w.n_rope_particles = self.n_ropes, NR
         w.rope_blocks = r_blk
         w.max_rope_n = max([r.n for r in rope_rows], default=0)
+        w.r_work = t["r_work"].data_ptr() if t["r_work"] is not None else None
+        w.max_rope_iters = max_iters if t["r_work"] is not None else 1
         w.p_svd = t["p_svd"].data_ptr() if t["p_svd"] is not None else None
         self.w = w
         self.wp = C.pointer(w)

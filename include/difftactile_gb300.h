@@ -50,7 +50,7 @@
 extern "C" {
 #endif
 
-#define DT_ABI_VERSION 3
+#define DT_ABI_VERSION 4
 
 #define DT_OK 0
 #define DT_ERR_ARG (-1)        /* null pointer, bad size or frame index */
@@ -61,6 +61,8 @@ extern "C" {
 #define DT_DEVERR_PARTICLE_OOB 1   /* a particle's B-spline stencil left the grid: it was skipped */
 #define DT_DEVERR_TAPE_FULL    2   /* more active grid blocks than tape_blocks in one frame */
 #define DT_DEVERR_NONFINITE    4   /* NaN/Inf met in a grid node, a particle or a sensor vertex */
+#define DT_DEVERR_ROPE_ITERS   8   /* a rope's iters exceeds max_rope_iters (or r_work is NULL): its
+                                      adjoint was skipped */
 
 #define DT_MAX_SENSORS_PER_ENV 4
 #define DT_BLOCK_NODES 64
@@ -125,6 +127,8 @@ typedef struct dt_rope {
   float dt_g[3];        /* dt * gravity */
   float pin[3];         /* position of node 0 */
   float kn, kd, kt, mu_t;   /* rope-sensor contact (no clamp of the normal approach speed) */
+  int iters;            /* stretch + bending pass pairs per substep (<= 1: one, as PBDRope.update); the
+                           adjoint of more than one needs dt_world.r_work */
 } dt_rope;
 
 /* World descriptor: host struct holding device pointers and sizes. */
@@ -217,6 +221,11 @@ typedef struct dt_world {
                                     backward reads (the first pass of a checkpointed rollout, whose
                                     backward sweep recomputes each step); the active-block lists are
                                     still kept.  0: both are written */
+  /* ---- PBD rope solver iterations ---- */
+  float* r_work;                 /* [2 * max_rope_iters][n_rope_particles][4] adjoint workspace: the input
+                                    positions of every pass, recomputed by dt_rope_update_bwd; may be NULL
+                                    when no rope has iters > 1 */
+  int max_rope_iters;            /* largest iters over the ropes that r_work is sized for */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared

@@ -64,7 +64,7 @@ typedef struct orc_sensor {
 // PBD rope (PBD_rope.py) with its sensor contact parameters (cable_straightening.py:212-224)
 typedef struct orc_rope {
   int n;              // particles; node 0 is pinned at pin
-  int pad_;
+  int iters;          // repetitions of the stretch + bending pass pair (<= 1: one, as PBD_rope.py:132-172)
   double mass, rad;   // p_mass = rho 4/3 pi rad^3, contact offset = rad
   double rest, bend;  // rest_length, bending_length
   double alpha_s, alpha_b;    // compliance / dt^2
@@ -685,8 +685,10 @@ void rope_fwd(const orc_scene* sc, const orc_rope& R, orc_rope_io& io, T* const*
   std::vector<unsigned char> fl;
   rope_integrate(R, dt, rp, rv, re, tp, fl);
   const T w = T(1) / T(R.mass);
-  rope_pass(tp, n, 1, T(R.rest), T(R.alpha_s), T(R.relax_s), w);
-  rope_pass(tp, n, 2, T(R.bend), T(R.alpha_b), T(R.relax_b), w);
+  for (int it = 0; it < std::max(R.iters, 1); ++it) {
+    rope_pass(tp, n, 1, T(R.rest), T(R.alpha_s), T(R.relax_s), w);
+    rope_pass(tp, n, 2, T(R.bend), T(R.alpha_b), T(R.relax_b), w);
+  }
   T* rp1 = static_cast<T*>(io.pos1);
   T* rv1 = static_cast<T*>(io.vel1);
   for (int i = 0; i < n; ++i)
@@ -1090,11 +1092,21 @@ void rope_bwd(const orc_scene* sc, const orc_rope& R, orc_rope_io& io, T* const*
   T* rvb = static_cast<T*>(io.velb);
   T* rtb = static_cast<T*>(io.travb);
   const T w = T(1) / T(R.mass);
-  std::vector<T> tp0, tp1;
+  std::vector<T> tp0;
   std::vector<unsigned char> fl;
   rope_integrate(R, dt, rp, rv, re, tp0, fl);
-  tp1 = tp0;
-  rope_pass(tp1, n, 1, T(R.rest), T(R.alpha_s), T(R.relax_s), w);
+  // the input positions of every pass, recomputed: ins[2 it] stretch, ins[2 it + 1] bending
+  const int iters = std::max(R.iters, 1);
+  std::vector<std::vector<T>> ins(2 * iters);
+  {
+    std::vector<T> tp = tp0;
+    for (int it = 0; it < iters; ++it) {
+      ins[2 * it] = tp;
+      rope_pass(tp, n, 1, T(R.rest), T(R.alpha_s), T(R.relax_s), w);
+      ins[2 * it + 1] = tp;
+      rope_pass(tp, n, 2, T(R.bend), T(R.alpha_b), T(R.relax_b), w);
+    }
+  }
   // vel1 = (pos1 - pos) / dt; pos1[0] = pin, pos1[i] = tp2[i]
   std::vector<T> tpb(3 * n, T(0));
   for (int i = 0; i < n; ++i)
@@ -1104,8 +1116,10 @@ void rope_bwd(const orc_scene* sc, const orc_rope& R, orc_rope_io& io, T* const*
       rpb[q] = -vb1[q] / dt;
       tpb[q] = i == 0 ? T(0) : p1b;
     }
-  rope_pass_bwd(tp1, tpb, n, 2, T(R.bend), T(R.alpha_b), T(R.relax_b), w);
-  rope_pass_bwd(tp0, tpb, n, 1, T(R.rest), T(R.alpha_s), T(R.relax_s), w);
+  for (int it = iters - 1; it >= 0; --it) {
+    rope_pass_bwd(ins[2 * it + 1], tpb, n, 2, T(R.bend), T(R.alpha_b), T(R.relax_b), w);
+    rope_pass_bwd(ins[2 * it], tpb, n, 1, T(R.rest), T(R.alpha_s), T(R.relax_s), w);
+  }
   std::vector<T> reb(3 * n);
   for (int i = 0; i < n; ++i) {
     T nvb[3];

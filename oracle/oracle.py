@@ -28,7 +28,7 @@ class OrcSensor(C.Structure):
 
 
 class OrcRope(C.Structure):
-    _fields_ = [("n", C.c_int), ("pad_", C.c_int), ("mass", C.c_double), ("rad", C.c_double),
+    _fields_ = [("n", C.c_int), ("iters", C.c_int), ("mass", C.c_double), ("rad", C.c_double),
                 ("rest", C.c_double), ("bend", C.c_double), ("alpha_s", C.c_double), ("alpha_b", C.c_double),
                 ("relax_s", C.c_double), ("relax_b", C.c_double), ("table_h", C.c_double), ("friction", C.c_double),
                 ("grav", C.c_double * 3), ("pin", C.c_double * 3),
@@ -142,6 +142,7 @@ class Oracle:
         for i, rp in enumerate(ropes):
             r = rr[i]
             r.n = rp.n
+            r.iters = int(getattr(rp, "iters", 1))
             r.mass, r.rad, r.rest, r.bend = rp.mass, rp.rad, rp.rest, rp.bend
             cs, cb = rp.compliance
             r.alpha_s, r.alpha_b = cs / self.dt ** 2, cb / self.dt ** 2

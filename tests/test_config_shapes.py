@@ -50,7 +50,9 @@ def test_configuration_4_batched_population():
 def test_configuration_5_rope_pads():
     c = configs.rope_pads()
     e = c.envs[0]
-    assert len(c.envs) == 16 and c.n_particles == 16 * 32_768 and e.n_grid == (160, 160, 160)
-    assert [r.n for r in e.ropes] == [2_000]
+    assert len(c.envs) == 16 and abs(c.n_particles - 16 * 512_000) < 0.001 * 16 * 512_000 and e.n_grid == (160,) * 3
+    assert e.materials[0].model == 1 and e.materials[0].yield_stress > 0  # elastoplastic slab
+    assert [r.n for r in e.ropes] == [2_000] and e.ropes[0].iters == 50 and e.ropes[0].compliance == (1e-6, 1e-6)
+    assert c.ckpt_every == 10 and len(c.rope_terms) == 16
     assert (len(e.sensors[0].verts), len(e.sensors[0].tets)) == (10_086, 48_000)  # 40x40x5 hexes
     assert (c.n_steps, c.substeps) == (500, 20)

@@ -1,6 +1,6 @@
 """CPU restatement of the PBD rope (PBDRope.update, PBD_rope.py:112-180) and its sensor contact
-(cable_straightening.py:288-319): known answers, and the hand-written adjoint against central
-finite differences in float64."""
+(cable_straightening.py:288-319): known answers, more solver iterations converging the constraints,
+and the hand-written adjoint against central finite differences in float64."""
 import numpy as np
 
 from difftactile_gb300 import scene as S
@@ -74,8 +74,14 @@ def _loss(o, st0, W, n_sub):
     return L
 
 
-def test_rope_adjoint_matches_finite_differences():
+import pytest  # noqa: E402
+
+
+@pytest.mark.parametrize("iters", [1, 4])
+def test_rope_adjoint_matches_finite_differences(iters):
+    """One stretch + bending pass pair (the reference) and four of them per substep."""
     env = SS.rope_under_pad()
+    env = env.replace(ropes=[env.ropes[0].replace(iters=iters)])
     o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
     st0 = o.initial_state()
     rng = np.random.default_rng(3)
@@ -100,3 +106,19 @@ def test_rope_adjoint_matches_finite_differences():
 
         fd = (shifted(1) - shifted(-1)) / (2 * eps)
         assert abs(pred - fd) <= 1e-6 * max(abs(fd), 1e-9), (trial, pred, fd)
+
+
+def test_more_iterations_converge_the_stretch_constraints():
+    """A rope stretched by 20% relaxes towards its rest length faster with more pass pairs (the
+    compliance-weighted Jacobi passes converge); one pair is the reference's single pass.  The first
+    segment is left out: node 0 is put back on its pin after the passes (PBD_rope.py:174-177)."""
+    n = 8
+    x = np.stack([0.3 + 1.2 * 0.016 * np.arange(n), np.full(n, 0.5), np.full(n, 0.5)], 1).astype(np.float32)
+    errs = []
+    for iters in (1, 5, 50):
+        env = free_rope(n=n, x=x)
+        env = env.replace(ropes=[env.ropes[0].replace(iters=iters)])
+        st1, _ = O.Oracle(env, DT, np.float64).substep(O.Oracle(env, DT, np.float64).initial_state())
+        L = np.linalg.norm(np.diff(st1["rpos"][0], axis=0), axis=1)
+        errs.append(float(np.abs(L[1:] - 0.016).max()))
+    assert errs[0] > errs[1] > errs[2], errs

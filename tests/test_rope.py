@@ -87,8 +87,12 @@ def test_ropes_in_two_envs_beside_an_mpm_env(cuda_lib):
         assert SS.rel_err(rs["vel"].cpu().numpy(), st["rvel"][0]) < 1e-4, r
 
 
-def test_rope_adjoint_matches_oracle(cuda_lib):
+@pytest.mark.parametrize("iters", [1, 6])
+def test_rope_adjoint_matches_oracle(cuda_lib, iters):
+    """One pass pair (the reference's PBDRope.update) and six (the adjoint recomputes the pass inputs
+    into the dt_world.r_work workspace)."""
     env = SS.rope_under_pad()
+    env = env.replace(ropes=[env.ropes[0].replace(iters=iters)])
     rng = np.random.default_rng(4)
     o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
     st0 = o.initial_state()
@@ -134,3 +138,21 @@ def test_rope_argmin_on_a_large_pad(cuda_lib):
         assert np.array_equal(cid, d["rope_cidx"][0][:, 0]), f
     rs = {k: v.cpu().numpy() for k, v in w.rope_state(n_sub, 0).items()}
     assert SS.rel_err(rs["pos"], st["rpos"][0]) < 1e-5
+
+
+def test_rope_iterations_forward_match_the_oracle(cuda_lib):
+    """50 pass pairs per substep (configuration 5's solver) over three substeps under the pad: state as
+    the oracle's, and the stretch constraints closer to their rest length than with one pair."""
+    env = SS.rope_under_pad(n_rope=40)
+    cv = [SS.control_velocity(sp, scale=0.02, down=-0.05) for sp in env.sensors]
+    res = {}
+    for iters in (1, 50):
+        e = env.replace(ropes=[env.ropes[0].replace(iters=iters)])
+        w = run_gpu([e], 3, cv)
+        st, _ = oracle_run(e, 3, cv)
+        rs = {k: v.cpu().numpy() for k, v in w.rope_state(3, 0).items()}
+        assert SS.rel_err(rs["pos"], st["rpos"][0]) < 1e-5, iters
+        assert SS.rel_err(rs["vel"], st["rvel"][0]) < 1e-3, iters
+        L = np.linalg.norm(np.diff(rs["pos"], axis=0), axis=1)[1:]
+        res[iters] = float(np.abs(L - e.ropes[0].rest).max())
+    assert res[50] < res[1], res
