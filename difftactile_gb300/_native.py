@@ -29,7 +29,7 @@ class DtSensor(C.Structure):
         ("v_off", C.c_int), ("nv", C.c_int), ("t_off", C.c_int), ("nt", C.c_int),
         ("f_off", C.c_int), ("nf", C.c_int), ("env", C.c_int), ("carry", C.c_int),
         ("dt_over_m", C.c_float), ("mu", C.c_float), ("lam", C.c_float), ("alpha", C.c_float),
-        ("out_dir", C.c_float * 3), ("pad_", C.c_float),
+        ("out_dir", C.c_float * 3), ("model", C.c_int),
     ]
 
 

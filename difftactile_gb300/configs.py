@@ -66,8 +66,9 @@ def _press_env(n_grid=96, box_cells=20, pad=(20, 20, 5), pad_h=0.0125, seed=1, y
     # steps).  Node masses then grow in proportion to h, and the penalty contact (stiffness 1e4 per
     # node) keeps k dt^2 / m below 0.2 down to the smallest pads of the population (0.005 m)
     rho_pad = 1000.0 * (0.0125 / pad_h) ** 2
+    # configuration 2's pad is linear corotated (its text), configuration 4 takes the same pad
     sp = S.hex_pad_sensor([cx, hi[1] + gap_cells * dx, cz], nx=pad[0], nz=pad[1], ny=pad[2], h=pad_h, E=1.5e5,
-                          nu=0.45, rho=rho_pad)
+                          nu=0.45, rho=rho_pad, model=S.FEM_LINEAR_COROTATED)
     env = S.EnvSpec(x=x, materials=[S.Material(E, nu, yield_stress, S.MODEL_VON_MISES)],
                     n_grid=(n_grid, n_grid, n_grid), dx=dx, rho=1000.0, sensors=[sp],
                     kn=1e4, kd=100.0, kt=friction_stiffness(1000.0, dx), mu_t=0.5)
@@ -88,7 +89,7 @@ def press_actions(n_steps, n_sensors=1, seed=2, press=0.15, slide=0.1, noise=0.0
 
 def sensor_press(n_steps=100, substeps=20, seed=1) -> Config:
     """Config 2: FEM pad (20x20x5 hex, 6 tets/hex: 2646 nodes, 12000 tets, 800 surface triangles,
-    E 1.5e5, nu 0.45, driven base layer) pressing and sliding on a von-Mises elastoplastic box of
+    linear corotated, E 1.5e5, nu 0.45, driven base layer) pressing and sliding on a von-Mises elastoplastic box of
     64,000 particles (20^3 cells x 8) on a 96^3 grid, yield stress 50, penalty contact 1e4;
     100 steps x 20 substeps, actions ~ N(0, 0.01) around press-and-slide; loss = L2 of the surface
     nodes' displacement field against a seeded target field.

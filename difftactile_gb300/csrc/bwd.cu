@@ -617,6 +617,38 @@ __device__ void fem_tet_bwd(const dt_world& w, int f, int t) {
   const float detD = mdet(D);
   const float Vi = fabsf(detD) / 6.f;
   const m3 Fe = mmul(D, B);
+  const float4* aVm0 = reinterpret_cast<const float4*>(w.v_adj_velmid);
+  float4* aPos0 = reinterpret_cast<float4*>(w.v_adj_pos) + cb * V;
+  if (S.model == DT_FEM_LINEAR_COROTATED) {
+    // P = 2 mu (F - R) + lam c R, c = sum sigma - 3, H = -V0 P B^T with the rest volume V0
+    m3 U, Vm;
+    v3 sg;
+    svd3(Fe, U, sg, Vm, w.svd_sweeps);
+    const m3 R = mmulT(U, Vm);
+    const float c = ((sg.x + sg.y) + sg.z) - 3.f;
+    const float sc0 = -S.dt_over_m / (6.f * fabsf(mdet(B)));
+    const v3 g3 = f4to3(aVm0[tv.w]);
+    const v3 hb[3] = {f4to3(aVm0[tv.x]) - g3, f4to3(aVm0[tv.y]) - g3, f4to3(aVm0[tv.z]) - g3};
+    m3 Hb;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      Hb.a[0][k] = sc0 * hb[k].x;
+      Hb.a[1][k] = sc0 * hb[k].y;
+      Hb.a[2][k] = sc0 * hb[k].z;
+    }
+    const m3 Pb = mmul(Hb, B);  // H = P B^T
+    const m3 Rb = mscale(S.lam * c - 2.f * S.mu, Pb);
+    const float cb_ = S.lam * mdot(Pb, R);
+    const m3 Fb = madd(mscale(2.f * S.mu, Pb),
+                       svd_grad(U, sg, Vm, mzero(), v3{cb_, cb_, cb_}, mzero(), Rb, DT_SVDGRAD_STABLE));
+    const m3 Db = mmulT(Fb, B);  // F = D B
+    const v3 ab = mcol(Db, 0), bb = mcol(Db, 1), cbv = mcol(Db, 2);
+    red_add_v4(aPos0 + tv.x, v3to4(ab));
+    red_add_v4(aPos0 + tv.y, v3to4(bb));
+    red_add_v4(aPos0 + tv.z, v3to4(cbv));
+    red_add_v4(aPos0 + tv.w, v3to4(-((ab + bb) + cbv)));
+    return;
+  }
   const float J = mdet(Fe);
   const float IC = mdot(Fe, Fe);
   const m3 cof = mcof(Fe);

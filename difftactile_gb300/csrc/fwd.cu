@@ -123,8 +123,9 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
                                       reinterpret_cast<float4*>(w.g_acc), mark_box, mark_one);
 }
 
-// FEM elastic forces of one tet (fem_sensor.py:409-440): stable-Neo-Hookean-like P with current
-// volume weighting; velocity increments accumulated into velmid[f] with vector REDs
+// FEM elastic forces of one tet (fem_sensor.py:409-440): the reference's stable-Neo-Hookean-like P with
+// current volume weighting, or linear corotated with rest volume (dt_sensor.model); velocity increments
+// accumulated into velmid[f] with vector REDs
 __device__ void fem_tet(const dt_world& w, int f, int t) {
   const int4 tv = __ldg(reinterpret_cast<const int4*>(w.tets) + t);
   const dt_sensor& S = w.sensors[__ldg(w.tet_sensor + t)];
@@ -147,18 +148,32 @@ __device__ void fem_tet(const dt_world& w, int f, int t) {
     D.a[1][k] = cols[k].y;
     D.a[2][k] = cols[k].z;
   }
-  const float Vi = fabsf(mdet(D)) / 6.f;
+  float Vi = fabsf(mdet(D)) / 6.f;
   const m3 Fe = mmul(D, B);
-  const float J = mdet(Fe);
-  const float IC = mdot(Fe, Fe);
-  const m3 cof = mcof(Fe);
-  const float k1 = S.mu * (1.f - 1.f / (IC + 1.f));
-  const float k2 = S.lam * (J - S.alpha);
   m3 Pk;
+  if (S.model == DT_FEM_LINEAR_COROTATED) {
+    // P = 2 mu (F - R) + lam tr(R^T F - I) R (tr(R^T F) = sum of the singular values), rest volume
+    m3 U, V;
+    v3 sg;
+    svd3(Fe, U, sg, V, w.svd_sweeps);
+    const m3 R = mmulT(U, V);
+    const float c = ((sg.x + sg.y) + sg.z) - 3.f;
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) Pk.a[i][j] = k1 * Fe.a[i][j] + k2 * cof.a[i][j];
+      for (int j = 0; j < 3; ++j) Pk.a[i][j] = 2.f * S.mu * (Fe.a[i][j] - R.a[i][j]) + S.lam * c * R.a[i][j];
+    Vi = 1.f / (6.f * fabsf(mdet(B)));
+  } else {
+    const float J = mdet(Fe);
+    const float IC = mdot(Fe, Fe);
+    const m3 cof = mcof(Fe);
+    const float k1 = S.mu * (1.f - 1.f / (IC + 1.f));
+    const float k2 = S.lam * (J - S.alpha);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Pk.a[i][j] = k1 * Fe.a[i][j] + k2 * cof.a[i][j];
+  }
   const m3 H = mmulT(Pk, B);  // P B^T
   const float s = -Vi * S.dt_over_m;
   float4* VM = vframe(w.v_velmid, w, f);

@@ -15,6 +15,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 MODEL_COROTATED, MODEL_VON_MISES, MODEL_NEOHOOKEAN = 0, 1, 2
+# elastomer force models of the FEM sensors: the reference's (fem_sensor.py:424-435) and linear corotated
+FEM_REFERENCE, FEM_LINEAR_COROTATED = 0, 1
 BC_SLIP_WALLS, BC_STICKY_FLOOR = 0, 1
 
 
@@ -65,6 +67,7 @@ class SensorSpec:
     out_dir: tuple = (0.0, 1.0, 0.0)
     carry: int = 0             # gripper_fem.py:415 control-velocity carry term
     trans_world: np.ndarray | None = None  # 4x4 sensor pose used by pose control
+    model: int = FEM_REFERENCE  # FEM_* elastomer force model
 
     def lame(self):
         if self.mu is not None and self.lam is not None:
@@ -240,7 +243,7 @@ def hex_pad_local(nx=20, nz=20, ny=5, h=0.0125):
     return verts, tets.astype(np.int32), tris.astype(np.int32), layer.astype(np.int32)
 
 
-def hex_pad_sensor(center_bottom, nx=20, nz=20, ny=5, h=0.0125, rho=1000.0, E=1.5e5, nu=0.45):
+def hex_pad_sensor(center_bottom, nx=20, nz=20, ny=5, h=0.0125, rho=1000.0, E=1.5e5, nu=0.45, model=FEM_REFERENCE):
     """Pad pressing down: the local pad is flipped by 180 deg about x so that its contact surface
     faces -y, and placed with the centre of that surface at ``center_bottom``."""
     v, tets, tris, layer = hex_pad_local(nx, nz, ny, h)
@@ -252,7 +255,7 @@ def hex_pad_sensor(center_bottom, nx=20, nz=20, ny=5, h=0.0125, rho=1000.0, E=1.
     vol = (nx * h) * (nz * h) * (ny * h)
     mass = rho * vol / len(v)
     return SensorSpec(verts=world.astype(np.float32), tets=tets, tris=tris, layer=layer, mass=mass, E=E, nu=nu,
-                      out_dir=tuple(out_dir), trans_world=M)
+                      out_dir=tuple(out_dir), trans_world=M, model=model)
 
 
 def finger_pad_sensor(pose, nx=6, nz=6, ny=2, h=1.0 / 32, rho=1000.0, E=1.5e5, nu=0.45, shift=(0.0, 0.0)):

@@ -152,6 +152,7 @@ class World:
             r.mu, r.lam = mu, lam
             r.alpha = float(np.float32(1) + np.float32(0.75) * np.float32(mu) / np.float32(lam))
             r.out_dir[:] = [float(c) for c in sp.out_dir]
+            r.model = int(getattr(sp, "model", 0))
             srows.append(r)
             v_off, t_off, f_off = v_off + nv, t_off + nt, f_off + nf
         self.sensor_specs = [sp for _, sp in sensors]

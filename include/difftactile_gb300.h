@@ -104,8 +104,14 @@ typedef struct dt_sensor {
   float dt_over_m;      /* dt / node mass */
   float mu, lam, alpha; /* elastomer Lame parameters, alpha = 1 + 0.75 mu/lam */
   float out_dir[3];     /* rot_h @ (0,1,0): orients surface normals (fem_sensor.py:340,370) */
-  float pad_;
+  int model;            /* DT_FEM_*: elastomer force model */
 } dt_sensor;
+
+/* elastomer force models of the FEM sensors */
+#define DT_FEM_REFERENCE 0          /* the reference's: P = mu (1 - 1/(I_C + 1)) F + lam (J - alpha) dJ/dF, current
+                                       volume (fem_sensor.py:424-435) */
+#define DT_FEM_LINEAR_COROTATED 1   /* P = 2 mu (F - R) + lam tr(R^T F - I) R, R the polar rotation of F, rest
+                                       volume */
 
 typedef struct dt_material {
   float mu, lam, yield_stress;

@@ -58,7 +58,7 @@ typedef struct orc_sensor {
   double mass, mu, lam;
   double out_dir[3];
   int carry;          // 1: gripper_fem.py:415 velocity carry term
-  int pad_;
+  int model;          // 0: the reference's elastomer force (fem_sensor.py:424-435), 1: linear corotated
 } orc_sensor;
 
 // PBD rope (PBD_rope.py) with its sensor contact parameters (cable_straightening.py:212-224)
@@ -766,20 +766,33 @@ static int substep_impl(const orc_scene* sc, const T* x, const T* v, const T* C,
         }
       T Vi = std::fabs(mdet(D)) / T(6);
       M3<T> Fe = mmul(D, B);
-      T J = mdet(Fe);
-      T IC = T(0);
-      for (int i = 0; i < 3; ++i) {
-        T cc = Fe.a[0][i] * Fe.a[0][i];
-        cc = cc + Fe.a[1][i] * Fe.a[1][i];
-        cc = cc + Fe.a[2][i] * Fe.a[2][i];
-        IC = IC + cc;
-      }
-      M3<T> cof = mcof(Fe);  // columns: F1xF2, F2xF0, F0xF1
       M3<T> Pk;
-      T k1 = mu * (T(1) - T(1) / (IC + T(1)));
-      T k2 = lam * (J - alpha);
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) Pk.a[i][j] = k1 * Fe.a[i][j] + k2 * cof.a[i][j];
+      if (S.model == 1) {
+        // linear corotated: P = 2 mu (F - R) + lam tr(R^T F - I) R with F = R S (R = U V^T of the SVD,
+        // tr(R^T F) = sum sigma), weighted by the rest volume 1 / (6 |det B|)
+        M3<T> U, Vs;
+        T sg[3];
+        svd3(Fe, U, sg, Vs, sc->svd_sweeps);
+        const M3<T> R = mmul(U, mT(Vs));
+        const T c = ((sg[0] + sg[1]) + sg[2]) - T(3);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) Pk.a[i][j] = T(2) * mu * (Fe.a[i][j] - R.a[i][j]) + lam * c * R.a[i][j];
+        Vi = T(1) / (T(6) * std::fabs(mdet(B)));
+      } else {
+        T J = mdet(Fe);
+        T IC = T(0);
+        for (int i = 0; i < 3; ++i) {
+          T cc = Fe.a[0][i] * Fe.a[0][i];
+          cc = cc + Fe.a[1][i] * Fe.a[1][i];
+          cc = cc + Fe.a[2][i] * Fe.a[2][i];
+          IC = IC + cc;
+        }
+        M3<T> cof = mcof(Fe);  // columns: F1xF2, F2xF0, F0xF1
+        T k1 = mu * (T(1) - T(1) / (IC + T(1)));
+        T k2 = lam * (J - alpha);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) Pk.a[i][j] = k1 * Fe.a[i][j] + k2 * cof.a[i][j];
+      }
       M3<T> H = mmul(Pk, mT(B));
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) H.a[i][j] = -Vi * H.a[i][j];
@@ -1395,6 +1408,39 @@ static int substep_bwd_impl(const orc_scene* sc, const T* x, const T* v, const T
       T detD = mdet(D);
       T Vi = std::fabs(detD) / T(6);
       M3<T> Fe = mmul(D, B);
+      if (S.model == 1) {
+        // linear corotated (see the forward): P = 2 mu (F - R) + lam c R, c = sum sigma - 3, rest volume
+        M3<T> U, Vs;
+        T sg[3];
+        svd3(Fe, U, sg, Vs, sc->svd_sweeps);
+        const M3<T> R = mmul(U, mT(Vs));
+        const T c = ((sg[0] + sg[1]) + sg[2]) - T(3);
+        const T V0 = T(1) / (T(6) * std::fabs(mdet(B)));
+        const T sc_ = -V0 * dt / mass;
+        M3<T> Hb;
+        for (int k = 0; k < 3; ++k)
+          for (int r = 0; r < 3; ++r) Hb.a[r][k] = sc_ * (vmb[s][3 * tv[k] + r] - vmb[s][3 * tv[3] + r]);
+        const M3<T> Pb = mmul(Hb, B);  // H = P B^T
+        M3<T> Fb_, Rb, zero = mzero<T>();
+        T cb = T(0);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            Fb_.a[i][j] = T(2) * mu * Pb.a[i][j];
+            Rb.a[i][j] = (lam * c - T(2) * mu) * Pb.a[i][j];
+            cb += lam * Pb.a[i][j] * R.a[i][j];
+          }
+        const T sb[3] = {cb, cb, cb};  // d c / d sigma = 1
+        const M3<T> g = svd_grad(U, sg, Vs, zero, sb, zero, Rb, svd_grad_mode);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) Fb_.a[i][j] += g.a[i][j];
+        M3<T> Db = mmul(Fb_, mT(B));
+        for (int k = 0; k < 3; ++k)
+          for (int r = 0; r < 3; ++r) {
+            posb[s][3 * tv[k] + r] += Db.a[r][k];
+            posb[s][3 * tv[3] + r] -= Db.a[r][k];
+          }
+        continue;
+      }
       T J = mdet(Fe);
       T IC = T(0);
       for (int i = 0; i < 3; ++i)

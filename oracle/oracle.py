@@ -24,7 +24,7 @@ _lib = None
 class OrcSensor(C.Structure):
     _fields_ = [("nv", C.c_int), ("nt", C.c_int), ("nf", C.c_int), ("tets", C.c_void_p), ("tris", C.c_void_p),
                 ("layer", C.c_void_p), ("B", C.c_void_p), ("mass", C.c_double), ("mu", C.c_double),
-                ("lam", C.c_double), ("out_dir", C.c_double * 3), ("carry", C.c_int), ("pad_", C.c_int)]
+                ("lam", C.c_double), ("out_dir", C.c_double * 3), ("carry", C.c_int), ("model", C.c_int)]
 
 
 class OrcRope(C.Structure):
@@ -131,6 +131,7 @@ class Oracle:
             s.mass, s.mu, s.lam = float(sp.mass), float(m_), float(l_)
             s.out_dir[:] = [float(c) for c in sp.out_dir]
             s.carry = int(sp.carry)
+            s.model = int(getattr(sp, "model", 0))
         self.keep.append(sens)
         sc.n_sensors = len(env.sensors)
         sc.sensors = C.cast(sens, C.c_void_p)

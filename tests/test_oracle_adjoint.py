@@ -41,14 +41,20 @@ def _scene(name):
         return SS.elastic_cube(center=(0.5, 4.5 / 32, 0.5), v=(0.0, -0.5, 0.0), bc=S.BC_STICKY_FLOOR), 1
     if name == "pad_3_substeps":
         return SS.pad_over_box(yield_stress=50.0), 3
+    if name == "linear_corotated_pad":  # the pad's elastomer with the linear corotated force
+        import dataclasses
+        env = SS.pad_over_box()
+        return env.replace(sensors=[dataclasses.replace(env.sensors[0], model=S.FEM_LINEAR_COROTATED)]), 2
     raise KeyError(name)
 
 
-@pytest.mark.parametrize("name", ["two_pads", "dome", "gripper", "sticky_floor", "pad_3_substeps"])
+@pytest.mark.parametrize("name", ["two_pads", "dome", "gripper", "sticky_floor", "pad_3_substeps",
+                                  "linear_corotated_pad"])
 def test_oracle_adjoint_matches_finite_differences_per_scene(name):
     """The same check on the other parity scenes: two pads in one environment, the reference's dome
     (unordered triangles, tilted contact normal), the gripper's two finger pads, a cube on the sticky
-    floor, and a three-substep chain (the adjoint carried through the per-frame grid and sensor state)."""
+    floor, a three-substep chain (the adjoint carried through the per-frame grid and sensor state) and the
+    pad with the linear corotated elastomer force."""
     env, n_sub = _scene(name)
     if env.v is None:
         env = env.replace(v=np.zeros_like(env.x))

@@ -223,3 +223,36 @@ def test_dome_mesh_matches_reference_counts():
     nodes, tets, tris, layer = S.dome_mesh()
     assert (len(nodes), len(tets), len(tris)) == (1910, 8198, 1543)
     assert (np.bincount(layer) == np.array([200, 355, 555, 800])).all()
+
+
+def test_linear_corotated_tet_force_known_answer():
+    """One tet of the linear corotated elastomer: the velocity change of its vertices is
+    dt / m times -V0 P B^T (and minus their sum on the fourth vertex), P = 2 mu (F - R) + lam tr(R^T F - I) R
+    with R the polar rotation of F = D B (scipy.linalg.polar), V0 the rest volume."""
+    import scipy.linalg
+    from difftactile_gb300 import scene as S_
+    rest = np.array([[0.0, 0.0, 0.0], [0.02, 0.0, 0.0], [0.0, 0.02, 0.0], [0.0, 0.0, 0.02]], np.float32) + 0.4
+    sp = S_.SensorSpec(verts=rest, tets=np.array([[1, 2, 3, 0]], np.int32), tris=np.zeros((0, 3), np.int32),
+                       layer=np.ones(4, np.int32), mass=1e-3, E=1.5e5, nu=0.45, model=S_.FEM_LINEAR_COROTATED)
+    env = S_.EnvSpec(x=np.zeros((0, 3), np.float32), materials=[S_.Material(5e3, 0.3)], n_grid=(16,) * 3,
+                     dx=1 / 16, sensors=[sp], gravity=(0.0, 0.0, 0.0))
+    rng = np.random.default_rng(2)
+    pos = rest.astype(np.float64) + 0.002 * rng.standard_normal(rest.shape)
+    o = O.Oracle(env, 1e-4, np.float64)
+    st = o.initial_state()
+    st["pos"] = [pos]
+    _, d = o.substep(st)
+    B = sp.rest_inverse()[0].astype(np.float64)
+    t = sp.tets[0]
+    D = np.stack([pos[t[k]] - pos[t[3]] for k in range(3)], 1)
+    F = D @ B
+    R, _ = scipy.linalg.polar(F)
+    mu, lam = sp.lame()
+    P = 2 * mu * (F - R) + lam * (np.trace(R.T @ F) - 3) * R
+    H = -(1.0 / (6 * abs(np.linalg.det(B)))) * P @ B.T
+    dv = np.zeros((4, 3))
+    for k in range(3):
+        dv[t[k]] += 1e-4 * H[:, k] / 1e-3
+        dv[t[3]] -= 1e-4 * H[:, k] / 1e-3
+    assert np.abs(dv).max() > 1e-3
+    assert np.allclose(d["vel_mid"][0], dv, rtol=1e-9, atol=1e-12 * np.abs(dv).max())

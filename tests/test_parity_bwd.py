@@ -139,10 +139,14 @@ def test_adjoint_matches_finite_differences(cuda_lib, model, ys):
     assert not failures, failures
 
 
-@pytest.mark.parametrize("model,ys", [(S.MODEL_COROTATED, 50.0), (S.MODEL_VON_MISES, 2.0)])
-def test_adjoint_matches_oracle_adjoint(cuda_lib, model, ys):
-    """Whole adjoint arrays of one substep against the oracle's float64 adjoint (norm-wise 1e-3)."""
+@pytest.mark.parametrize("model,ys,fem", [(S.MODEL_COROTATED, 50.0, S.FEM_REFERENCE), (S.MODEL_VON_MISES, 2.0, S.FEM_REFERENCE),
+                                          (S.MODEL_VON_MISES, 2.0, S.FEM_LINEAR_COROTATED)])
+def test_adjoint_matches_oracle_adjoint(cuda_lib, model, ys, fem):
+    """Whole adjoint arrays of one substep against the oracle's float64 adjoint (norm-wise 1e-3), with the
+    reference's elastomer force and with the linear corotated one."""
+    import dataclasses
     env = SS.pad_over_box(n=40, box_cells=(10, 6, 10), pad=(10, 10, 3), model=model, yield_stress=ys)
+    env = env.replace(sensors=[dataclasses.replace(sp, model=fem) for sp in env.sensors])
     st0, cv = base_point(env, 7)
     W = loss_weights(env, env.n_particles, 8)
     g = gpu_grads(env, st0, cv, W, 1)

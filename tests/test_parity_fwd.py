@@ -197,3 +197,16 @@ def test_contact_argmin_large_pad(cuda_lib, lanes):
     assert occ.sum() > 1000
     ci = g["cidx"].cpu().numpy()[..., 0]
     assert np.array_equal(ci[occ], dbg[0]["cidx"][..., 0][occ])
+
+
+def test_one_substep_linear_corotated_pad(cuda_lib):
+    """The pad's elastomer with the linear corotated force (configuration 2's model): one substep in
+    contact against the oracle."""
+    import dataclasses
+    env = SS.pad_over_box()
+    env = env.replace(sensors=[dataclasses.replace(env.sensors[0], model=S.FEM_LINEAR_COROTATED)])
+    cv = [SS.control_velocity(sp) for sp in env.sensors]
+    w = run_gpu([env], 2, cv)
+    st, _ = run_oracle(env, 2, cv)
+    assert w.error_word() == 0
+    compare(w, 2, st)
