@@ -8,7 +8,7 @@ compute_grid_m_kernel of object_model/mpm_plastic.py:169-178, read out of the re
 of it; the target's distance field (2 n passes of the nearest-seed propagation, as update_target
 runs them), the particles' grid mass and the weighted loss go to tests/golden/deform_ref.npz.
 
-    python tests/golden/make_deform.py [REFERENCE_ROOT]
+    python tests/golden/make_deform.py REFERENCE_ROOT
 """
 import os
 import sys
@@ -18,6 +18,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from tests.golden.refroot import reference_root  # noqa: E402
 
 from tests.golden import ti_numpy as ti  # noqa: E402
 
@@ -42,7 +44,7 @@ def grid_mass(x, mpm_src):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_root()
     mpm_src = os.path.join(ref, "difftactile", "object_model", "mpm_plastic.py")
     loss_src = os.path.join(ref, "difftactile", "tasks", "deform_loss.py")
     x = cloud(0)

@@ -5,7 +5,7 @@ numpy + scipy; their module needs taichi, which this environment lacks, so the t
 taken out of the reference source with `ast` and run on a stand-in object carrying the sensor's
 constructor constants (N_node 200, N_t 4, t_res 0.25, inner_radius 0.75, fem_sensor.py:24-27).
 
-    python tests/golden/make_dome.py [REFERENCE_ROOT]     # writes tests/golden/dome_ref.npz
+    python tests/golden/make_dome.py REFERENCE_ROOT     # writes tests/golden/dome_ref.npz
 """
 import ast
 import os
@@ -15,11 +15,18 @@ import types
 import numpy as np
 from scipy.spatial import Delaunay
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-SRC = os.path.join(REF, "difftactile", "sensor_model", "fem_sensor.py")
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from tests.golden.refroot import reference_root  # noqa: E402
+
+
+def source():
+    return os.path.join(reference_root(), "difftactile", "sensor_model", "fem_sensor.py")
 
 
 def reference_methods():
+    SRC = source()
     tree = ast.parse(open(SRC).read())
     cls = next(n for n in tree.body if isinstance(n, ast.ClassDef) and n.name == "FEMDomeSensor")
     fns = [n for n in cls.body if isinstance(n, ast.FunctionDef) and n.name in ("fibonacci_sphere", "init_mesh")]

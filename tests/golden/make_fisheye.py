@@ -6,7 +6,7 @@ taken out of the reference source with `ast` and run alone with numpy.  Camera-f
 seeded (the size of the sensor pad seen by its camera: x, y within 12 mm of the axis, 8-20 mm in
 front of the image plane once the plane offset is added).
 
-    python tests/golden/make_fisheye.py [REFERENCE_ROOT]     # writes tests/golden/fisheye_ref.npz
+    python tests/golden/make_fisheye.py REFERENCE_ROOT     # writes tests/golden/fisheye_ref.npz
 """
 import ast
 import os
@@ -14,11 +14,18 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-SRC = os.path.join(REF, "difftactile", "sensor_model", "fisheye_model.py")
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from tests.golden.refroot import reference_root  # noqa: E402
+
+
+def source():
+    return os.path.join(reference_root(), "difftactile", "sensor_model", "fisheye_model.py")
 
 
 def reference_function():
+    SRC = source()
     tree = ast.parse(open(SRC).read())
     fn = next(n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name == "project_points_to_pix")
     ns = {"np": np}

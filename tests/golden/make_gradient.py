@@ -11,7 +11,7 @@ rope_pads case: PBD rope under a gripper pad) along the rope's and the pads' sta
 control velocities.  Derivatives go to tests/golden/gradient_ref.npz (the directions are rebuilt from
 their seeds).
 
-    python tests/golden/make_gradient.py [REFERENCE_ROOT]
+    python tests/golden/make_gradient.py REFERENCE_ROOT
 """
 import os
 import sys
@@ -20,6 +20,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from tests.golden.refroot import reference_root  # noqa: E402
 
 from difftactile_gb300 import scene as S  # noqa: E402
 from tests.golden import make_substep as MS  # noqa: E402
@@ -112,7 +114,7 @@ def rope_loss(env, st, W, d, h):
 
 
 def main():
-    MS.PKG = os.path.join(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", "difftactile")
+    MS.PKG = os.path.join(reference_root(), "difftactile")
     env, st, W = base()
     fd = []
     for gr, d in directions(env, st, seed=300):

@@ -7,7 +7,7 @@ control step of a tilted gripper (end-effector pose, finger offsets) with a seed
 finger poses over the step's substeps and the control velocities of two finger pads.  Inputs and
 outputs go to tests/golden/gripper_ref.npz.
 
-    python tests/golden/make_gripper.py [REFERENCE_ROOT]
+    python tests/golden/make_gripper.py REFERENCE_ROOT
 """
 import os
 import sys
@@ -17,6 +17,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from tests.golden.refroot import reference_root  # noqa: E402
 
 from tests.golden import ti_numpy as ti  # noqa: E402
 
@@ -38,7 +40,7 @@ def kinematics():
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_root()
     src = os.path.join(ref, "difftactile", "sensor_model", "gripper_kinematics.py")
     sens = []
     for sp, F0 in zip(pads(kinematics()), kinematics().finger_poses0()):

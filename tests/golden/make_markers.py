@@ -9,7 +9,7 @@ from is replaced by a seeded marker set (its only output).  The sensor is the re
 the dome parity scene of tests/small_scenes.py; the readout runs on a displaced surface and a moved
 sensor pose.  Inputs and outputs go to tests/golden/markers_ref.npz.
 
-    python tests/golden/make_markers.py [REFERENCE_ROOT]
+    python tests/golden/make_markers.py REFERENCE_ROOT
 """
 import os
 import sys
@@ -19,6 +19,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from tests.golden.refroot import reference_root  # noqa: E402
 
 from tests import small_scenes as SS  # noqa: E402
 from tests.golden import ti_numpy as ti  # noqa: E402
@@ -38,7 +40,7 @@ def pose_shift():
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_root()
     fem = os.path.join(ref, "difftactile", "sensor_model", "fem_sensor.py")
     fish = os.path.join(ref, "difftactile", "sensor_model", "fisheye_model.py")
     sp = sensor()

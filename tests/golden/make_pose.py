@@ -7,7 +7,7 @@ seeded actions applied one after the other, the step transform dtrans_h of each 
 velocity of every vertex from the virtual positions.  Inputs and outputs go to
 tests/golden/pose_ref.npz.
 
-    python tests/golden/make_pose.py [REFERENCE_ROOT]
+    python tests/golden/make_pose.py REFERENCE_ROOT
 """
 import os
 import sys
@@ -17,6 +17,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from tests.golden.refroot import reference_root  # noqa: E402
 
 from tests import small_scenes as SS  # noqa: E402
 from tests.golden import ti_numpy as ti  # noqa: E402
@@ -31,7 +33,7 @@ def sensor():
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_root()
     src = os.path.join(ref, "difftactile", "sensor_model", "fem_sensor.py")
     sp = sensor()
     M = np.asarray(sp.trans_world, np.float64)

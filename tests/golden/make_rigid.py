@@ -6,7 +6,7 @@ folder (ti_numpy.py): a seeded particle cloud of which 60% carry the rigid mater
 one substep by a rotation about z plus noise; the centres (divided by the whole particle count, as the
 reference does), the covariance H and R = V U^T go to tests/golden/rigid_ref.npz.
 
-    python tests/golden/make_rigid.py [REFERENCE_ROOT]
+    python tests/golden/make_rigid.py REFERENCE_ROOT
 """
 import os
 import sys
@@ -17,13 +17,15 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
+from tests.golden.refroot import reference_root  # noqa: E402
+
 from tests.golden import ti_numpy as ti  # noqa: E402
 
 DT = 1e-4
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_root()
     src = os.path.join(ref, "difftactile", "object_model", "multi_obj.py")
     rng = np.random.default_rng(8)
     N = 300

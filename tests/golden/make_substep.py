@@ -29,7 +29,7 @@ The scenes come from tests/small_scenes.py (the parity scenes); states, constant
 (particles, the grid at occupied nodes, contact indices, the sensors' forces and next frame) go to
 tests/golden/substep_ref.npz.
 
-    python tests/golden/make_substep.py [REFERENCE_ROOT]
+    python tests/golden/make_substep.py REFERENCE_ROOT
 """
 import dataclasses
 import os
@@ -40,6 +40,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from tests.golden.refroot import reference_root  # noqa: E402
 
 from tests import small_scenes as SS  # noqa: E402
 from tests.golden import ti_numpy as ti  # noqa: E402
@@ -236,7 +238,7 @@ def run_rope(env, st, n_sub=1):
 
 def main():
     global PKG
-    PKG = os.path.join(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", "difftactile")
+    PKG = os.path.join(reference_root(), "difftactile")
     f32 = lambda a: np.asarray(a, np.float32)  # noqa: E731 - the inputs are float32 values
     out = {}
     for name, env in scenes().items():

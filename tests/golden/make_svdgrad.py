@@ -5,7 +5,7 @@ ti.svd) read out of the reference source with `ast` and run in float64 through t
 module of this folder (ti_numpy.py), on 64 seeded decompositions with seeded adjoints of U, S
 (diagonal, as the substep produces it) and V.  Inputs and outputs go to tests/golden/svdgrad_ref.npz.
 
-    python tests/golden/make_svdgrad.py [REFERENCE_ROOT]
+    python tests/golden/make_svdgrad.py REFERENCE_ROOT
 """
 import os
 import sys
@@ -16,11 +16,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
+from tests.golden.refroot import reference_root  # noqa: E402
+
 from tests.golden import ti_numpy as ti  # noqa: E402
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_root()
     src = os.path.join(ref, "difftactile", "object_model", "mpm_elastic.py")
     rng = np.random.default_rng(9)
     n = 64
