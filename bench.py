@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="batched_population", choices=["batched_population", "sensor_press"])
+    ap.add_argument("--config", default="batched_population", choices=["batched_population", "sensor_press",
+                                                                        "rope_pads"])
     ap.add_argument("--horizon", type=int, default=None, help="control steps (default: the config's)")
     ap.add_argument("--envs", type=int, default=None, help="batched_population: the first N environments only")
     ap.add_argument("--plain", type=int, default=8,
@@ -81,6 +82,8 @@ def make_config(name, horizon, envs=None):
     from difftactile_gb300 import configs
     if name == "sensor_press":
         return configs.sensor_press(n_steps=horizon or 100)
+    if name == "rope_pads":
+        return configs.rope_pads(n_steps=horizon or 500, n_envs=envs or 16)
     return configs.batched_population(n_steps=horizon or 200, n_envs=envs or 64)
 
 

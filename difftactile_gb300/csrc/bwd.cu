@@ -239,7 +239,7 @@ __device__ void integrate_bwd(const dt_world& w, int f, int i) {
 }
 
 template <int MODE, int NT>
-__global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
+__global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_BWD_G2P, NT)) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
   pdl_entry();
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(NT) k_bwd_g2p_fem(dt_world w, int f, int nb_p,
 // ---------------------------------------------------------------------------------------------
 // B2: grid op + contact adjoint
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(GRID_NT) k_bwd_grid(dt_world w, int f) {
+__global__ void __launch_bounds__(GRID_NT, DT_MINB(DT_MINB_BWD_GRID, GRID_NT)) k_bwd_grid(dt_world w, int f) {
   pdl_entry();
   const int cnt = min(w.tape_bcount[f], w.tape_blocks);
   const int l = threadIdx.x;

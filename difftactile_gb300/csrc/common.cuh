@@ -6,6 +6,27 @@
 
 #define DT_DEV __device__ __forceinline__
 
+// Minimum resident CTAs per SM of the particle kernels, stated for 128-thread CTAs (the register cap
+// follows: 65536 / (128 * n)); 0 leaves the register count to the compiler.  Measured on the
+// 64-environment population (one forward + backward substep at mid-rollout): capping the forward P2G
+// at 72 registers (from 80; 44-84 B of spills), G2P at 64 (from 72), the G2P adjoint at 80 (from 96)
+// and the grid adjoint at 64 (from 96) raises the resident warps enough to take the substep from 3.50
+// to 2.97 ms; a 64-register forward P2G times the same as 72 with more spills
+#ifndef DT_MINB_FWD_P2G
+#define DT_MINB_FWD_P2G 7
+#endif
+#ifndef DT_MINB_FWD_G2P
+#define DT_MINB_FWD_G2P 8
+#endif
+#ifndef DT_MINB_BWD_G2P
+#define DT_MINB_BWD_G2P 6
+#endif
+#ifndef DT_MINB_BWD_GRID
+#define DT_MINB_BWD_GRID 8
+#endif
+// the launch-bounds minimum of a CTA of NT threads for a per-128-thread minimum n
+#define DT_MINB(n, NT) ((n) > 0 ? ((n) * 128 + (NT) - 1) / (NT) : 1)
+
 // ------------------------------------------------------------------------------------------
 // small fixed-size linear algebra, row-major, fully unrolled into registers
 // ------------------------------------------------------------------------------------------

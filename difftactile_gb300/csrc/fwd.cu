@@ -201,7 +201,7 @@ __device__ void tri_centroid(const dt_world& w, int f, int t) {
 }
 
 template <int MODE, int NT>
-__global__ void __launch_bounds__(NT) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
+__global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_FWD_P2G, NT)) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
   pdl_entry();
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
@@ -455,7 +455,7 @@ __device__ void fem_integrate(const dt_world& w, int f, int i) {
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT) k_fwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
+__global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_FWD_G2P, NT)) k_fwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
   pdl_entry();
   int b = blockIdx.x;
   if (b < nb_p) {

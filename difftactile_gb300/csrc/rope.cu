@@ -22,7 +22,7 @@
 namespace {
 
 constexpr int RC_NT = 256;  // contact: 64 particles x 4 lanes
-constexpr int RS_NT = 256;  // solver: one CTA per rope
+constexpr int RS_NT = 1024;  // solver: one CTA per rope (about two particles per thread for 2,000)
 constexpr int SMEM_CENT_MAX = 12288;  // triangle centroids staged in shared memory (192 KB)
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 inline int launched() { return launch_status(cudaGetLastError()); }
