@@ -72,6 +72,8 @@ def parse():
                     "reading the forward's from the tape")
     ap.add_argument("--no-graph", action="store_true", help="launch every substep from the host instead of "
                     "replaying the rollout's recorded CUDA graphs")
+    ap.add_argument("--rebin", type=int, default=1,
+                    help="checkpointed rollouts: sort the particles by cell again at every N-th checkpoint (0: never)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the gradient check")
     ap.add_argument("--no-nested", action="store_true", help="skip the nested sensor-press measurement")
@@ -175,6 +177,8 @@ def build(cfg, dev, args, **extra):
         kw["scatter_depth"] = args.depth
     if args.lanes is not None:
         kw["contact_lanes"] = args.lanes
+    if args.rebin and cfg.ckpt_every > 0:
+        kw["rebin_every"] = args.rebin
     return cfg.build(dev, **kw)
 
 
@@ -492,6 +496,7 @@ def run_ours(args):
                       "control_steps": cfg.n_steps, "substeps": cfg.substeps,
                       "grids": sorted({e.n_grid[0] for e in cfg.envs}), "fem_tets": w.n_tets, "fem_nodes": w.n_verts,
                       "surface_tris": w.n_tris, "checkpoint_every": cfg.ckpt_every, "tape_blocks": w.tape_blocks,
+                      "rebin_every": int(getattr(traj, "rebin_every", 0)),
                       "scatter": ["tile", "global", "warp"][w.w.scatter_mode], "p_block": int(w.w.p_block),
                       "scatter_depth": int(w.w.scatter_depth),
                       "contact_lanes": 4 if int(w.w.contact_lanes) == 4 else 8,

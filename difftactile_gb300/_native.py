@@ -94,6 +94,9 @@ SIGNATURES = {
     "dt_substep_fwd": (C.c_int, [_W, C.c_int, _P]),
     "dt_substep_fwd_stage": (C.c_int, [_W, C.c_int, C.c_int, _P]),
     "dt_substep_fwd_noalloc": (C.c_int, [_W, C.c_int, _P]),
+    "dt_rebin_scratch_bytes": (C.c_size_t, [_W]),
+    "dt_rebin": (C.c_int, [_W, C.c_int, _P, _P, _P, _P]),
+    "dt_rebin_permute": (C.c_int, [_W, C.c_int, C.c_int, _P, _P, _P, _P]),
     "dt_p2g": (C.c_int, [_W, C.c_int, _P]),
     "dt_fem_update": (C.c_int, [_W, C.c_int, _P]),
     "dt_grid_op": (C.c_int, [_W, C.c_int, _P]),

@@ -43,13 +43,15 @@ class Config:
     def n_particles(self):
         return sum(e.n_particles for e in self.envs)
 
-    def build(self, device="cuda", **world_kw):
-        """World sized for this configuration's rollout and its PoseTrajectory."""
+    def build(self, device="cuda", rebin_every: int = 0, **world_kw):
+        """World sized for this configuration's rollout and its PoseTrajectory (``rebin_every``: see
+        Trajectory; checkpointed configurations only)."""
         from .trajectory import PoseTrajectory
         from .world import World
         nf = PoseTrajectory.frames_needed(self.n_steps, self.substeps, self.ckpt_every)
         w = World(self.envs, n_frames=nf, dt=self.dt, device=device, tape_blocks=self.tape_blocks, **world_kw)
-        return w, PoseTrajectory(w, self.n_steps, self.ckpt_every, self.loss_terms, rope_terms=self.rope_terms)
+        return w, PoseTrajectory(w, self.n_steps, self.ckpt_every, self.loss_terms, rope_terms=self.rope_terms,
+                                 rebin_every=rebin_every)
 
 
 def _press_env(n_grid=96, box_cells=20, pad=(20, 20, 5), pad_h=0.0125, seed=1, yield_stress=50.0, E=5e3, nu=0.3,

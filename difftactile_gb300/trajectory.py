@@ -59,6 +59,12 @@ class Trajectory:
     final frame; ``rope_terms``: list of (rope, target [3]) terms |tip - target|^2 of the rope's last
     particle at the final frame (the cable task's tip-position loss).
 
+    ``rebin_every`` = r >= 1 (checkpointed trajectories only): at the start of every r-th segment after
+    the first, before its checkpoint is saved, the particles are sorted by cell again (World.rebin), so
+    that the scatters' same-cell runs survive long horizons; the permutation of each such checkpoint is
+    kept, and the backward sweep, having reached the segment's first frame, maps the particle adjoint
+    (and the material index) back to the previous segment's order.  0: the construction order is kept.
+
     ``graph``: the launch sequence of a forward (and of a backward) is the same on every call, so the
     first call runs eagerly and then records it as a CUDA graph; later calls copy the new controls
     into the recorded buffer and replay the graph (one launch from the host per rollout).  The
@@ -67,7 +73,7 @@ class Trajectory:
     """
 
     def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=(), graph: bool = False,
-                 rope_terms=()):
+                 rope_terms=(), rebin_every: int = 0):
         self.w = world
         self.graph = bool(graph)
         self._graphs = {}     # "fwd" / ("bwd", loss_bar) -> torch.cuda.CUDAGraph
@@ -92,6 +98,13 @@ class Trajectory:
             self.ck_p = torch.zeros((self.n_ck, 6, Np, 4), device=dev)
             self.ck_v = torch.zeros((self.n_ck, 3, V, 4), device=dev)
             self.ck_r = torch.zeros((self.n_ck, 2, NR, 4), device=dev)
+        self.rebin_every = int(rebin_every)
+        if self.rebin_every < 0 or (self.rebin_every and self.full):
+            raise ValueError("rebin_every needs a checkpointed trajectory (ckpt_every >= 1) and must be >= 0")
+        self.ck_src = (torch.zeros((self.n_ck, Np), dtype=torch.int32, device=dev) if self.rebin_every else None)
+        self._epoch = 0  # the re-binned segment (0: none) whose particle order the world holds
+        self._fin = None  # checkpointed: a copy of the final frame (the backward sweep overwrites it)
+        self._fin_live = False
         if not self.full and self.k > 1:
             self.seg_p = torch.zeros((self.k, 6, Np, 4), device=dev)
             self.seg_v = torch.zeros((self.k, 3, V, 4), device=dev)
@@ -145,6 +158,54 @@ class Trajectory:
         t["v_vel"][0].copy_(Vv[i, 1])
         t["v_vpos"][0].copy_(Vv[i, 2])
         t["r_state"][0].copy_(Rr[i])
+
+    # ------------------------------------------------------------------ particle order (rebin_every)
+    def _rebinned(self, seg: int) -> bool:
+        return self.rebin_every > 0 and seg > 0 and seg % self.rebin_every == 0
+
+    def _epoch_of(self, seg: int) -> int:
+        """The re-binned segment whose order segment ``seg`` runs in (0: the rollout's start order)."""
+        return (seg // self.rebin_every) * self.rebin_every if self.rebin_every else 0
+
+    def _to_epoch(self, e: int):
+        """Bring the world's material index and slot maps (not its state or adjoints) to the order of
+        re-binned segment ``e``, through the stored permutations of the segments in between."""
+        while self._epoch < e:
+            self._epoch += self.rebin_every
+            self.w.rebin_permute(self.ck_src[self._epoch], inverse=False)
+            self.launches += 1
+        while self._epoch > e:
+            self.w.rebin_permute(self.ck_src[self._epoch], inverse=True)
+            self.launches += 1
+            self._epoch -= self.rebin_every
+
+    def _final_frame_ready(self):
+        """A checkpointed backward sweep recomputes each step on the world's frames and so overwrites
+        the final frame the loss adjoint is seeded from: keep a copy of it before the first sweep after
+        a forward, put it back before every later one (a second backward, or one after adjoint_at)."""
+        if self.full:
+            return
+        if self._fin_live:
+            if self._fin is None:
+                dev, Np, V, NR = self.w.device, self.w.n_particles, self.w.n_verts, self.w.n_rope_particles
+                self._fin = (torch.zeros((1, 6, Np, 4), device=dev), torch.zeros((1, 3, V, 4), device=dev),
+                             torch.zeros((1, 2, NR, 4), device=dev))
+            self._save(*self._fin, 0)  # the forward left the final state in frames 0 and S
+            self._fin_live = False
+        elif self._fin is not None:
+            self._load(*self._fin, 0)
+            self.w.copy_frame(0, self.S)
+        else:
+            raise RuntimeError("the backward sweep needs a forward rollout first")
+
+    def _leave_segment(self, seg: int):
+        """The backward sweep reached segment ``seg``'s first frame: map the adjoint of that frame (the
+        buffer the previous segment's last step reads) and the material index back to the order the
+        previous segment ran in."""
+        if self._rebinned(seg):
+            self.w.rebin_permute(self.ck_src[seg], inverse=True, adj_buf=self.S & 1)
+            self.launches += 1
+            self._epoch = self._epoch_of(seg - 1)
 
     # ------------------------------------------------------------------ one control step
     def _f0(self, t):
@@ -202,6 +263,10 @@ class Trajectory:
             self.launches += 1
         for t in range(self.T):
             if not self.full and t % self.k == 0:
+                if self._rebinned(t // self.k):
+                    self.w.rebin(0, self.ck_src[t // self.k])
+                    self._epoch = t // self.k
+                    self.launches += 8
                 self._save(self.ck_p, self.ck_v, self.ck_r, t // self.k)
             self._step(t, tape=self.full)  # checkpointed: the backward sweep recomputes each step's tape
         self.readout()
@@ -213,14 +278,18 @@ class Trajectory:
         self.actions = actions.detach().double().requires_grad_(True)
         self.ctrl = self.controls(self.actions)
         c32 = self.ctrl.detach().float().contiguous()
+        self._epoch = 0  # the world's present particle order is this rollout's start order
         if self.graph and "fwd" in self._graphs:
             self.ctrl32.copy_(c32)
             self._replay("fwd")
+            self._epoch = self._epoch_of(self.n_ck - 1)
+            self._fin_live = True
             return self.loss
         self.ctrl32 = c32
         self._forward_body()
         if self.graph:
             self._capture("fwd", self._forward_body)
+        self._fin_live = True
         return self.loss
 
     def readout(self) -> torch.Tensor:
@@ -252,15 +321,19 @@ class Trajectory:
         """Adjoint sweep; returns d loss / d actions (float64, the actions' shape).  Initial-state
         adjoints are left in the world's frame-0 adjoint buffers, material grads in mat_adj."""
         key = ("bwd", float(loss_bar))
+        self._to_epoch(self._epoch_of(self.n_ck - 1))  # after adjoint_at the world may hold an earlier order
+        self._final_frame_ready()
         if self.graph and key in self._graphs:
             self._replay(key)
+            self._epoch = 0
         else:
             if self.ctrl_bar is None or self.ctrl_bar.shape != self.ctrl32.shape:
                 self.ctrl_bar = torch.zeros_like(self.ctrl32)
             self._backward_body(loss_bar)
             if self.graph:
                 self._capture(key, lambda: self._backward_body(loss_bar))
-        (g,) = torch.autograd.grad(self.ctrl, self.actions, self.ctrl_bar.double())
+        # the action -> control graph is kept: a second sweep of the same forward differentiates it again
+        (g,) = torch.autograd.grad(self.ctrl, self.actions, self.ctrl_bar.double(), retain_graph=True)
         return g
 
     def material_grad(self) -> torch.Tensor:
@@ -285,10 +358,13 @@ class Trajectory:
         ``t`` (host-launched, no graph) and stop there: the step's forward tape (frames of step t, its
         grid tape) is valid and the adjoint of its frame f + 1 is in the world's adjoint buffers
         ((f + 1) & 1).  Returns the world frame index of step t's frame f.  For inspecting gradients
-        mid-rollout (the adjoint of one substep from a real loss); a following backward() starts over."""
+        mid-rollout (the adjoint of one substep from a real loss); a following backward() starts over
+        (from the final frame of the last forward, which is kept for it)."""
         if not (0 <= t < self.T and 0 <= f < self.S):
             raise ValueError(f"(t, f) = ({t}, {f}) outside [0, {self.T}) x [0, {self.S})")
         w = self.w
+        self._to_epoch(self._epoch_of(self.n_ck - 1))
+        self._final_frame_ready()
         w.adj_clear()
         for s, layer, tg in self.loss_terms:
             N.check(w.lib.dt_marker_loss_bwd(w.wp, s, self.f_end, layer, tg.data_ptr(), float(loss_bar), w.stream),
@@ -300,7 +376,8 @@ class Trajectory:
 
         def stop(tt):
             f0 = self._f0(tt)
-            w.substeps_bwd(f0 + self.S, f0 + f + 1)
+            if f + 1 < self.S:  # (f = S - 1: the adjoint of frame S is the step's incoming one)
+                w.substeps_bwd(f0 + self.S, f0 + f + 1)
             return f0 + f
 
         if self.full:
@@ -327,6 +404,7 @@ class Trajectory:
                 if self.S & 1:
                     for name in ("p_adj", "v_adj_pos", "v_adj_vel", "v_adj_vpos", "r_adj"):
                         w.t[name][1].copy_(w.t[name][0])
+            self._leave_segment(seg)
         raise AssertionError("unreachable")
 
     def _backward_body(self, loss_bar):
@@ -357,6 +435,7 @@ class Trajectory:
                 if self.S & 1:  # frame 0's adjoint (buffer 0) is frame S's of the previous step (buffer 1)
                     for name in ("p_adj", "v_adj_pos", "v_adj_vel", "v_adj_vpos", "r_adj"):
                         w.t[name][1].copy_(w.t[name][0])
+            self._leave_segment(seg)
 
 
 class PoseTrajectory(Trajectory):
@@ -364,8 +443,8 @@ class PoseTrajectory(Trajectory):
     [T, n_sensors, 6] = (d_pos[3], d_ori[3] in degrees per unit time)."""
 
     def __init__(self, world: World, n_steps: int, ckpt_every: int = 1, loss_terms=(), graph: bool = False,
-                 rope_terms=()):
-        super().__init__(world, n_steps, ckpt_every, loss_terms, graph, rope_terms)
+                 rope_terms=(), rebin_every: int = 0):
+        super().__init__(world, n_steps, ckpt_every, loss_terms, graph, rope_terms, rebin_every)
         dev = world.device
         self.inv_T = 1.0 / (world.dt * self.S)
         Ms = [sp.trans_world if sp.trans_world is not None else np.eye(4) for sp in world.sensor_specs]
@@ -417,8 +496,8 @@ class GripperTrajectory(Trajectory):
     GripperKinematics; ``fingers`` the two sensors' indices in the world."""
 
     def __init__(self, world: World, n_steps: int, kin, fingers=(0, 1), ckpt_every: int = 1, loss_terms=(),
-                 graph: bool = False, rope_terms=()):
-        super().__init__(world, n_steps, ckpt_every, loss_terms, graph, rope_terms)
+                 graph: bool = False, rope_terms=(), rebin_every: int = 0):
+        super().__init__(world, n_steps, ckpt_every, loss_terms, graph, rope_terms, rebin_every)
         self.kin = kin
         self.fingers = tuple(fingers)
         dev = world.device

@@ -117,11 +117,14 @@ class World:
         self.n_envs = len(envs)
         self.n_particles = p_off
         self.n_nodes, self.n_blocks = node_off, blk_off
-        self.perm = np.concatenate(perm) if perm else np.zeros(0, np.int64)  # sorted slot -> user index
+        # construction order: sorted slot -> user index (the device copies below follow later re-binning)
+        self.perm = np.concatenate(perm) if perm else np.zeros(0, np.int64)
         self.inv_perm = np.empty_like(self.perm)
         self.inv_perm[self.perm] = np.arange(len(self.perm))
-        self._perm_t = torch.as_tensor(self.perm, device=dev)
+        self._perm_t = torch.as_tensor(self.perm, device=dev)  # current slot -> user index (follows rebin)
         self._inv_perm_t = torch.as_tensor(self.inv_perm, device=dev)
+        self._slot_t = torch.arange(len(self.perm), device=dev)
+        self._rb_scratch = None
         self.env_rows = env_rows
 
         # ---------------- sensors ----------------
@@ -607,6 +610,43 @@ class World:
     def copy_frame(self, src, dst):
         self.call("dt_copy_frame", int(src), int(dst))
         self.touch(dst)
+
+    # ---- particle re-binning (dt_rebin): the slot order follows the cells again ----
+    def _rebin_scratch(self) -> torch.Tensor:
+        if self._rb_scratch is None:
+            n = int(self.lib.dt_rebin_scratch_bytes(self.wp))
+            self._rb_scratch = torch.empty(max(n, 256), dtype=torch.uint8, device=self.device)
+        return self._rb_scratch
+
+    def _perm_follow(self, s: torch.Tensor, inverse: bool):
+        """slot -> user index (and its inverse) after the slots were permuted by s (new j <- old s[j])."""
+        if inverse:
+            tmp = torch.empty_like(self._perm_t)
+            tmp[s] = self._perm_t
+            self._perm_t.copy_(tmp)
+        else:
+            self._perm_t.copy_(self._perm_t[s])
+        self._inv_perm_t[self._perm_t] = self._slot_t
+
+    def rebin(self, frame: int, src: torch.Tensor):
+        """Sort the particles of ``frame`` by cell: ``src`` ([n_particles] int32, on the device) receives
+        the permutation (new slot j <- old slot src[j]); the frame's records, the material index and the
+        slot <-> caller-index maps follow it.  Other frames, the tapes and the adjoints keep the old
+        order: re-bin a frame the next substeps start from."""
+        if src.dtype != I32 or src.numel() != self.n_particles or not src.is_contiguous():
+            raise ValueError("src must be a contiguous int32 tensor of n_particles entries")
+        self.call("dt_rebin", int(frame), self.t["p_mat"].data_ptr(), src.data_ptr(),
+                  self._rebin_scratch().data_ptr())
+        self._perm_follow(src.long(), False)
+        self.touch()
+
+    def rebin_permute(self, src: torch.Tensor, inverse: bool, adj_buf: int = -1):
+        """Apply a rebin's permutation (``inverse``: undo it) to the material index, the slot maps and,
+        for ``adj_buf`` 0 or 1, to that particle adjoint buffer."""
+        self.call("dt_rebin_permute", int(adj_buf), int(bool(inverse)), self.t["p_mat"].data_ptr(), src.data_ptr(),
+                  self._rebin_scratch().data_ptr())
+        self._perm_follow(src.long(), bool(inverse))
+        self.touch()
 
     def adj_clear(self):
         self.call("dt_adj_clear")

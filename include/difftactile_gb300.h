@@ -302,6 +302,28 @@ int dt_substep_fwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
  * nothing (no cudaMalloc, cudaFree or allocating library routine). */
 int dt_substep_fwd_noalloc(const dt_world* w, int f, cudaStream_t stream);
 
+/* ---- particle re-binning (keeps the particles sorted by cell over a rollout) ----
+ * Replaces nothing in the reference, whose particle loops visit particles in their fixed order
+ * (mpm_elastic.py:176-208); the scatter here merges same-cell runs of consecutive particles, which
+ * the material's motion breaks up.  dt_rebin sorts the particles of frame f by the grid node of their
+ * base cell (block-major node order; within a cell by current slot): src[j] = the current slot of
+ * new slot j ([n_particles] device ints, written).  It permutes frame f's particle records and
+ * p_mat (which must be the buffer w->p_mat points to: the material index follows its particle)
+ * accordingly.  Every other frame, the SVD tape and the adjoints are not touched: re-bin only a frame
+ * from which the next substeps start, with no tape frame before it still to be read in this order.
+ * Requirements: the environments' node ranges (node_off) increase with the environment index, as
+ * their particle ranges do (the sort then keeps every particle in its environment's range).
+ * scratch: dt_rebin_scratch_bytes(w) bytes of device memory, 256-byte aligned.
+ * Cells that hold more than 256 particles keep the (unordered) placement of the atomics. */
+size_t dt_rebin_scratch_bytes(const dt_world* w);
+int dt_rebin(const dt_world* w, int f, int* p_mat, int* src, void* scratch, cudaStream_t stream);
+/* Applies the permutation src of a dt_rebin (inverse = 0: new[j] = old[src[j]]; inverse = 1:
+ * old[src[j]] = new[j]) to p_mat and, for buf = 0 or 1, to the particle adjoint buffer p_adj[buf]
+ * (buf = -1: p_mat only).  The backward sweep crosses a re-binning of frame f with inverse = 1 on the
+ * buffer that holds frame f's adjoint: the adjoint then follows the order before the re-binning. */
+int dt_rebin_permute(const dt_world* w, int buf, int inverse, int* p_mat, const int* src, void* scratch,
+                     cudaStream_t stream);
+
 /* The same substep split into the reference's per-object calls, for drop-in use of the
  * reference method sequence.  dt_substep_fwd(f) == p2g(f); fem_update(f); grid_op(f) (which
  * includes check_grid_occupy, check_collision and collision); rope_update(f); g2p(f);

@@ -74,31 +74,65 @@ class FakeWorld:
         self.sensor_rows = [types.SimpleNamespace(nv=NV)]
         self.t = {k: torch.zeros((n_frames,) + s) for k, s in zip(STATE, SHAPES)}
         self.t.update({k: torch.zeros((2,) + s) for k, s in zip(ADJ, SHAPES)})
+        # slot j holds particle p_mat[j] (the CUDA world's material index plays this part: it follows its
+        # particle through a re-binning); the system runs in particle order, whatever the slot order
+        self.t["p_mat"] = torch.arange(NP, dtype=torch.int32)
+        self.rebins = 0
         self.cv = torch.zeros((n_frames, NC))
         self.adj_cv = torch.zeros((n_frames, NC))
         self.lib = FakeLib(self)
         self.calls = []
         self.taped = [False] * n_frames
 
+    def _canon(self, k, x):
+        """particle-order view of a slot-ordered particle tensor [6, NP, 4]"""
+        return x[:, torch.argsort(self.t["p_mat"].long())] if k in ("p_state", "p_adj") else x
+
+    def _slots(self, k, x):
+        return x[:, self.t["p_mat"].long()] if k in ("p_state", "p_adj") else x
+
     def z(self, f):
-        return torch.cat([self.t[k][f].reshape(-1) for k in STATE])
+        return torch.cat([self._canon(k, self.t[k][f]).reshape(-1) for k in STATE])
 
     def set_z(self, f, z):
         o = 0
         for k in STATE:
             n = self.t[k][f].numel()
-            self.t[k][f].copy_(z[o:o + n].reshape(self.t[k][f].shape))
+            self.t[k][f].copy_(self._slots(k, z[o:o + n].reshape(self.t[k][f].shape)))
             o += n
 
     def adj(self, b):
-        return torch.cat([self.t[k][b].reshape(-1) for k in ADJ])
+        return torch.cat([self._canon(k, self.t[k][b]).reshape(-1) for k in ADJ])
 
     def set_adj(self, b, a):
         o = 0
         for k in ADJ:
             n = self.t[k][b].numel()
-            self.t[k][b].copy_(a[o:o + n].reshape(self.t[k][b].shape))
+            self.t[k][b].copy_(self._slots(k, a[o:o + n].reshape(self.t[k][b].shape)))
             o += n
+
+    def rebin(self, frame, src):
+        """World.rebin's contract: src[j] = the old slot of new slot j (here: slots sorted by the first
+        coordinate); frame's records and the slot -> particle map follow it, nothing else does."""
+        src.copy_(torch.argsort(self.t["p_state"][frame, 0, :, 0], stable=True).to(torch.int32))
+        s = src.long()
+        self.rebins += int(not torch.equal(s, torch.arange(NP)))
+        self.t["p_state"][frame].copy_(self.t["p_state"][frame][:, s])
+        self.t["p_mat"].copy_(self.t["p_mat"][s])
+
+    def rebin_permute(self, src, inverse, adj_buf=-1):
+        s = src.long()
+
+        def perm(x):  # x indexed by slot along dim 0
+            if not inverse:
+                return x[s]
+            out = torch.empty_like(x)
+            out[s] = x
+            return out
+
+        self.t["p_mat"].copy_(perm(self.t["p_mat"]))
+        if adj_buf >= 0:
+            self.t["p_adj"][adj_buf].copy_(perm(self.t["p_adj"][adj_buf].transpose(0, 1)).transpose(0, 1))
 
     tape_on = True
 
@@ -175,10 +209,50 @@ def test_schedule_gives_the_rollouts_gradient(T, S, k):
     assert float((g - g_ref).norm() / g_ref.norm()) < 1e-4
     gz = w.adj(0).double()                          # initial-state adjoint in frame 0's buffer
     assert float((gz - gz_ref).norm() / gz_ref.norm()) < 1e-4
+    # a second sweep of the same forward, and one after adjoint_at stopped mid-rollout (both re-run the
+    # steps over the world's frames: the final frame the loss adjoint starts from is kept for them)
+    assert float((tr.backward() - g_ref).norm() / g_ref.norm()) < 1e-4
+    tr.adjoint_at(T - 1, S - 1)
+    tr.adjoint_at(T // 2, 0)
+    assert float((tr.backward() - g_ref).norm() / g_ref.norm()) < 1e-4
     # a second rollout from the same start repeats the first (checkpoints are rewritten, not appended)
     w.set_z(0, sys.z0.float())
     assert abs(float(tr.forward(actions)) - L) <= 1e-6 * abs(L)
     assert float((tr.backward() - g).abs().max()) <= 1e-6 * float(g.abs().max())
+
+
+@pytest.mark.parametrize("T,S,k,r", [(6, 3, 1, 1), (6, 4, 1, 2), (7, 3, 2, 1), (7, 2, 3, 1), (9, 1, 2, 2)])
+def test_rebinning_schedule_gives_the_rollouts_gradient(T, S, k, r):
+    """Checkpointed rollouts that re-sort the particle slots at checkpoints (rebin_every = r) give
+    autograd's action and initial-state gradients: every re-binning the backward sweep crosses is
+    undone on the adjoint it carries and on the slot -> particle map; the slot order at the end of the
+    sweep is the rollout's start order again.  Also after adjoint_at left the world mid-rollout."""
+    sys = System(seed=T * 100 + S * 10 + k + r)
+    actions = torch.randn(T, NC, generator=torch.Generator().manual_seed(7), dtype=torch.float64)
+    w = FakeWorld(Trajectory.frames_needed(T, S, k), sys)
+    w.set_z(0, sys.z0.float())
+    tr = LinearTrajectory(w, T, ckpt_every=k, loss_terms=[(0, 0, np.zeros((NV, 3)))], rebin_every=r)
+    w.lib.traj = tr
+    L = float(tr.forward(actions))
+    assert w.rebins > 0
+    g = tr.backward()
+    L_ref, g_ref, gz_ref = autograd_reference(sys, actions, S)
+    assert abs(L - L_ref) <= 1e-4 * abs(L_ref)
+    assert float((g - g_ref).norm() / g_ref.norm()) < 1e-4
+    assert float((w.adj(0).double() - gz_ref).norm() / gz_ref.norm()) < 1e-4
+    assert torch.equal(w.t["p_mat"], torch.arange(NP, dtype=torch.int32))
+    # inspect an adjoint mid-rollout, then a full backward again from the same forward
+    w.set_z(0, sys.z0.float())
+    tr.forward(actions)
+    tr.adjoint_at(T // 2, 0)
+    assert float((tr.backward() - g_ref).norm() / g_ref.norm()) < 1e-4
+    assert torch.equal(w.t["p_mat"], torch.arange(NP, dtype=torch.int32))
+
+
+def test_rebinning_needs_checkpoints():
+    sys = System()
+    with pytest.raises(ValueError, match="rebin_every"):
+        LinearTrajectory(FakeWorld(Trajectory.frames_needed(4, 3, 0), sys), 4, ckpt_every=0, rebin_every=1)
 
 
 def test_checkpoint_storage_per_mode():
