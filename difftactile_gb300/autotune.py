@@ -13,6 +13,9 @@ scene (particle count and density, how many environments share the launch):
   lanes     lanes per active grid node in the contact search (dt_world.contact_lanes): 8 shortens
             each node's dependent chain (latency-bound launches), 4 issues fewer instructions per node
             (throughput-bound launches);
+  ppt       particles per thread of the particle-role launches (dt_world.p_per_thread): each CTA
+            takes 1 or 2 consecutive chunks of p_block particles (fewer, longer-lived CTAs; the second
+            chunk finds the first one's grid neighbourhood in L1);
   pdl       programmatic dependent launch of the substep kernels (dt_set_pdl, library-wide).
 
 ``tune_substep`` times every candidate on one forward + backward substep of the world at a chosen
@@ -31,21 +34,22 @@ import statistics
 import torch
 
 SCATTERS = {"tile": 0, "global": 1, "warp": 2}
-DEFAULT = {"scatter": "warp", "p_block": 128, "depth": 0, "lanes": 8, "pdl": 1}
+DEFAULT = {"scatter": "warp", "p_block": 128, "depth": 0, "lanes": 8, "pdl": 1, "ppt": 1}
 
 _cache: dict[str, dict] = {}
 
 
 def candidates(scatters=("warp", "global", "tile"), p_blocks=(64, 128, 256), depths=(0, 1, 2), lanes=(8, 4),
-               pdl=(1, 0)):
+               pdl=(1, 0), ppts=(1, 2)):
     out = []
     for s in scatters:
         for b in (p_blocks if s != "tile" else (128,)):
             for d in (depths if s == "warp" else (0,)):
                 for ln in lanes:
                     for p in pdl:
-                        out.append({"scatter": s, "p_block": int(b), "depth": int(d), "lanes": int(ln),
-                                    "pdl": int(p)})
+                        for k in ppts:
+                            out.append({"scatter": s, "p_block": int(b), "depth": int(d), "lanes": int(ln),
+                                        "pdl": int(p), "ppt": int(k)})
     return out
 
 
@@ -55,6 +59,7 @@ def apply(world, cfg: dict):
     world.w.p_block = int(cfg["p_block"])
     world.w.scatter_depth = int(cfg.get("depth", 0))
     world.w.contact_lanes = int(cfg.get("lanes", 8))
+    world.w.p_per_thread = int(cfg.get("ppt", 1))
     world.lib.dt_set_pdl(int(cfg["pdl"]))  # returns the previous setting
 
 
@@ -62,7 +67,7 @@ def current(world) -> dict:
     inv = {v: k for k, v in SCATTERS.items()}
     return {"scatter": inv.get(int(world.w.scatter_mode), "warp"), "p_block": int(world.w.p_block) or 128,
             "depth": int(world.w.scatter_depth), "lanes": 4 if int(world.w.contact_lanes) == 4 else 8,
-            "pdl": int(world.lib.dt_get_pdl())}
+            "pdl": int(world.lib.dt_get_pdl()), "ppt": max(1, int(world.w.p_per_thread))}
 
 
 def signature(world, tag: str = "") -> str:
@@ -161,4 +166,5 @@ def tune_substep(world, frame: int = 0, **kw) -> dict:
 
 def label(c: dict) -> str:
     depth = f"/d{c.get('depth', 0)}" if c["scatter"] == "warp" else ""
-    return f"{c['scatter']}/{c['p_block']}{depth}/l{c.get('lanes', 8)}/{'pdl' if c['pdl'] else 'nopdl'}"
+    ppt = f"/ppt{c['ppt']}" if c.get("ppt", 1) != 1 else ""
+    return f"{c['scatter']}/{c['p_block']}{depth}/l{c.get('lanes', 8)}/{'pdl' if c['pdl'] else 'nopdl'}{ppt}"

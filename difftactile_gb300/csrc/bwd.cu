@@ -238,14 +238,23 @@ __device__ void integrate_bwd(const dt_world& w, int f, int i) {
   if (S.carry) *cvb_n = v3to4(cvbn);
 }
 
-template <int MODE, int NT>
+template <int MODE, int NT, int PPT>
 __global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_BWD_G2P, NT)) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
   pdl_entry();
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
-    g2p_bwd_chunk<MODE, NT>(w, f, b, tile, sh);
+    if (PPT == 1) {
+      g2p_bwd_chunk<MODE, NT>(w, f, b, tile, sh);
+    } else {
+      int c0, c1;
+      cta_chunks(w, NT, PPT, b, c0, c1);
+      for (int c = c0; c < c1; ++c) {
+        if (c > c0) __syncthreads();  // the shared tile and flags of the previous chunk
+        g2p_bwd_chunk<MODE, NT>(w, f, c, tile, sh);
+      }
+    }
     return;
   }
   b -= nb_p;
@@ -707,34 +716,44 @@ __device__ void fem_tet_bwd(const dt_world& w, int f, int t) {
   red_add_v4(aPos + tv.w, v3to4(-((ab + bb) + cbv)));
 }
 
+// P2G adjoint of particle p (all 32 lanes of the warp call it: the material grads are summed over
+// the warp when it shares one material, then added with one atomic per warp)
+__device__ void p2g_bwd_particle(const dt_world& w, int f, int p) {
+  float mub = 0.f, lamb = 0.f;
+  int mat = -1;
+  if (p < w.n_particles) p2g_bwd(w, f, p, mub, lamb, mat);
+  const int m0 = __shfl_sync(0xffffffffu, mat, 0);
+  const bool same = __all_sync(0xffffffffu, mat == m0 || mat < 0);
+  if (same) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mub += __shfl_xor_sync(0xffffffffu, mub, o);
+      lamb += __shfl_xor_sync(0xffffffffu, lamb, o);
+    }
+    if ((threadIdx.x & 31) == 0 && m0 >= 0) {
+      atomicAdd(w.mat_adj + 4 * m0 + 0, mub);
+      atomicAdd(w.mat_adj + 4 * m0 + 1, lamb);
+    }
+  } else if (mat >= 0) {
+    atomicAdd(w.mat_adj + 4 * mat + 0, mub);
+    atomicAdd(w.mat_adj + 4 * mat + 1, lamb);
+  }
+}
+
 // nb_r > 0: the last nb_r CTAs restore frame f - 1's grid velocities for the next backward substep
 // (only stage 1 reads g_vout, so this overlaps stage 3 of frame f)
-template <int NT>  // 512 / NT CTAs per SM: 128 registers per thread
+template <int NT, int PPT>  // 512 / NT CTAs per SM: 128 registers per thread
 __global__ void __launch_bounds__(NT, 512 / NT) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v,
                                                              int nb_r) {
   pdl_entry();
   int b = blockIdx.x;
   if (b < nb_p) {
-    const int p = b * NT + threadIdx.x;
-    float mub = 0.f, lamb = 0.f;
-    int mat = -1;
-    if (p < w.n_particles) p2g_bwd(w, f, p, mub, lamb, mat);
-    // material grads: warp-aggregate when the warp shares one material
-    const int m0 = __shfl_sync(0xffffffffu, mat, 0);
-    const bool same = __all_sync(0xffffffffu, mat == m0 || mat < 0);
-    if (same) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        mub += __shfl_xor_sync(0xffffffffu, mub, o);
-        lamb += __shfl_xor_sync(0xffffffffu, lamb, o);
-      }
-      if ((threadIdx.x & 31) == 0 && m0 >= 0) {
-        atomicAdd(w.mat_adj + 4 * m0 + 0, mub);
-        atomicAdd(w.mat_adj + 4 * m0 + 1, lamb);
-      }
-    } else if (mat >= 0) {
-      atomicAdd(w.mat_adj + 4 * mat + 0, mub);
-      atomicAdd(w.mat_adj + 4 * mat + 1, lamb);
+    if (PPT == 1) {
+      p2g_bwd_particle(w, f, b * NT + threadIdx.x);
+    } else {
+      int c0, c1;
+      cta_chunks(w, NT, PPT, b, c0, c1);
+      for (int c = c0; c < c1; ++c) p2g_bwd_particle(w, f, c * NT + threadIdx.x);
     }
     return;
   }
@@ -762,12 +781,16 @@ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 inline int launched() { return launch_status(cudaGetLastError()); }
 
 // stage 1: G2P adjoint (particles) + integration adjoint (vertices)
-template <int MODE, int NT>
-cudaError_t b1(const dt_world* w, int f, cudaStream_t stream) {
-  const int nb_p = cdiv(w->n_particles, NT), nb_v = cdiv(w->n_verts, NT);
+template <int MODE, int NT, int PPT>
+cudaError_t b1_ppt(const dt_world* w, int f, cudaStream_t stream) {
+  const int nb_p = particle_ctas(w, NT, PPT), nb_v = cdiv(w->n_verts, NT);
   if (nb_p + nb_v == 0) return cudaSuccess;
   const size_t smem = MODE == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0;
-  return launch_k(k_bwd_g2p_fem<MODE, NT>, nb_p + nb_v, NT, smem, stream, *w, f, nb_p, nb_v);
+  return launch_k(k_bwd_g2p_fem<MODE, NT, PPT>, nb_p + nb_v, NT, smem, stream, *w, f, nb_p, nb_v);
+}
+template <int MODE, int NT>
+cudaError_t b1(const dt_world* w, int f, cudaStream_t stream) {
+  return per_thread(w) == 2 ? b1_ppt<MODE, NT, 2>(w, f, stream) : b1_ppt<MODE, NT, 1>(w, f, stream);
 }
 
 template <int MODE>
@@ -781,13 +804,17 @@ cudaError_t b1_nt(const dt_world* w, int f, cudaStream_t stream) {
 
 // stage 3: P2G / F adjoint (particles), tet adjoint, vertex hand-over; with `restore`, the last
 // CTAs also restore frame f - 1's grid velocities
-template <int NT>
-cudaError_t b3_nt(const dt_world* w, int f, bool restore, cudaStream_t stream) {
-  const int nb_p = cdiv(w->n_particles, NT), nb_v = cdiv(w->n_verts, NT), nb_t = cdiv(w->n_tets, NT);
+template <int NT, int PPT>
+cudaError_t b3_ppt(const dt_world* w, int f, bool restore, cudaStream_t stream) {
+  const int nb_p = particle_ctas(w, NT, PPT), nb_v = cdiv(w->n_verts, NT), nb_t = cdiv(w->n_tets, NT);
   const int per = NT / 64;  // 64-node blocks a restoring CTA copies per pass
   const int nb_r = !restore ? 0 : (w->n_blocks < 152 * 4 * per ? cdiv(w->n_blocks, per) : 152 * 4);
   if (nb_p + nb_t + nb_v + nb_r == 0) return cudaSuccess;
-  return launch_k(k_bwd_p2g_fem<NT>, nb_p + nb_t + nb_v + nb_r, NT, 0, stream, *w, f, nb_p, nb_t, nb_v, nb_r);
+  return launch_k(k_bwd_p2g_fem<NT, PPT>, nb_p + nb_t + nb_v + nb_r, NT, 0, stream, *w, f, nb_p, nb_t, nb_v, nb_r);
+}
+template <int NT>
+cudaError_t b3_nt(const dt_world* w, int f, bool restore, cudaStream_t stream) {
+  return per_thread(w) == 2 ? b3_ppt<NT, 2>(w, f, restore, stream) : b3_ppt<NT, 1>(w, f, restore, stream);
 }
 cudaError_t b3(const dt_world* w, int f, bool restore, cudaStream_t stream) {
   switch (particle_block(w)) {

@@ -174,25 +174,24 @@ DT_DEV v3 mTvec(const m3& m, v3 v) {
 // Correctly rounded divisions and square roots in the rotations: with approximate reciprocals the
 // factors reconstruct F only to ~2e-7, which the corotated stress 2 mu (F - R) F^T of a stiff material
 // near F = I amplifies (E = 4e5, F - R ~ 0.05: 1e-5 relative in the grid momentum; 6e-6 with these)
-DT_DEV void jacobi_rot(float S[3][3], float V[3][3], int p, int q) {
-  float apq = S[p][q];
+// One Jacobi rotation of the symmetric S = A^T A in the (p, q) plane, on its six distinct entries:
+// app, aqq, apq and the third row's arp, arq (r the index other than p, q).  The rotation angle is the
+// classical one, cot 2theta = (aqq - app) / (2 apq) with the smaller tangent; the update is the
+// symmetric form of J^T S J (Golub & Van Loan, "Matrix Computations", 4th ed., sec. 8.5.2; Rutishauser
+// 1966): app - t apq, aqq + t apq, apq = 0 exactly, and the third row rotated — 6 products instead of
+// the 24 of the two-sided update; V accumulates the rotations.
+DT_DEV void jacobi_rot(float& app, float& aqq, float& apq, float& arp, float& arq, float V[3][3], int p, int q) {
   if (apq == 0.f) return;
-  float tau = (S[q][q] - S[p][p]) / (2.f * apq);
-  float t = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.f)));
-  float c = 1.f / sqrtf(fmaf(t, t, 1.f));
-  float s = t * c;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    float sp = S[k][p], sq = S[k][q];
-    S[k][p] = c * sp - s * sq;
-    S[k][q] = s * sp + c * sq;
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    float sp = S[p][k], sq = S[q][k];
-    S[p][k] = c * sp - s * sq;
-    S[q][k] = s * sp + c * sq;
-  }
+  const float tau = (aqq - app) / (2.f * apq);
+  const float t = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.f)));
+  const float c = 1.f / sqrtf(fmaf(t, t, 1.f));
+  const float s = t * c;
+  app = fmaf(-t, apq, app);
+  aqq = fmaf(t, apq, aqq);
+  apq = 0.f;
+  const float rp = arp, rq = arq;
+  arp = c * rp - s * rq;
+  arq = s * rp + c * rq;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     float vp = V[k][p], vq = V[k][q];
@@ -257,20 +256,20 @@ DT_DEV void orthonormalize(float M[3][3]) {
 }
 
 DT_DEV void svd3(const m3& A, m3& U, v3& sv, m3& V, int sweeps) {
-  float S[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) S[i][j] = A.a[0][i] * A.a[0][j] + A.a[1][i] * A.a[1][j] + A.a[2][i] * A.a[2][j];
+  // the six distinct entries of S = A^T A
+#define DT_ATA(i, j) (A.a[0][i] * A.a[0][j] + A.a[1][i] * A.a[1][j] + A.a[2][i] * A.a[2][j])
+  float s00 = DT_ATA(0, 0), s11 = DT_ATA(1, 1), s22 = DT_ATA(2, 2);
+  float s01 = DT_ATA(0, 1), s02 = DT_ATA(0, 2), s12 = DT_ATA(1, 2);
+#undef DT_ATA
   float Vm[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
   for (int it = 0; it < sweeps; ++it) {
     // converged once the off-diagonal is below fp32 resolution of the diagonal
-    const float off = S[0][1] * S[0][1] + S[0][2] * S[0][2] + S[1][2] * S[1][2];
-    const float dia = S[0][0] * S[0][0] + S[1][1] * S[1][1] + S[2][2] * S[2][2];
+    const float off = s01 * s01 + s02 * s02 + s12 * s12;
+    const float dia = s00 * s00 + s11 * s11 + s22 * s22;
     if (off <= 1e-15f * dia) break;
-    jacobi_rot(S, Vm, 0, 1);
-    jacobi_rot(S, Vm, 0, 2);
-    jacobi_rot(S, Vm, 1, 2);
+    jacobi_rot(s00, s11, s01, s02, s12, Vm, 0, 1);  // third row r = 2: (S20, S21) = (s02, s12)
+    jacobi_rot(s00, s22, s02, s01, s12, Vm, 0, 2);  // r = 1: (S10, S12) = (s01, s12)
+    jacobi_rot(s11, s22, s12, s01, s02, Vm, 1, 2);  // r = 0: (S01, S02) = (s01, s02)
   }
   float B[3][3];
 #pragma unroll
@@ -363,6 +362,21 @@ inline int scatter_kind(const dt_world* w) {
 }
 // threads per CTA of the particle / tet / vertex launches (dt_world.p_block)
 inline int particle_block(const dt_world* w) { return (w->p_block == 64 || w->p_block == 256) ? w->p_block : 128; }
+// particles per thread (dt_world.p_per_thread): PPT consecutive chunks of NT particles per CTA, a
+// template parameter of the particle-role kernels (1 or 2) so that the one-chunk kernels keep their
+// register allocation
+inline int per_thread(const dt_world* w) { return w->p_per_thread == 2 ? 2 : 1; }
+// CTAs of a particle-role launch of NT-thread CTAs, PPT chunks each
+inline int particle_ctas(const dt_world* w, int NT, int PPT) {
+  const int chunks = (w->n_particles + NT - 1) / NT;
+  return (chunks + PPT - 1) / PPT;
+}
+// the chunks [c0, c1) of NT particles that CTA b of a particle-role launch of PPT chunks takes
+DT_DEV void cta_chunks(const dt_world& w, int NT, int PPT, int b, int& c0, int& c1) {
+  const int chunks = (w.n_particles + NT - 1) / NT;
+  c0 = b * PPT;
+  c1 = min(chunks, c0 + PPT);
+}
 
 // Opt a kernel into more than 48 KB of dynamic shared memory on the current device (the attribute
 // is per device; `cache` remembers the largest size already set on each of up to 64 devices).

@@ -200,14 +200,23 @@ __device__ void tri_centroid(const dt_world& w, int f, int t) {
   reinterpret_cast<float4*>(w.tri_cent)[t] = o;
 }
 
-template <int MODE, int NT>
+template <int MODE, int NT, int PPT>
 __global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_FWD_P2G, NT)) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
   pdl_entry();
   extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
-    p2g_chunk<MODE, NT>(w, f, b, tile, sh);
+    if (PPT == 1) {
+      p2g_chunk<MODE, NT>(w, f, b, tile, sh);
+    } else {
+      int c0, c1;
+      cta_chunks(w, NT, PPT, b, c0, c1);
+      for (int c = c0; c < c1; ++c) {
+        if (c > c0) __syncthreads();  // the shared tile and flags of the previous chunk
+        p2g_chunk<MODE, NT>(w, f, c, tile, sh);
+      }
+    }
     return;
   }
   b -= nb_p;
@@ -454,13 +463,22 @@ __device__ void fem_integrate(const dt_world& w, int f, int i) {
   vframe(w.v_ext, w, f + 1)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-template <int NT>
+template <int NT, int PPT>
 __global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_FWD_G2P, NT)) k_fwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
   pdl_entry();
   int b = blockIdx.x;
   if (b < nb_p) {
-    int p = b * NT + threadIdx.x;
-    if (p < w.n_particles) g2p_particle(w, f, p);
+    if (PPT == 1) {
+      const int p = b * NT + threadIdx.x;
+      if (p < w.n_particles) g2p_particle(w, f, p);
+    } else {
+      int c0, c1;
+      cta_chunks(w, NT, PPT, b, c0, c1);
+      for (int c = c0; c < c1; ++c) {
+        const int p = c * NT + threadIdx.x;
+        if (p < w.n_particles) g2p_particle(w, f, p);
+      }
+    }
     return;
   }
   b -= nb_p;
@@ -478,14 +496,18 @@ inline int check(const dt_world* w, int f) {
 }
 inline int launched() { return launch_status(cudaGetLastError()); }
 
-template <int MODE, int NT>
-cudaError_t l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
-  const int nb_p = parts ? cdiv(w->n_particles, NT) : 0;
+template <int MODE, int NT, int PPT>
+cudaError_t l1_ppt(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
+  const int nb_p = parts ? particle_ctas(w, NT, PPT) : 0;
   const int nb_t = fem ? cdiv(w->n_tets, NT) : 0;
   const int nb_f = fem ? cdiv(w->n_tris, NT) : 0;
   if (nb_p + nb_t + nb_f == 0) return cudaSuccess;
   const size_t smem = MODE == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0;
-  return launch_k(k_fwd_p2g_fem<MODE, NT>, nb_p + nb_t + nb_f, NT, smem, st, *w, f, nb_p, nb_t, nb_f);
+  return launch_k(k_fwd_p2g_fem<MODE, NT, PPT>, nb_p + nb_t + nb_f, NT, smem, st, *w, f, nb_p, nb_t, nb_f);
+}
+template <int MODE, int NT>
+cudaError_t l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
+  return per_thread(w) == 2 ? l1_ppt<MODE, NT, 2>(w, f, parts, fem, st) : l1_ppt<MODE, NT, 1>(w, f, parts, fem, st);
 }
 template <int MODE>
 cudaError_t l1_nt(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
@@ -521,12 +543,16 @@ int launch_l2(const dt_world* w, int f, cudaStream_t st) {
   if (w->contact_lanes == 4) return big ? l2<4, true>(w, f, st) : l2<4, false>(w, f, st);
   return big ? l2<8, true>(w, f, st) : l2<8, false>(w, f, st);
 }
-template <int NT>
-cudaError_t l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
-  const int nb_p = parts ? cdiv(w->n_particles, NT) : 0;
+template <int NT, int PPT>
+cudaError_t l3_ppt(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
+  const int nb_p = parts ? particle_ctas(w, NT, PPT) : 0;
   const int nb_v = fem ? cdiv(w->n_verts, NT) : 0;
   if (nb_p + nb_v == 0) return cudaSuccess;
-  return launch_k(k_fwd_g2p_fem<NT>, nb_p + nb_v, NT, 0, st, *w, f, nb_p, nb_v);
+  return launch_k(k_fwd_g2p_fem<NT, PPT>, nb_p + nb_v, NT, 0, st, *w, f, nb_p, nb_v);
+}
+template <int NT>
+cudaError_t l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
+  return per_thread(w) == 2 ? l3_ppt<NT, 2>(w, f, parts, fem, st) : l3_ppt<NT, 1>(w, f, parts, fem, st);
 }
 int launch_l3(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
   cudaError_t e;

@@ -50,7 +50,7 @@
 extern "C" {
 #endif
 
-#define DT_ABI_VERSION 4
+#define DT_ABI_VERSION 5
 
 #define DT_OK 0
 #define DT_ERR_ARG (-1)        /* null pointer, bad size or frame index */
@@ -232,6 +232,10 @@ typedef struct dt_world {
                                     positions of every pass, recomputed by dt_rope_update_bwd; may be NULL
                                     when no rope has iters > 1 */
   int max_rope_iters;            /* largest iters over the ropes that r_work is sized for */
+  /* ---- launch shape (ABI 5) ---- */
+  int p_per_thread;              /* particles per thread of the particle-role launches (P2G, G2P and their
+                                    adjoints): each CTA takes this many consecutive chunks of p_block
+                                    particles; 1 or 2 (anything else means 1) */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared

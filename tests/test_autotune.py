@@ -11,8 +11,9 @@ from difftactile_gb300 import autotune as AT
 
 def test_candidates_cover_the_shapes():
     c = AT.candidates()
-    assert len(c) == 2 * (3 * 3 * 2 + 3 * 2 + 2)
+    assert len(c) == 2 * 2 * (3 * 3 * 2 + 3 * 2 + 2)
     assert {x["lanes"] for x in c} == {8, 4}
+    assert {x["ppt"] for x in c} == {1, 2}
     assert {x["p_block"] for x in c if x["scatter"] == "tile"} == {128}
     assert {(x["scatter"], x["p_block"]) for x in c if x["scatter"] != "tile"} == \
         {(s, b) for s in ("warp", "global") for b in (64, 128, 256)}
@@ -84,7 +85,7 @@ class _FakeWorld:
     """The fields the tuner sets, without a device: the 'time' of a shape is a fixed function of it."""
     def __init__(self, n_particles=1000):
         import types
-        self.w = types.SimpleNamespace(scatter_mode=2, p_block=128, scatter_depth=0, contact_lanes=8)
+        self.w = types.SimpleNamespace(scatter_mode=2, p_block=128, scatter_depth=0, contact_lanes=8, p_per_thread=1)
         self.lib = _FakeLib()
         self.device = "cpu"
         self.n_envs, self.n_particles, self.n_verts, self.n_tets, self.n_tris = 1, n_particles, 10, 10, 10
@@ -110,7 +111,7 @@ def test_tuner_picks_the_fastest_shape_and_keeps_the_default_within_the_margin()
     run.world = world
     cur = lambda w: AT.current(w)  # noqa: E731
     # a shape 10% faster than the default wins
-    fast = {"scatter": "warp", "p_block": 256, "depth": 1, "lanes": 4, "pdl": 1}
+    fast = {"scatter": "warp", "p_block": 256, "depth": 1, "lanes": 4, "pdl": 1, "ppt": 2}
     cost = lambda w: 0.9 if cur(w) == fast else 1.0  # noqa: E731
     r = AT.tune(world, run, timer=_timer_for(cost), use_cache=False)
     assert r["best"] == fast and AT.current(world) == fast and not r["cached"]

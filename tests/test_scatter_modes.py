@@ -65,15 +65,19 @@ def test_warp_runs_across_env_boundaries(cuda_lib):
         compare(w, 2, st, env_idx=e)
 
 
-@pytest.mark.parametrize("mode,p_block,depth", [("warp", 64, 0), ("warp", 256, 0), ("global", 64, 0),
-                                                ("global", 256, 0), ("warp", 128, 1), ("warp", 128, 2),
-                                                ("warp", 256, 1)])
-def test_particle_block_sizes(cuda_lib, mode, p_block, depth):
-    """Particle-role CTAs of 64 and 256 threads and capped segmented reductions (the autotuner's
-    other shapes) give the oracle's forward state after three substeps and its one-substep adjoint."""
+@pytest.mark.parametrize("mode,p_block,depth,ppt", [("warp", 64, 0, 1), ("warp", 256, 0, 1), ("global", 64, 0, 1),
+                                                    ("global", 256, 0, 1), ("warp", 128, 1, 1), ("warp", 128, 2, 1),
+                                                    ("warp", 256, 1, 1), ("warp", 128, 1, 2), ("warp", 64, 0, 2),
+                                                    ("global", 256, 0, 2), ("tile", 128, 0, 2)])
+def test_particle_block_sizes(cuda_lib, mode, p_block, depth, ppt):
+    """Particle-role CTAs of 64 and 256 threads, capped segmented reductions and two chunks of
+    particles per CTA (the autotuner's other shapes; 1,152 particles: an odd number of chunks, so the
+    last two-chunk CTA has one) give the oracle's forward state after three substeps and its
+    one-substep adjoint."""
     env = SS.pad_over_box()
     cv = [SS.control_velocity(sp) for sp in env.sensors]
-    w = World([env], n_frames=4, dt=DT, scatter_mode=MODES[mode], p_block=p_block, scatter_depth=depth)
+    kw = dict(scatter_mode=MODES[mode], p_block=p_block, scatter_depth=depth, p_per_thread=ppt)
+    w = World([env], n_frames=4, dt=DT, **kw)
     for s, c in enumerate(cv):
         w.set_control_velocity(s, c)
     w.step_begin()
@@ -85,7 +89,7 @@ def test_particle_block_sizes(cuda_lib, mode, p_block, depth):
     compare(w, 3, st)
     st0, cv0 = base_point(env, 7)
     W = loss_weights(env, env.n_particles, 8)
-    g = gpu_grads(env, st0, cv0, W, 1, scatter_mode=MODES[mode], p_block=p_block, scatter_depth=depth)
+    g = gpu_grads(env, st0, cv0, W, 1, **kw)
     o = O.Oracle(env, DT, np.float64, grad_clip=0.0)
     ref = o.substep_bwd({k: (v if not isinstance(v, list) else [a.copy() for a in v]) for k, v in st0.items()}, W,
                         cv=cv0, cv1=cv0)
