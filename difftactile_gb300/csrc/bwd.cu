@@ -861,6 +861,37 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
 int dt_substeps_bwd(const dt_world* w, int f_hi, int f_lo, cudaStream_t stream) {
   if (!w || f_lo < 0 || f_hi <= f_lo || f_hi >= w->n_frames) return DT_ERR_ARG;
   int rc = dt_substep_bwd_stage(w, f_hi - 1, 0, stream);
+  if (w->n_ropes > 0 && has_aux(w)) {
+    // The solver's adjoint of frame f reads only the rope adjoint of frame f + 1, complete once the rope
+    // contact adjoint of f + 1 has run: it runs on the aux stream beside stage 3 of f + 1 and stages 1
+    // and the grid adjoint of f, and the contact adjoint of f (which reads its output) waits for it.
+    // Work forked onto the aux stream is joined back before the call returns, on errors too.
+    bool pending = false;
+    auto fork_solve = [&](int g) {
+      if (aux_fork(w, stream) != cudaSuccess) return DT_ERR_LAUNCH;
+      pending = true;
+      return rope_part(w, g, ROPE_SOLVE_BWD, w->aux_stream);
+    };
+    if (!rc) rc = fork_solve(f_hi - 1);
+    const int ng = w->n_blocks < 152 * 16 ? w->n_blocks : 152 * 16;
+    for (int f = f_hi - 1; f >= f_lo && !rc; --f) {
+      if ((rc = dt_substep_bwd_stage(w, f, 1, stream))) break;
+      if (ng > 0 && launch_k(k_bwd_grid, ng, GRID_NT, 0, stream, *w, f) != cudaSuccess) {
+        rc = DT_ERR_LAUNCH;
+        break;
+      }
+      pending = false;
+      if (aux_join(w, stream) != cudaSuccess) {
+        rc = DT_ERR_LAUNCH;
+        break;
+      }
+      if ((rc = rope_part(w, f, ROPE_CONTACT_BWD, stream))) break;
+      if (f > f_lo && (rc = fork_solve(f - 1))) break;
+      if (b3(w, f, f > f_lo, stream) != cudaSuccess) rc = DT_ERR_LAUNCH;
+    }
+    if (pending && aux_join(w, stream) != cudaSuccess && !rc) rc = DT_ERR_LAUNCH;
+    return rc;
+  }
   for (int f = f_hi - 1; f >= f_lo && !rc; --f) {
     if ((rc = dt_substep_bwd_stage(w, f, 1, stream)) || (rc = dt_substep_bwd_stage(w, f, 2, stream))) break;
     // the next (lower) frame's restore rides along

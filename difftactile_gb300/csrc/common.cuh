@@ -362,6 +362,23 @@ inline int scatter_kind(const dt_world* w) {
 }
 // threads per CTA of the particle / tet / vertex launches (dt_world.p_block)
 inline int particle_block(const dt_world* w) { return (w->p_block == 64 || w->p_block == 256) ? w->p_block : 128; }
+// The rope stages one at a time (rope.cu): the contact and the solver of dt_rope_update, the solver's
+// adjoint and the contact's adjoint of dt_rope_update_bwd.
+enum { ROPE_CONTACT = 0, ROPE_SOLVE = 1, ROPE_SOLVE_BWD = 2, ROPE_CONTACT_BWD = 3 };
+int rope_part(const dt_world* w, int f, int part, cudaStream_t stream);
+
+// Fork / join of work onto dt_world.aux_stream: fork() makes the aux stream wait for what the call's
+// stream has queued so far; join() makes the call's stream wait for what was queued on the aux stream.
+inline bool has_aux(const dt_world* w) { return w->aux_stream && w->aux_events[0] && w->aux_events[1]; }
+inline cudaError_t aux_fork(const dt_world* w, cudaStream_t st) {
+  cudaError_t e = note_error(cudaEventRecord(w->aux_events[0], st));
+  return e == cudaSuccess ? note_error(cudaStreamWaitEvent(w->aux_stream, w->aux_events[0], 0)) : e;
+}
+inline cudaError_t aux_join(const dt_world* w, cudaStream_t st) {
+  cudaError_t e = note_error(cudaEventRecord(w->aux_events[1], w->aux_stream));
+  return e == cudaSuccess ? note_error(cudaStreamWaitEvent(st, w->aux_events[1], 0)) : e;
+}
+
 // particles per thread (dt_world.p_per_thread): PPT consecutive chunks of NT particles per CTA, a
 // template parameter of the particle-role kernels (1 or 2) so that the one-chunk kernels keep their
 // register allocation

@@ -573,6 +573,17 @@ int dt_substep_fwd(const dt_world* w, int f, cudaStream_t stream) {
   if (rc) return rc;
   if ((rc = launch_l1(w, f, true, true, stream))) return rc;
   if ((rc = launch_l2(w, f, stream))) return rc;
+  if (w->n_ropes > 0 && has_aux(w)) {
+    // the solver reads the rope contact's impulses and writes rope frame f + 1, which nothing in G2P
+    // reads: it runs on the aux stream beside G2P and is joined before the call returns
+    if ((rc = rope_part(w, f, ROPE_CONTACT, stream))) return rc;
+    if (aux_fork(w, stream) != cudaSuccess) return DT_ERR_LAUNCH;
+    rc = rope_part(w, f, ROPE_SOLVE, w->aux_stream);
+    if (!rc) rc = launch_l3(w, f, true, true, stream);
+    // joined on errors too: nothing stays queued on the aux stream past the call
+    const cudaError_t j = aux_join(w, stream);
+    return rc ? rc : (j == cudaSuccess ? DT_OK : DT_ERR_LAUNCH);
+  }
   if ((rc = dt_rope_update(w, f, stream))) return rc;
   return launch_l3(w, f, true, true, stream);
 }

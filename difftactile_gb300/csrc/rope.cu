@@ -354,43 +354,61 @@ int set_smem(const void* fn, size_t bytes, size_t (&configured)[64]) {
 
 }  // namespace
 
+// the parts of dt_rope_update / dt_rope_update_bwd, for the substep drivers that overlap the solver
+// with the MPM stages (declared in common.cuh)
+int rope_part(const dt_world* w, int f, int part, cudaStream_t stream) {
+  if (w->n_ropes <= 0) return DT_OK;
+  int rc;
+  if (part == ROPE_CONTACT || part == ROPE_SOLVE) {
+    if (!w->ropes || !w->r_state || !w->r_ext || !w->r_cidx || w->max_rope_n <= 0) return DT_ERR_ARG;
+    const size_t solve_smem = (size_t)2 * w->max_rope_n * sizeof(float4);
+    if (solve_smem > 227 * 1024) return DT_ERR_CAPACITY;
+    if (part == ROPE_SOLVE) {
+      static size_t conf_s[64] = {};
+      if ((rc = set_smem((const void*)k_rope_solve, solve_smem, conf_s))) return rc;
+      return launch_k(k_rope_solve, w->n_ropes, RS_NT, solve_smem, stream, *w, f) == cudaSuccess ? DT_OK
+                                                                                                  : DT_ERR_LAUNCH;
+    }
+    const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
+    const size_t smem = stage_bytes(cap);
+    static size_t conf_c[64] = {}, conf_cc[64] = {};
+    const bool big = w->max_sensor_tris > 32 * 32;  // some sensor has more than 32 groups
+    if ((rc = set_smem(big ? (const void*)k_rope_contact<true> : (const void*)k_rope_contact<false>, smem,
+                       big ? conf_cc : conf_c)))
+      return rc;
+    if (w->rope_blocks > 0 &&
+        launch_k(big ? k_rope_contact<true> : k_rope_contact<false>, w->rope_blocks, RC_NT, smem, stream, *w, f,
+                 cap) != cudaSuccess)
+      return DT_ERR_LAUNCH;
+    return DT_OK;
+  }
+  if (!w->ropes || !w->r_adj || !w->r_extb || w->max_rope_n <= 0) return DT_ERR_ARG;
+  if (part == ROPE_SOLVE_BWD) {
+    const size_t smem = (size_t)4 * w->max_rope_n * sizeof(float4);
+    if (smem > 227 * 1024) return DT_ERR_CAPACITY;
+    static size_t conf[64] = {};
+    if ((rc = set_smem((const void*)k_rope_solve_bwd, smem, conf))) return rc;
+    return launch_k(k_rope_solve_bwd, w->n_ropes, RS_NT, smem, stream, *w, f) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
+  }
+  if (part == ROPE_CONTACT_BWD)
+    return launch_k(k_rope_contact_bwd, cdiv(w->n_rope_particles, 128), 128, 0, stream, *w, f) == cudaSuccess
+               ? DT_OK
+               : DT_ERR_LAUNCH;
+  return DT_ERR_ARG;
+}
+
 extern "C" {
 
 int dt_rope_update(const dt_world* w, int f, cudaStream_t stream) {
   if (!w || f < 0 || f + 1 >= w->n_frames) return DT_ERR_ARG;
-  if (w->n_ropes <= 0) return DT_OK;
-  if (!w->ropes || !w->r_state || !w->r_ext || !w->r_cidx || w->max_rope_n <= 0) return DT_ERR_ARG;
-  const size_t solve_smem = (size_t)2 * w->max_rope_n * sizeof(float4);
-  if (solve_smem > 227 * 1024) return DT_ERR_CAPACITY;
-  int rc;
-  const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
-  const size_t smem = stage_bytes(cap);
-  static size_t conf_c[64] = {}, conf_cc[64] = {}, conf_s[64] = {};
-  const bool big = w->max_sensor_tris > 32 * 32;  // some sensor has more than 32 groups
-  if ((rc = set_smem(big ? (const void*)k_rope_contact<true> : (const void*)k_rope_contact<false>, smem,
-                     big ? conf_cc : conf_c)))
-    return rc;
-  if ((rc = set_smem((const void*)k_rope_solve, solve_smem, conf_s))) return rc;
-  if (w->rope_blocks > 0 &&
-      launch_k(big ? k_rope_contact<true> : k_rope_contact<false>, w->rope_blocks, RC_NT, smem, stream, *w, f, cap) !=
-          cudaSuccess)
-    return DT_ERR_LAUNCH;
-  return launch_k(k_rope_solve, w->n_ropes, RS_NT, solve_smem, stream, *w, f) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;
+  int rc = rope_part(w, f, ROPE_CONTACT, stream);
+  return rc ? rc : rope_part(w, f, ROPE_SOLVE, stream);
 }
 
 int dt_rope_update_bwd(const dt_world* w, int f, cudaStream_t stream) {
   if (!w || f < 0 || f + 1 >= w->n_frames) return DT_ERR_ARG;
-  if (w->n_ropes <= 0) return DT_OK;
-  if (!w->ropes || !w->r_adj || !w->r_extb || w->max_rope_n <= 0) return DT_ERR_ARG;
-  const size_t smem = (size_t)4 * w->max_rope_n * sizeof(float4);
-  if (smem > 227 * 1024) return DT_ERR_CAPACITY;
-  static size_t conf[64] = {};
-  int rc;
-  if ((rc = set_smem((const void*)k_rope_solve_bwd, smem, conf))) return rc;
-  if (launch_k(k_rope_solve_bwd, w->n_ropes, RS_NT, smem, stream, *w, f) != cudaSuccess) return DT_ERR_LAUNCH;
-  return launch_k(k_rope_contact_bwd, cdiv(w->n_rope_particles, 128), 128, 0, stream, *w, f) == cudaSuccess
-             ? DT_OK
-             : DT_ERR_LAUNCH;
+  int rc = rope_part(w, f, ROPE_SOLVE_BWD, stream);
+  return rc ? rc : rope_part(w, f, ROPE_CONTACT_BWD, stream);
 }
 
 }  // extern "C"

@@ -57,7 +57,7 @@ class World:
     def __init__(self, envs: list[EnvSpec], n_frames: int, dt: float, device="cuda", tape_blocks: int | None = None,
                  grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True,
                  svd_grad_mode: int = 0, scatter_mode: int = 2, svd_tape: bool = True, p_block: int = 128,
-                 scatter_depth: int = 0, contact_lanes: int = 8, p_per_thread: int = 1):
+                 scatter_depth: int = 0, contact_lanes: int = 8, p_per_thread: int = 1, overlap_ropes: bool = True):
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise ValueError(f"World buffers must live on a CUDA device (the kernels take device pointers), "
@@ -291,6 +291,16 @@ class World:
         w.r_work = t["r_work"].data_ptr() if t["r_work"] is not None else None
         w.max_rope_iters = max_iters if t["r_work"] is not None else 1
         w.p_svd = t["p_svd"].data_ptr() if t["p_svd"] is not None else None
+        # ropes: the solver (one CTA per rope) and its adjoint run on a second stream beside the MPM
+        # stages (dt_world.aux_stream); the events are created by recording them once
+        self._aux = None
+        if self.n_ropes and overlap_ropes:
+            self._aux = torch.cuda.Stream(device=dev)
+            self._aux_ev = [torch.cuda.Event(), torch.cuda.Event()]
+            for ev in self._aux_ev:
+                ev.record(torch.cuda.current_stream(dev))
+            w.aux_stream = self._aux.cuda_stream
+            w.aux_events[0], w.aux_events[1] = self._aux_ev[0].cuda_event, self._aux_ev[1].cuda_event
         self.w = w
         self.wp = C.pointer(w)
 

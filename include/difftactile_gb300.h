@@ -50,7 +50,7 @@
 extern "C" {
 #endif
 
-#define DT_ABI_VERSION 5
+#define DT_ABI_VERSION 6
 
 #define DT_OK 0
 #define DT_ERR_ARG (-1)        /* null pointer, bad size or frame index */
@@ -236,6 +236,14 @@ typedef struct dt_world {
   int p_per_thread;              /* particles per thread of the particle-role launches (P2G, G2P and their
                                     adjoints): each CTA takes this many consecutive chunks of p_block
                                     particles; 1 or 2 (anything else means 1) */
+  /* ---- concurrency (ABI 6) ---- */
+  cudaStream_t aux_stream;       /* optional second stream of the same device: dt_substep_fwd runs the rope
+                                    solver on it beside G2P, dt_substeps_bwd the solver's adjoint beside
+                                    the P2G, G2P and grid adjoints (one CTA per rope leaves most SMs to
+                                    the MPM stages).  Work forked onto it is joined back into the call's
+                                    stream before the call returns.  NULL: everything on the call's
+                                    stream. */
+  cudaEvent_t aux_events[2];     /* fork and join events (cudaEventDisableTiming), required with aux_stream */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared

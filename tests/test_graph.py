@@ -67,6 +67,27 @@ def test_pose_trajectory_graph_replay(cuda_lib, ckpt):
     assert graph.launches > 0
 
 
+@pytest.mark.parametrize("ckpt", [0, 1])
+def test_rope_trajectory_graph_replay(cuda_lib, ckpt):
+    """A pad pressing a rope of five pass pairs per substep, rope-tip loss: the rope solver and its
+    adjoint run on the world's second stream (forked and joined inside every substep call), which the
+    recorded graph holds as a branch; replays give the host-launched loss and gradient."""
+    env = SS.rope_under_pad(n_rope=16)
+    env = env.replace(ropes=[env.ropes[0].replace(iters=5)])
+    tip = env.ropes[0].init_positions()[-1].astype(np.float64)
+    rope_terms = ((0, tip + np.array([0.003, 0.002, -0.001])),)
+    nf = PoseTrajectory.frames_needed(TT.T_STEPS, TT.SUB, ckpt)
+    w = World([env], n_frames=nf, dt=TT.DT, grad_clip=0.0)
+    assert w.w.aux_stream
+    acts = []
+    for s in (5, 6):
+        a = TT.actions(s)
+        a[:, 0, 1] = 0.2
+        acts.append(a)
+    compare(lambda: PoseTrajectory(w, TT.T_STEPS, ckpt, (), rope_terms=rope_terms),
+            lambda: PoseTrajectory(w, TT.T_STEPS, ckpt, (), rope_terms=rope_terms, graph=True), w, acts)
+
+
 def test_gripper_trajectory_graph_replay(cuda_lib):
     env, kin, terms = TG.setup()
     nf = Trajectory.frames_needed(TG.T_STEPS, TG.SUB, 0)

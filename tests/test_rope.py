@@ -87,6 +87,40 @@ def test_ropes_in_two_envs_beside_an_mpm_env(cuda_lib):
         assert SS.rel_err(rs["vel"].cpu().numpy(), st["rvel"][0]) < 1e-4, r
 
 
+def test_rope_solver_on_the_second_stream_matches_one_stream(cuda_lib):
+    """The rope solver on the world's second stream beside G2P, and its adjoint beside the MPM adjoint
+    stages (World(overlap_ropes=True), the default), against everything on one stream: four substeps
+    of two rope environments (six pass pairs each) beside an MPM environment, then the adjoint sweep
+    down to frame 0 from seeded adjoints.  The two differ only in the atomics' summation order."""
+    e0 = SS.rope_under_pad(n_rope=70, seed=1)
+    e0 = e0.replace(ropes=[e0.ropes[0].replace(iters=6)])
+    e1 = SS.pad_over_box()
+    e2 = SS.rope_under_pad(n_rope=9, seed=2, press=0.5)
+    cvs = [SS.control_velocity(e.sensors[0], seed=5 + i, scale=0.02, down=-0.05) for i, e in enumerate((e0, e1, e2))]
+    n = 4
+    out = {}
+    for overlap in (False, True):
+        w = World([e0, e1, e2], n_frames=n + 1, dt=DT, grad_clip=0.0, overlap_ropes=overlap)
+        assert bool(w.w.aux_stream) == overlap
+        for s, cv in enumerate(cvs):
+            w.set_control_velocity(s, cv)
+        w.step_begin()
+        for f in range(n):
+            w.substep(f)
+        w.adj_clear()
+        g = torch.Generator(device=w.device).manual_seed(3)
+        for name in ("r_adj", "v_adj_pos", "v_adj_vel"):
+            w.t[name][n & 1].copy_(torch.randn(w.t[name][n & 1].shape, device=w.device, generator=g))
+        w.substeps_bwd(n, 0)
+        torch.cuda.synchronize()
+        assert w.error_word() == 0
+        out[overlap] = {"rstate": w.t["r_state"][n].clone(), "r_adj": w.t["r_adj"][0].clone(),
+                        "v_adj_pos": w.t["v_adj_pos"][0].clone(), "p_adj": w.t["p_adj"][0].clone()}
+    errs = {k: SS.rel_err(out[True][k].cpu().numpy(), out[False][k].cpu().numpy()) for k in out[True]}
+    print("second stream vs one stream", errs)
+    assert max(errs.values()) < 1e-5, errs
+
+
 @pytest.mark.parametrize("iters", [1, 6])
 def test_rope_adjoint_matches_oracle(cuda_lib, iters):
     """One pass pair (the reference's PBDRope.update) and six (the adjoint recomputes the pass inputs
