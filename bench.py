@@ -64,6 +64,8 @@ def parse():
                     help="threads per CTA of the particle launches")
     ap.add_argument("--depth", type=int, default=None, choices=[0, 1, 2, 3, 4, 5],
                     help="shuffle steps of the warp scatter's segmented reduction (0: whole runs)")
+    ap.add_argument("--ppt", type=int, default=None, choices=[1, 2],
+                    help="particles per thread of the particle-role launches (default: the tuner's choice)")
     ap.add_argument("--lanes", type=int, default=None, choices=[4, 8],
                     help="lanes per active grid node in the contact search")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shape instead of "
@@ -177,6 +179,8 @@ def build(cfg, dev, args, **extra):
         kw["scatter_depth"] = args.depth
     if args.lanes is not None:
         kw["contact_lanes"] = args.lanes
+    if args.ppt is not None:
+        kw["p_per_thread"] = args.ppt
     if args.rebin and cfg.ckpt_every > 0:
         kw["rebin_every"] = args.rebin
     return cfg.build(dev, **kw)
@@ -184,7 +188,7 @@ def build(cfg, dev, args, **extra):
 
 def tune_launch(args):
     return not (args.no_tune or args.scatter or args.no_pdl or args.p_block or args.depth is not None
-                or args.lanes is not None)
+                or args.lanes is not None or args.ppt is not None)
 
 
 def mid_frame(traj):
@@ -500,6 +504,7 @@ def run_ours(args):
                       "scatter": ["tile", "global", "warp"][w.w.scatter_mode], "p_block": int(w.w.p_block),
                       "scatter_depth": int(w.w.scatter_depth),
                       "contact_lanes": 4 if int(w.w.contact_lanes) == 4 else 8,
+                      "particles_per_thread": max(1, int(w.w.p_per_thread)),
                       "programmatic_dependent_launch": bool(w.lib.dt_get_pdl()),
                       "launch_shape": "autotuned" if res["tuned"] else "fixed", "cuda_graph": not args.no_graph,
                       "svd_tape": w.t["p_svd"] is not None, "active_blocks_mean": res["active_blocks_mean"],
