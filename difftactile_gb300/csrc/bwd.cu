@@ -379,19 +379,6 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   for (int k = 0; k < 6; ++k) q[k] = ldg4(pplane(w, f, k) + p);
   PRec r;
   unpack_rec(q, r);
-  // adjoint of F[f+1]
-  const float4 n3 = ld4(padj(w, nb, 3) + p), n4 = ld4(padj(w, nb, 4) + p), n5 = ld4(padj(w, nb, 5) + p);
-  m3 Fpb;
-  Fpb.a[0][0] = n3.w;
-  Fpb.a[0][1] = n4.x;
-  Fpb.a[0][2] = n4.y;
-  Fpb.a[1][0] = n4.z;
-  Fpb.a[1][1] = n4.w;
-  Fpb.a[1][2] = n5.x;
-  Fpb.a[2][0] = n5.y;
-  Fpb.a[2][1] = n5.z;
-  Fpb.a[2][2] = n5.w;
-  const float4 xpart = ld4(padj(w, cb, 0) + p);  // x adjoint from the G2P adjoint
   const dt_env& E = w.envs[__ldg(w.p_env + p)];
   int base[3];
   float fx[3];
@@ -400,8 +387,9 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   mub = lamb = 0.f;
   if (!particle_base(E, r.x, base, fx)) {
     // carried unchanged in the forward pass: adjoint passes straight through
+    const float4 xpart = ld4(padj(w, cb, 0) + p);  // x adjoint from the G2P adjoint
     const float4 a0 = ld4(padj(w, nb, 0) + p), a1 = ld4(padj(w, nb, 1) + p), a2 = ld4(padj(w, nb, 2) + p),
-                 a3 = ld4(padj(w, nb, 3) + p);
+                 a3 = ld4(padj(w, nb, 3) + p), n4 = ld4(padj(w, nb, 4) + p), n5 = ld4(padj(w, nb, 5) + p);
     float4 o[6] = {make_float4(xpart.x, xpart.y, xpart.z, a0.w), a1, a2, a3, n4, n5};
 #pragma unroll
     for (int k = 0; k < 6; ++k) padj(w, cb, k)[p] = o[k];
@@ -459,6 +447,23 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
         fxb[1] += Wb * (wts[oi][0] * dws[oj][1] * wts[ok][2]);
         fxb[2] += Wb * (wts[oi][0] * wts[oj][1] * dws[ok][2]);
       }
+#if DT_BWD_P2G_RECOMPUTE
+  // the constitutive state again, from the SVD tape: not kept live across the gather above
+  constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s, &w, w.p_svd ? f : -1, p);
+#endif
+  // adjoint of F[f+1], and the x adjoint from the G2P adjoint
+  const float4 n3 = ld4(padj(w, nb, 3) + p), n4 = ld4(padj(w, nb, 4) + p), n5 = ld4(padj(w, nb, 5) + p);
+  m3 Fpb;
+  Fpb.a[0][0] = n3.w;
+  Fpb.a[0][1] = n4.x;
+  Fpb.a[0][2] = n4.y;
+  Fpb.a[1][0] = n4.z;
+  Fpb.a[1][1] = n4.w;
+  Fpb.a[1][2] = n5.x;
+  Fpb.a[2][0] = n5.y;
+  Fpb.a[2][1] = n5.z;
+  Fpb.a[2][2] = n5.w;
+  const float4 xpart = ld4(padj(w, cb, 0) + p);
   const v3 vb = pm * S0;
   m3 Ab;
 #pragma unroll
@@ -632,7 +637,10 @@ __device__ void fem_tet_bwd(const dt_world& w, int f, int t) {
     // P = 2 mu (F - R) + lam c R, c = sum sigma - 3, H = -V0 P B^T with the rest volume V0
     m3 U, Vm;
     v3 sg;
-    svd3(Fe, U, sg, Vm, w.svd_sweeps);
+    if (w.t_svd)
+      load_svd_of(w.t_svd, w.n_tets, f, t, U, sg, Vm);  // the forward's decomposition
+    else
+      svd3(Fe, U, sg, Vm, w.svd_sweeps);
     const m3 R = mmulT(U, Vm);
     const float c = ((sg.x + sg.y) + sg.z) - 3.f;
     const float sc0 = -S.dt_over_m / (6.f * fabsf(mdet(B)));
@@ -742,8 +750,8 @@ __device__ void p2g_bwd_particle(const dt_world& w, int f, int p) {
 
 // nb_r > 0: the last nb_r CTAs restore frame f - 1's grid velocities for the next backward substep
 // (only stage 1 reads g_vout, so this overlaps stage 3 of frame f)
-template <int NT, int PPT>  // 512 / NT CTAs per SM: 128 registers per thread
-__global__ void __launch_bounds__(NT, 512 / NT) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v,
+template <int NT, int PPT>  // DT_MINB_BWD_P2G (4) 128-thread CTAs per SM: 128 registers per thread
+__global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_BWD_P2G, NT)) k_bwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_v,
                                                              int nb_r) {
   pdl_entry();
   int b = blockIdx.x;

@@ -24,6 +24,20 @@
 #ifndef DT_MINB_BWD_GRID
 #define DT_MINB_BWD_GRID 8
 #endif
+#ifndef DT_MINB_BWD_P2G
+#define DT_MINB_BWD_P2G 4
+#endif
+// 1: the P2G adjoint recomputes the particle's constitutive state (from the SVD tape) after its
+// 27-node gather instead of keeping it live across it (fewer live registers, more arithmetic)
+#ifndef DT_BWD_P2G_RECOMPUTE
+#define DT_BWD_P2G_RECOMPUTE 0
+#endif
+// Contact searches over sensors of more than this many groups of 32 centroids first reduce the groups to
+// the candidates of the query block (contact.cuh: block_candidates); smaller sensors keep every group's
+// box distance in registers.  At most 32 (the register cache's size).
+#ifndef DT_CAND_MIN_GROUPS
+#define DT_CAND_MIN_GROUPS 32
+#endif
 // the launch-bounds minimum of a CTA of NT threads for a per-128-thread minimum n
 #define DT_MINB(n, NT) ((n) > 0 ? ((n) * 128 + (NT) - 1) / (NT) : 1)
 
@@ -523,25 +537,34 @@ DT_DEV void von_mises(Stress& s, float mu, float ys) {
 // the SVD of F_new as stored on the tape: 6 float4 planes per particle and frame,
 // (U00 U01 U02 U10) (U11 U12 U20 U21) (U22 V00 V01 V02) (V10 V11 V12 V20) (V21 V22 s0 s1) (s2 y 0 0)
 // with y = 1 where the von Mises return map yielded (the branch its adjoint differentiates), else 0
-DT_DEV float4* svd_plane(const dt_world& w, int f, int k) {
-  return reinterpret_cast<float4*>(w.p_svd) + ((size_t)f * 6 + k) * w.n_particles;
+// (the tets' tape t_svd has the same planes over n_tets)
+DT_DEV float4* svd_plane_of(float* base, int n, int f, int k) {
+  return reinterpret_cast<float4*>(base) + ((size_t)f * 6 + k) * (size_t)n;
+}
+DT_DEV float4* svd_plane(const dt_world& w, int f, int k) { return svd_plane_of(w.p_svd, w.n_particles, f, k); }
+DT_DEV void store_svd_of(float* base, int n, int f, int p, const m3& U, v3 sg, const m3& V, bool yield) {
+  svd_plane_of(base, n, f, 0)[p] = make_float4(U.a[0][0], U.a[0][1], U.a[0][2], U.a[1][0]);
+  svd_plane_of(base, n, f, 1)[p] = make_float4(U.a[1][1], U.a[1][2], U.a[2][0], U.a[2][1]);
+  svd_plane_of(base, n, f, 2)[p] = make_float4(U.a[2][2], V.a[0][0], V.a[0][1], V.a[0][2]);
+  svd_plane_of(base, n, f, 3)[p] = make_float4(V.a[1][0], V.a[1][1], V.a[1][2], V.a[2][0]);
+  svd_plane_of(base, n, f, 4)[p] = make_float4(V.a[2][1], V.a[2][2], sg.x, sg.y);
+  svd_plane_of(base, n, f, 5)[p] = make_float4(sg.z, yield ? 1.f : 0.f, 0.f, 0.f);
 }
 DT_DEV void store_svd(const dt_world& w, int f, int p, const m3& U, v3 sg, const m3& V, bool yield) {
-  svd_plane(w, f, 0)[p] = make_float4(U.a[0][0], U.a[0][1], U.a[0][2], U.a[1][0]);
-  svd_plane(w, f, 1)[p] = make_float4(U.a[1][1], U.a[1][2], U.a[2][0], U.a[2][1]);
-  svd_plane(w, f, 2)[p] = make_float4(U.a[2][2], V.a[0][0], V.a[0][1], V.a[0][2]);
-  svd_plane(w, f, 3)[p] = make_float4(V.a[1][0], V.a[1][1], V.a[1][2], V.a[2][0]);
-  svd_plane(w, f, 4)[p] = make_float4(V.a[2][1], V.a[2][2], sg.x, sg.y);
-  svd_plane(w, f, 5)[p] = make_float4(sg.z, yield ? 1.f : 0.f, 0.f, 0.f);
+  store_svd_of(w.p_svd, w.n_particles, f, p, U, sg, V, yield);
 }
-DT_DEV void load_svd(const dt_world& w, int f, int p, m3& U, v3& sg, m3& V) {
-  const float4 a = svd_plane(w, f, 0)[p], b = svd_plane(w, f, 1)[p], c = svd_plane(w, f, 2)[p],
-               d = svd_plane(w, f, 3)[p], e = svd_plane(w, f, 4)[p], g = svd_plane(w, f, 5)[p];
+DT_DEV void load_svd_of(float* base, int n, int f, int p, m3& U, v3& sg, m3& V) {
+  const float4 a = svd_plane_of(base, n, f, 0)[p], b = svd_plane_of(base, n, f, 1)[p],
+               c = svd_plane_of(base, n, f, 2)[p], d = svd_plane_of(base, n, f, 3)[p],
+               e = svd_plane_of(base, n, f, 4)[p], g = svd_plane_of(base, n, f, 5)[p];
   U.a[0][0] = a.x; U.a[0][1] = a.y; U.a[0][2] = a.z; U.a[1][0] = a.w;
   U.a[1][1] = b.x; U.a[1][2] = b.y; U.a[2][0] = b.z; U.a[2][1] = b.w;
   U.a[2][2] = c.x; V.a[0][0] = c.y; V.a[0][1] = c.z; V.a[0][2] = c.w;
   V.a[1][0] = d.x; V.a[1][1] = d.y; V.a[1][2] = d.z; V.a[2][0] = d.w;
   V.a[2][1] = e.x; V.a[2][2] = e.y; sg = v3{e.z, e.w, g.x};
+}
+DT_DEV void load_svd(const dt_world& w, int f, int p, m3& U, v3& sg, m3& V) {
+  load_svd_of(w.p_svd, w.n_particles, f, p, U, sg, V);
 }
 
 // constitutive update of one particle (compute_new_F + svd + stress, mpm_elastic.py:135-187,

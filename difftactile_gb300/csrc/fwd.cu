@@ -156,6 +156,7 @@ __device__ void fem_tet(const dt_world& w, int f, int t) {
     m3 U, V;
     v3 sg;
     svd3(Fe, U, sg, V, w.svd_sweeps);
+    if (w.t_svd && !w.skip_tape) store_svd_of(w.t_svd, w.n_tets, f, t, U, sg, V, false);  // for the adjoint
     const m3 R = mmulT(U, V);
     const float c = ((sg.x + sg.y) + sg.z) - 3.f;
 #pragma unroll
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w
         const int Gall = (S.nf + 31) >> 5;
         int nc = 0;
         const int* cand = nullptr;
-        if (CAND && in_smem && Gall > 32) {  // block-uniform: the groups any node of this block can need
+        if (CAND && in_smem && Gall > DT_CAND_MIN_GROUPS) {  // block-uniform: the groups any node of this block can need
           const float4 qlo = make_float4(__fmul_rn(__fadd_rn((float)(4 * bi), 0.5f), E.dx),
                                          __fmul_rn(__fadd_rn((float)(4 * bj), 0.5f), E.dx),
                                          __fmul_rn(__fadd_rn((float)(4 * bk), 0.5f), E.dx), 0.f);
@@ -539,7 +540,7 @@ int l2(const dt_world* w, int f, cudaStream_t st) {
   return launch_status(launch_k(k_fwd_grid<LPN, CAND>, nb, 64 * LPN, smem, st, *w, f, cap));
 }
 int launch_l2(const dt_world* w, int f, cudaStream_t st) {
-  const bool big = w->max_sensor_tris > 32 * 32;  // some sensor has more than 32 groups
+  const bool big = w->max_sensor_tris > 32 * DT_CAND_MIN_GROUPS;  // a sensor of more groups than that
   if (w->contact_lanes == 4) return big ? l2<4, true>(w, f, st) : l2<4, false>(w, f, st);
   return big ? l2<8, true>(w, f, st) : l2<8, false>(w, f, st);
 }

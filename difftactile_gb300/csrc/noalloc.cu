@@ -83,6 +83,7 @@ int dt_substep_fwd_noalloc(const dt_world* w, int f, cudaStream_t stream) {
     v.r_cidx = w->r_cidx + (size_t)f * R;
   }
   if (w->p_svd) v.p_svd = w->p_svd + (size_t)f * 6 * w->n_particles * 4;
+  if (w->t_svd) v.t_svd = w->t_svd + (size_t)f * 6 * w->n_tets * 4;
   v.n_frames = 2;
   v.tape_blocks = w->n_blocks;
   v.g_acc = reinterpret_cast<float*>(S + NA_OFF_ACC);

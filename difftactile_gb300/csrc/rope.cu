@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(RC_NT) k_rope_contact(dt_world w, int f, int s
     const int Gall = (S.nf + 31) >> 5;
     int nc = 0;
     const int* cand = nullptr;
-    if (CAND && in_smem && Gall > 32) {  // block-uniform: the groups any particle of this CTA can need
+    if (CAND && in_smem && Gall > DT_CAND_MIN_GROUPS) {  // block-uniform: the groups any particle of this CTA can need
       if (threadIdx.x == 0) {
         s_box[0] = s_box[1] = s_box[2] = f2ord(3.4e38f);
         s_box[3] = s_box[4] = s_box[5] = f2ord(-3.4e38f);
@@ -372,7 +372,7 @@ int rope_part(const dt_world* w, int f, int part, cudaStream_t stream) {
     const int cap = w->max_sensor_tris < SMEM_CENT_MAX ? w->max_sensor_tris : SMEM_CENT_MAX;
     const size_t smem = stage_bytes(cap);
     static size_t conf_c[64] = {}, conf_cc[64] = {};
-    const bool big = w->max_sensor_tris > 32 * 32;  // some sensor has more than 32 groups
+    const bool big = w->max_sensor_tris > 32 * DT_CAND_MIN_GROUPS;  // a sensor of more groups than that
     if ((rc = set_smem(big ? (const void*)k_rope_contact<true> : (const void*)k_rope_contact<false>, smem,
                        big ? conf_cc : conf_c)))
       return rc;

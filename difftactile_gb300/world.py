@@ -268,6 +268,9 @@ class World:
         t["r_work"] = zeros((2 * max_iters, NR, 4)) if (max_iters > 1 and NR) else None
         # the forward's SVD per frame, so that the adjoint need not recompute it (96 B per particle-frame)
         t["p_svd"] = zeros((Fn, 6, Np, 4)) if (svd_tape and Np) else None
+        # the linear corotated tets' SVD, likewise (read by the tet adjoint)
+        lin = any(int(getattr(sp, "model", 0)) == 1 for sp in self.sensor_specs)
+        t["t_svd"] = zeros((Fn, 6, self.n_tets, 4)) if (svd_tape and lin and self.n_tets) else None
 
         w = N.DtWorld()
         for name in N.WORLD_PTR_FIELDS:
@@ -291,6 +294,7 @@ class World:
         w.r_work = t["r_work"].data_ptr() if t["r_work"] is not None else None
         w.max_rope_iters = max_iters if t["r_work"] is not None else 1
         w.p_svd = t["p_svd"].data_ptr() if t["p_svd"] is not None else None
+        w.t_svd = t["t_svd"].data_ptr() if t["t_svd"] is not None else None
         # ropes: the solver (one CTA per rope) and its adjoint run on a second stream beside the MPM
         # stages (dt_world.aux_stream); the events are created by recording them once
         self._aux = None

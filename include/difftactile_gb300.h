@@ -50,7 +50,7 @@
 extern "C" {
 #endif
 
-#define DT_ABI_VERSION 6
+#define DT_ABI_VERSION 7
 
 #define DT_OK 0
 #define DT_ERR_ARG (-1)        /* null pointer, bad size or frame index */
@@ -244,6 +244,10 @@ typedef struct dt_world {
                                     stream before the call returns.  NULL: everything on the call's
                                     stream. */
   cudaEvent_t aux_events[2];     /* fork and join events (cudaEventDisableTiming), required with aux_stream */
+  /* ---- optional SVD tape of the linear corotated tets (ABI 7) ---- */
+  float* t_svd;                  /* [n_frames][6][n_tets][4]: U, V, sigma of each DT_FEM_LINEAR_COROTATED
+                                    tet's F per frame, in p_svd's plane layout, written by the forward,
+                                    read by the tet adjoint instead of recomputing; NULL: recomputed */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared
