@@ -152,12 +152,15 @@ NAMES = {("fwd", 0): "k_fwd_p2g_fem", ("fwd", 1): "k_fwd_grid", ("fwd", 2): "k_f
          ("bwd", 3): "k_bwd_p2g_fem"}
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch, from one ncu capture of the
-# 16-environment population (the first 16 environments, 843,880 particles; ncu --set full, one launch
-# each, --clock-control none) scaled to the full population by its particle count (3,221,208 / 843,880):
-# a static capture, not a live measurement, valid for the kernel build it was taken of
-NCU_TRAFFIC = {"captured_at": "the build of commit 1bb8388 (before the no-tape forward)",
-               "per_launch_bytes": {"k_fwd_p2g_fem": 193.3e6 * 3.817, "k_fwd_grid": 4.71e6 * 3.817,
-                                    "k_bwd_p2g_fem": 311.8e6 * 3.817, "k_bwd_g2p_fem": 85.4e6 * 3.817}}
+# 16-environment population (the first 16 environments, 843,880 particles; ncu --set full, the sixth
+# launch of each kernel, --clock-control none; the forward P2G's is a launch of the first, untaped
+# forward pass) scaled to the full population by its particle count (3,221,208 / 843,880): a static
+# capture, not a live measurement, valid for the kernel build it was taken of
+NCU_TRAFFIC = {"captured_at": "the build of commit d5aa2b7 (re-binning, two particles per thread, tet SVD tape)",
+               "per_launch_bytes": {k: b * 3.817 for k, b in (
+                   ("k_fwd_p2g_fem", 129.9e6), ("k_fwd_grid", 4.64e6), ("k_fwd_g2p_fem", 31.5e6),
+                   ("k_bwd_restore", 3.92e6), ("k_bwd_g2p_fem", 89.8e6), ("k_bwd_grid", 12.1e6),
+                   ("k_bwd_p2g_fem", 349.5e6))}}
 
 
 def algo_bytes(key, units):

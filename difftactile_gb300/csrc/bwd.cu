@@ -379,6 +379,19 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   for (int k = 0; k < 6; ++k) q[k] = ldg4(pplane(w, f, k) + p);
   PRec r;
   unpack_rec(q, r);
+  // adjoint of F[f+1]
+  const float4 n3 = ld4(padj(w, nb, 3) + p), n4 = ld4(padj(w, nb, 4) + p), n5 = ld4(padj(w, nb, 5) + p);
+  m3 Fpb;
+  Fpb.a[0][0] = n3.w;
+  Fpb.a[0][1] = n4.x;
+  Fpb.a[0][2] = n4.y;
+  Fpb.a[1][0] = n4.z;
+  Fpb.a[1][1] = n4.w;
+  Fpb.a[1][2] = n5.x;
+  Fpb.a[2][0] = n5.y;
+  Fpb.a[2][1] = n5.z;
+  Fpb.a[2][2] = n5.w;
+  const float4 xpart = ld4(padj(w, cb, 0) + p);  // x adjoint from the G2P adjoint
   const dt_env& E = w.envs[__ldg(w.p_env + p)];
   int base[3];
   float fx[3];
@@ -387,9 +400,8 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   mub = lamb = 0.f;
   if (!particle_base(E, r.x, base, fx)) {
     // carried unchanged in the forward pass: adjoint passes straight through
-    const float4 xpart = ld4(padj(w, cb, 0) + p);  // x adjoint from the G2P adjoint
     const float4 a0 = ld4(padj(w, nb, 0) + p), a1 = ld4(padj(w, nb, 1) + p), a2 = ld4(padj(w, nb, 2) + p),
-                 a3 = ld4(padj(w, nb, 3) + p), n4 = ld4(padj(w, nb, 4) + p), n5 = ld4(padj(w, nb, 5) + p);
+                 a3 = ld4(padj(w, nb, 3) + p);
     float4 o[6] = {make_float4(xpart.x, xpart.y, xpart.z, a0.w), a1, a2, a3, n4, n5};
 #pragma unroll
     for (int k = 0; k < 6; ++k) padj(w, cb, k)[p] = o[k];
@@ -447,23 +459,6 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
         fxb[1] += Wb * (wts[oi][0] * dws[oj][1] * wts[ok][2]);
         fxb[2] += Wb * (wts[oi][0] * wts[oj][1] * dws[ok][2]);
       }
-#if DT_BWD_P2G_RECOMPUTE
-  // the constitutive state again, from the SVD tape: not kept live across the gather above
-  constitutive(r.C, r.F, w.dt, M, w.svd_sweeps, s, &w, w.p_svd ? f : -1, p);
-#endif
-  // adjoint of F[f+1], and the x adjoint from the G2P adjoint
-  const float4 n3 = ld4(padj(w, nb, 3) + p), n4 = ld4(padj(w, nb, 4) + p), n5 = ld4(padj(w, nb, 5) + p);
-  m3 Fpb;
-  Fpb.a[0][0] = n3.w;
-  Fpb.a[0][1] = n4.x;
-  Fpb.a[0][2] = n4.y;
-  Fpb.a[1][0] = n4.z;
-  Fpb.a[1][1] = n4.w;
-  Fpb.a[1][2] = n5.x;
-  Fpb.a[2][0] = n5.y;
-  Fpb.a[2][1] = n5.z;
-  Fpb.a[2][2] = n5.w;
-  const float4 xpart = ld4(padj(w, cb, 0) + p);
   const v3 vb = pm * S0;
   m3 Ab;
 #pragma unroll

@@ -24,13 +24,12 @@
 #ifndef DT_MINB_BWD_GRID
 #define DT_MINB_BWD_GRID 8
 #endif
+// the P2G adjoint: 4 CTAs of 128 threads (128 registers, ~250 B of spills).  Measured on the
+// re-binned population at mid-rollout: 5 CTAs (96 registers, ~1 KB of spills) 616 -> 772 us; keeping
+// the constitutive state out of registers across the 27-node gather (recomputed from the SVD tape
+// after it: 48 B of spills) 627 -> 657 us at 4 CTAs, 631 us at 5
 #ifndef DT_MINB_BWD_P2G
 #define DT_MINB_BWD_P2G 4
-#endif
-// 1: the P2G adjoint recomputes the particle's constitutive state (from the SVD tape) after its
-// 27-node gather instead of keeping it live across it (fewer live registers, more arithmetic)
-#ifndef DT_BWD_P2G_RECOMPUTE
-#define DT_BWD_P2G_RECOMPUTE 0
 #endif
 // Contact searches over sensors of more than this many groups of 32 centroids first reduce the groups to
 // the candidates of the query block (contact.cuh: block_candidates); smaller sensors keep every group's
