@@ -29,6 +29,13 @@ def test_argument_errors_are_status_codes_without_a_device():
     assert lib.dt_copy_frame(wp, 0, 3, None) == -1
     assert lib.dt_pose_control_vel_all(wp, None, 1.0, 0, 1, None) == -1
     assert lib.dt_pose_control_vel_bwd_all(wp, None, 1.0, None, 0, 1, None) == -1
+    buf = ctypes.c_int(0)
+    assert lib.dt_rebin(wp, 0, None, None, None, None) == -1                  # no material index / permutation
+    assert lib.dt_rebin(wp, 3, ctypes.byref(buf), ctypes.byref(buf), ctypes.byref(buf), None) == -1  # frame
+    assert lib.dt_rebin(None, 0, ctypes.byref(buf), ctypes.byref(buf), ctypes.byref(buf), None) == -1
+    assert lib.dt_rebin_permute(wp, 2, 0, ctypes.byref(buf), ctypes.byref(buf), ctypes.byref(buf), None) == -1
+    assert lib.dt_rebin_permute(wp, 0, 1, ctypes.byref(buf), ctypes.byref(buf), ctypes.byref(buf), None) == -1
+    assert lib.dt_rebin_scratch_bytes(None) == 0
     with pytest.raises(N.DtError, match="DT_ERR_ARG"):
         N.check(lib.dt_substep_fwd(wp, 7, None), "dt_substep_fwd")
 
@@ -93,6 +100,36 @@ def test_undersized_grid_tape_is_flagged_not_overrun(cuda_lib):
     big.substep(0)
     torch.cuda.synchronize()
     assert big.error_word() == 0
+
+
+@pytest.mark.gpu
+def test_rope_iterations_beyond_the_workspace_are_flagged_not_overrun(cuda_lib):
+    """A rope of six pass pairs whose adjoint workspace is declared for only two (max_rope_iters = 2):
+    the adjoint of that rope is skipped and DT_DEVERR_ROPE_ITERS set, nothing is written past the
+    workspace, and with the workspace declared again the same world's adjoint runs clean."""
+    from difftactile_gb300.world import World
+    env = SS.rope_under_pad()
+    env = env.replace(ropes=[env.ropes[0].replace(iters=6)])
+    w = World([env], n_frames=2, dt=DT, grad_clip=0.0)
+    assert w.t["r_work"] is not None and w.w.max_rope_iters == 6
+    guard = w.t["r_work"].clone()
+    w.step_begin()
+    w.substep(0)
+    w.adj_clear()
+    w.t["r_adj"][1].fill_(1.0)
+    w.w.max_rope_iters = 2
+    w.substep_bwd(0)
+    torch.cuda.synchronize()
+    assert w.error_word() & 8                            # the rope's passes exceed the declared workspace
+    assert torch.equal(w.t["r_work"][4:], guard[4:])     # nothing written beyond 2 x 2 pass inputs
+    w.clear_error()
+    w.w.max_rope_iters = 6
+    w.adj_clear()
+    w.t["r_adj"][1].fill_(1.0)
+    w.substep_bwd(0)
+    torch.cuda.synchronize()
+    assert w.error_word() == 0
+    assert torch.isfinite(w.t["r_adj"][0]).all() and float(w.t["r_adj"][0].abs().sum()) > 0
 
 
 @pytest.mark.gpu
