@@ -76,6 +76,8 @@ def parse():
                     "replaying the rollout's recorded CUDA graphs")
     ap.add_argument("--rebin", type=int, default=1,
                     help="checkpointed rollouts: sort the particles by cell again at every N-th checkpoint (0: never)")
+    ap.add_argument("--readouts", action="store_true",
+                    help="run every readout / action / deform-loss entry point once (for a profiler) and exit")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the gradient check")
     ap.add_argument("--no-nested", action="store_true", help="skip the nested sensor-press measurement")
@@ -645,9 +647,59 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def exercise_readouts():
+    """Every readout, action and deform-loss entry point once, forward and adjoint, at configuration 2's
+    size (and the gripper's affine control velocities on a small grasp): the launches a profiler
+    captures for them (no timing, no JSON line)."""
+    import numpy as np
+    import torch
+    from difftactile_gb300 import _native as N
+    from difftactile_gb300 import configs, deform, markers, rigid
+    from difftactile_gb300.trajectory import GripperTrajectory, Trajectory
+    from difftactile_gb300.world import World
+    dev = torch.device("cuda", 0)
+    cfg = configs.sensor_press(n_steps=1)
+    w, tr = cfg.build(dev)
+    tr.forward(torch.as_tensor(cfg.actions, dtype=torch.float64, device=dev))
+    tr.backward()  # step begin, pose control, substeps, marker loss; their adjoints
+    f = 1
+    w.com(f)
+    gb = torch.zeros((w.n_envs, 4), device=dev)
+    gb[:, 1] = 1.0
+    N.check(w.lib.dt_com_bwd(w.wp, f, gb.data_ptr(), w.stream), "dt_com_bwd")
+    out = torch.zeros((1, 4), device=dev)
+    N.check(w.lib.dt_contact_force(w.wp, 0, f, out.data_ptr(), w.stream), "dt_contact_force")
+    ob = torch.ones((1, 4), device=dev)
+    N.check(w.lib.dt_contact_force_bwd(w.wp, 0, ob.data_ptr(), w.stream), "dt_contact_force_bwd")
+    mm = markers.MarkerModel(w, 0)
+    pred, virt = mm.readout(f)
+    mm.readout_bwd(f, torch.ones_like(pred), torch.ones_like(virt))
+    dl = deform.DeformLoss(w, 0)
+    n = dl.n
+    tgt = np.zeros(tuple(n), np.float32)
+    tgt[n[0] // 3:2 * n[0] // 3, 4:12, n[2] // 3:2 * n[2] // 3] = 1.0
+    dl.initialize(tgt, passes=2)
+    dl.grid_mass(f)
+    dl.compute_loss(f)
+    dl.compute_loss_grad(f)
+    rm = rigid.RigidMatch(w, 0, 0)
+    rm.H(f)
+    rm.backward(f, torch.ones(9, device=dev), 0)
+    cfg3, kin = configs.grasp_sphere(n_steps=2, substeps=5, n_grid=64, n_core=2_000, n_shell=18_000, ckpt_every=1)
+    w3 = World(cfg3.envs, n_frames=Trajectory.frames_needed(2, 5, 1), dt=cfg3.dt)
+    t3 = GripperTrajectory(w3, 2, kin, (0, 1), 1, ())
+    t3.forward(torch.as_tensor(cfg3.actions, dtype=torch.float64, device=dev))
+    t3.backward()
+    torch.cuda.synchronize()
+    if w.error_word() or w3.error_word():
+        raise SystemExit(f"device error word {w.error_word()} / {w3.error_word()}")
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.readouts:
+        exercise_readouts()
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
