@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--plain", type=int, default=8,
                     help="batched_population: time K environments (evenly spaced over the population) one "
                     "World each, one after the other, and report the batched / plain ratio (0: skip)")
-    ap.add_argument("--scatter", default=None, choices=["tile", "global", "warp"],
+    ap.add_argument("--scatter", default=None, choices=["tile", "global", "warp", "smem"],
                     help="27-node scatter strategy (default: the library's)")
     ap.add_argument("--no-pdl", action="store_true", help="launch the substep kernels without programmatic "
                     "dependent launch")
@@ -175,7 +175,7 @@ def algo_bytes(key, units):
 def build(cfg, dev, args, **extra):
     kw = dict(extra)
     if args.scatter is not None:
-        kw["scatter_mode"] = {"tile": 0, "global": 1, "warp": 2}[args.scatter]
+        kw["scatter_mode"] = {"tile": 0, "global": 1, "warp": 2, "smem": 3}[args.scatter]
     if args.no_svd_tape:
         kw["svd_tape"] = False
     if args.p_block is not None:
@@ -506,7 +506,7 @@ def run_ours(args):
                       "grids": sorted({e.n_grid[0] for e in cfg.envs}), "fem_tets": w.n_tets, "fem_nodes": w.n_verts,
                       "surface_tris": w.n_tris, "checkpoint_every": cfg.ckpt_every, "tape_blocks": w.tape_blocks,
                       "rebin_every": int(getattr(traj, "rebin_every", 0)),
-                      "scatter": ["tile", "global", "warp"][w.w.scatter_mode], "p_block": int(w.w.p_block),
+                      "scatter": ["tile", "global", "warp", "smem"][w.w.scatter_mode], "p_block": int(w.w.p_block),
                       "scatter_depth": int(w.w.scatter_depth),
                       "contact_lanes": 4 if int(w.w.contact_lanes) == 4 else 8,
                       "particles_per_thread": max(1, int(w.w.p_per_thread)),

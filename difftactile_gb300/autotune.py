@@ -3,8 +3,10 @@
 The substep's particle-role launches can be shaped three ways, and which is fastest depends on the
 scene (particle count and density, how many environments share the launch):
   scatter   how P2G and the G2P adjoint accumulate into the grid (dt_world.scatter_mode): a warp
-            segmented reduction before one RED per run and node ("warp"), one RED per particle and
-            node ("global"), or a shared-memory gather tile per CTA ("tile", 128 threads only);
+            segmented reduction before one RED per run and node ("warp"), whole-run sums added into a
+            shared-memory tile of the CTA's nodes flushed with one RED per node ("smem"), one RED per
+            particle and node ("global"), or a shared-memory gather tile per CTA ("tile", 128 threads
+            only);
   p_block   threads per CTA of the particle / tet / vertex launches (dt_world.p_block): 64, 128, 256;
   depth     with the warp scatter, the shuffle steps of the segmented reduction before the REDs
             (dt_world.scatter_depth): 0 sums whole runs (fewest REDs, longest shuffle chain), 1 or 2
@@ -33,13 +35,13 @@ import statistics
 
 import torch
 
-SCATTERS = {"tile": 0, "global": 1, "warp": 2}
+SCATTERS = {"tile": 0, "global": 1, "warp": 2, "smem": 3}
 DEFAULT = {"scatter": "warp", "p_block": 128, "depth": 0, "lanes": 8, "pdl": 1, "ppt": 1}
 
 _cache: dict[str, dict] = {}
 
 
-def candidates(scatters=("warp", "global", "tile"), p_blocks=(64, 128, 256), depths=(0, 1, 2), lanes=(8, 4),
+def candidates(scatters=("warp", "smem", "global", "tile"), p_blocks=(64, 128, 256), depths=(0, 1, 2), lanes=(8, 4),
                pdl=(1, 0), ppts=(1, 2)):
     out = []
     for s in scatters:

@@ -241,7 +241,7 @@ __device__ void integrate_bwd(const dt_world& w, int f, int i) {
 template <int MODE, int NT, int PPT>
 __global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_BWD_G2P, NT)) k_bwd_g2p_fem(dt_world w, int f, int nb_p, int nb_v) {
   pdl_entry();
-  extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
+  extern __shared__ float4 tile[];  // stencil records (TILE mode) or the grid tile (SMEM mode); none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
@@ -788,7 +788,7 @@ template <int MODE, int NT, int PPT>
 cudaError_t b1_ppt(const dt_world* w, int f, cudaStream_t stream) {
   const int nb_p = particle_ctas(w, NT, PPT), nb_v = cdiv(w->n_verts, NT);
   if (nb_p + nb_v == 0) return cudaSuccess;
-  const size_t smem = MODE == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0;
+  const size_t smem = scatter_smem(MODE, NT);
   return launch_k(k_bwd_g2p_fem<MODE, NT, PPT>, nb_p + nb_v, NT, smem, stream, *w, f, nb_p, nb_v);
 }
 template <int MODE, int NT>
@@ -846,6 +846,7 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
         case DT_SCATTER_GLOBAL: e = b1_nt<DT_SCATTER_GLOBAL>(w, f, stream); break;
         case DT_SCATTER_WARP + 1: e = b1_nt<DT_SCATTER_WARP + 1>(w, f, stream); break;
         case DT_SCATTER_WARP + 2: e = b1_nt<DT_SCATTER_WARP + 2>(w, f, stream); break;
+        case DT_MODE_SMEM: e = b1_nt<DT_MODE_SMEM>(w, f, stream); break;
         default: e = b1_nt<DT_SCATTER_WARP>(w, f, stream);
       }
       break;

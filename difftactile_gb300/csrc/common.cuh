@@ -369,9 +369,18 @@ inline cudaError_t note_error(cudaError_t e) {
 inline int launch_status(cudaError_t e) { return note_error(e) == cudaSuccess ? DT_OK : DT_ERR_LAUNCH; }
 
 // template scatter mode of the particle launches: DT_SCATTER_WARP + scatter_depth (depth 1 or 2)
+// (template MODE: DT_SCATTER_TILE, DT_SCATTER_GLOBAL, DT_SCATTER_WARP + depth, DT_MODE_SMEM + depth)
+constexpr int DT_MODE_SMEM = 8;
+constexpr int DT_SMEM_TILE = 512;  // nodes of the shared-memory tile of the SMEM scatter (8 KB)
 inline int scatter_kind(const dt_world* w) {
+  const int d = (w->scatter_depth == 1 || w->scatter_depth == 2) ? w->scatter_depth : 0;
+  if (w->scatter_mode == DT_SCATTER_SMEM) return DT_MODE_SMEM;  // whole runs only (the fastest SMEM variant)
   if (w->scatter_mode != DT_SCATTER_WARP) return w->scatter_mode == DT_SCATTER_TILE ? DT_SCATTER_TILE : DT_SCATTER_GLOBAL;
-  return DT_SCATTER_WARP + ((w->scatter_depth == 1 || w->scatter_depth == 2) ? w->scatter_depth : 0);
+  return DT_SCATTER_WARP + d;
+}
+// dynamic shared memory of a particle-role launch with scatter MODE and NT threads
+constexpr size_t scatter_smem(int MODE, int NT) {
+  return MODE == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : (MODE >= DT_MODE_SMEM ? DT_SMEM_TILE * 16 : 0);
 }
 // threads per CTA of the particle / tet / vertex launches (dt_world.p_block)
 inline int particle_block(const dt_world* w) { return (w->p_block == 64 || w->p_block == 256) ? w->p_block : 128; }
@@ -855,7 +864,15 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
     }
   } else if constexpr (MODE >= DT_SCATTER_WARP) {
     // segmented reduction over runs of lanes with the same base node (same env and cell): every
-    // lane of the warp takes part in the shuffles; lanes without a particle form runs of their own
+    // lane of the warp takes part in the shuffles; lanes without a particle form runs of their own.
+    // SMEM: the run sums go into a shared-memory tile of the CTA's box of nodes (shared atomics),
+    // flushed with one vector RED per touched node once every warp has added
+    constexpr bool SMEM = MODE >= DT_MODE_SMEM;
+    const bool in_tile = SMEM && compact && tile_n <= DT_SMEM_TILE;  // CTA-uniform
+    if (in_tile) {
+      for (int n = tid; n < 4 * tile_n; n += NT) sm[n] = 0.f;
+      __syncthreads();
+    }
     int node_off = 0, nb1 = 1, nb2 = 1;
     if (ok) {
       const dt_env& E = w.envs[env];
@@ -873,8 +890,9 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
     const int seg_end = after ? __ffs(after) - 1 : 32;
     const int run = __reduce_max_sync(0xffffffffu, head ? seg_end - lane : 0);
     int steps = run > 1 ? 32 - __clz(run - 1) : 0;
-    // MODE = DT_SCATTER_WARP + depth: at most `depth` shuffle steps (0: the whole run)
-    constexpr int DEPTH = MODE - DT_SCATTER_WARP;
+    // MODE = DT_SCATTER_WARP + depth (or DT_MODE_SMEM + depth): at most `depth` shuffle steps (0: the
+    // whole run)
+    constexpr int DEPTH = SMEM ? MODE - DT_MODE_SMEM : MODE - DT_SCATTER_WARP;
     if constexpr (DEPTH > 0) steps = min(steps, DEPTH);
     // after `steps` steps a lane holds the sum of its window of 2^steps lanes (clipped to the run);
     // the first lane of every window issues the RED
@@ -904,12 +922,35 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
             }
           }
           if (issuer && ok) {
-            const int i = base[0] + oi, j = base[1] + oj, k = base[2] + ok_;
-            const int n = node_off + ((((i >> 2) * nb1 + (j >> 2)) * nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
-                          ((j & 3) << 2) + (k & 3);
-            red_add_v4(dst + n, a);
+            if (in_tile) {
+              float* t = sm + 4 * (((base[0] - L0 + oi) * ey + (base[1] - L1 + oj)) * ez + (base[2] - L2 + ok_));
+              atomicAdd(t + 0, a.x);
+              atomicAdd(t + 1, a.y);
+              atomicAdd(t + 2, a.z);
+              if (a.w != 0.f) atomicAdd(t + 3, a.w);
+            } else {
+              const int i = base[0] + oi, j = base[1] + oj, k = base[2] + ok_;
+              const int n = node_off + ((((i >> 2) * nb1 + (j >> 2)) * nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
+                            ((j & 3) << 2) + (k & 3);
+              red_add_v4(dst + n, a);
+            }
           }
         }
+    if (in_tile) {
+      __syncthreads();
+      const dt_env& E0 = w.envs[w.p_env[min(chunk * NT, w.n_particles - 1)]];
+      const int t_off = E0.node_off, t_nb1 = E0.nb[1], t_nb2 = E0.nb[2];
+      const float4* tl = reinterpret_cast<const float4*>(sm);
+      for (int n = tid; n < tile_n; n += NT) {
+        const float4 v = tl[n];
+        if (v.x == 0.f && v.y == 0.f && v.z == 0.f && v.w == 0.f) continue;
+        const int nc = n % ez, nbb = (n / ez) % ey, na = n / (ey * ez);
+        const int i = L0 + na, j = L1 + nbb, k = L2 + nc;
+        const int g = t_off + ((((i >> 2) * t_nb1 + (j >> 2)) * t_nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
+                      ((j & 3) << 2) + (k & 3);
+        red_add_v4(dst + g, v);
+      }
+    }
     if (ok && !compact) mark_one(w.envs[env]);
   } else if (ok) {
     const dt_env& E = w.envs[env];

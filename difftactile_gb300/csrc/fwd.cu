@@ -204,7 +204,7 @@ __device__ void tri_centroid(const dt_world& w, int f, int t) {
 template <int MODE, int NT, int PPT>
 __global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_FWD_P2G, NT)) k_fwd_p2g_fem(dt_world w, int f, int nb_p, int nb_t, int nb_f) {
   pdl_entry();
-  extern __shared__ float4 tile[];  // 25 * NT words of stencil records in gather mode, none otherwise
+  extern __shared__ float4 tile[];  // stencil records (TILE mode) or the grid tile (SMEM mode); none otherwise
   __shared__ int sh[8];
   int b = blockIdx.x;
   if (b < nb_p) {
@@ -503,7 +503,7 @@ cudaError_t l1_ppt(const dt_world* w, int f, bool parts, bool fem, cudaStream_t 
   const int nb_t = fem ? cdiv(w->n_tets, NT) : 0;
   const int nb_f = fem ? cdiv(w->n_tris, NT) : 0;
   if (nb_p + nb_t + nb_f == 0) return cudaSuccess;
-  const size_t smem = MODE == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : 0;
+  const size_t smem = scatter_smem(MODE, NT);
   return launch_k(k_fwd_p2g_fem<MODE, NT, PPT>, nb_p + nb_t + nb_f, NT, smem, st, *w, f, nb_p, nb_t, nb_f);
 }
 template <int MODE, int NT>
@@ -525,6 +525,7 @@ int launch_l1(const dt_world* w, int f, bool parts, bool fem, cudaStream_t st) {
     case DT_SCATTER_GLOBAL: e = l1_nt<DT_SCATTER_GLOBAL>(w, f, parts, fem, st); break;
     case DT_SCATTER_WARP + 1: e = l1_nt<DT_SCATTER_WARP + 1>(w, f, parts, fem, st); break;
     case DT_SCATTER_WARP + 2: e = l1_nt<DT_SCATTER_WARP + 2>(w, f, parts, fem, st); break;
+    case DT_MODE_SMEM: e = l1_nt<DT_MODE_SMEM>(w, f, parts, fem, st); break;
     default: e = l1_nt<DT_SCATTER_WARP>(w, f, parts, fem, st);
   }
   return e == cudaSuccess ? DT_OK : DT_ERR_LAUNCH;

@@ -253,11 +253,15 @@ typedef struct dt_world {
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared
  * memory and issues one vector RED per touched node; GLOBAL issues one 16-byte vector RED per
  * particle and node (L2 atomics); WARP first sums, over each run of consecutive lanes whose particles
- * share a base cell (particles are kept in Morton order, so runs are long), with a segmented
- * shuffle reduction, then issues one RED per run and node. */
+ * share a base cell (particles are kept sorted by cell, so runs are long), with a segmented
+ * shuffle reduction, then issues one RED per run and node; SMEM sums whole runs the same way, then
+ * adds into a shared-memory tile of the grid around the CTA's particles (shared atomics) and flushes
+ * the tile with one RED per touched node (falling back to WARP for a CTA whose particles' stencils
+ * do not fit the tile).  scatter_depth caps the segmented reduction of WARP (SMEM ignores it). */
 #define DT_SCATTER_TILE 0
 #define DT_SCATTER_GLOBAL 1
 #define DT_SCATTER_WARP 2
+#define DT_SCATTER_SMEM 3
 
 /* SVD adjoint of the rotation R = U V^T used by the corotated stress:
  * STABLE evaluates the reference formula's rotation term in the algebraically equal form

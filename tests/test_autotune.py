@@ -11,12 +11,12 @@ from difftactile_gb300 import autotune as AT
 
 def test_candidates_cover_the_shapes():
     c = AT.candidates()
-    assert len(c) == 2 * 2 * (3 * 3 * 2 + 3 * 2 + 2)
+    assert len(c) == 2 * 2 * (3 * 3 * 2 + 2 * 3 * 2 + 2)
     assert {x["lanes"] for x in c} == {8, 4}
     assert {x["ppt"] for x in c} == {1, 2}
     assert {x["p_block"] for x in c if x["scatter"] == "tile"} == {128}
     assert {(x["scatter"], x["p_block"]) for x in c if x["scatter"] != "tile"} == \
-        {(s, b) for s in ("warp", "global") for b in (64, 128, 256)}
+        {(s, b) for s in ("warp", "smem", "global") for b in (64, 128, 256)}
     assert {x["depth"] for x in c if x["scatter"] == "warp"} == {0, 1, 2}
     assert {x["depth"] for x in c if x["scatter"] != "warp"} == {0}
     assert len({AT.label(x) for x in c}) == len(c)

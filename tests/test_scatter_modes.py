@@ -14,7 +14,7 @@ from tests.test_parity_fwd import compare, run_oracle
 
 pytestmark = pytest.mark.gpu
 DT = 1e-4
-MODES = {"tile": 0, "global": 1, "warp": 2}
+MODES = {"tile": 0, "global": 1, "warp": 2, "smem": 3}
 
 
 @pytest.mark.parametrize("sort", [True, False])
@@ -68,7 +68,8 @@ def test_warp_runs_across_env_boundaries(cuda_lib):
 @pytest.mark.parametrize("mode,p_block,depth,ppt", [("warp", 64, 0, 1), ("warp", 256, 0, 1), ("global", 64, 0, 1),
                                                     ("global", 256, 0, 1), ("warp", 128, 1, 1), ("warp", 128, 2, 1),
                                                     ("warp", 256, 1, 1), ("warp", 128, 1, 2), ("warp", 64, 0, 2),
-                                                    ("global", 256, 0, 2), ("tile", 128, 0, 2)])
+                                                    ("global", 256, 0, 2), ("tile", 128, 0, 2), ("smem", 128, 0, 1),
+                                                    ("smem", 128, 0, 2), ("smem", 64, 0, 1), ("smem", 256, 0, 2)])
 def test_particle_block_sizes(cuda_lib, mode, p_block, depth, ppt):
     """Particle-role CTAs of 64 and 256 threads, capped segmented reductions and two chunks of
     particles per CTA (the autotuner's other shapes; 1,152 particles: an odd number of chunks, so the
