@@ -28,6 +28,12 @@
 // re-binned population at mid-rollout: 5 CTAs (96 registers, ~1 KB of spills) 616 -> 772 us; keeping
 // the constitutive state out of registers across the 27-node gather (recomputed from the SVD tape
 // after it: 48 B of spills) 627 -> 657 us at 4 CTAs, 631 us at 5
+// the grid kernel: minimum resident CTAs per SM stated for its 256-thread (4-lane) form, halved for
+// the 512-thread (8-lane) form; 4: 64 registers.  Measured on the population substep: 5 (48 registers,
+// 260 B of spills) 217 -> 222 us, 6 (40 registers) 238 us
+#ifndef DT_MINB_FWD_GRID
+#define DT_MINB_FWD_GRID 4
+#endif
 #ifndef DT_MINB_BWD_P2G
 #define DT_MINB_BWD_P2G 4
 #endif

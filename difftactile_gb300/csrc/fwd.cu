@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_FWD_P2G, NT)) k_fwd_p2g_fe
 // ---------------------------------------------------------------------------------------------
 // CAND: sensors of more than 32 groups of centroids are searched over per-block candidate groups
 template <int GRID_LPN, bool CAND, int GRID_NT = 64 * GRID_LPN>
-__global__ void __launch_bounds__(GRID_NT, 1024 / GRID_NT) k_fwd_grid(dt_world w, int f, int smem_cap) {
+__global__ void __launch_bounds__(GRID_NT, DT_MINB_FWD_GRID * 1024 / GRID_NT / 4) k_fwd_grid(dt_world w, int f, int smem_cap) {
   pdl_entry();
   extern __shared__ float4 scent[];
   float4* gbox = scent + smem_cap;  // 2 float4 per group of 32 centroids
