@@ -194,7 +194,7 @@ __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile,
   rec.c2 = c2;
   auto no_box = [](const dt_env&, int, int, int, int, int, int) {};
   auto no_one = [](const dt_env&) {};
-  stencil_scatter<NT, TILE_MAX, MODE>(w, chunk, ok, env, base, rec, reinterpret_cast<float*>(tile), sh,
+  stencil_scatter<NT, TILE_MAX, MODE, false>(w, chunk, ok, env, base, rec, reinterpret_cast<float*>(tile), sh,
                                 reinterpret_cast<float4*>(w.g_adj_vout), no_box, no_one);
 }
 
@@ -251,7 +251,8 @@ __global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_BWD_G2P, NT)) k_bwd_g2p_fe
       int c0, c1;
       cta_chunks(w, NT, PPT, b, c0, c1);
       for (int c = c0; c < c1; ++c) {
-        if (c > c0) __syncthreads();  // the shared tile and flags of the previous chunk
+        // the shared tile of the previous chunk (the modes without one share nothing between chunks)
+        if (c > c0 && (MODE == DT_SCATTER_TILE || MODE >= DT_MODE_SMEM)) __syncthreads();
         g2p_bwd_chunk<MODE, NT>(w, f, c, tile, sh);
       }
     }

@@ -775,47 +775,58 @@ struct StencilRec {
 };
 
 // MODE: DT_SCATTER_TILE, DT_SCATTER_GLOBAL, or DT_SCATTER_WARP + d for the warp reduction capped at
-// d shuffle steps (d = 0: whole runs; dt_world.scatter_depth selects d at launch)
-template <int NT, int TILE_MAX, int MODE, typename MarkBox, typename MarkOne>
+// d shuffle steps (d = 0: whole runs; dt_world.scatter_depth selects d at launch).  MARK: the scatter
+// marks the grid blocks it touches (P2G); without it (the G2P adjoint) the warp and global modes need
+// no bounding box and skip its two CTA barriers.
+template <int NT, int TILE_MAX, int MODE, bool MARK = true, typename MarkBox, typename MarkOne>
 DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, const int base[3], const StencilRec& r,
                             float* sm, int* sh, float4* dst, const MarkBox& mark_box, const MarkOne& mark_one) {
   const int tid = threadIdx.x;
   const int lane = tid & 31;
-  if (tid == 0) {
-    sh[0] = sh[1] = sh[2] = 0x7fffffff;
-    sh[3] = sh[4] = sh[5] = (int)0x80000000;
-    const int p0 = chunk * NT, p1 = min(p0 + NT, w.n_particles) - 1;
-    sh[6] = (w.p_env[p0] == w.p_env[p1]) ? 1 : 0;
-  }
-  __syncthreads();
-  int lo0 = ok ? base[0] : 0x7fffffff, lo1 = ok ? base[1] : 0x7fffffff, lo2 = ok ? base[2] : 0x7fffffff;
-  int hi0 = ok ? base[0] : (int)0x80000000, hi1 = ok ? base[1] : (int)0x80000000,
-      hi2 = ok ? base[2] : (int)0x80000000;
-  lo0 = __reduce_min_sync(0xffffffffu, lo0);
-  lo1 = __reduce_min_sync(0xffffffffu, lo1);
-  lo2 = __reduce_min_sync(0xffffffffu, lo2);
-  hi0 = __reduce_max_sync(0xffffffffu, hi0);
-  hi1 = __reduce_max_sync(0xffffffffu, hi1);
-  hi2 = __reduce_max_sync(0xffffffffu, hi2);
-  if (lane == 0 && hi0 != (int)0x80000000) {
-    atomicMin(sh + 0, lo0);
-    atomicMin(sh + 1, lo1);
-    atomicMin(sh + 2, lo2);
-    atomicMax(sh + 3, hi0);
-    atomicMax(sh + 4, hi1);
-    atomicMax(sh + 5, hi2);
-  }
-  __syncthreads();
-  const int L0 = sh[0], L1 = sh[1], L2 = sh[2];
-  const bool any = sh[3] != (int)0x80000000;
-  const int ex = any ? sh[3] - L0 + 3 : 0, ey = any ? sh[4] - L1 + 3 : 0, ez = any ? sh[5] - L2 + 3 : 0;
-  const int tile_n = ex * ey * ez;
-  const bool compact = any && sh[6] && tile_n <= TILE_MAX;
+  constexpr bool BOX = MARK || MODE == DT_SCATTER_TILE || MODE >= DT_MODE_SMEM;
+  int L0 = 0, L1 = 0, L2 = 0, ex = 0, ey = 0, ez = 0, tile_n = 0;
+  bool compact = false;
+  if constexpr (BOX) {
+    if (tid == 0) {
+      sh[0] = sh[1] = sh[2] = 0x7fffffff;
+      sh[3] = sh[4] = sh[5] = (int)0x80000000;
+      const int p0 = chunk * NT, p1 = min(p0 + NT, w.n_particles) - 1;
+      sh[6] = (w.p_env[p0] == w.p_env[p1]) ? 1 : 0;
+    }
+    __syncthreads();
+    int lo0 = ok ? base[0] : 0x7fffffff, lo1 = ok ? base[1] : 0x7fffffff, lo2 = ok ? base[2] : 0x7fffffff;
+    int hi0 = ok ? base[0] : (int)0x80000000, hi1 = ok ? base[1] : (int)0x80000000,
+        hi2 = ok ? base[2] : (int)0x80000000;
+    lo0 = __reduce_min_sync(0xffffffffu, lo0);
+    lo1 = __reduce_min_sync(0xffffffffu, lo1);
+    lo2 = __reduce_min_sync(0xffffffffu, lo2);
+    hi0 = __reduce_max_sync(0xffffffffu, hi0);
+    hi1 = __reduce_max_sync(0xffffffffu, hi1);
+    hi2 = __reduce_max_sync(0xffffffffu, hi2);
+    if (lane == 0 && hi0 != (int)0x80000000) {
+      atomicMin(sh + 0, lo0);
+      atomicMin(sh + 1, lo1);
+      atomicMin(sh + 2, lo2);
+      atomicMax(sh + 3, hi0);
+      atomicMax(sh + 4, hi1);
+      atomicMax(sh + 5, hi2);
+    }
+    __syncthreads();
+    L0 = sh[0];
+    L1 = sh[1];
+    L2 = sh[2];
+    const bool any = sh[3] != (int)0x80000000;
+    ex = any ? sh[3] - L0 + 3 : 0;
+    ey = any ? sh[4] - L1 + 3 : 0;
+    ez = any ? sh[5] - L2 + 3 : 0;
+    tile_n = ex * ey * ez;
+    compact = any && sh[6] && tile_n <= TILE_MAX;
+    if (compact) {
+      const dt_env& E0 = w.envs[w.p_env[min(chunk * NT, w.n_particles - 1)]];
+      mark_box(E0, L0, L1, L2, L0 + ex - 1, L1 + ey - 1, L2 + ez - 1);
+    }
+  }  // BOX
   const bool gather = MODE == DT_SCATTER_TILE && compact;
-  if (compact) {
-    const dt_env& E0 = w.envs[w.p_env[min(chunk * NT, w.n_particles - 1)]];
-    mark_box(E0, L0, L1, L2, L0 + ex - 1, L1 + ey - 1, L2 + ez - 1);
-  }
   if (gather) {
     // stencil records, structure of arrays: rows 0-2 base (int bits), 3-11 weights, 12-15 q, 16-24 c
     float* rec = sm;
@@ -957,7 +968,7 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
         red_add_v4(dst + g, v);
       }
     }
-    if (ok && !compact) mark_one(w.envs[env]);
+    if (MARK && ok && !compact) mark_one(w.envs[env]);
   } else if (ok) {
     const dt_env& E = w.envs[env];
     const int node_off = E.node_off, nb1 = E.nb[1], nb2 = E.nb[2];
