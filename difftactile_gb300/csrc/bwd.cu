@@ -192,7 +192,7 @@ __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile,
   rec.c0 = c0;
   rec.c1 = c1;
   rec.c2 = c2;
-  auto no_box = [](const dt_env&, int, int, int, int, int, int) {};
+  auto no_box = [](const dt_env&, int, int, int, int, int, int, int, int) {};
   auto no_one = [](const dt_env&) {};
   stencil_scatter<NT, TILE_MAX, MODE, false>(w, chunk, ok, env, base, rec, reinterpret_cast<float*>(tile), sh,
                                 reinterpret_cast<float4*>(w.g_adj_vout), no_box, no_one);

@@ -783,7 +783,9 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
                             float* sm, int* sh, float4* dst, const MarkBox& mark_box, const MarkOne& mark_one) {
   const int tid = threadIdx.x;
   const int lane = tid & 31;
-  constexpr bool BOX = MARK || MODE == DT_SCATTER_TILE || MODE >= DT_MODE_SMEM;
+  // the CTA's box of base cells: for the tile modes, and for marking in the global mode; the warp mode
+  // marks per warp (below), without CTA barriers
+  constexpr bool BOX = MODE == DT_SCATTER_TILE || MODE >= DT_MODE_SMEM || (MARK && MODE == DT_SCATTER_GLOBAL);
   int L0 = 0, L1 = 0, L2 = 0, ex = 0, ey = 0, ez = 0, tile_n = 0;
   bool compact = false;
   if constexpr (BOX) {
@@ -823,7 +825,7 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
     compact = any && sh[6] && tile_n <= TILE_MAX;
     if (compact) {
       const dt_env& E0 = w.envs[w.p_env[min(chunk * NT, w.n_particles - 1)]];
-      mark_box(E0, L0, L1, L2, L0 + ex - 1, L1 + ey - 1, L2 + ez - 1);
+      mark_box(E0, L0, L1, L2, L0 + ex - 1, L1 + ey - 1, L2 + ez - 1, tid, NT);
     }
   }  // BOX
   const bool gather = MODE == DT_SCATTER_TILE && compact;
@@ -968,7 +970,28 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
         red_add_v4(dst + g, v);
       }
     }
-    if (MARK && ok && !compact) mark_one(w.envs[env]);
+    if constexpr (MARK && !SMEM) {
+      // the blocks this warp's stencils touch: the warp's box of base cells (+2 nodes) when its
+      // particles share one environment and the box spans at most 32 blocks, else per particle
+      const int e_lo = __reduce_min_sync(0xffffffffu, ok ? env : 0x7fffffff);
+      const int e_hi = __reduce_max_sync(0xffffffffu, ok ? env : -1);
+      if (e_hi >= 0) {  // warp-uniform: some particle of the warp was scattered
+        const int l0 = __reduce_min_sync(0xffffffffu, ok ? base[0] : 0x7fffffff);
+        const int l1 = __reduce_min_sync(0xffffffffu, ok ? base[1] : 0x7fffffff);
+        const int l2 = __reduce_min_sync(0xffffffffu, ok ? base[2] : 0x7fffffff);
+        const int h0 = __reduce_max_sync(0xffffffffu, ok ? base[0] + 2 : -1);
+        const int h1 = __reduce_max_sync(0xffffffffu, ok ? base[1] + 2 : -1);
+        const int h2 = __reduce_max_sync(0xffffffffu, ok ? base[2] + 2 : -1);
+        const int nbx = (h0 >> 2) - (l0 >> 2) + 1, nby = (h1 >> 2) - (l1 >> 2) + 1, nbz = (h2 >> 2) - (l2 >> 2) + 1;
+        if (e_lo == e_hi && nbx * nby * nbz <= 32) {
+          mark_box(w.envs[e_lo], l0, l1, l2, h0, h1, h2, lane, 32);
+        } else if (ok) {
+          mark_one(w.envs[env]);
+        }
+      }
+    } else if (MARK && ok && !compact) {
+      mark_one(w.envs[env]);
+    }
   } else if (ok) {
     const dt_env& E = w.envs[env];
     const int node_off = E.node_off, nb1 = E.nb[1], nb2 = E.nb[2];

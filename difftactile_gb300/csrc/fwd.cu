@@ -104,10 +104,11 @@ __device__ void p2g_chunk(const dt_world& w, int f, int chunk, float4* tile, int
   rec.c0 = c0;
   rec.c1 = c1;
   rec.c2 = c2;
-  auto mark_box = [&](const dt_env& E0, int l0, int l1, int l2, int h0, int h1, int h2) {
+  // the blocks of the node box [l, h], shared out as i = start, start + stride, ...
+  auto mark_box = [&](const dt_env& E0, int l0, int l1, int l2, int h0, int h1, int h2, int start, int stride) {
     const int b0 = l0 >> 2, b1 = l1 >> 2, b2 = l2 >> 2;
     const int n0 = (h0 >> 2) - b0 + 1, n1 = (h1 >> 2) - b1 + 1, n2 = (h2 >> 2) - b2 + 1;
-    for (int i = threadIdx.x; i < n0 * n1 * n2; i += NT) {
+    for (int i = start; i < n0 * n1 * n2; i += stride) {
       const int c = i % n2, bb = (i / n2) % n1, a = i / (n1 * n2);
       mark_block(w, f, block_index(E0, b0 + a, b1 + bb, b2 + c));
     }
@@ -214,7 +215,8 @@ __global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_FWD_P2G, NT)) k_fwd_p2g_fe
       int c0, c1;
       cta_chunks(w, NT, PPT, b, c0, c1);
       for (int c = c0; c < c1; ++c) {
-        if (c > c0) __syncthreads();  // the shared tile and flags of the previous chunk
+        // the shared box and tile of the previous chunk (the warp scatter shares nothing between chunks)
+        if (c > c0 && !(MODE >= DT_SCATTER_WARP && MODE < DT_MODE_SMEM)) __syncthreads();
         p2g_chunk<MODE, NT>(w, f, c, tile, sh);
       }
     }
