@@ -249,9 +249,12 @@ __global__ void __launch_bounds__(GRID_NT, DT_MINB_FWD_GRID * 1024 / GRID_NT / 4
   pdl_entry();
   extern __shared__ float4 scent[];
   float4* gbox = scent + smem_cap;  // 2 float4 per group of 32 centroids
-  // argmin of every node of the block per sensor slot, double-buffered over the CTA's run of blocks:
-  // the search (all lanes) fills one buffer while the node pass of the previous block reads the other
-  __shared__ int s_cid[2][DT_MAX_SENSORS_PER_ENV][64];
+  // The CTA takes its run of the active list KB blocks at a time: all lanes search the KB blocks one
+  // after the other, then each 64-thread group runs one block's node pass.  The argmins of every node
+  // per sensor slot are double-buffered over these steps: the search of the next KB blocks fills one
+  // buffer while the node passes of the previous ones read the other.
+  constexpr int KB = GRID_NT / 64 < 4 ? GRID_NT / 64 : 4;
+  __shared__ int s_cid[2][KB][DT_MAX_SENSORS_PER_ENV][64];
   __shared__ int s_cand[CAND ? SMEM_CENT_MAX / 32 : 1];  // candidate groups of the block
   __shared__ int s_csh[2];
   const int cnt = *((volatile int*)(w.tape_bcount + f));
@@ -271,13 +274,14 @@ __global__ void __launch_bounds__(GRID_NT, DT_MINB_FWD_GRID * 1024 / GRID_NT / 4
   const int per = (cnt + (int)gridDim.x - 1) / (int)gridDim.x;
   const int e_end = min(cnt, ((int)blockIdx.x + 1) * per);
   int it = 0;
-  for (int e = blockIdx.x * per; e < e_end; ++e, it ^= 1) {
-    const int b = w.tape_blist[(size_t)f * w.n_blocks + e];
-    const dt_env& E = w.envs[__ldg(w.blk_env + b)];
-    const int lb = b - E.blk_off;
-    const int bk = lb % E.nb[2], bj = (lb / E.nb[2]) % E.nb[1], bi = lb / (E.nb[1] * E.nb[2]);
-    // ---- search: GRID_LPN lanes per node ----
-    {
+  for (int e0 = blockIdx.x * per; e0 < e_end; e0 += KB, it ^= 1) {
+    const int nk = min(KB, e_end - e0);  // blocks in this step (CTA-uniform)
+    // ---- search: GRID_LPN lanes per node, block after block ----
+    for (int h = 0; h < nk; ++h) {
+      const int b = w.tape_blist[(size_t)f * w.n_blocks + e0 + h];
+      const dt_env& E = w.envs[__ldg(w.blk_env + b)];
+      const int lb = b - E.blk_off;
+      const int bk = lb % E.nb[2], bj = (lb / E.nb[2]) % E.nb[1], bi = lb / (E.nb[1] * E.nb[2]);
       const int i = 4 * bi + (l >> 4), j = 4 * bj + ((l >> 2) & 3), k = 4 * bk + (l & 3);
       const bool occ = acc[E.node_off + (lb << 6) + l].w > E.eps;  // check_grid_occupy, mpm_elastic.py:213
       const float px = __fmul_rn(__fadd_rn((float)i, 0.5f), E.dx), py = __fmul_rn(__fadd_rn((float)j, 0.5f), E.dx),
@@ -306,14 +310,20 @@ __global__ void __launch_bounds__(GRID_NT, DT_MINB_FWD_GRID * 1024 / GRID_NT / 4
           cand = s_cand;
         }
         const int kk = closest_tri<GRID_LPN>(w, S, scent, gbox, in_smem, occ, px, py, pz, sub, cand, nc);
-        if (sub == 0) s_cid[it][q][l] = kk;
+        if (sub == 0) s_cid[it][h][q][l] = kk;
       }
     }
     __syncthreads();
-    // ---- node pass: one thread per node (two warps), contact force and grid update ----
-    if (tid >= 64) continue;
-    const int i = 4 * bi + (tid >> 4), j = 4 * bj + ((tid >> 2) & 3), k = 4 * bk + (tid & 3);
-    const int g = E.node_off + (lb << 6) + tid;
+    // ---- node passes: one thread per node, 64-thread group h for block h of the step ----
+    const int h = tid >> 6, nd = tid & 63;
+    if (h >= nk) continue;
+    const int e = e0 + h;
+    const int b = w.tape_blist[(size_t)f * w.n_blocks + e];
+    const dt_env& E = w.envs[__ldg(w.blk_env + b)];
+    const int lb = b - E.blk_off;
+    const int bk = lb % E.nb[2], bj = (lb / E.nb[2]) % E.nb[1], bi = lb / (E.nb[1] * E.nb[2]);
+    const int i = 4 * bi + (nd >> 4), j = 4 * bj + ((nd >> 2) & 3), k = 4 * bk + (nd & 3);
+    const int g = E.node_off + (lb << 6) + nd;
     const float4 a = acc[g];
     const float m = a.w;
     const bool occ = m > E.eps;
@@ -328,7 +338,7 @@ __global__ void __launch_bounds__(GRID_NT, DT_MINB_FWD_GRID * 1024 / GRID_NT / 4
     for (int q = 0; q < DT_MAX_SENSORS_PER_ENV; ++q) {
       const int si = E.s_begin + q;
       if (si >= E.s_end) break;
-      const int kk = s_cid[it][q][tid];
+      const int kk = s_cid[it][h][q][nd];
       if (q == 0) cid.x = kk;
       else if (q == 1) cid.y = kk;
       else if (q == 2) cid.z = kk;
@@ -366,15 +376,15 @@ __global__ void __launch_bounds__(GRID_NT, DT_MINB_FWD_GRID * 1024 / GRID_NT / 4
     if (w.skip_tape) {
       // a forward whose tape no backward reads
     } else if (e < w.tape_blocks) {
-      const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + tid;
+      const size_t ti = ((size_t)f * w.tape_blocks + e) * 64 + nd;
       reinterpret_cast<float4*>(w.tape_acc)[ti] = a;
       reinterpret_cast<float4*>(w.tape_vout)[ti] = vo;
       reinterpret_cast<int4*>(w.tape_cidx)[ti] = cid;
-    } else if (tid == 0) {
+    } else if (nd == 0) {
       set_err(w, DT_DEVERR_TAPE_FULL);
     }
     acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (tid == 0) w.blk_flag[b] = 0;
+    if (nd == 0) w.blk_flag[b] = 0;
   }
 }
 
