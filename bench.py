@@ -158,11 +158,11 @@ NAMES = {("fwd", 0): "k_fwd_p2g_fem", ("fwd", 1): "k_fwd_grid", ("fwd", 2): "k_f
 # launch of each kernel, --clock-control none; the forward P2G's is a launch of the first, untaped
 # forward pass) scaled to the full population by its particle count (3,221,208 / 843,880): a static
 # capture, not a live measurement, valid for the kernel build it was taken of
-NCU_TRAFFIC = {"captured_at": "the build of commit d5aa2b7 (re-binning, two particles per thread, tet SVD tape)",
+NCU_TRAFFIC = {"captured_at": "the build of commit 09b239f (re-binning, two particles per thread, tet SVD tape, four-block grid steps)",
                "per_launch_bytes": {k: b * 3.817 for k, b in (
-                   ("k_fwd_p2g_fem", 129.9e6), ("k_fwd_grid", 4.64e6), ("k_fwd_g2p_fem", 31.5e6),
-                   ("k_bwd_restore", 3.92e6), ("k_bwd_g2p_fem", 89.8e6), ("k_bwd_grid", 12.1e6),
-                   ("k_bwd_p2g_fem", 349.5e6))}}
+                   ("k_fwd_p2g_fem", 130.2e6), ("k_fwd_grid", 4.64e6), ("k_fwd_g2p_fem", 31.9e6),
+                   ("k_bwd_restore", 3.92e6), ("k_bwd_g2p_fem", 88.9e6), ("k_bwd_grid", 12.1e6),
+                   ("k_bwd_p2g_fem", 349.8e6))}}
 
 
 def algo_bytes(key, units):
