@@ -150,23 +150,27 @@ __device__ void g2p_bwd_chunk(const dt_world& w, int f, int chunk, float4* tile,
       const v3 k0 = gk * mcol(Cb, 0), k1 = gk * mcol(Cb, 1), k2 = gk * mcol(Cb, 2);
       const v3 u1 = vnb + mvec(Cb, v3{(1.f - fx[0]) * gk, (1.f - fx[1]) * gk, (1.f - fx[2]) * gk});
       v3 S0 = v3{0.f, 0.f, 0.f};
+      const StencilNodes sn = stencil_nodes(E, base);
 #pragma unroll
       for (int oi = 0; oi < 3; ++oi) {
         const v3 ui = oi == 0 ? u1 - k0 : (oi == 1 ? u1 : u1 + k0);  // offsets about the middle node
 #pragma unroll
         for (int oj = 0; oj < 3; ++oj) {
           const v3 uij = oj == 0 ? ui - k1 : (oj == 1 ? ui : ui + k1);
+          float Z = 0.f, Zd = 0.f;  // the row's sum_k wz_k Wb and sum_k dwz_k Wb
 #pragma unroll
           for (int ok_ = 0; ok_ < 3; ++ok_) {
             const v3 u = ok_ == 0 ? uij - k2 : (ok_ == 1 ? uij : uij + k2);
-            const v3 gv = f4to3(__ldg(vout + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok_)));
+            const v3 gv = f4to3(__ldg(vout + ((sn.x[oi] + sn.y[oj]) + sn.z[ok_])));
             const float W = (wx[oi] * wy[oj]) * wz[ok_];
             const float Wb = dot(gv, u);
             S0 = S0 + W * gv;
-            fxb[0] += Wb * (dws[oi][0] * wy[oj] * wz[ok_]);
-            fxb[1] += Wb * (wx[oi] * dws[oj][1] * wz[ok_]);
-            fxb[2] += Wb * (wx[oi] * wy[oj] * dws[ok_][2]);
+            Z += wz[ok_] * Wb;
+            Zd += dws[ok_][2] * Wb;
           }
+          fxb[0] += (dws[oi][0] * wy[oj]) * Z;
+          fxb[1] += (wx[oi] * dws[oj][1]) * Z;
+          fxb[2] += (wx[oi] * wy[oj]) * Zd;
         }
       }
       const v3 CtS0 = mTvec(Cb, S0);
@@ -421,7 +425,9 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   // dp_o = (o - fx) dx:  v_bar = p_mass S0,  A_bar = dx (S1 - S0 (fx - 1)^T)  with  S0 = sum W_o m_o and
   // S1 = sum W_o m_o (o - 1)^T (the moment about the stencil's middle node),  and
   // fx_bar_d = sum dW_o/dfx_d Wb_o - dx (A^T S0)_d  with
-  // Wb_o = m_o . (p_mass v + A dp_o) + p_mass mass_bar_o  — the per-node work is two moments and Wb_o
+  // Wb_o = m_o . u_o + p_mass mass_bar_o,  u_o = p_mass v + A dp_o = u_1 + sum_c (o_c - 1) a_c
+  // (u_1 = p_mass v + A (1 - fx) dx, the middle node's; a_c = dx A column c): the per-node work is two
+  // moments, u_o by one add per axis that moves, and Wb_o
   const float4* aacc = reinterpret_cast<const float4*>(w.g_adj_acc);
   v3 S0 = v3{0.f, 0.f, 0.f};
   m3 S1 = mzero();
@@ -434,14 +440,22 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
       wts[i][d] = bsw(i, fx[d]);
       dws[i][d] = bsdw(i, fx[d]);
     }
-  const v3 pmv = pm * r.v;
+  const v3 a0 = dx * mcol(A, 0), a1 = dx * mcol(A, 1), a2 = dx * mcol(A, 2);
+  const v3 u1 = pm * r.v + mvec(A, v3{(1.f - fx[0]) * dx, (1.f - fx[1]) * dx, (1.f - fx[2]) * dx});
+  const StencilNodes sn = stencil_nodes(E, base);
+  // fx_bar: per row (oi, oj) of three nodes the sums Z = sum_k wz_k Wb and Zd = sum_k dwz_k Wb, then
+  // fx_bar += (dwx wy Z, wx dwy Z, wx wy Zd)
 #pragma unroll
   for (int oi = 0; oi < 3; ++oi)
 #pragma unroll
-    for (int oj = 0; oj < 3; ++oj)
+    for (int oj = 0; oj < 3; ++oj) {
+      float Z = 0.f, Zd = 0.f;
 #pragma unroll
       for (int ok = 0; ok < 3; ++ok) {
-        const float4 gb = __ldg(aacc + node_index(E, base[0] + oi, base[1] + oj, base[2] + ok));
+        const v3 ui = oi == 0 ? u1 - a0 : (oi == 1 ? u1 : u1 + a0);  // resolved at compile time
+        const v3 uij = oj == 0 ? ui - a1 : (oj == 1 ? ui : ui + a1);
+        const v3 u = ok == 0 ? uij - a2 : (ok == 1 ? uij : uij + a2);
+        const float4 gb = __ldg(aacc + ((sn.x[oi] + sn.y[oj]) + sn.z[ok]));
         const v3 mvb = f4to3(gb);
         const float W = (wts[oi][0] * wts[oj][1]) * wts[ok][2];
         const v3 Wm = W * mvb;
@@ -454,12 +468,14 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
           S1.a[1][c] += o[c] * Wm.y;
           S1.a[2][c] += o[c] * Wm.z;
         }
-        const v3 dp = v3{((float)oi - fx[0]) * dx, ((float)oj - fx[1]) * dx, ((float)ok - fx[2]) * dx};
-        const float Wb = dot(mvb, pmv + mvec(A, dp)) + pm * gb.w;
-        fxb[0] += Wb * (dws[oi][0] * wts[oj][1] * wts[ok][2]);
-        fxb[1] += Wb * (wts[oi][0] * dws[oj][1] * wts[ok][2]);
-        fxb[2] += Wb * (wts[oi][0] * wts[oj][1] * dws[ok][2]);
+        const float Wb = dot(mvb, u) + pm * gb.w;
+        Z += wts[ok][2] * Wb;
+        Zd += dws[ok][2] * Wb;
       }
+      fxb[0] += (dws[oi][0] * wts[oj][1]) * Z;
+      fxb[1] += (wts[oi][0] * dws[oj][1]) * Z;
+      fxb[2] += (wts[oi][0] * wts[oj][1]) * Zd;
+    }
   const v3 vb = pm * S0;
   m3 Ab;
 #pragma unroll
@@ -468,12 +484,9 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
 #pragma unroll
     for (int c = 0; c < 3; ++c) Ab.a[rr][c] = dx * (S1.a[rr][c] - s0 * (fx[c] - 1.f));
   }
-  {
-    const v3 AtS0 = mTvec(A, S0);
-    fxb[0] -= dx * AtS0.x;
-    fxb[1] -= dx * AtS0.y;
-    fxb[2] -= dx * AtS0.z;
-  }
+  fxb[0] -= dot(a0, S0);  // dx (A^T S0)
+  fxb[1] -= dot(a1, S0);
+  fxb[2] -= dot(a2, S0);
   // affine = stress_k * cauchy + p_mass * C
   m3 Cb = mscale(pm, Ab);
   const m3 G = mscale(E.stress_k, Ab);  // cauchy adjoint

@@ -24,7 +24,8 @@
 #ifndef DT_MINB_BWD_GRID
 #define DT_MINB_BWD_GRID 8
 #endif
-// the P2G adjoint: 4 CTAs of 128 threads (128 registers, ~250 B of spills).  Measured on the
+// the P2G adjoint: 4 CTAs of 128 threads (128 registers; 86 B of spill stores with one particle per
+// thread, 178 B with two; 168 registers would hold it without spills).  Measured on the
 // re-binned population at mid-rollout: 5 CTAs (96 registers, ~1 KB of spills) 616 -> 772 us; keeping
 // the constitutive state out of registers across the 27-node gather (recomputed from the SVD tape
 // after it: 48 B of spills) 627 -> 657 us at 4 CTAs, 631 us at 5
@@ -335,6 +336,27 @@ DT_DEV float bsdw(int i, float fx) { return i == 0 ? fx - 1.5f : (i == 1 ? -2.f 
 DT_DEV int node_index(const dt_env& E, int i, int j, int k) {
   int b = ((i >> 2) * E.nb[1] + (j >> 2)) * E.nb[2] + (k >> 2);
   return E.node_off + (b << 6) + ((i & 3) << 4) + ((j & 3) << 2) + (k & 3);
+}
+// The 27 node indices of the stencil at `base`, per axis: node_index(E, base + o) = x[o_x] + y[o_y] + z[o_z]
+// (the block term ((bi nb1 + bj) nb2 + bk) 64 distributed over the axes), so that a node costs one add
+// on the row's x + y instead of the block product
+struct StencilNodes {
+  int x[3], y[3], z[3];
+};
+DT_DEV StencilNodes stencil_nodes(int node_off, int nb1, int nb2, const int base[3]) {
+  StencilNodes s;
+  const int ry = nb2 << 6, rx = nb1 * ry;
+#pragma unroll
+  for (int o = 0; o < 3; ++o) {
+    const int i = base[0] + o, j = base[1] + o, k = base[2] + o;
+    s.x[o] = node_off + (i >> 2) * rx + ((i & 3) << 4);
+    s.y[o] = (j >> 2) * ry + ((j & 3) << 2);
+    s.z[o] = ((k >> 2) << 6) + (k & 3);
+  }
+  return s;
+}
+DT_DEV StencilNodes stencil_nodes(const dt_env& E, const int base[3]) {
+  return stencil_nodes(E.node_off, E.nb[1], E.nb[2], base);
 }
 DT_DEV int block_index(const dt_env& E, int bi, int bj, int bk) {
   return E.blk_off + (bi * E.nb[1] + bj) * E.nb[2] + bk;
@@ -899,9 +921,8 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
       nb1 = E.nb[1];
       nb2 = E.nb[2];
     }
-    const int key = ok ? node_off + ((((base[0] >> 2) * nb1 + (base[1] >> 2)) * nb2 + (base[2] >> 2)) << 6) +
-                             ((base[0] & 3) << 4) + ((base[1] & 3) << 2) + (base[2] & 3)
-                       : -1 - lane;
+    const StencilNodes sn = stencil_nodes(node_off, nb1, nb2, base);
+    const int key = ok ? sn.x[0] + sn.y[0] + sn.z[0] : -1 - lane;
     const int prev = __shfl_up_sync(0xffffffffu, key, 1);
     const bool head = lane == 0 || prev != key;
     const unsigned heads = __ballot_sync(0xffffffffu, head);
@@ -948,10 +969,7 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
               atomicAdd(t + 2, a.z);
               if (a.w != 0.f) atomicAdd(t + 3, a.w);
             } else {
-              const int i = base[0] + oi, j = base[1] + oj, k = base[2] + ok_;
-              const int n = node_off + ((((i >> 2) * nb1 + (j >> 2)) * nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
-                            ((j & 3) << 2) + (k & 3);
-              red_add_v4(dst + n, a);
+              red_add_v4(dst + ((sn.x[oi] + sn.y[oj]) + sn.z[ok_]), a);
             }
           }
         }
@@ -994,16 +1012,14 @@ DT_DEV void stencil_scatter(const dt_world& w, int chunk, bool ok, int env, cons
     }
   } else if (ok) {
     const dt_env& E = w.envs[env];
-    const int node_off = E.node_off, nb1 = E.nb[1], nb2 = E.nb[2];
+    const StencilNodes sn = stencil_nodes(E, base);
 #pragma unroll
     for (int oi = 0; oi < 3; ++oi)
 #pragma unroll
       for (int oj = 0; oj < 3; ++oj)
 #pragma unroll
         for (int ok_ = 0; ok_ < 3; ++ok_) {
-          const int i = base[0] + oi, j = base[1] + oj, k = base[2] + ok_;
-          const int n = node_off + ((((i >> 2) * nb1 + (j >> 2)) * nb2 + (k >> 2)) << 6) + ((i & 3) << 4) +
-                        ((j & 3) << 2) + (k & 3);
+          const int n = (sn.x[oi] + sn.y[oj]) + sn.z[ok_];
           const float W = (r.wx[oi] * r.wy[oj]) * r.wz[ok_];
           const float fi = (float)(oi - 1), fj = (float)(oj - 1), fk = (float)(ok_ - 1);
           const v3 t = ((v3{r.q.x, r.q.y, r.q.z} + fi * r.c0) + fj * r.c1) + fk * r.c2;
