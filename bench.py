@@ -158,11 +158,12 @@ NAMES = {("fwd", 0): "k_fwd_p2g_fem", ("fwd", 1): "k_fwd_grid", ("fwd", 2): "k_f
 # launch of each kernel, --clock-control none; the forward P2G's is a launch of the first, untaped
 # forward pass) scaled to the full population by its particle count (3,221,208 / 843,880): a static
 # capture, not a live measurement, valid for the kernel build it was taken of
-NCU_TRAFFIC = {"captured_at": "the build of commit 09b239f (re-binning, two particles per thread, tet SVD tape, four-block grid steps)",
+NCU_TRAFFIC = {"captured_at": "the build of commit aa5e952 (re-binning, two particles per thread, tet SVD tape, four-block grid "
+                              "steps, per-axis stencil node indices)",
                "per_launch_bytes": {k: b * 3.817 for k, b in (
-                   ("k_fwd_p2g_fem", 130.2e6), ("k_fwd_grid", 4.64e6), ("k_fwd_g2p_fem", 31.9e6),
-                   ("k_bwd_restore", 3.92e6), ("k_bwd_g2p_fem", 88.9e6), ("k_bwd_grid", 12.1e6),
-                   ("k_bwd_p2g_fem", 349.8e6))}}
+                   ("k_fwd_p2g_fem", 130.55e6), ("k_fwd_grid", 4.65e6), ("k_fwd_g2p_fem", 31.89e6),
+                   ("k_bwd_restore", 3.92e6), ("k_bwd_g2p_fem", 87.06e6), ("k_bwd_grid", 12.11e6),
+                   ("k_bwd_p2g_fem", 335.46e6))}}
 
 
 def algo_bytes(key, units):
