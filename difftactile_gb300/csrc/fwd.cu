@@ -25,8 +25,10 @@ namespace {
 constexpr int NT_TILE = 128;      // threads per CTA of the particle roles with the TILE scatter
 constexpr int TILE_MAX = 1728;    // shared P2G tile capacity in nodes (12^3), 27 KB of float4
 // lanes per node in the grid kernel's contact search (dt_world.contact_lanes): 8 (shorter chains,
-// for launches with few active blocks) or 4 (fewer issued instructions per node); one 4x4x4 node
-// block per CTA of 64 * lanes threads
+// for launches with few active blocks) or 4 (fewer issued instructions per node); a CTA of
+// 64 * lanes threads takes its blocks four at a time.  Two lanes per node measured slower on the
+// population (grid kernel 201 -> 267 us: each lane's chain twice as long, and its 16 cached group
+// distances spill)
 constexpr int SMEM_CENT_MAX = 12288;  // triangle centroids staged in shared memory (192 KB)
 
 __device__ void mark_block(const dt_world& w, int f, int b) {
@@ -239,9 +241,10 @@ __global__ void __launch_bounds__(NT, DT_MINB(DT_MINB_FWD_P2G, NT)) k_fwd_p2g_fe
 // L2: grid update + contact over the frame's active blocks.  64 x GRID_LPN threads per 4x4x4 block:
 // GRID_LPN (8 or 4) lanes per node share the node's argmin over the sensor's triangle centroids
 // (staged in shared memory, contact.cuh: closest_tri); the (distance, index) pairs are combined
-// lexicographically, which is exactly the sequential scan's first-minimum-wins result.  Then the
-// first two warps take one node per thread for the contact force and the grid update, so the serial
-// per-node work issues from 2 warps instead of from one lane in GRID_LPN of every warp.
+// lexicographically, which is exactly the sequential scan's first-minimum-wins result.  Then each
+// 64-thread group takes one block's nodes, one per thread, for the contact force and the grid update,
+// so the serial per-node work issues from 2 warps per block instead of from one lane in GRID_LPN of
+// every warp.
 // ---------------------------------------------------------------------------------------------
 // CAND: sensors of more than 32 groups of centroids are searched over per-block candidate groups
 template <int GRID_LPN, bool CAND, int GRID_NT = 64 * GRID_LPN>
