@@ -64,12 +64,15 @@ def parse():
                     help="threads per CTA of the particle launches")
     ap.add_argument("--depth", type=int, default=None, choices=[0, 1, 2, 3, 4, 5],
                     help="shuffle steps of the warp scatter's segmented reduction (0: whole runs)")
+    ap.add_argument("--adj-depth", type=int, default=None, choices=[0, 1, 2],
+                    help="shuffle steps of the G2P adjoint's warp scatter (0: whole runs; default: the P2G's)")
     ap.add_argument("--ppt", type=int, default=None, choices=[1, 2],
                     help="particles per thread of the particle-role launches (default: the tuner's choice)")
     ap.add_argument("--lanes", type=int, default=None, choices=[4, 8],
                     help="lanes per active grid node in the contact search")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shape instead of "
-                    "the autotuner's choice (also implied by --scatter, --no-pdl, --p-block, --depth or --lanes)")
+                    "the autotuner's choice (also implied by --scatter, --no-pdl, --p-block, --depth, --adj-depth, "
+                    "--ppt or --lanes)")
     ap.add_argument("--no-svd-tape", action="store_true", help="the adjoint recomputes the SVD instead of "
                     "reading the forward's from the tape")
     ap.add_argument("--no-graph", action="store_true", help="launch every substep from the host instead of "
@@ -159,10 +162,11 @@ NAMES = {("fwd", 0): "k_fwd_p2g_fem", ("fwd", 1): "k_fwd_grid", ("fwd", 2): "k_f
 # forward pass) scaled to the full population by its particle count (3,221,208 / 843,880): a static
 # capture, not a live measurement, valid for the kernel build it was taken of
 NCU_TRAFFIC = {"captured_at": "the build of commit aa5e952 (re-binning, two particles per thread, tet SVD tape, four-block grid "
-                              "steps, per-axis stencil node indices)",
+                              "steps, per-axis stencil node indices); the G2P adjoint's with 4-lane scatter windows, "
+                              "ABI 8",
                "per_launch_bytes": {k: b * 3.817 for k, b in (
                    ("k_fwd_p2g_fem", 130.55e6), ("k_fwd_grid", 4.65e6), ("k_fwd_g2p_fem", 31.89e6),
-                   ("k_bwd_restore", 3.92e6), ("k_bwd_g2p_fem", 87.06e6), ("k_bwd_grid", 12.11e6),
+                   ("k_bwd_restore", 3.92e6), ("k_bwd_g2p_fem", 85.5e6), ("k_bwd_grid", 12.11e6),
                    ("k_bwd_p2g_fem", 335.46e6))}}
 
 
@@ -187,6 +191,8 @@ def build(cfg, dev, args, **extra):
         kw["contact_lanes"] = args.lanes
     if args.ppt is not None:
         kw["p_per_thread"] = args.ppt
+    if args.adj_depth is not None:
+        kw["scatter_depth_adj"] = 3 if args.adj_depth == 0 else args.adj_depth
     if args.rebin and cfg.ckpt_every > 0:
         kw["rebin_every"] = args.rebin
     return cfg.build(dev, **kw)
@@ -194,7 +200,7 @@ def build(cfg, dev, args, **extra):
 
 def tune_launch(args):
     return not (args.no_tune or args.scatter or args.no_pdl or args.p_block or args.depth is not None
-                or args.lanes is not None or args.ppt is not None)
+                or args.lanes is not None or args.ppt is not None or args.adj_depth is not None)
 
 
 def mid_frame(traj):
@@ -509,6 +515,7 @@ def run_ours(args):
                       "rebin_every": int(getattr(traj, "rebin_every", 0)),
                       "scatter": ["tile", "global", "warp", "smem"][w.w.scatter_mode], "p_block": int(w.w.p_block),
                       "scatter_depth": int(w.w.scatter_depth),
+                      "scatter_depth_adjoint": {1: 1, 2: 2, 3: 0}.get(int(w.w.scatter_depth_adj), int(w.w.scatter_depth)),
                       "contact_lanes": 4 if int(w.w.contact_lanes) == 4 else 8,
                       "particles_per_thread": max(1, int(w.w.p_per_thread)),
                       "programmatic_dependent_launch": bool(w.lib.dt_get_pdl()),

@@ -76,7 +76,8 @@ class DtWorld(C.Structure):
                 + [(n, _P) for n in ROPE_PTR_FIELDS] + [(n, C.c_int) for n in ROPE_INT_FIELDS]
                 + [("p_svd", _P), ("p_block", C.c_int), ("scatter_depth", C.c_int), ("contact_lanes", C.c_int),
                    ("skip_tape", C.c_int), ("r_work", _P), ("max_rope_iters", C.c_int), ("p_per_thread", C.c_int)]
-                + [("aux_stream", _P), ("aux_events", _P * 2), ("t_svd", _P)])
+                + [("aux_stream", _P), ("aux_events", _P * 2), ("t_svd", _P)]
+                + [("scatter_depth_adj", C.c_int)])
 
 
 # entry points: name -> (restype, argtypes)
@@ -166,7 +167,7 @@ def load(path: str | None = None):
         n = getattr(lib, f"dt_sizeof_{name}")()
         if n != C.sizeof(cls):
             raise ImportError(f"ABI mismatch: sizeof(dt_{name}) = {n} in the library, {C.sizeof(cls)} in ctypes")
-    if lib.dt_abi_version() != 7:
+    if lib.dt_abi_version() != 8:
         raise ImportError("ABI version mismatch")
     _lib = lib
     return lib

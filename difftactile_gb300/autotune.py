@@ -18,11 +18,13 @@ scene (particle count and density, how many environments share the launch):
   ppt       particles per thread of the particle-role launches (dt_world.p_per_thread): each CTA
             takes 1 or 2 consecutive chunks of p_block particles (fewer, longer-lived CTAs; the second
             chunk finds the first one's grid neighbourhood in L1);
+  adj_depth with the warp scatter, the G2P adjoint's own depth (dt_world.scatter_depth_adj; absent:
+            the P2G's): tried after the search, on the fastest shape, with the other depths;
   pdl       programmatic dependent launch of the substep kernels (dt_set_pdl, library-wide).
 
 ``tune_substep`` times every candidate on one forward + backward substep of the world at a chosen
-frame (CUDA events on the launching stream, median of ``reps`` after ``warmup``) and applies the
-fastest; ``tune`` does the same for any callable (e.g. a whole rollout).  Results are kept per
+frame (CUDA events on the launching stream, median of ``reps`` after ``warmup``), then the fastest
+one's variants with another adjoint depth, and applies the fastest; ``tune`` does the same for any callable (e.g. a whole rollout).  Results are kept per
 device and world shape, in memory and optionally in a JSON file, so a second world of the same
 shape skips the measurement.  Recorded CUDA graphs hold the launch shape they were recorded with:
 re-record them (Trajectory.reset_graphs) after tuning.
@@ -55,21 +57,40 @@ def candidates(scatters=("warp", "smem", "global", "tile"), p_blocks=(64, 128, 2
     return out
 
 
+# dt_world.scatter_depth_adj of an adjoint depth (0: whole runs) and back; 0 in the field: the P2G's depth
+_ADJ_CODE = {0: 3, 1: 1, 2: 2}
+_ADJ_DEPTH = {v: k for k, v in _ADJ_CODE.items()}
+
+
 def apply(world, cfg: dict):
-    """Set ``cfg`` (scatter, p_block, depth, pdl) on ``world`` (and the library's PDL switch)."""
+    """Set ``cfg`` (scatter, p_block, depth, lanes, ppt, adj_depth, pdl) on ``world`` (and the
+    library's PDL switch)."""
     world.w.scatter_mode = SCATTERS[cfg["scatter"]]
     world.w.p_block = int(cfg["p_block"])
     world.w.scatter_depth = int(cfg.get("depth", 0))
     world.w.contact_lanes = int(cfg.get("lanes", 8))
     world.w.p_per_thread = int(cfg.get("ppt", 1))
+    adj = cfg.get("adj_depth")
+    world.w.scatter_depth_adj = _ADJ_CODE[int(adj)] if adj is not None else 0
     world.lib.dt_set_pdl(int(cfg["pdl"]))  # returns the previous setting
 
 
 def current(world) -> dict:
     inv = {v: k for k, v in SCATTERS.items()}
-    return {"scatter": inv.get(int(world.w.scatter_mode), "warp"), "p_block": int(world.w.p_block) or 128,
-            "depth": int(world.w.scatter_depth), "lanes": 4 if int(world.w.contact_lanes) == 4 else 8,
-            "pdl": int(world.lib.dt_get_pdl()), "ppt": max(1, int(world.w.p_per_thread))}
+    out = {"scatter": inv.get(int(world.w.scatter_mode), "warp"), "p_block": int(world.w.p_block) or 128,
+           "depth": int(world.w.scatter_depth), "lanes": 4 if int(world.w.contact_lanes) == 4 else 8,
+           "pdl": int(world.lib.dt_get_pdl()), "ppt": max(1, int(world.w.p_per_thread))}
+    adj = _ADJ_DEPTH.get(int(getattr(world.w, "scatter_depth_adj", 0)))
+    if adj is not None:
+        out["adj_depth"] = adj
+    return out
+
+
+def adjoint_depths(best: dict) -> list[dict]:
+    """The variants of a warp-scatter shape whose G2P adjoint takes each other depth."""
+    if best["scatter"] != "warp":
+        return []
+    return [dict(best, adj_depth=d) for d in (0, 1, 2) if d != int(best.get("depth", 0))]
 
 
 def signature(world, tag: str = "") -> str:
@@ -111,9 +132,10 @@ def _time(run, reps, warmup):
 
 
 def tune(world, run, cands=None, reps: int = 5, warmup: int = 1, tag: str = "", cache_path: str | None = None,
-         use_cache: bool = True, prepare=None, margin: float = 0.02, timer=None) -> dict:
+         use_cache: bool = True, prepare=None, margin: float = 0.02, timer=None, refine=None) -> dict:
     """Time ``run()`` under every candidate launch shape (``prepare()``, untimed, before each
-    candidate's runs), apply the fastest and return {"best": cfg, "ms": {label: median ms}, "cached": bool}.
+    candidate's runs), then under ``refine(fastest)`` (variants of the fastest shape), apply the
+    fastest and return {"best": cfg, "ms": {label: median ms}, "cached": bool}.
     The library default (``DEFAULT``) is kept unless a candidate beats it by more than ``margin``
     (relative), so that timing noise between near-equal shapes does not flip the choice.  ``timer``
     replaces the CUDA-event timing (called as timer(run, reps, warmup) -> ms)."""
@@ -127,7 +149,8 @@ def tune(world, run, cands=None, reps: int = 5, warmup: int = 1, tag: str = "", 
     cands = cands or candidates()
     times = {}
     best, best_ms = None, float("inf")
-    for c in cands:
+
+    def measure(c):
         apply(world, c)
         if prepare is not None:
             prepare()
@@ -135,6 +158,14 @@ def tune(world, run, cands=None, reps: int = 5, warmup: int = 1, tag: str = "", 
         if world.error_word():
             raise RuntimeError(f"device error word {world.error_word()} while tuning {c}")
         times[label(c)] = ms
+        return ms
+
+    for c in cands:
+        ms = measure(c)
+        if ms < best_ms:
+            best, best_ms = c, ms
+    for c in (refine(best) if refine is not None else []):
+        ms = measure(c)
         if ms < best_ms:
             best, best_ms = c, ms
     d_ms = times.get(label(DEFAULT))
@@ -160,6 +191,7 @@ def tune_substep(world, frame: int = 0, **kw) -> dict:
         world.substeps_bwd(frame + 1, frame)
 
     kw.setdefault("prepare", world.adj_clear)
+    kw.setdefault("refine", adjoint_depths)
     kw.setdefault("tag", "substep")
     kw.setdefault("reps", 15)
     kw.setdefault("warmup", 2)
@@ -169,4 +201,5 @@ def tune_substep(world, frame: int = 0, **kw) -> dict:
 def label(c: dict) -> str:
     depth = f"/d{c.get('depth', 0)}" if c["scatter"] == "warp" else ""
     ppt = f"/ppt{c['ppt']}" if c.get("ppt", 1) != 1 else ""
-    return f"{c['scatter']}/{c['p_block']}{depth}/l{c.get('lanes', 8)}/{'pdl' if c['pdl'] else 'nopdl'}{ppt}"
+    adj = f"/a{c['adj_depth']}" if c["scatter"] == "warp" and c.get("adj_depth") is not None else ""
+    return f"{c['scatter']}/{c['p_block']}{depth}/l{c.get('lanes', 8)}/{'pdl' if c['pdl'] else 'nopdl'}{ppt}{adj}"

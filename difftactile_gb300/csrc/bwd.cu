@@ -855,7 +855,7 @@ int dt_substep_bwd_stage(const dt_world* w, int f, int stage, cudaStream_t strea
       break;
     }
     case 1:
-      switch (scatter_kind(w)) {
+      switch (scatter_kind_adj(w)) {
         case DT_SCATTER_TILE: e = b1<DT_SCATTER_TILE, NT_TILE>(w, f, stream); break;
         case DT_SCATTER_GLOBAL: e = b1_nt<DT_SCATTER_GLOBAL>(w, f, stream); break;
         case DT_SCATTER_WARP + 1: e = b1_nt<DT_SCATTER_WARP + 1>(w, f, stream); break;

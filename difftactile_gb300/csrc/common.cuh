@@ -406,6 +406,13 @@ inline int scatter_kind(const dt_world* w) {
   if (w->scatter_mode != DT_SCATTER_WARP) return w->scatter_mode == DT_SCATTER_TILE ? DT_SCATTER_TILE : DT_SCATTER_GLOBAL;
   return DT_SCATTER_WARP + d;
 }
+// template scatter mode of the G2P adjoint's launch: scatter_kind, with the WARP reduction's depth
+// taken from scatter_depth_adj when that is 1, 2 or 3 (3: whole runs)
+inline int scatter_kind_adj(const dt_world* w) {
+  const int k = scatter_kind(w), a = w->scatter_depth_adj;
+  if (k < DT_SCATTER_WARP || k > DT_SCATTER_WARP + 2 || a < 1 || a > 3) return k;
+  return DT_SCATTER_WARP + (a == 3 ? 0 : a);
+}
 // dynamic shared memory of a particle-role launch with scatter MODE and NT threads
 constexpr size_t scatter_smem(int MODE, int NT) {
   return MODE == DT_SCATTER_TILE ? 25 * NT * sizeof(float) : (MODE >= DT_MODE_SMEM ? DT_SMEM_TILE * 16 : 0);

@@ -57,7 +57,8 @@ class World:
     def __init__(self, envs: list[EnvSpec], n_frames: int, dt: float, device="cuda", tape_blocks: int | None = None,
                  grad_clip: float = 1000.0, svd_sweeps: int = 4, sort_particles: bool = True,
                  svd_grad_mode: int = 0, scatter_mode: int = 2, svd_tape: bool = True, p_block: int = 128,
-                 scatter_depth: int = 0, contact_lanes: int = 8, p_per_thread: int = 1, overlap_ropes: bool = True):
+                 scatter_depth: int = 0, contact_lanes: int = 8, p_per_thread: int = 1, overlap_ropes: bool = True,
+                 scatter_depth_adj: int = 0):
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise ValueError(f"World buffers must live on a CUDA device (the kernels take device pointers), "
@@ -286,6 +287,7 @@ class World:
         w.scatter_depth = int(scatter_depth)
         w.contact_lanes = int(contact_lanes)
         w.p_per_thread = int(p_per_thread)
+        w.scatter_depth_adj = int(scatter_depth_adj)
         for name in N.ROPE_PTR_FIELDS:
             setattr(w, name, t[name].data_ptr() if (self.n_ropes and t[name].numel()) else None)
         w.n_ropes, w.n_rope_particles = self.n_ropes, NR

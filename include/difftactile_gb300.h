@@ -50,7 +50,7 @@
 extern "C" {
 #endif
 
-#define DT_ABI_VERSION 7
+#define DT_ABI_VERSION 8
 
 #define DT_OK 0
 #define DT_ERR_ARG (-1)        /* null pointer, bad size or frame index */
@@ -248,6 +248,12 @@ typedef struct dt_world {
   float* t_svd;                  /* [n_frames][6][n_tets][4]: U, V, sigma of each DT_FEM_LINEAR_COROTATED
                                     tet's F per frame, in p_svd's plane layout, written by the forward,
                                     read by the tet adjoint instead of recomputing; NULL: recomputed */
+  /* ---- launch shape (ABI 8) ---- */
+  int scatter_depth_adj;         /* the G2P adjoint's WARP scatter: 1 or 2 caps its segmented reduction at
+                                    that many shuffle steps, 3 sums whole runs; any other value (0): the
+                                    P2G's scatter_depth.  The two scatters weigh shuffles against REDs
+                                    differently (the adjoint has no block marking and fewer registers
+                                    live across the stencil) */
 } dt_world;
 
 /* 27-node particle scatters: TILE gathers each CTA's stencil contributions per node in shared

@@ -35,7 +35,7 @@ def test_exports_every_declared_symbol(lib_path):
 def test_struct_layout_matches_ctypes(lib_path):
     from difftactile_gb300 import _native
     lib = _native.load(lib_path)  # loads without a GPU; only size queries are called
-    assert lib.dt_abi_version() == 7
+    assert lib.dt_abi_version() == 8
     assert lib.dt_sizeof_world() == ctypes.sizeof(_native.DtWorld)
     assert lib.dt_sizeof_env() == ctypes.sizeof(_native.DtEnv)
     assert lib.dt_sizeof_sensor() == ctypes.sizeof(_native.DtSensor)

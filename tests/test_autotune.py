@@ -48,7 +48,8 @@ def test_tune_substep_applies_and_caches(cuda_lib, tmp_path):
         w.substep(1)
         AT._cache.clear()
         r = AT.tune_substep(w, frame=1, reps=3, warmup=1, cache_path=path)
-        assert not r["cached"] and len(r["ms"]) == len(AT.candidates())
+        n = len(AT.candidates())
+        assert not r["cached"] and len(r["ms"]) in (n, n + 2)  # + the warp winner's two other adjoint depths
         assert all(0.0 < v < 1e3 for v in r["ms"].values())
         fastest = min(r["ms"], key=r["ms"].get)
         # the default is kept unless the fastest beats it by more than the 2% margin
@@ -85,7 +86,8 @@ class _FakeWorld:
     """The fields the tuner sets, without a device: the 'time' of a shape is a fixed function of it."""
     def __init__(self, n_particles=1000):
         import types
-        self.w = types.SimpleNamespace(scatter_mode=2, p_block=128, scatter_depth=0, contact_lanes=8, p_per_thread=1)
+        self.w = types.SimpleNamespace(scatter_mode=2, p_block=128, scatter_depth=0, contact_lanes=8, p_per_thread=1,
+                                       scatter_depth_adj=0)
         self.lib = _FakeLib()
         self.device = "cpu"
         self.n_envs, self.n_particles, self.n_verts, self.n_tets, self.n_tris = 1, n_particles, 10, 10, 10
@@ -127,4 +129,34 @@ def test_tuner_picks_the_fastest_shape_and_keeps_the_default_within_the_margin()
     run.world = other
     r5 = AT.tune(other, run, timer=_timer_for(cost2), tag="t")
     assert not r5["cached"]
+    AT._cache.clear()
+
+
+def test_tuner_refines_the_adjoint_depth_of_the_fastest_shape():
+    """After the search, the fastest warp shape is timed with the G2P adjoint at each other depth; a
+    faster variant wins and is applied (dt_world.scatter_depth_adj 3 for whole runs, else the depth),
+    and the field reads back through current()."""
+    AT._cache.clear()
+    world = _FakeWorld()
+
+    def run():
+        pass
+    run.world = world
+    fast = {"scatter": "warp", "p_block": 64, "depth": 1, "lanes": 4, "pdl": 0, "ppt": 2}
+    for adj, code in ((2, 2), (0, 3)):
+        def cost(w, adj=adj):
+            c = AT.current(w)
+            base = {k: v for k, v in c.items() if k != "adj_depth"}
+            if base != fast:
+                return 1.0
+            return 0.8 if c.get("adj_depth") == adj else 0.9
+        r = AT.tune(world, run, timer=_timer_for(cost), use_cache=False, refine=AT.adjoint_depths)
+        assert r["best"] == dict(fast, adj_depth=adj) and world.w.scatter_depth_adj == code
+        assert AT.current(world) == r["best"]
+        assert len(r["ms"]) == len(AT.candidates()) + 2
+    # a variant no faster leaves the adjoint on the P2G's depth
+    cost = lambda w: 0.9 if {k: v for k, v in AT.current(w).items() if k != "adj_depth"} == fast else 1.0  # noqa: E731
+    r = AT.tune(world, run, timer=_timer_for(cost), use_cache=False, refine=AT.adjoint_depths)
+    assert r["best"] == fast and world.w.scatter_depth_adj == 0 and "adj_depth" not in AT.current(world)
+    assert AT.adjoint_depths(dict(fast, scatter="global")) == []
     AT._cache.clear()

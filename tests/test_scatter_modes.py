@@ -65,19 +65,21 @@ def test_warp_runs_across_env_boundaries(cuda_lib):
         compare(w, 2, st, env_idx=e)
 
 
-@pytest.mark.parametrize("mode,p_block,depth,ppt", [("warp", 64, 0, 1), ("warp", 256, 0, 1), ("global", 64, 0, 1),
-                                                    ("global", 256, 0, 1), ("warp", 128, 1, 1), ("warp", 128, 2, 1),
-                                                    ("warp", 256, 1, 1), ("warp", 128, 1, 2), ("warp", 64, 0, 2),
-                                                    ("global", 256, 0, 2), ("tile", 128, 0, 2), ("smem", 128, 0, 1),
-                                                    ("smem", 128, 0, 2), ("smem", 64, 0, 1), ("smem", 256, 0, 2)])
-def test_particle_block_sizes(cuda_lib, mode, p_block, depth, ppt):
-    """Particle-role CTAs of 64 and 256 threads, capped segmented reductions and two chunks of
-    particles per CTA (the autotuner's other shapes; 1,152 particles: an odd number of chunks, so the
-    last two-chunk CTA has one) give the oracle's forward state after three substeps and its
-    one-substep adjoint."""
+@pytest.mark.parametrize("mode,p_block,depth,ppt,adj", [
+    ("warp", 64, 0, 1, 0), ("warp", 256, 0, 1, 0), ("global", 64, 0, 1, 0), ("global", 256, 0, 1, 0),
+    ("warp", 128, 1, 1, 0), ("warp", 128, 2, 1, 0), ("warp", 256, 1, 1, 0), ("warp", 128, 1, 2, 0),
+    ("warp", 64, 0, 2, 0), ("global", 256, 0, 2, 0), ("tile", 128, 0, 2, 0), ("smem", 128, 0, 1, 0),
+    ("smem", 128, 0, 2, 0), ("smem", 64, 0, 1, 0), ("smem", 256, 0, 2, 0),
+    ("warp", 64, 1, 2, 2), ("warp", 64, 1, 2, 3), ("warp", 128, 0, 1, 1), ("global", 128, 0, 1, 2)])
+def test_particle_block_sizes(cuda_lib, mode, p_block, depth, ppt, adj):
+    """Particle-role CTAs of 64 and 256 threads, capped segmented reductions, two chunks of particles
+    per CTA and a G2P adjoint scatter of another depth than the P2G's (scatter_depth_adj: 1, 2, or 3
+    for whole runs; ignored outside the warp scatter) — the autotuner's other shapes; 1,152
+    particles: an odd number of chunks, so the last two-chunk CTA has one — give the oracle's forward
+    state after three substeps and its one-substep adjoint."""
     env = SS.pad_over_box()
     cv = [SS.control_velocity(sp) for sp in env.sensors]
-    kw = dict(scatter_mode=MODES[mode], p_block=p_block, scatter_depth=depth, p_per_thread=ppt)
+    kw = dict(scatter_mode=MODES[mode], p_block=p_block, scatter_depth=depth, p_per_thread=ppt, scatter_depth_adj=adj)
     w = World([env], n_frames=4, dt=DT, **kw)
     for s, c in enumerate(cv):
         w.set_control_velocity(s, c)
