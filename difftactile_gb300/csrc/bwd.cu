@@ -41,30 +41,43 @@ DT_DEV float gap_clamp(float a) { return a >= 0.f ? fmaxf(a, 1e-8f) : fminf(a, -
 // + S (ff o (V^T Vb - Vb^T V)) ] V^T with ff_ij = 1/clamp(s_j^2 - s_i^2).  The adjoint Rb of the
 // rotation R = U V^T is passed separately: with M = U^T Rb V it contributes Ub = Rb V, Vb = Rb^T U,
 // i.e. ff_ij (M - M^T)_ij (s_j - s_i), which the stable mode evaluates as (M - M^T)_ij / (s_i + s_j).
-DT_DEV m3 svd_grad(const m3& U, v3 s, const m3& V, const m3& Ub_in, v3 sb, const m3& Vb_in, const m3& Rb, int mode) {
+// uv false: the caller's Ub and Vb are zero, and in the stable mode their ff terms (zero) are skipped
+// (the result differs at most in the sign of an exact zero).
+DT_DEV m3 svd_grad(const m3& U, v3 s, const m3& V, const m3& Ub_in, v3 sb, const m3& Vb_in, const m3& Rb, int mode,
+                   bool uv = true) {
   const float sv[3] = {s.x, s.y, s.z};
   m3 Ub = Ub_in, Vb = Vb_in;
   if (mode == DT_SVDGRAD_REFERENCE) {
     Ub = madd(Ub, mmul(Rb, V));
     Vb = madd(Vb, mTmul(Rb, U));
+    uv = true;
   }
   const m3 M = mmul(mTmul(U, Rb), V);
-  const m3 UtUb = mTmul(U, Ub), UbtU = mTmul(Ub, U), VtVb = mTmul(V, Vb), VbtV = mTmul(Vb, V);
   m3 inner;
+  if (uv) {
+    const m3 UtUb = mTmul(U, Ub), UbtU = mTmul(Ub, U), VtVb = mTmul(V, Vb), VbtV = mTmul(Vb, V);
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      float v = 0.f;
-      if (i != j) {
-        const float ff = 1.f / gap_clamp(sv[j] * sv[j] - sv[i] * sv[i]);
-        v = ff * (UtUb.a[i][j] - UbtU.a[i][j]) * sv[j] + sv[i] * ff * (VtVb.a[i][j] - VbtV.a[i][j]);
-        if (mode != DT_SVDGRAD_REFERENCE) v += (M.a[i][j] - M.a[j][i]) / gap_clamp(sv[i] + sv[j]);
-      } else {
-        v = i == 0 ? sb.x : (i == 1 ? sb.y : sb.z);
+      for (int j = 0; j < 3; ++j) {
+        float v = 0.f;
+        if (i != j) {
+          const float ff = 1.f / gap_clamp(sv[j] * sv[j] - sv[i] * sv[i]);
+          v = ff * (UtUb.a[i][j] - UbtU.a[i][j]) * sv[j] + sv[i] * ff * (VtVb.a[i][j] - VbtV.a[i][j]);
+          if (mode != DT_SVDGRAD_REFERENCE) v += (M.a[i][j] - M.a[j][i]) / gap_clamp(sv[i] + sv[j]);
+        } else {
+          v = i == 0 ? sb.x : (i == 1 ? sb.y : sb.z);
+        }
+        inner.a[i][j] = v;
       }
-      inner.a[i][j] = v;
-    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        inner.a[i][j] = i != j ? (M.a[i][j] - M.a[j][i]) / gap_clamp(sv[i] + sv[j])
+                               : (i == 0 ? sb.x : (i == 1 ? sb.y : sb.z));
+  }
   return mmulT(mmul(U, inner), V);
 }
 
@@ -492,6 +505,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   const m3 G = mscale(E.stress_k, Ab);  // cauchy adjoint
   m3 Ub = mzero(), Vb = mzero(), Rb = mzero();
   m3 Frm = mzero();  // the return map's rotation-part adjoint when formed directly (von Mises)
+  bool uv = false;   // Ub or Vb set (the return map's adjoint through U and V)
   v3 sb = v3{0.f, 0.f, 0.f};
   float Jb;
   if (M.model == DT_MODEL_NEOHOOKEAN) {
@@ -557,6 +571,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
           }
         Frm = mmulT(mmul(s.U, inner), s.V);
       } else {
+        uv = true;
         m3 Ue = s.U, Ve = s.V;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -595,7 +610,8 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
       Fnb = Fpb;
     }
   }
-  if (M.model != DT_MODEL_NEOHOOKEAN) Fnb = madd(madd(Fnb, Frm), svd_grad(s.U, s.sig, s.V, Ub, sb, Vb, Rb, w.svd_grad_mode));
+  if (M.model != DT_MODEL_NEOHOOKEAN)
+    Fnb = madd(madd(Fnb, Frm), svd_grad(s.U, s.sig, s.V, Ub, sb, Vb, Rb, w.svd_grad_mode, uv));
   // F_new = (I + dt C) F
   m3 Ad = meye();
 #pragma unroll
@@ -666,7 +682,7 @@ __device__ void fem_tet_bwd(const dt_world& w, int f, int t) {
     const m3 Rb = mscale(S.lam * c - 2.f * S.mu, Pb);
     const float cb_ = S.lam * mdot(Pb, R);
     const m3 Fb = madd(mscale(2.f * S.mu, Pb),
-                       svd_grad(U, sg, Vm, mzero(), v3{cb_, cb_, cb_}, mzero(), Rb, DT_SVDGRAD_STABLE));
+                       svd_grad(U, sg, Vm, mzero(), v3{cb_, cb_, cb_}, mzero(), Rb, DT_SVDGRAD_STABLE, false));
     const m3 Db = mmulT(Fb, B);  // F = D B
     const v3 ab = mcol(Db, 0), bb = mcol(Db, 1), cbv = mcol(Db, 2);
     red_add_v4(aPos0 + tv.x, v3to4(ab));
