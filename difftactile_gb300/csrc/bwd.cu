@@ -42,9 +42,10 @@ DT_DEV float gap_clamp(float a) { return a >= 0.f ? fmaxf(a, 1e-8f) : fminf(a, -
 // rotation R = U V^T is passed separately: with M = U^T Rb V it contributes Ub = Rb V, Vb = Rb^T U,
 // i.e. ff_ij (M - M^T)_ij (s_j - s_i), which the stable mode evaluates as (M - M^T)_ij / (s_i + s_j).
 // uv false: the caller's Ub and Vb are zero, and in the stable mode their ff terms (zero) are skipped
-// (the result differs at most in the sign of an exact zero).
+// (the result differs at most in the sign of an exact zero).  `extra` is added to the bracket before
+// the final U [.] V^T (a caller's own term of that form, for one product instead of two).
 DT_DEV m3 svd_grad(const m3& U, v3 s, const m3& V, const m3& Ub_in, v3 sb, const m3& Vb_in, const m3& Rb, int mode,
-                   bool uv = true) {
+                   bool uv = true, const m3& extra = mzero()) {
   const float sv[3] = {s.x, s.y, s.z};
   m3 Ub = Ub_in, Vb = Vb_in;
   if (mode == DT_SVDGRAD_REFERENCE) {
@@ -78,7 +79,7 @@ DT_DEV m3 svd_grad(const m3& U, v3 s, const m3& V, const m3& Ub_in, v3 sb, const
         inner.a[i][j] = i != j ? (M.a[i][j] - M.a[j][i]) / gap_clamp(sv[i] + sv[j])
                                : (i == 0 ? sb.x : (i == 1 ? sb.y : sb.z));
   }
-  return mmulT(mmul(U, inner), V);
+  return mmulT(mmul(U, madd(inner, extra)), V);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -504,7 +505,8 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
   m3 Cb = mscale(pm, Ab);
   const m3 G = mscale(E.stress_k, Ab);  // cauchy adjoint
   m3 Ub = mzero(), Vb = mzero(), Rb = mzero();
-  m3 Frm = mzero();  // the return map's rotation-part adjoint when formed directly (von Mises)
+  m3 Frm = mzero();  // the return map's rotation-part adjoint when formed directly (von Mises), as
+                     // U Frm V^T: added inside the SVD adjoint's final product
   bool uv = false;   // Ub or Vb set (the return map's adjoint through U and V)
   v3 sb = v3{0.f, 0.f, 0.f};
   float Jb;
@@ -569,7 +571,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
             inner.a[i][j] = UtFV.a[i][j] * A + UtFV.a[j][i] * B;
             inner.a[j][i] = UtFV.a[j][i] * A + UtFV.a[i][j] * B;
           }
-        Frm = mmulT(mmul(s.U, inner), s.V);
+        Frm = inner;
       } else {
         uv = true;
         m3 Ue = s.U, Ve = s.V;
@@ -611,7 +613,7 @@ __device__ void p2g_bwd(const dt_world& w, int f, int p, float& mub, float& lamb
     }
   }
   if (M.model != DT_MODEL_NEOHOOKEAN)
-    Fnb = madd(madd(Fnb, Frm), svd_grad(s.U, s.sig, s.V, Ub, sb, Vb, Rb, w.svd_grad_mode, uv));
+    Fnb = madd(Fnb, svd_grad(s.U, s.sig, s.V, Ub, sb, Vb, Rb, w.svd_grad_mode, uv, Frm));
   // F_new = (I + dt C) F
   m3 Ad = meye();
 #pragma unroll
